@@ -1,0 +1,305 @@
+"""Benchmark: LJ fluid, N = 864,000 (FCC 60^3 x 4), NVE, fp32, Dense neighbour list.
+
+One step = the reference's loop body (jax_md/partition.py:841-854):
+    nbrs = nbrs.update(state.position); state = apply_fn(state, neighbor=nbrs)
+i.e. the device-side skin test, the (conditional) cell-list + neighbour rebuild,
+the velocity-Verlet step with the LJ pair-force kernel.
+
+  value : atom-steps/s, state resident in HBM, steps replayed from a CUDA graph;
+  e2e   : the same through the public API with host (pinned) buffers: every
+          step copies positions and momenta host->device, runs the step, and
+          copies them back device->host;
+  roofline: the pair-force kernel timed alone (CUDA events), algorithmic bytes
+          per launch / duration vs the measured HBM copy bandwidth;
+  cpu_baseline: the oracle's float32 OpenMP restatement (kind "port") on a
+          bounded sample of the same workload.
+
+--impl reference runs only the CPU arm (the reference is JAX, absent here; the
+oracle port stands in for it) and prints its own line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = 'atom-steps/s LJ N=864k NVE fp32'
+N_CELLS = 60
+DENSITY, KT, DT, SKIN = 0.8442, 0.722, 0.005, 0.3
+
+
+def peaks():
+    p = ROOT / 'MEASURED_PEAKS.json'
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d['hbm_gbs']), 'measured'
+    return 6800.0, 'fallback'
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ('clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,'
+             'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+             'clocks_event_reasons.sw_power_cap')
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', os.environ.get('CUDA_VISIBLE_DEVICES', '0').split(',')[0],
+                                          f'--query-gpu={q}', '--format=csv,noheader,nounits',
+                                          '-lms', '100'], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [s.strip() for s in line.split(',')]
+            if len(parts) == 6:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unavailable']}
+        sm = [float(s[0]) for s in self.samples if s[0].replace('.', '').isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace('.', '').isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if s[2 + k].lower() == 'active'})
+        return {'sm_mhz': float(np.median(sm)) if sm else None,
+                'sm_max_mhz': max(mx) if mx else None, 'reasons': reasons, 'samples': len(self.samples)}
+
+
+def cpu_port_run(R, P, L, steps, threads=0):
+    from oracle import build as ob
+    lib = ctypes.CDLL(str(ob.build()))
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib.md_cpu_run.argtypes = [fp, fp, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                               ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    x = np.ascontiguousarray(R, np.float32).copy()
+    p = np.ascontiguousarray(P, np.float32).copy()
+    t0 = time.perf_counter()
+    rb = lib.md_cpu_run(x.ctypes.data_as(fp), p.ctypes.data_as(fp), len(x), float(L), 2.0, 2.5,
+                        SKIN, DT, 128, steps, threads)
+    dt = time.perf_counter() - t0
+    return dt, rb, lib.md_cpu_max_threads()
+
+
+def cpu_baseline(R, P, L, budget_s=15.0):
+    """Times the float32 OpenMP port on a bounded number of steps of the same system."""
+    dt1, _, threads = cpu_port_run(R, P, L, 2)
+    steps = max(2, int(budget_s / max(dt1 / 2, 1e-3)))
+    steps = min(steps, 200)
+    dt, rb, threads = cpu_port_run(R, P, L, steps)
+    return {'value': len(R) * steps / dt, 'unit': 'atom-steps/s', 'cores': threads, 'kind': 'port',
+            'sample': f'{steps} NVE steps of the N={len(R)} LJ system (full size, '
+                      f'{rb} rebuilds), float32 OpenMP restatement, {threads} threads'}
+
+
+def run_reference(args):
+    import torch.distributed as dist  # noqa: F401
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    from oracle import md_oracle as O
+    R, L = O.fcc_lattice(N_CELLS, DENSITY, 0.05, 0)
+    P = O.maxwell_boltzmann(len(R), 3, KT, 1)
+    # warmup + timed, each step a bounded sample (the whole run stays within minutes)
+    sample_steps = 5
+    for _ in range(args.warmup):
+        cpu_port_run(R, P, L, 1)
+    times = []
+    threads = 0
+    for _ in range(args.steps):
+        dt, rb, threads = cpu_port_run(R, P, L, sample_steps)
+        times.append(dt / sample_steps)
+    per = float(np.median(times))
+    v = len(R) / per
+    line = {'metric': METRIC, 'value': v, 'unit': 'atom-steps/s', 'n_gpus': args.gpus,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': per * 1e3,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+            'data': 'synthetic', 'impl': 'reference',
+            'config': {'workload': 'LJ fluid FCC 60^3x4 N=864000 rho=0.8442 rc=2.5 skin=0.3 '
+                                   'dt=0.005 NVE Dense', 'inputs': 'host memory (CPU run)'},
+            'cpu_baseline': {'value': v, 'unit': 'atom-steps/s', 'cores': threads, 'kind': 'port',
+                             'sample': f'{sample_steps} NVE steps per timed step incl. cell list, '
+                                       'neighbour list and forces (float32 OpenMP restatement; '
+                                       'JAX is not installed on this box)'},
+            'e2e': {'value': v, 'unit': 'atom-steps/s', 'h2d_bytes_per_step': 0,
+                    'd2h_bytes_per_step': 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=200)
+    ap.add_argument('--warmup', type=int, default=20)
+    ap.add_argument('--impl', default='native')
+    ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--cells', type=int, default=N_CELLS)
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        return run_reference(args)
+
+    import torch
+    from jax_md_gb300 import _build
+    _build.build()
+    from jax_md_gb300 import energy, partition, quantity, simulate, space
+    from jax_md_gb300 import _native as NAT
+    from oracle import md_oracle as O
+
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    dev = torch.device(f'cuda:{local}')
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl')
+
+    R, L = O.fcc_lattice(args.cells, DENSITY, 0.05, 0)
+    P = O.maxwell_boltzmann(len(R), 3, KT, 1)
+    n = len(R)
+    disp, shift = space.periodic(float(L))
+    nfn, efn = energy.lennard_jones_neighbor_list(disp, float(L), dr_threshold=SKIN,
+                                                  format=partition.Dense)
+    Rt = torch.tensor(R, device=dev)
+    nb = nfn.allocate(Rt)
+    init, apply = simulate.nve(efn, shift, DT)
+    st = init(0, Rt, momenta=torch.tensor(P, device=dev), neighbor=nb)
+
+    def step():
+        nb.update(st.position)
+        apply(st, neighbor=nb)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    # capture one step in a CUDA graph; replay it K times
+    s = torch.cuda.Stream(dev)
+    s.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(s):
+        step()
+    torch.cuda.current_stream(dev).wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        step()
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    E0 = float(efn.energy_f64(st.position, nb) + quantity._ke_f64(st.momentum))
+    cur = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks() as clk:
+        ev0.record(cur)
+        for _ in range(args.steps):
+            g.replay()
+        ev1.record(cur)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t)
+    ms_per_step = ms / args.steps
+    value = n * world * args.steps / (ms / 1e3)
+    E1 = float(efn.energy_f64(st.position, nb) + quantity._ke_f64(st.momentum))
+    overflow = bool(nb.did_buffer_overflow)
+
+    # dominant kernel alone: the LJ pair-force kernel
+    nbar = float(nb.nbr_count.float().mean())
+    f_out = st.force
+    for _ in range(3):
+        efn.forces(st.position, nb, out=f_out)
+    torch.cuda.synchronize()
+    reps = 50
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(cur)
+    for _ in range(reps):
+        efn.forces(st.position, nb, out=f_out)
+    e1.record(cur)
+    torch.cuda.synchronize()
+    pair_ms = e0.elapsed_time(e1) / reps
+    # algorithmic bytes of one force launch: index rows + counts + own position + force row
+    pair_bytes = n * (4 * nbar + 4 + 16 + 16)
+    hbm, src = peaks()
+    achieved = pair_bytes / (pair_ms / 1e3) / 1e9
+    step_bytes = n * (4 * nbar + 96)
+
+    # e2e: host pinned buffers through the public API, every step
+    xh = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    ph = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    xh.copy_(st.position)
+    ph.copy_(st.momentum)
+    e2e_steps = max(5, min(args.steps, 50))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        st.position.copy_(xh, non_blocking=True)
+        st.momentum.copy_(ph, non_blocking=True)
+        g.replay()
+        xh.copy_(st.position, non_blocking=True)
+        ph.copy_(st.momentum, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = n * world * e2e_steps / e2e_s
+
+    launches_per_step = 3 + 1 + 7  # kick-drift, pair, kick, skin test, rebuild chain
+    line = {
+        'metric': METRIC, 'value': value, 'unit': 'atom-steps/s', 'n_gpus': world,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_per_step,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+        'data': 'synthetic',
+        'config': {'workload': f'LJ fluid FCC {args.cells}^3x4 N={n} rho=0.8442 rc=2.5 '
+                               'r_onset=2.0 skin=0.3 dt=0.005 NVE Dense, replicas only',
+                   'l2': 'inputs larger than L2 (neighbour rows ~%d MB)' % int(n * 4 * nbar / 1e6),
+                   'mean_neighbors': nbar, 'max_occupancy': nb.max_occupancy,
+                   'energy_drift_per_atom': (E1 - E0) / n, 'overflow': overflow},
+        'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
+                     'frac': achieved / hbm, 'traffic': None, 'peak_source': src,
+                     'kernel': 'k_pair_dense (LJ, Dense)', 'kernel_ms': pair_ms,
+                     'step_algorithmic_GBps': step_bytes * args.steps / (ms / 1e3) / 1e9},
+        'e2e': {'value': e2e_value, 'unit': 'atom-steps/s', 'h2d_bytes_per_step': 2 * n * 12,
+                'd2h_bytes_per_step': 2 * n * 12},
+        'gpu_launches': launches_per_step * args.steps,
+        'clocks': clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu:
+        line['cpu_baseline'] = cpu_baseline(R, P, L)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,243 @@
+/*
+ * jax_md_gb300.h — C ABI of the GB300-native short-range MD path.
+ *
+ * Every entry point is `extern "C"`, takes plain device pointers, element
+ * strides and sizes, and a CUDA stream (`cudaStream_t`, passed here as
+ * `void*` so this header needs no CUDA include).  All buffers are owned by the
+ * caller.  Functions that need scratch memory take a caller-provided workspace
+ * and a `*_workspace_bytes` query.  Nothing here synchronises the stream, so
+ * every call is stream-ordered and may be captured into a CUDA graph.
+ *
+ * Return value: JMD_OK (0) or a JMD_ERR_* code for argument / launch errors;
+ * `jmd_last_error()` gives a message (per thread).  Data-dependent conditions
+ * (neighbour-list overflow, cell-list overflow, cell size too small, malformed
+ * box) are NOT errors: they are OR-ed into a device-side uint8 `error_code`
+ * with the bit values of JAX MD's PartitionErrorCode
+ * (jax_md/partition.py:494-520), which keeps `did_buffer_overflow` semantics.
+ *
+ * Positions, momenta and forces are float32 rows of `dim` (2 or 3) components
+ * with a row stride given in floats; a stride of 4 (float4 rows) is the fast
+ * layout.  Neighbour indices are int32 with sentinel N (jax_md/partition.py:972).
+ */
+#ifndef JAX_MD_GB300_H_
+#define JAX_MD_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JMD_OK 0
+#define JMD_ERR_INVALID_ARGUMENT 1
+#define JMD_ERR_CUDA 2
+#define JMD_ERR_WORKSPACE 3
+#define JMD_ERR_UNSUPPORTED 4
+
+/* PartitionErrorCode bits, jax_md/partition.py:494-520. */
+#define JMD_NEIGHBOR_LIST_OVERFLOW 1
+#define JMD_CELL_LIST_OVERFLOW 2
+#define JMD_CELL_SIZE_TOO_SMALL 4
+#define JMD_MALFORMED_BOX 8
+
+/* NeighborListFormat, jax_md/partition.py:641-657. */
+#define JMD_DENSE 0
+#define JMD_SPARSE 1
+#define JMD_ORDERED_SPARSE 2
+
+/* Pair potentials. */
+#define JMD_LJ 0            /* energy.lennard_jones x multiplicative_isotropic_cutoff (energy.py:246-272,534-580) */
+#define JMD_LJ_TRUNCATED 1  /* energy.lennard_jones, hard truncation at r_cutoff */
+#define JMD_SOFT_SPHERE 2   /* energy.soft_sphere (energy.py:125-173) */
+
+#define JMD_MAX_SPECIES 8
+
+/* Geometry: space.periodic (jax_md/space.py:275-329) or space.free (:258-272). */
+typedef struct {
+  int32_t dim;       /* 2 or 3 */
+  int32_t periodic;  /* 1: minimum-image displacement and wrapped shift; 0: free */
+  float box[3];      /* side lengths; box[2] unused for dim 2 */
+} jmd_space;
+
+/* Static description of a neighbour list, the C mirror of the static fields
+ * of jax_md's NeighborList (partition.py:684-737) plus the cell grid from
+ * _cell_dimensions (partition.py:146-188). */
+typedef struct {
+  jmd_space space;
+  float cutoff_sq;            /* (r_cutoff + dr_threshold)^2, partition.py:882-883 */
+  int32_t use_cell_list;      /* 0: all-pairs candidates (partition.py:893-898) */
+  int32_t cells_per_side[3];  /* floor(L / cutoff) per dimension */
+  float cell_size[3];         /* L / cells_per_side, float32 as the reference bins */
+  int32_t cell_capacity;      /* cell-list capacity (slot rule, overflow test) */
+  int32_t format;             /* JMD_DENSE / JMD_SPARSE / JMD_ORDERED_SPARSE */
+  int32_t mask_self;          /* partition.py:953-958 */
+  int64_t max_occupancy;      /* Dense: row width; Sparse: pair capacity */
+} jmd_nlist;
+
+/* Pair potential parameters.  n_species == 0 means scalar parameters stored
+ * at [0][0]; otherwise species matrices [S][S] (smap.py:778-823). */
+typedef struct {
+  int32_t kind;            /* JMD_LJ / JMD_LJ_TRUNCATED / JMD_SOFT_SPHERE */
+  int32_t n_species;
+  int32_t per_pair_cutoff; /* 1: r_onset/r_cutoff scale with sigma_ij instead of max sigma */
+  int32_t pad_;
+  float r_onset;           /* absolute onset radius (LJ), energy.py:319 */
+  float r_cutoff;          /* absolute cutoff radius (LJ), energy.py:320 */
+  float sigma[JMD_MAX_SPECIES][JMD_MAX_SPECIES];
+  float epsilon[JMD_MAX_SPECIES][JMD_MAX_SPECIES];
+  float alpha[JMD_MAX_SPECIES][JMD_MAX_SPECIES];
+} jmd_pair;
+
+const char* jmd_last_error(void);
+int jmd_version(void);
+
+/* ---------------------------------------------------------------- cells -- */
+
+/* Workspace for the binning stage shared by cell-list and neighbour builds. */
+size_t jmd_cell_workspace_bytes(int64_t n_atoms, int64_t cell_count);
+
+/* Maximum number of atoms in any cell; the device half of
+ * _estimate_cell_capacity (partition.py:191-209, 243-250).  Writes one int32
+ * to `max_filling` (device). */
+int jmd_cell_max_filling(const float* position, int64_t pos_stride, int64_t n,
+                         const jmd_nlist* nl, int32_t* max_filling,
+                         void* workspace, size_t workspace_bytes, void* stream);
+
+/* partition.cell_list update (partition.py:349-471): fills the reference
+ * layout buffers id_buffer [cell_count*cap] (empty = N) and position_buffer
+ * [cell_count*cap*dim] (empty = 0) with the reference slot rule
+ * slot = hash*cap + (sorted_rank mod cap), particle_cell_id [N*dim], and ORs
+ * JMD_CELL_LIST_OVERFLOW into error_code when a cell holds more than cap. */
+int jmd_cell_list_build(const float* position, int64_t pos_stride, int64_t n,
+                        const jmd_nlist* nl, int32_t* id_buffer,
+                        float* position_buffer, int32_t* particle_cell_id,
+                        uint8_t* error_code, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------- neighbour lists -- */
+
+size_t jmd_neighbor_list_workspace_bytes(const jmd_nlist* nl, int64_t n);
+
+/* Builds the neighbour list of partition.neighbor_list's neighbor_fn
+ * (partition.py:1034-1121): candidates from the 3^d cells in the reference's
+ * order, self mask, strict d^2 < cutoff^2, stable compaction.
+ *   Dense:  idx is [n, idx_ld], rows hold max_occupancy entries padded with n.
+ *   Sparse: idx is [2, idx_ld]: row 0 receivers (neighbour j), row 1 senders
+ *           (atom i), ordered by sender then candidate order; OrderedSparse
+ *           keeps j < i only (partition.py:997-998).
+ * idx == NULL computes only `occupancy` (count pass of allocate).
+ * occupancy (device int64): Dense max row count / Sparse total pair count.
+ * nbr_count (device [n], optional): per-atom counts (Dense only).
+ * Sets JMD_NEIGHBOR_LIST_OVERFLOW when occupancy > max_occupancy and
+ * JMD_CELL_LIST_OVERFLOW when a cell holds more than cell_capacity.
+ * reference_position (optional, row stride ref_stride) receives a copy of
+ * `position` (NeighborList.reference_position).
+ * rebuild_flag (optional device int32): when given, the build runs only if
+ * *rebuild_flag != 0 and clears it; this is the lax.cond of
+ * partition.py:1146-1154 kept on the device. */
+int jmd_neighbor_list_build(const jmd_nlist* nl, const float* position,
+                            int64_t pos_stride, int64_t n, int32_t* idx,
+                            int64_t idx_ld, int32_t* nbr_count,
+                            int64_t* occupancy, uint8_t* error_code,
+                            float* reference_position, int64_t ref_stride,
+                            int32_t* rebuild_flag, void* workspace,
+                            size_t workspace_bytes, void* stream);
+
+/* Skin test of partition.py:1146-1154: ORs 1 into *rebuild_flag when any
+ * |d(position_i, reference_i)|^2 > threshold_sq. */
+int jmd_skin_check(const float* position, int64_t pos_stride,
+                   const float* reference_position, int64_t ref_stride,
+                   int64_t n, const jmd_space* space, float threshold_sq,
+                   int32_t* rebuild_flag, void* stream);
+
+/* --------------------------------------------------------- pair kernels -- */
+
+size_t jmd_pair_workspace_bytes(int64_t n);
+
+/* smap.pair_neighbor_list energy (smap.py:922-979) and its gradient for the
+ * potential in `pp`, over a neighbour list of `format`:
+ *   force  [n, force_stride] (optional): -dE/dR;
+ *   energy (optional device double): total energy, sum over pairs / 2
+ *          (Dense, Sparse) or / 1 (OrderedSparse), f64 reduction;
+ *   per_atom_energy [n] (optional, Dense/Sparse): reduce_axis=(1,);
+ *   virial [6] (optional device double): dU/d(strain) = sum_pairs
+ *          U'(r)/r dR_a dR_b, order xx yy zz xy xz yz (2D: xx yy xy).
+ * species (optional [n] int32) selects rows of the species matrices.
+ * nbr_count (optional, Dense) bounds each row; otherwise rows end at the
+ * first sentinel.  The Dense path assumes a symmetric list (every list this
+ * library builds without overflow is). */
+int jmd_pair_forces(const jmd_pair* pp, const jmd_space* space, int32_t format,
+                    const float* position, int64_t pos_stride,
+                    const int32_t* species, int64_t n, const int32_t* idx,
+                    int64_t idx_ld, int64_t idx_width,
+                    const int32_t* nbr_count, float* force,
+                    int64_t force_stride, double* energy,
+                    float* per_atom_energy, double* virial, void* workspace,
+                    size_t workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------- integrators -- */
+
+/* momentum_step (simulate.py:168-173): p += dt * f. */
+int jmd_momentum_step(float* momentum, int64_t p_stride, const float* force,
+                      int64_t f_stride, int64_t n, int32_t dim, float dt,
+                      void* stream);
+
+/* position_step with shift_fn (simulate.py:176-188, space.py:250-252):
+ * x = shift(x, dt * p / m).  mass (optional [n]) else mass_scalar. */
+int jmd_position_step(float* position, int64_t x_stride, const float* momentum,
+                      int64_t p_stride, const float* mass, float mass_scalar,
+                      int64_t n, const jmd_space* space, float dt,
+                      void* stream);
+
+/* The first half of velocity_verlet (simulate.py:235-239) fused:
+ *   p = p_scale * p + dt/2 * f ; x = shift(x, dt * p / m)
+ * p_scale (optional device double, else 1) applies a pending Nose-Hoover
+ * rescale.  When reference_position is given it also runs the skin test on
+ * the new x and ORs 1 into *rebuild_flag. */
+int jmd_verlet_kick_drift(float* position, int64_t x_stride, float* momentum,
+                          int64_t p_stride, const float* force,
+                          int64_t f_stride, const float* mass,
+                          float mass_scalar, int64_t n,
+                          const jmd_space* space, float dt,
+                          const double* p_scale,
+                          const float* reference_position, int64_t ref_stride,
+                          float threshold_sq, int32_t* rebuild_flag,
+                          void* stream);
+
+/* Kinetic energy 0.5 sum p^2/m in f64 (quantity.py:124-159). */
+size_t jmd_reduce_workspace_bytes(int64_t n);
+int jmd_kinetic_energy(const float* momentum, int64_t p_stride,
+                       const float* mass, float mass_scalar, int64_t n,
+                       int32_t dim, double* out, void* workspace,
+                       size_t workspace_bytes, void* stream);
+
+/* Nose-Hoover chain state on the device, f64 (simulate.py:350-374). */
+typedef struct {
+  int32_t chain_length;  /* M + 1 <= 16 */
+  int32_t chain_steps;
+  int32_t sy_steps;      /* 1, 3, 5, 7 */
+  int32_t dof;
+  double dt;
+  double tau;
+} jmd_nhc;
+
+/* chain [4*16 + 2] doubles: xi[16], p_xi[16], Q[16], spare[16], KE, kT.
+ * Runs update_mass (simulate.py:509-515) when update_mass != 0, then
+ * half_step (simulate.py:492-507) with the kinetic energy stored in the chain
+ * (or *kinetic_energy when given), and writes the total momentum scale to
+ * *p_scale (the caller applies it, e.g. through jmd_verlet_kick_drift or
+ * jmd_scale_momentum). */
+int jmd_nhc_half_step(const jmd_nhc* c, double* chain,
+                      const double* kinetic_energy, int32_t update_mass,
+                      double* p_scale, void* stream);
+
+/* p *= *scale. */
+int jmd_scale_momentum(float* momentum, int64_t p_stride, int64_t n,
+                       int32_t dim, const double* scale, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif  /* JAX_MD_GB300_H_ */

@@ -1,0 +1,152 @@
+"""ctypes binding of the C ABI in ``include/jax_md_gb300.h``.
+
+The shared library is the only compute path: if it is missing or no CUDA
+device is present, every call raises.  PyTorch supplies device memory and the
+current CUDA stream; the library sees only raw pointers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import torch
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / 'libjaxmd_gb300.so'
+
+MAX_SPECIES = 8
+DENSE, SPARSE, ORDERED_SPARSE = 0, 1, 2
+LJ, LJ_TRUNCATED, SOFT_SPHERE = 0, 1, 2
+
+NEIGHBOR_LIST_OVERFLOW = 1
+CELL_LIST_OVERFLOW = 2
+CELL_SIZE_TOO_SMALL = 4
+MALFORMED_BOX = 8
+
+
+class Space(C.Structure):
+    _fields_ = [('dim', C.c_int32), ('periodic', C.c_int32), ('box', C.c_float * 3)]
+
+
+class NList(C.Structure):
+    _fields_ = [('space', Space), ('cutoff_sq', C.c_float), ('use_cell_list', C.c_int32),
+                ('cells_per_side', C.c_int32 * 3), ('cell_size', C.c_float * 3),
+                ('cell_capacity', C.c_int32), ('format', C.c_int32), ('mask_self', C.c_int32),
+                ('max_occupancy', C.c_int64)]
+
+
+class Pair(C.Structure):
+    _fields_ = [('kind', C.c_int32), ('n_species', C.c_int32), ('per_pair_cutoff', C.c_int32),
+                ('pad_', C.c_int32), ('r_onset', C.c_float), ('r_cutoff', C.c_float),
+                ('sigma', (C.c_float * MAX_SPECIES) * MAX_SPECIES),
+                ('epsilon', (C.c_float * MAX_SPECIES) * MAX_SPECIES),
+                ('alpha', (C.c_float * MAX_SPECIES) * MAX_SPECIES)]
+
+
+class Nhc(C.Structure):
+    _fields_ = [('chain_length', C.c_int32), ('chain_steps', C.c_int32), ('sy_steps', C.c_int32),
+                ('dof', C.c_int32), ('dt', C.c_double), ('tau', C.c_double)]
+
+
+P = C.c_void_p
+I64 = C.c_int64
+I32 = C.c_int32
+F32 = C.c_float
+SZ = C.c_size_t
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    'jmd_last_error': (C.c_char_p, []),
+    'jmd_version': (C.c_int, []),
+    'jmd_cell_workspace_bytes': (SZ, [I64, I64]),
+    'jmd_cell_max_filling': (C.c_int, [P, I64, I64, C.POINTER(NList), P, P, SZ, P]),
+    'jmd_cell_list_build': (C.c_int, [P, I64, I64, C.POINTER(NList), P, P, P, P, P, SZ, P]),
+    'jmd_neighbor_list_workspace_bytes': (SZ, [C.POINTER(NList), I64]),
+    'jmd_neighbor_list_build': (C.c_int, [C.POINTER(NList), P, I64, I64, P, I64, P, P, P, P, I64,
+                                          P, P, SZ, P]),
+    'jmd_skin_check': (C.c_int, [P, I64, P, I64, I64, C.POINTER(Space), F32, P, P]),
+    'jmd_pair_workspace_bytes': (SZ, [I64]),
+    'jmd_set_pair_threads_per_atom': (C.c_int, [C.c_int]),
+    'jmd_pair_forces': (C.c_int, [C.POINTER(Pair), C.POINTER(Space), I32, P, I64, P, I64, P, I64,
+                                  I64, P, P, I64, P, P, P, P, SZ, P]),
+    'jmd_momentum_step': (C.c_int, [P, I64, P, I64, I64, I32, F32, P]),
+    'jmd_position_step': (C.c_int, [P, I64, P, I64, P, F32, I64, C.POINTER(Space), F32, P]),
+    'jmd_verlet_kick_drift': (C.c_int, [P, I64, P, I64, P, I64, P, F32, I64, C.POINTER(Space), F32,
+                                        P, P, I64, F32, P, P]),
+    'jmd_reduce_workspace_bytes': (SZ, [I64]),
+    'jmd_kinetic_energy': (C.c_int, [P, I64, P, F32, I64, I32, P, P, SZ, P]),
+    'jmd_nhc_half_step': (C.c_int, [C.POINTER(Nhc), P, P, I32, P, P]),
+    'jmd_scale_momentum': (C.c_int, [P, I64, I64, I32, P, P]),
+}
+
+_lib = None
+
+
+class NativeError(RuntimeError):
+    pass
+
+
+def lib():
+    """Loads the library (building it first when absent) and binds symbols."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        from . import _build
+        _build.build()
+    L = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def load_without_gpu():
+    """Loads the library for symbol checks on a machine without a GPU."""
+    return lib()
+
+
+def check(rc: int, what: str = ''):
+    if rc != 0:
+        msg = lib().jmd_last_error().decode(errors='replace')
+        raise NativeError(f'{what or "jax_md_gb300"} failed ({rc}): {msg}')
+
+
+def require_cuda(*tensors):
+    if not torch.cuda.is_available():
+        raise NativeError('jax_md_gb300 needs a CUDA device: the GB300 kernels are the only '
+                          'compute path')
+    for t in tensors:
+        if t is not None and isinstance(t, torch.Tensor) and not t.is_cuda:
+            raise NativeError('jax_md_gb300 operates on CUDA tensors; got a tensor on ' + str(t.device))
+
+
+def stream_ptr(device=None) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def ptr(t):
+    return None if t is None else t.data_ptr()
+
+
+def row_stride(t: torch.Tensor) -> int:
+    """Row stride (in elements) of a 2-D tensor whose rows are contiguous."""
+    if t.dim() != 2 or t.stride(1) != 1:
+        raise NativeError('expected a [N, d] tensor with contiguous rows')
+    return t.stride(0)
+
+
+_ws_cache = {}
+
+
+def workspace(nbytes: int, device, key='default') -> torch.Tensor:
+    """A cached uint8 device buffer of at least nbytes (per device and key)."""
+    k = (str(device), key)
+    t = _ws_cache.get(k)
+    if t is None or t.numel() < nbytes:
+        t = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=device)
+        _ws_cache[k] = t
+    return t

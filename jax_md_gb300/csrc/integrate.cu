@@ -1,0 +1,343 @@
+// Integrator kernels: velocity Verlet pieces, kinetic energy, Nose-Hoover chain.
+//
+// Reference: jax_md/simulate.py
+//   momentum_step / position_step  :168-188
+//   velocity_verlet                :227-243
+//   nose_hoover_chain              :384-517  (substep :444-490, half step :492-507)
+// and jax_md/quantity.py:124-159 (kinetic_energy, f64 sum).
+#include "common.cuh"
+
+namespace jmd {
+namespace {
+
+template <int DIM, bool V4P, bool V4F>
+__global__ void k_momentum(float* p, int64_t ps, const float* f, int64_t fs, int n, float dt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 a = load_row_rw<DIM, V4P>(p, ps, i);
+  float4 b = load_row<DIM, V4F>(f, fs, i);
+  a.x = fmaf(dt, b.x, a.x);
+  a.y = fmaf(dt, b.y, a.y);
+  a.z = fmaf(dt, b.z, a.z);
+  store_row<DIM, V4P>(p, ps, i, a);
+}
+
+template <int DIM, bool V4X, bool V4P>
+__global__ void k_position(float* x, int64_t xs, const float* p, int64_t ps, const float* mass,
+                           float m0, int n, Geo g, float dt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 r = load_row_rw<DIM, V4X>(x, xs, i);
+  float4 q = load_row<DIM, V4P>(p, ps, i);
+  float m = mass ? mass[i] : m0;
+  // shift_fn(R, dt * p / m)  (simulate.py:184)
+  float dx = dt * q.x / m, dy = dt * q.y / m, dz = dt * q.z / m;
+  if (g.periodic) {
+    r.x = wrap(r.x + dx, g.L[0]);
+    r.y = wrap(r.y + dy, g.L[1]);
+    if (DIM == 3) r.z = wrap(r.z + dz, g.L[2]);
+  } else {
+    r.x += dx;
+    r.y += dy;
+    r.z += dz;
+  }
+  store_row<DIM, V4X>(x, xs, i, r);
+}
+
+struct KickDriftArgs {
+  float* x;
+  int64_t xs;
+  float* p;
+  int64_t ps;
+  const float* f;
+  int64_t fs;
+  const float* mass;
+  float m0;
+  int n;
+  Geo g;
+  float dt;
+  const double* p_scale;
+  const float* ref;
+  int64_t rs;
+  float thr2;
+  int32_t* flag;
+};
+
+template <int DIM, bool V4>
+__global__ void k_kick_drift(KickDriftArgs a) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool over = false;
+  if (i < a.n) {
+    float4 q = load_row_rw<DIM, V4>(a.p, a.ps, i);
+    float4 f = load_row<DIM, V4>(a.f, a.fs, i);
+    float4 r = load_row_rw<DIM, V4>(a.x, a.xs, i);
+    const float h = 0.5f * a.dt;
+    if (a.p_scale) {
+      float s = (float)(*a.p_scale);
+      q.x *= s;
+      q.y *= s;
+      q.z *= s;
+    }
+    q.x = fmaf(h, f.x, q.x);
+    q.y = fmaf(h, f.y, q.y);
+    q.z = fmaf(h, f.z, q.z);
+    float m = a.mass ? a.mass[i] : a.m0;
+    float dx = a.dt * q.x / m, dy = a.dt * q.y / m, dz = a.dt * q.z / m;
+    if (a.g.periodic) {
+      r.x = wrap(r.x + dx, a.g.L[0]);
+      r.y = wrap(r.y + dy, a.g.L[1]);
+      if (DIM == 3) r.z = wrap(r.z + dz, a.g.L[2]);
+    } else {
+      r.x += dx;
+      r.y += dy;
+      r.z += dz;
+    }
+    store_row<DIM, V4>(a.p, a.ps, i, q);
+    store_row<DIM, V4>(a.x, a.xs, i, r);
+    if (a.ref) {
+      float4 c = load_row<DIM, false>(a.ref, a.rs, i);
+      float ex = a.g.periodic ? min_image(r.x, c.x, a.g.L[0], a.g.halfL[0]) : r.x - c.x;
+      float ey = a.g.periodic ? min_image(r.y, c.y, a.g.L[1], a.g.halfL[1]) : r.y - c.y;
+      float ez = 0.f;
+      if (DIM == 3) ez = a.g.periodic ? min_image(r.z, c.z, a.g.L[2], a.g.halfL[2]) : r.z - c.z;
+      over = ex * ex + ey * ey + ez * ez > a.thr2;
+    }
+  }
+  if (a.flag && __any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(a.flag, 1);
+}
+
+template <int DIM>
+__global__ void k_ke(const float* p, int64_t ps, const float* mass, float m0, int n,
+                     double* partials, unsigned int* counter, double* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[1] = {0.0};
+  if (i < n) {
+    float4 q = load_row<DIM, false>(p, ps, i);
+    float m = mass ? mass[i] : m0;
+    float s = q.x * q.x + q.y * q.y + (DIM == 3 ? q.z * q.z : 0.f);
+    v[0] = 0.5 * (double)s / (double)m;
+  }
+  grid_reduce<1>(v, partials, counter, out, false);
+}
+
+template <int DIM>
+__global__ void k_scale(float* p, int64_t ps, int n, const double* scale) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = (float)(*scale);
+  float* r = p + i * ps;
+  r[0] *= s;
+  r[1] *= s;
+  if (DIM == 3) r[2] *= s;
+}
+
+// ------------------------------------------------------- Nose-Hoover -------
+struct NhcArgs {
+  int M1;  // chain length
+  int chain_steps;
+  int sy_steps;
+  double dof;
+  double dt;
+  double tau;
+  double w[7];
+  int update_mass;
+};
+
+// Chain layout: xi[16] p[16] Q[16] spare[16] KE kT
+__device__ void nhc_substep(double delta, double* xi, double* p, const double* Q, double& KE,
+                            double& scale_total, int M1, double dof, double kT) {
+  const int M = M1 - 1;
+  const double d2 = delta / 2.0, d4 = d2 / 2.0, d8 = d4 / 2.0;
+  double G = p[M - 1] * p[M - 1] / Q[M - 1] - kT;
+  p[M] += d4 * G;
+  double pnew = p[M];
+  for (int m = M - 1; m > 0; --m) {
+    G = p[m - 1] * p[m - 1] / Q[m - 1] - kT;
+    double s = exp(-d8 * pnew / Q[m + 1]);
+    pnew = s * (s * p[m] + d4 * G);
+    p[m] = pnew;
+  }
+  G = 2.0 * KE - dof * kT;
+  double s = exp(-d8 * p[1] / Q[1]);
+  p[0] = s * (s * p[0] + d4 * G);
+  s = exp(-d2 * p[0] / Q[0]);
+  KE = KE * s * s;
+  scale_total *= s;
+  for (int m = 0; m <= M; ++m) xi[m] += d2 * p[m] / Q[m];
+  G = 2.0 * KE - dof * kT;
+  for (int m = 0; m < M; ++m) {
+    double sc = exp(-d8 * p[m + 1] / Q[m + 1]);
+    p[m] = sc * (sc * p[m] + d4 * G);
+    G = p[m] * p[m] / Q[m] - kT;
+  }
+  p[M] += d4 * G;
+}
+
+__global__ void k_nhc_half(NhcArgs a, double* chain, const double* ke_in, double* p_scale) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double* xi = chain;
+  double* p = chain + 16;
+  double* Q = chain + 32;
+  double& KE = chain[64];
+  const double kT = chain[65];
+  if (ke_in) KE = *ke_in;
+  if (a.update_mass) {
+    for (int m = 0; m < a.M1; ++m) Q[m] = kT * a.tau * a.tau;
+    Q[0] *= a.dof;
+  }
+  double scale = 1.0;
+  if (a.chain_steps == 1 && a.sy_steps == 1) {
+    nhc_substep(a.dt, xi, p, Q, KE, scale, a.M1, a.dof, kT);
+  } else {
+    const double delta = a.dt / a.chain_steps;
+    for (int k = 0; k < a.chain_steps * a.sy_steps; ++k)
+      nhc_substep(delta * a.w[k % a.sy_steps], xi, p, Q, KE, scale, a.M1, a.dof, kT);
+  }
+  *p_scale = scale;
+}
+
+struct ReduceWs {
+  double* partials;
+  unsigned int* counter;
+};
+
+constexpr int64_t kMaxReduceBlocks = 1 << 18;
+
+}  // namespace
+}  // namespace jmd
+
+using namespace jmd;
+
+extern "C" {
+
+int jmd_momentum_step(float* momentum, int64_t p_stride, const float* force, int64_t f_stride,
+                      int64_t n, int32_t dim, float dt, void* stream) {
+  JMD_REQUIRE(dim == 2 || dim == 3, "dim must be 2 or 3");
+  if (n <= 0) return JMD_OK;
+  cudaStream_t st = as_stream(stream);
+  unsigned gr = (unsigned)ceil_div(n, 256);
+  const bool v4 = is_vec4(momentum, p_stride) && is_vec4(force, f_stride);
+  if (dim == 3) {
+    if (v4) k_momentum<3, true, true><<<gr, 256, 0, st>>>(momentum, p_stride, force, f_stride, (int)n, dt);
+    else k_momentum<3, false, false><<<gr, 256, 0, st>>>(momentum, p_stride, force, f_stride, (int)n, dt);
+  } else {
+    k_momentum<2, false, false><<<gr, 256, 0, st>>>(momentum, p_stride, force, f_stride, (int)n, dt);
+  }
+  return check_launch("jmd_momentum_step");
+}
+
+int jmd_position_step(float* position, int64_t x_stride, const float* momentum, int64_t p_stride,
+                      const float* mass, float mass_scalar, int64_t n, const jmd_space* space,
+                      float dt, void* stream) {
+  JMD_REQUIRE(space && (space->dim == 2 || space->dim == 3), "bad space");
+  if (n <= 0) return JMD_OK;
+  cudaStream_t st = as_stream(stream);
+  unsigned gr = (unsigned)ceil_div(n, 256);
+  Geo g = make_geo(*space);
+  const bool v4 = is_vec4(position, x_stride) && is_vec4(momentum, p_stride);
+  if (space->dim == 3) {
+    if (v4) k_position<3, true, true><<<gr, 256, 0, st>>>(position, x_stride, momentum, p_stride, mass, mass_scalar, (int)n, g, dt);
+    else k_position<3, false, false><<<gr, 256, 0, st>>>(position, x_stride, momentum, p_stride, mass, mass_scalar, (int)n, g, dt);
+  } else {
+    k_position<2, false, false><<<gr, 256, 0, st>>>(position, x_stride, momentum, p_stride, mass, mass_scalar, (int)n, g, dt);
+  }
+  return check_launch("jmd_position_step");
+}
+
+int jmd_verlet_kick_drift(float* position, int64_t x_stride, float* momentum, int64_t p_stride,
+                          const float* force, int64_t f_stride, const float* mass,
+                          float mass_scalar, int64_t n, const jmd_space* space, float dt,
+                          const double* p_scale, const float* reference_position,
+                          int64_t ref_stride, float threshold_sq, int32_t* rebuild_flag,
+                          void* stream) {
+  JMD_REQUIRE(space && (space->dim == 2 || space->dim == 3), "bad space");
+  JMD_REQUIRE(reference_position == nullptr || rebuild_flag != nullptr,
+              "skin test needs a rebuild flag");
+  if (n <= 0) return JMD_OK;
+  cudaStream_t st = as_stream(stream);
+  KickDriftArgs a{position, x_stride, momentum, p_stride, force, f_stride, mass, mass_scalar,
+                  (int)n, make_geo(*space), dt, p_scale, reference_position, ref_stride,
+                  threshold_sq, rebuild_flag};
+  unsigned gr = (unsigned)ceil_div(n, 256);
+  const bool v4 = is_vec4(position, x_stride) && is_vec4(momentum, p_stride) &&
+                  is_vec4(force, f_stride);
+  if (space->dim == 3) {
+    if (v4) k_kick_drift<3, true><<<gr, 256, 0, st>>>(a);
+    else k_kick_drift<3, false><<<gr, 256, 0, st>>>(a);
+  } else {
+    k_kick_drift<2, false><<<gr, 256, 0, st>>>(a);
+  }
+  return check_launch("jmd_verlet_kick_drift");
+}
+
+size_t jmd_reduce_workspace_bytes(int64_t n) {
+  (void)n;
+  Carver cv(nullptr, 0);
+  cv.take<double>(kMaxReduceBlocks);
+  cv.take<unsigned int>(1);
+  return cv.used + 256;
+}
+
+int jmd_kinetic_energy(const float* momentum, int64_t p_stride, const float* mass,
+                       float mass_scalar, int64_t n, int32_t dim, double* out, void* workspace,
+                       size_t workspace_bytes, void* stream) {
+  JMD_REQUIRE(dim == 2 || dim == 3, "dim must be 2 or 3");
+  JMD_REQUIRE(out != nullptr, "out is null");
+  cudaStream_t st = as_stream(stream);
+  Carver cv(workspace, workspace_bytes);
+  ReduceWs w;
+  w.partials = cv.take<double>(kMaxReduceBlocks);
+  w.counter = cv.take<unsigned int>(1);
+  if (!cv.ok()) return fail(JMD_ERR_WORKSPACE, "reduce workspace too small");
+  if (n <= 0) {
+    JMD_CUDA(cudaMemsetAsync(out, 0, sizeof(double), st));
+    return JMD_OK;
+  }
+  int64_t gr = ceil_div(n, 256);
+  if (gr > kMaxReduceBlocks) return fail(JMD_ERR_UNSUPPORTED, "system too large");
+  if (dim == 3) k_ke<3><<<(unsigned)gr, 256, 0, st>>>(momentum, p_stride, mass, mass_scalar, (int)n, w.partials, w.counter, out);
+  else k_ke<2><<<(unsigned)gr, 256, 0, st>>>(momentum, p_stride, mass, mass_scalar, (int)n, w.partials, w.counter, out);
+  return check_launch("jmd_kinetic_energy");
+}
+
+int jmd_nhc_half_step(const jmd_nhc* c, double* chain, const double* kinetic_energy,
+                      int32_t update_mass, double* p_scale, void* stream) {
+  JMD_REQUIRE(c != nullptr && chain != nullptr && p_scale != nullptr, "null argument");
+  JMD_REQUIRE(c->chain_length >= 2 && c->chain_length <= 16, "chain_length must be in [2, 16]");
+  JMD_REQUIRE(c->chain_steps >= 1, "chain_steps must be >= 1");
+  JMD_REQUIRE(c->sy_steps == 1 || c->sy_steps == 3 || c->sy_steps == 5 || c->sy_steps == 7,
+              "sy_steps must be 1, 3, 5 or 7");
+  // Suzuki-Yoshida weights (Yoshida 1990): the values simulate.py:328-347 uses.
+  static const double w3[3] = {0.828981543588751, -0.657963087177502, 0.828981543588751};
+  static const double w5[5] = {0.2967324292201065, 0.2967324292201065, -0.186929716880426,
+                               0.2967324292201065, 0.2967324292201065};
+  static const double w7[7] = {0.784513610477560, 0.235573213359357, -1.17767998417887,
+                               1.31518632068391, -1.17767998417887, 0.235573213359357,
+                               0.784513610477560};
+  NhcArgs a;
+  a.M1 = c->chain_length;
+  a.chain_steps = c->chain_steps;
+  a.sy_steps = c->sy_steps;
+  a.dof = (double)c->dof;
+  a.dt = c->dt;
+  a.tau = c->tau;
+  a.update_mass = update_mass;
+  for (int k = 0; k < 7; ++k) a.w[k] = 0.0;
+  const double* src = c->sy_steps == 3 ? w3 : c->sy_steps == 5 ? w5 : c->sy_steps == 7 ? w7 : nullptr;
+  if (src) for (int k = 0; k < c->sy_steps; ++k) a.w[k] = src[k];
+  else a.w[0] = 1.0;
+  k_nhc_half<<<1, 32, 0, as_stream(stream)>>>(a, chain, kinetic_energy, p_scale);
+  return check_launch("jmd_nhc_half_step");
+}
+
+int jmd_scale_momentum(float* momentum, int64_t p_stride, int64_t n, int32_t dim,
+                       const double* scale, void* stream) {
+  JMD_REQUIRE(dim == 2 || dim == 3, "dim must be 2 or 3");
+  if (n <= 0) return JMD_OK;
+  unsigned gr = (unsigned)ceil_div(n, 256);
+  if (dim == 3) k_scale<3><<<gr, 256, 0, as_stream(stream)>>>(momentum, p_stride, (int)n, scale);
+  else k_scale<2><<<gr, 256, 0, as_stream(stream)>>>(momentum, p_stride, (int)n, scale);
+  return check_launch("jmd_scale_momentum");
+}
+
+}  // extern "C"

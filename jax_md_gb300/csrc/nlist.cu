@@ -1,0 +1,742 @@
+// Cell binning (counting sort) and neighbour-list construction.
+//
+// Reference: jax_md/partition.py
+//   cell hashing            :212-224, 421-423
+//   cell slot rule          :438-447  slot = hash*cap + (sorted_rank mod cap)
+//   candidate order         :911-951  3^d shifted cells (first axis slowest),
+//                                     slots 0..cap-1 within each cell
+//   self mask / prune       :953-1032 strict d^2 < cutoff^2, stable compaction
+//   capacity / overflow     :1090-1117
+//   skin test               :1146-1154
+//
+// GB300 design.  Binning is a counting sort: a histogram (atomics), one
+// exclusive scan, a scatter, and a per-cell rank pass that restores the
+// stable (ascending id) order of the reference's argsort; atoms end up
+// reordered by cell in `sorted_pos` (float4) so that the neighbour search
+// reads every candidate cell as one contiguous, coalesced range.  The search
+// runs one warp per atom, visits candidates in the reference's order
+// (including the slot rotation that the reference's `rank mod cap` slot rule
+// implies), and compacts hits with a warp ballot straight into the atom's
+// row, so the Dense list is bit-identical to the reference's, order included.
+#include "common.cuh"
+
+namespace jmd {
+namespace {
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;  // per thread per tile
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+// Internal scalars kept in the workspace.
+struct Scalars {
+  unsigned int max_fill;
+  unsigned int flags;
+  unsigned long long occupancy;  // Dense: max row count; Sparse: total
+  unsigned int sparse_total_hi;  // unused padding
+  unsigned int counter;
+};
+
+struct Bins {
+  int32_t* cell_of;    // [N]
+  int32_t* count;      // [C]
+  int32_t* start;      // [C+1]
+  int32_t* cursor;     // [C]
+  int32_t* tmp_id;     // [N]
+  int32_t* sorted_id;  // [N]
+  float4* sorted_pos;  // [N]
+  int32_t* blocksum;   // [ceil(C/tile)] (also used for atom scans)
+  int32_t* atom_off;   // [N+1] sparse row offsets
+  Scalars* sc;
+};
+
+struct Grid {
+  int dim;
+  int cps[3];
+  float cs[3];
+  int mult[3];
+  int64_t count;
+};
+
+inline Grid make_grid(const jmd_nlist& nl) {
+  Grid g;
+  g.dim = nl.space.dim;
+  g.count = 1;
+  for (int d = 0; d < 3; ++d) {
+    g.cps[d] = d < g.dim ? nl.cells_per_side[d] : 1;
+    g.cs[d] = d < g.dim ? nl.cell_size[d] : 1.f;
+  }
+  g.mult[0] = 1;
+  g.mult[1] = g.cps[0];
+  g.mult[2] = g.cps[0] * g.cps[1];
+  for (int d = 0; d < g.dim; ++d) g.count *= g.cps[d];
+  return g;
+}
+
+int64_t grid_count(const jmd_nlist& nl) {
+  if (!nl.use_cell_list) return 1;
+  return make_grid(nl).count;
+}
+
+size_t bins_bytes(int64_t n, int64_t c) {
+  Carver cv(nullptr, 0);
+  cv.take<int32_t>(n);
+  cv.take<int32_t>(c);
+  cv.take<int32_t>(c + 1);
+  cv.take<int32_t>(c);
+  cv.take<int32_t>(n);
+  cv.take<int32_t>(n);
+  cv.take<float4>(n);
+  cv.take<int32_t>(ceil_div(std::max(c, n + 1), kScanTile) + 1);
+  cv.take<int32_t>(n + 1);
+  cv.take<Scalars>(1);
+  return cv.used + 256;
+}
+
+Bins carve_bins(void* ws, size_t bytes, int64_t n, int64_t c, bool* ok) {
+  Carver cv(ws, bytes);
+  Bins b;
+  b.cell_of = cv.take<int32_t>(n);
+  b.count = cv.take<int32_t>(c);
+  b.start = cv.take<int32_t>(c + 1);
+  b.cursor = cv.take<int32_t>(c);
+  b.tmp_id = cv.take<int32_t>(n);
+  b.sorted_id = cv.take<int32_t>(n);
+  b.sorted_pos = cv.take<float4>(n);
+  b.blocksum = cv.take<int32_t>(ceil_div(std::max(c, n + 1), kScanTile) + 1);
+  b.atom_off = cv.take<int32_t>(n + 1);
+  b.sc = cv.take<Scalars>(1);
+  *ok = cv.ok();
+  return b;
+}
+
+__device__ __forceinline__ bool skip(const int32_t* flag) { return flag != nullptr && *flag == 0; }
+
+// int(x / cell_size) mod cells_per_side, float32 division as the reference.
+__device__ __forceinline__ int cell_coord(float x, float cs, int cps) {
+  int q = __float2int_rz(__fdiv_rn(x, cs));
+  int m = q % cps;
+  return m < 0 ? m + cps : m;
+}
+
+template <int DIM>
+__device__ __forceinline__ int cell_hash(float4 x, const Grid& g, int* c3) {
+  c3[0] = cell_coord(x.x, g.cs[0], g.cps[0]);
+  c3[1] = cell_coord(x.y, g.cs[1], g.cps[1]);
+  c3[2] = DIM == 3 ? cell_coord(x.z, g.cs[2], g.cps[2]) : 0;
+  return c3[0] + c3[1] * g.mult[1] + (DIM == 3 ? c3[2] * g.mult[2] : 0);
+}
+
+// ----------------------------------------------------------- binning -------
+__global__ void k_zero(int32_t* count, int64_t c, Scalars* sc, const int32_t* flag) {
+  if (skip(flag)) return;
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (int64_t k = t; k < c; k += (int64_t)gridDim.x * blockDim.x) count[k] = 0;
+  if (t == 0) {
+    sc->max_fill = 0;
+    sc->flags = 0;
+    sc->occupancy = 0;
+    sc->counter = 0;
+  }
+}
+
+template <int DIM, bool VEC4>
+__global__ void k_bin(const float* __restrict__ x, int64_t stride, int n, Grid g, Bins b,
+                      int32_t* particle_cell_id, const int32_t* flag) {
+  if (skip(flag)) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 r = load_row<DIM, VEC4>(x, stride, i);
+  int c3[3];
+  int h = cell_hash<DIM>(r, g, c3);
+  b.cell_of[i] = h;
+  atomicAdd(b.count + h, 1);
+  if (particle_cell_id) {
+    for (int d = 0; d < DIM; ++d) particle_cell_id[(int64_t)i * DIM + d] = c3[d];
+  }
+}
+
+// Exclusive scan of `in[0..len)` into out[0..len] (out[len] = total), also
+// copying the result into `copy` (cursor) when given and taking the max of
+// the inputs into *max_out.  One block walks the array tile by tile.
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_single(const int32_t* __restrict__ in, int64_t len, int32_t* out, int32_t* copy,
+              unsigned int* max_out, const int32_t* flag) {
+  if (skip(flag)) return;
+  __shared__ int32_t warp_tot[32];
+  __shared__ int32_t carry_s;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  int32_t carry = 0;
+  int32_t vmax = 0;
+  for (int64_t base = 0; base < len; base += kScanTile) {
+    int32_t v[kScanItems];
+    int32_t tsum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      int64_t idx = base + (int64_t)t * kScanItems + k;
+      v[k] = idx < len ? in[idx] : 0;
+      vmax = max(vmax, v[k]);
+      tsum += v[k];
+    }
+    // inclusive warp scan of thread sums
+    int32_t incl = tsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      int32_t w = warp_tot[lane];
+      int32_t wi = w;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+        if (lane >= o) wi += y;
+      }
+      warp_tot[lane] = wi - w;  // exclusive warp offsets
+      if (lane == 31) carry_s = wi;
+    }
+    __syncthreads();
+    int32_t run = carry + warp_tot[warp] + incl - tsum;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      int64_t idx = base + (int64_t)t * kScanItems + k;
+      if (idx < len) {
+        out[idx] = run;
+        if (copy) copy[idx] = run;
+      }
+      run += v[k];
+    }
+    carry += carry_s;
+    __syncthreads();
+  }
+  if (t == 0) out[len] = carry;
+  // block max
+  for (int o = 16; o > 0; o >>= 1) vmax = max(vmax, __shfl_down_sync(0xffffffffu, vmax, o));
+  if (lane == 0 && max_out) atomicMax(max_out, (unsigned int)vmax);
+}
+
+__global__ void k_scatter(int n, Bins b, const int32_t* flag) {
+  if (skip(flag)) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int pos = atomicAdd(b.cursor + b.cell_of[i], 1);
+  b.tmp_id[pos] = i;
+}
+
+// One warp per cell: rank every member by id (stable argsort order of the
+// reference) and write the cell-sorted id and position arrays.
+template <int DIM, bool VEC4>
+__global__ void k_cell_rank(const float* __restrict__ x, int64_t stride, int64_t ncell, Bins b,
+                            const int32_t* flag) {
+  if (skip(flag)) return;
+  int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (c >= ncell) return;
+  int beg = b.start[c], end = b.start[c + 1];
+  int k = end - beg;
+  for (int base = 0; base < k; base += 32) {
+    const int a = base + lane;
+    int mine = a < k ? b.tmp_id[beg + a] : INT32_MAX;
+    int rank = 0;
+    for (int q = 0; q < k; q += 32) {
+      int other = (q + lane) < k ? b.tmp_id[beg + q + lane] : INT32_MAX;
+#pragma unroll 8
+      for (int s = 0; s < 32; ++s) {
+        int o = __shfl_sync(0xffffffffu, other, s);
+        rank += (o < mine);
+      }
+    }
+    if (a < k) {
+      b.sorted_id[beg + rank] = mine;
+      float4 r = load_row<DIM, VEC4>(x, stride, mine);
+      r.w = 0.f;
+      b.sorted_pos[beg + rank] = r;
+    }
+  }
+}
+
+// Reference layout of the cell list (partition.py:425-452).
+template <int DIM>
+__global__ void k_fill_cell_buffers(int64_t ncell, int cap, int n, int32_t* id_buffer,
+                                    float* position_buffer) {
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t total = ncell * cap;
+  for (int64_t s = t; s < total; s += (int64_t)gridDim.x * blockDim.x) {
+    id_buffer[s] = n;
+    if (position_buffer)
+      for (int d = 0; d < DIM; ++d) position_buffer[s * DIM + d] = 0.f;
+  }
+}
+
+template <int DIM>
+__global__ void k_emplace(int n, int cap, Grid g, Bins b, int32_t* id_buffer,
+                          float* position_buffer) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  int i = b.sorted_id[s];
+  int h = b.cell_of[i];
+  int64_t slot = (int64_t)h * cap + (s % cap);
+  id_buffer[slot] = i;
+  if (position_buffer) {
+    float4 r = b.sorted_pos[s];
+    position_buffer[slot * DIM + 0] = r.x;
+    position_buffer[slot * DIM + 1] = r.y;
+    if (DIM == 3) position_buffer[slot * DIM + 2] = r.z;
+  }
+}
+
+// ---------------------------------------------------- neighbour search -----
+struct SearchArgs {
+  Geo geo;
+  Grid grid;
+  float cut2;
+  int mask_self;
+  int ordered;   // OrderedSparse: keep j < i
+  int cap;       // cell capacity (slot rotation)
+  int n;
+  int64_t width; // Dense row width (max_occupancy)
+};
+
+template <int DIM>
+__device__ __forceinline__ float dist2(const float4& a, const float4& b, const Geo& g) {
+  float dx, dy, dz = 0.f;
+  if (g.periodic) {
+    dx = min_image(a.x, b.x, g.L[0], g.halfL[0]);
+    dy = min_image(a.y, b.y, g.L[1], g.halfL[1]);
+    if (DIM == 3) dz = min_image(a.z, b.z, g.L[2], g.halfL[2]);
+  } else {
+    dx = a.x - b.x;
+    dy = a.y - b.y;
+    if (DIM == 3) dz = a.z - b.z;
+  }
+  float d2 = dx * dx;
+  d2 = fmaf(dy, dy, d2);
+  if (DIM == 3) d2 = fmaf(dz, dz, d2);
+  return d2;
+}
+
+// Visits candidates sid/spos[beg, end) in order; appends hits to `row`
+// (entries at positions >= row_cap are dropped but still counted).
+// Sparse rows also write the sender id into `row2`.
+template <int DIM>
+__device__ __forceinline__ void visit(int beg, int end, const int32_t* __restrict__ sid,
+                                      const float4* __restrict__ spos, float4 xi, int i,
+                                      const SearchArgs& a, int lane, int& count, int32_t* row,
+                                      int32_t* row2, int64_t row_cap) {
+  const unsigned lt = (1u << lane) - 1u;
+  for (int base = beg; base < end; base += 32) {
+    int s = base + lane;
+    bool ok = false;
+    int j = 0;
+    if (s < end) {
+      j = sid ? __ldg(sid + s) : s;
+      float4 xj = __ldg(spos + s);
+      float d2 = dist2<DIM>(xi, xj, a.geo);
+      ok = d2 < a.cut2;
+      if (a.mask_self) ok = ok && (j != i);
+      if (a.ordered) ok = ok && (j < i);
+    }
+    unsigned m = __ballot_sync(0xffffffffu, ok);
+    if (ok && row) {
+      int64_t p = (int64_t)count + __popc(m & lt);
+      if (p < row_cap) {
+        row[p] = j;
+        if (row2) row2[p] = i;
+      }
+    }
+    count += __popc(m);
+  }
+}
+
+// All candidates of atom i in the reference's order.  Cell-list path: 3^d
+// shifted cells, first axis slowest (partition.py:232-240), each cell's
+// members in slot order 0..cap-1; the slot of member r of a cell starting at
+// sorted position b is (b + r) mod cap, i.e. the members with r >= cap - o
+// (o = b mod cap) come first.
+template <int DIM, bool CELLS>
+__device__ __forceinline__ void search(const Bins& b, const float4* __restrict__ allpos,
+                                       float4 xi, int i, const SearchArgs& a, int lane,
+                                       int& count, int32_t* row, int32_t* row2, int64_t row_cap) {
+  if (!CELLS) {
+    visit<DIM>(0, a.n, nullptr, allpos, xi, i, a, lane, count, row, row2, row_cap);
+    return;
+  }
+  int c3[3];
+  cell_hash<DIM>(xi, a.grid, c3);
+  const int ns = DIM == 3 ? 27 : 9;
+  for (int k = 0; k < ns; ++k) {
+    int sh0, sh1, sh2;
+    if (DIM == 3) {
+      sh0 = k / 9 - 1;
+      sh1 = (k / 3) % 3 - 1;
+      sh2 = k % 3 - 1;
+    } else {
+      sh0 = k / 3 - 1;
+      sh1 = k % 3 - 1;
+      sh2 = 0;
+    }
+    int q0 = c3[0] + sh0, q1 = c3[1] + sh1, q2 = c3[2] + sh2;
+    q0 = q0 < 0 ? q0 + a.grid.cps[0] : (q0 >= a.grid.cps[0] ? q0 - a.grid.cps[0] : q0);
+    q1 = q1 < 0 ? q1 + a.grid.cps[1] : (q1 >= a.grid.cps[1] ? q1 - a.grid.cps[1] : q1);
+    if (DIM == 3)
+      q2 = q2 < 0 ? q2 + a.grid.cps[2] : (q2 >= a.grid.cps[2] ? q2 - a.grid.cps[2] : q2);
+    int h = q0 + q1 * a.grid.mult[1] + (DIM == 3 ? q2 * a.grid.mult[2] : 0);
+    int beg = __ldg(b.start + h), end = __ldg(b.start + h + 1);
+    int kk = end - beg;
+    int split = a.cap - (beg % a.cap);
+    if (kk <= split) {
+      visit<DIM>(beg, end, b.sorted_id, b.sorted_pos, xi, i, a, lane, count, row, row2, row_cap);
+    } else {
+      visit<DIM>(beg + split, end, b.sorted_id, b.sorted_pos, xi, i, a, lane, count, row, row2,
+                 row_cap);
+      visit<DIM>(beg, beg + split, b.sorted_id, b.sorted_pos, xi, i, a, lane, count, row, row2,
+                 row_cap);
+    }
+  }
+}
+
+// Mode: 0 = Dense write, 1 = count only (per atom into atom_off), 2 = Sparse write.
+template <int DIM, bool CELLS, bool VEC4, int MODE>
+__global__ void __launch_bounds__(256)
+k_search(const float* __restrict__ x, int64_t stride, Bins b, SearchArgs a, int32_t* idx,
+         int64_t ld, int32_t* nbr_count, float* ref, int64_t ref_stride, const int32_t* flag,
+         const float4* __restrict__ allpos) {
+  if (skip(flag)) return;
+  int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (w >= a.n) return;
+  int i;
+  float4 xi;
+  if (CELLS) {
+    i = b.sorted_id[w];
+    xi = b.sorted_pos[w];
+  } else {
+    i = (int)w;
+    xi = allpos[w];
+  }
+  int count = 0;
+  int32_t* row = nullptr;
+  int32_t* row2 = nullptr;
+  int64_t row_cap = 0;
+  if (MODE == 0 && idx) {
+    row = idx + (int64_t)i * ld;
+    row_cap = a.width;
+  } else if (MODE == 2) {
+    int64_t off = b.atom_off[i];
+    row = idx + off;
+    row2 = idx + ld + off;
+    row_cap = a.width - off;  // entries past the capacity are dropped
+  }
+  search<DIM, CELLS>(b, allpos, xi, i, a, lane, count, row, row2, row_cap);
+  if (MODE == 0) {
+    if (row) {
+      for (int64_t p = min((int64_t)count, a.width) + lane; p < a.width; p += 32) row[p] = a.n;
+    }
+    if (lane == 0) {
+      if (nbr_count) nbr_count[i] = count;
+      atomicMax(&b.sc->occupancy, (unsigned long long)count);
+      if (count > a.width) atomicOr(&b.sc->flags, (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
+    }
+  } else if (MODE == 1) {
+    if (lane == 0) b.atom_off[i] = count;
+  }
+  if (ref && lane == 0) {
+    float4 r = load_row<DIM, VEC4>(x, stride, i);
+    store_row_full<DIM, false>(ref, ref_stride, i, r);
+  }
+}
+
+// Copies the raw positions as float4 rows for the all-pairs path.
+template <int DIM, bool VEC4>
+__global__ void k_pack(const float* __restrict__ x, int64_t stride, int n, float4* out,
+                       const int32_t* flag) {
+  if (skip(flag)) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 r = load_row<DIM, VEC4>(x, stride, i);
+  r.w = 0.f;
+  out[i] = r;
+}
+
+__global__ void k_sparse_pad(int32_t* idx, int64_t ld, int64_t width, const int32_t* total_ptr,
+                             int n, const int32_t* flag) {
+  if (skip(flag)) return;
+  int64_t total = *total_ptr;
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (int64_t p = min(total, width) + t; p < width; p += (int64_t)gridDim.x * blockDim.x) {
+    idx[p] = n;
+    idx[ld + p] = n;
+  }
+}
+
+// Host-side constants carried into the finalize kernel.
+struct FinalizeArgs {
+  int format;
+  int64_t width;
+  int use_cells;
+  int cap;
+  int n;
+};
+
+__global__ void k_finalize(Bins b, FinalizeArgs f, int64_t* occupancy, uint8_t* error_code,
+                           int32_t* flag) {
+  if (skip(flag)) return;
+  unsigned flags = b.sc->flags;
+  if (f.use_cells && (int)b.sc->max_fill > f.cap) flags |= JMD_CELL_LIST_OVERFLOW;
+  unsigned long long occ = b.sc->occupancy;
+  if (f.format != JMD_DENSE) {
+    occ = (unsigned long long)b.atom_off[f.n];  // total written by the atom scan
+    if ((int64_t)occ > f.width) flags |= JMD_NEIGHBOR_LIST_OVERFLOW;
+  }
+  if (occupancy) *occupancy = (int64_t)occ;
+  if (error_code) *error_code = (uint8_t)(*error_code | flags);
+  if (flag) *flag = 0;
+}
+
+template <int DIM>
+__global__ void k_skin(const float* __restrict__ x, int64_t xs, const float* __restrict__ ref,
+                       int64_t rs, int n, Geo g, float thr2, int32_t* flag) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool over = false;
+  if (i < n) {
+    float4 a = load_row<DIM, false>(x, xs, i);
+    float4 c = load_row<DIM, false>(ref, rs, i);
+    over = dist2<DIM>(a, c, g) > thr2;
+  }
+  if (__any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+// ------------------------------------------------------------ host side ----
+int validate(const jmd_nlist* nl, int64_t n) {
+  JMD_REQUIRE(nl != nullptr, "nlist descriptor is null");
+  JMD_REQUIRE(nl->space.dim == 2 || nl->space.dim == 3, "dim must be 2 or 3");
+  JMD_REQUIRE(n >= 0 && n < (int64_t)INT32_MAX, "atom count out of range");
+  JMD_REQUIRE(nl->format >= 0 && nl->format <= 2, "unknown neighbour list format");
+  if (nl->use_cell_list) {
+    for (int d = 0; d < nl->space.dim; ++d) {
+      JMD_REQUIRE(nl->cells_per_side[d] >= 3, "cell list needs >= 3 cells per side");
+      JMD_REQUIRE(nl->cell_size[d] > 0.f, "cell size must be positive");
+    }
+    JMD_REQUIRE(nl->cell_capacity >= 1, "cell capacity must be >= 1");
+  }
+  return JMD_OK;
+}
+
+// Runs the binning stage (zero, histogram, scan, scatter, rank).
+template <int DIM, bool VEC4>
+void run_binning(const float* x, int64_t stride, int n, const Grid& g, const Bins& b,
+                 int32_t* particle_cell_id, const int32_t* flag, cudaStream_t st) {
+  int64_t c = g.count;
+  k_zero<<<(unsigned)std::min<int64_t>(ceil_div(c, 256), 1024), 256, 0, st>>>(b.count, c, b.sc,
+                                                                             flag);
+  if (n > 0) k_bin<DIM, VEC4><<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(x, stride, n, g, b,
+                                                                          particle_cell_id, flag);
+  k_scan_single<<<1, kScanThreads, 0, st>>>(b.count, c, b.start, b.cursor, &b.sc->max_fill, flag);
+  if (n > 0) {
+    k_scatter<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(n, b, flag);
+    k_cell_rank<DIM, VEC4><<<(unsigned)ceil_div(c * 32, 256), 256, 0, st>>>(x, stride, c, b, flag);
+  }
+}
+
+template <int DIM, bool VEC4>
+int build_impl(const jmd_nlist* nl, const float* x, int64_t stride, int64_t n64, int32_t* idx,
+               int64_t ld, int32_t* nbr_count, int64_t* occupancy, uint8_t* error_code,
+               float* ref, int64_t ref_stride, int32_t* flag, void* ws, size_t ws_bytes,
+               cudaStream_t st) {
+  const int n = (int)n64;
+  const bool cells = nl->use_cell_list != 0;
+  Grid g = cells ? make_grid(*nl) : Grid{};
+  int64_t c = cells ? g.count : 1;
+  bool ok;
+  Bins b = carve_bins(ws, ws_bytes, n, c, &ok);
+  if (!ok) return fail(JMD_ERR_WORKSPACE, "neighbour-list workspace too small");
+  SearchArgs a;
+  a.geo = make_geo(nl->space);
+  a.grid = g;
+  a.cut2 = nl->cutoff_sq;
+  a.mask_self = nl->mask_self;
+  a.ordered = nl->format == JMD_ORDERED_SPARSE;
+  a.cap = cells ? nl->cell_capacity : 1;
+  a.n = n;
+  a.width = nl->max_occupancy;
+  if (cells) {
+    run_binning<DIM, VEC4>(x, stride, n, g, b, nullptr, flag, st);
+  } else {
+    k_zero<<<1, 256, 0, st>>>(b.count, 1, b.sc, flag);
+    if (n > 0) k_pack<DIM, VEC4><<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(x, stride, n,
+                                                                             b.sorted_pos, flag);
+  }
+  const float4* allpos = b.sorted_pos;
+  const unsigned sgrid = (unsigned)std::max<int64_t>(1, ceil_div((int64_t)n * 32, 256));
+  FinalizeArgs f{nl->format, nl->max_occupancy, cells ? 1 : 0, a.cap, n};
+  if (nl->format == JMD_DENSE) {
+    if (n > 0) {
+      if (cells)
+        k_search<DIM, true, VEC4, 0><<<sgrid, 256, 0, st>>>(x, stride, b, a, idx, ld, nbr_count,
+                                                            ref, ref_stride, flag, allpos);
+      else
+        k_search<DIM, false, VEC4, 0><<<sgrid, 256, 0, st>>>(x, stride, b, a, idx, ld, nbr_count,
+                                                             ref, ref_stride, flag, allpos);
+    }
+  } else {
+    // count pass -> exclusive scan over atoms -> write pass -> pad
+    if (n > 0) {
+      if (cells)
+        k_search<DIM, true, VEC4, 1><<<sgrid, 256, 0, st>>>(x, stride, b, a, nullptr, ld, nullptr,
+                                                            nullptr, 0, flag, allpos);
+      else
+        k_search<DIM, false, VEC4, 1><<<sgrid, 256, 0, st>>>(x, stride, b, a, nullptr, ld,
+                                                             nullptr, nullptr, 0, flag, allpos);
+    }
+    // scan atom counts in place: atom_off[0..n) -> offsets, atom_off[n] = total
+    k_scan_single<<<1, kScanThreads, 0, st>>>(b.atom_off, n, b.atom_off, nullptr, nullptr, flag);
+    if (idx && n > 0) {
+      if (cells)
+        k_search<DIM, true, VEC4, 2><<<sgrid, 256, 0, st>>>(x, stride, b, a, idx, ld, nullptr, ref,
+                                                            ref_stride, flag, allpos);
+      else
+        k_search<DIM, false, VEC4, 2><<<sgrid, 256, 0, st>>>(x, stride, b, a, idx, ld, nullptr,
+                                                             ref, ref_stride, flag, allpos);
+    }
+    if (idx && nl->max_occupancy > 0)
+      k_sparse_pad<<<(unsigned)std::min<int64_t>(ceil_div(nl->max_occupancy, 256), 4096), 256, 0,
+                     st>>>(idx, ld, nl->max_occupancy, b.atom_off + n, n, flag);
+  }
+  k_finalize<<<1, 1, 0, st>>>(b, f, occupancy, error_code, flag);
+  return check_launch("jmd_neighbor_list_build");
+}
+
+}  // namespace
+}  // namespace jmd
+
+using namespace jmd;
+
+extern "C" {
+
+size_t jmd_cell_workspace_bytes(int64_t n_atoms, int64_t cell_count) {
+  return bins_bytes(n_atoms, cell_count);
+}
+
+size_t jmd_neighbor_list_workspace_bytes(const jmd_nlist* nl, int64_t n) {
+  if (!nl) return 0;
+  return bins_bytes(n, grid_count(*nl));
+}
+
+int jmd_cell_max_filling(const float* position, int64_t pos_stride, int64_t n,
+                         const jmd_nlist* nl, int32_t* max_filling, void* workspace,
+                         size_t workspace_bytes, void* stream) {
+  int e = validate(nl, n);
+  if (e) return e;
+  JMD_REQUIRE(nl->use_cell_list, "cell grid required");
+  JMD_REQUIRE(max_filling != nullptr, "max_filling is null");
+  cudaStream_t st = as_stream(stream);
+  Grid g = make_grid(*nl);
+  bool ok;
+  Bins b = carve_bins(workspace, workspace_bytes, n, g.count, &ok);
+  if (!ok) return fail(JMD_ERR_WORKSPACE, "cell workspace too small");
+  const int dim = nl->space.dim;
+  const bool v4 = is_vec4(position, pos_stride);
+  k_zero<<<(unsigned)std::min<int64_t>(ceil_div(g.count, 256), 1024), 256, 0, st>>>(
+      b.count, g.count, b.sc, nullptr);
+  if (n > 0) {
+    unsigned gr = (unsigned)ceil_div(n, 256);
+    if (dim == 3 && v4) k_bin<3, true><<<gr, 256, 0, st>>>(position, pos_stride, (int)n, g, b, nullptr, nullptr);
+    else if (dim == 3) k_bin<3, false><<<gr, 256, 0, st>>>(position, pos_stride, (int)n, g, b, nullptr, nullptr);
+    else if (v4) k_bin<2, true><<<gr, 256, 0, st>>>(position, pos_stride, (int)n, g, b, nullptr, nullptr);
+    else k_bin<2, false><<<gr, 256, 0, st>>>(position, pos_stride, (int)n, g, b, nullptr, nullptr);
+  }
+  k_scan_single<<<1, kScanThreads, 0, st>>>(b.count, g.count, b.start, nullptr, &b.sc->max_fill,
+                                            nullptr);
+  JMD_CUDA(cudaMemcpyAsync(max_filling, &b.sc->max_fill, sizeof(int32_t),
+                           cudaMemcpyDeviceToDevice, st));
+  return check_launch("jmd_cell_max_filling");
+}
+
+int jmd_cell_list_build(const float* position, int64_t pos_stride, int64_t n, const jmd_nlist* nl,
+                        int32_t* id_buffer, float* position_buffer, int32_t* particle_cell_id,
+                        uint8_t* error_code, void* workspace, size_t workspace_bytes,
+                        void* stream) {
+  int e = validate(nl, n);
+  if (e) return e;
+  JMD_REQUIRE(nl->use_cell_list, "cell grid required");
+  JMD_REQUIRE(id_buffer != nullptr, "id_buffer is null");
+  cudaStream_t st = as_stream(stream);
+  Grid g = make_grid(*nl);
+  bool ok;
+  Bins b = carve_bins(workspace, workspace_bytes, n, g.count, &ok);
+  if (!ok) return fail(JMD_ERR_WORKSPACE, "cell workspace too small");
+  const int dim = nl->space.dim;
+  const bool v4 = is_vec4(position, pos_stride);
+  const int cap = nl->cell_capacity;
+  if (dim == 3 && v4) run_binning<3, true>(position, pos_stride, (int)n, g, b, particle_cell_id, nullptr, st);
+  else if (dim == 3) run_binning<3, false>(position, pos_stride, (int)n, g, b, particle_cell_id, nullptr, st);
+  else if (v4) run_binning<2, true>(position, pos_stride, (int)n, g, b, particle_cell_id, nullptr, st);
+  else run_binning<2, false>(position, pos_stride, (int)n, g, b, particle_cell_id, nullptr, st);
+  int64_t total = g.count * cap;
+  unsigned fg = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(total, 256), 8192));
+  if (dim == 3) k_fill_cell_buffers<3><<<fg, 256, 0, st>>>(g.count, cap, (int)n, id_buffer, position_buffer);
+  else k_fill_cell_buffers<2><<<fg, 256, 0, st>>>(g.count, cap, (int)n, id_buffer, position_buffer);
+  if (n > 0) {
+    unsigned gr = (unsigned)ceil_div(n, 256);
+    if (dim == 3) k_emplace<3><<<gr, 256, 0, st>>>((int)n, cap, g, b, id_buffer, position_buffer);
+    else k_emplace<2><<<gr, 256, 0, st>>>((int)n, cap, g, b, id_buffer, position_buffer);
+  }
+  FinalizeArgs f{JMD_DENSE, INT64_MAX, 1, cap, (int)n};
+  k_finalize<<<1, 1, 0, st>>>(b, f, nullptr, error_code, nullptr);
+  return check_launch("jmd_cell_list_build");
+}
+
+int jmd_neighbor_list_build(const jmd_nlist* nl, const float* position, int64_t pos_stride,
+                            int64_t n, int32_t* idx, int64_t idx_ld, int32_t* nbr_count,
+                            int64_t* occupancy, uint8_t* error_code, float* reference_position,
+                            int64_t ref_stride, int32_t* rebuild_flag, void* workspace,
+                            size_t workspace_bytes, void* stream) {
+  int e = validate(nl, n);
+  if (e) return e;
+  JMD_REQUIRE(position != nullptr || n == 0, "position is null");
+  JMD_REQUIRE(nl->max_occupancy >= 0, "max_occupancy must be >= 0");
+  if (idx) {
+    if (nl->format == JMD_DENSE)
+      JMD_REQUIRE(idx_ld >= nl->max_occupancy, "idx leading dimension < max_occupancy");
+    else
+      JMD_REQUIRE(idx_ld >= nl->max_occupancy, "sparse idx row stride < capacity");
+  }
+  cudaStream_t st = as_stream(stream);
+  const bool v4 = is_vec4(position, pos_stride);
+  if (nl->space.dim == 3) {
+    return v4 ? build_impl<3, true>(nl, position, pos_stride, n, idx, idx_ld, nbr_count, occupancy,
+                                    error_code, reference_position, ref_stride, rebuild_flag,
+                                    workspace, workspace_bytes, st)
+              : build_impl<3, false>(nl, position, pos_stride, n, idx, idx_ld, nbr_count,
+                                     occupancy, error_code, reference_position, ref_stride,
+                                     rebuild_flag, workspace, workspace_bytes, st);
+  }
+  return v4 ? build_impl<2, true>(nl, position, pos_stride, n, idx, idx_ld, nbr_count, occupancy,
+                                  error_code, reference_position, ref_stride, rebuild_flag,
+                                  workspace, workspace_bytes, st)
+            : build_impl<2, false>(nl, position, pos_stride, n, idx, idx_ld, nbr_count, occupancy,
+                                   error_code, reference_position, ref_stride, rebuild_flag,
+                                   workspace, workspace_bytes, st);
+}
+
+int jmd_skin_check(const float* position, int64_t pos_stride, const float* reference_position,
+                   int64_t ref_stride, int64_t n, const jmd_space* space, float threshold_sq,
+                   int32_t* rebuild_flag, void* stream) {
+  JMD_REQUIRE(space && (space->dim == 2 || space->dim == 3), "bad space");
+  JMD_REQUIRE(rebuild_flag != nullptr, "rebuild_flag is null");
+  if (n <= 0) return JMD_OK;
+  cudaStream_t st = as_stream(stream);
+  Geo g = make_geo(*space);
+  unsigned gr = (unsigned)ceil_div(n, 256);
+  if (space->dim == 3)
+    k_skin<3><<<gr, 256, 0, st>>>(position, pos_stride, reference_position, ref_stride, (int)n, g,
+                                  threshold_sq, rebuild_flag);
+  else
+    k_skin<2><<<gr, 256, 0, st>>>(position, pos_stride, reference_position, ref_stride, (int)n, g,
+                                  threshold_sq, rebuild_flag);
+  return check_launch("jmd_skin_check");
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+// Pair-potential evaluation shared by the force, fused-step and adjoint
+// kernels.
+//
+// Reference: jax_md/energy.py
+//   lennard_jones                     :246-272  4 eps ((s/r)^12 - (s/r)^6)
+//   multiplicative_isotropic_cutoff   :534-580  S(r) between r_onset, r_cutoff
+//   soft_sphere                       :125-173  eps/alpha (1 - r/sigma)^alpha
+#pragma once
+
+#include "common.cuh"
+
+namespace jmd {
+
+// Per species-pair coefficients (host-precomputed, 32 bytes).
+struct PairCoef {
+  float sig2;     // sigma^2
+  float eps;      // epsilon
+  float alpha;    // soft-sphere exponent
+  float ro2;      // r_onset^2 (LJ smoothing)
+  float rc2;      // interaction cutoff^2 (LJ r_cutoff, soft sphere sigma^2)
+  float inv_den;  // 1 / (rc2 - ro2)^3
+  float inv_sig;  // 1 / sigma
+  float pad;
+};
+
+struct PairTable {
+  int kind;
+  int nsp;         // 0: scalar (entry 0)
+  float rc2_max;   // largest rc2 in the table
+  float pad;
+  PairCoef c[JMD_MAX_SPECIES * JMD_MAX_SPECIES];
+};
+
+PairTable make_pair_table(const jmd_pair& pp);
+
+// 1/x to ~0.5 ulp: hardware approximation plus one Newton step.
+__device__ __forceinline__ float rcp_nr(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  float e = fmaf(-x, y, 1.0f);
+  return fmaf(y, e, y);
+}
+
+// Evaluates one pair at squared distance r2 (0 < r2 < c.rc2 is the caller's
+// job).  Returns U and g = U'(r)/r; d2 = U''(r) (second derivative) when
+// SECOND, for the adjoint.
+template <int KIND, bool SECOND>
+__device__ __forceinline__ void pair_eval(float r2, const PairCoef& c, float& U, float& g,
+                                          float& h) {
+  if (KIND == JMD_SOFT_SPHERE) {
+    float r = sqrtf(r2);
+    float x = r * c.inv_sig;
+    float base = 1.0f - x;
+    float inv_r = rcp_nr(r);
+    if (c.alpha == 2.0f) {
+      U = 0.5f * c.eps * base * base;
+      float dU = -c.eps * c.inv_sig * base;  // U'(r)
+      g = dU * inv_r;
+      if (SECOND) h = c.eps * c.inv_sig * c.inv_sig;
+    } else {
+      float pa1 = __powf(base, c.alpha - 1.0f);
+      U = c.eps / c.alpha * pa1 * base;
+      float dU = -c.eps * c.inv_sig * pa1;
+      g = dU * inv_r;
+      if (SECOND) h = c.eps * (c.alpha - 1.0f) * c.inv_sig * c.inv_sig * __powf(base, c.alpha - 2.0f);
+    }
+    return;
+  }
+  float inv_r2 = rcp_nr(r2);
+  float s2 = c.sig2 * inv_r2;
+  float s6 = s2 * s2 * s2;
+  float s12 = s6 * s6;
+  float e4 = 4.0f * c.eps;
+  float u = e4 * (s12 - s6);
+  // U'(r)/r = 4 eps (6 s6 - 12 s12) / r^2
+  float gr = e4 * (6.0f * s6 - 12.0f * s12) * inv_r2;
+  float hh = 0.f;
+  if (SECOND) hh = e4 * (156.0f * s12 - 42.0f * s6) * inv_r2;  // U''(r)
+  if (KIND == JMD_LJ && r2 > c.ro2) {
+    // S(u) = (rc2-u)^2 (rc2+2u-3ro2) / den ; dS/dr / r = 12 (rc2-u)(ro2-u)/den
+    float a = c.rc2 - r2;
+    float bq = c.rc2 + 2.0f * r2 - 3.0f * c.ro2;
+    float S = a * a * bq * c.inv_den;
+    float dSr = 12.0f * a * (c.ro2 - r2) * c.inv_den;
+    if (SECOND) {
+      // d2S/dr2 = 4 r^2 S_uu + 2 S_u,  S_u = 6(rc2-u)(ro2-u)/den,
+      // S_uu = 6(2u - rc2 - ro2)/den
+      float Su = 6.0f * a * (c.ro2 - r2) * c.inv_den;
+      float Suu = 6.0f * (2.0f * r2 - c.rc2 - c.ro2) * c.inv_den;
+      float d2S = 4.0f * r2 * Suu + 2.0f * Su;
+      // U'(r) = gr * r ; (U S)'' = U'' S + 2 U' S' + U S''
+      hh = hh * S + 2.0f * (gr * r2) * dSr + u * d2S;  // U' S' = (gr r)(dSr r)
+    }
+    g = gr * S + u * dSr;
+    U = u * S;
+  } else {
+    g = gr;
+    U = u;
+  }
+  h = hh;
+}
+
+// Displacement a - b for atoms inside a periodic box: the plain difference,
+// re-done exactly only when a component wraps (see min_image).
+template <int DIM>
+__device__ __forceinline__ void displacement(const float4& a, const float4& b, const Geo& g,
+                                             float& dx, float& dy, float& dz) {
+  dx = a.x - b.x;
+  dy = a.y - b.y;
+  dz = DIM == 3 ? a.z - b.z : 0.f;
+  if (g.periodic) {
+    bool wrapped = fabsf(dx) > g.halfL[0] || fabsf(dy) > g.halfL[1];
+    if (DIM == 3) wrapped = wrapped || fabsf(dz) > g.halfL[2];
+    if (wrapped) {
+      dx = min_image(a.x, b.x, g.L[0], g.halfL[0]);
+      dy = min_image(a.y, b.y, g.L[1], g.halfL[1]);
+      if (DIM == 3) dz = min_image(a.z, b.z, g.L[2], g.halfL[2]);
+    }
+  }
+}
+
+}  // namespace jmd

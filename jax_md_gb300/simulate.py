@@ -1,0 +1,364 @@
+"""NVE and Nose-Hoover NVT integrators (jax_md/simulate.py) on the GB300 kernels.
+
+``nve`` and ``nvt_nose_hoover`` keep the reference signatures and return
+``(init_fn, apply_fn)``.  With a CUDA-backed energy (from
+``jax_md_gb300.energy`` / ``smap``) and a shift from ``jax_md_gb300.space``,
+``apply_fn(state, neighbor=nbrs)`` runs the velocity-Verlet step as three
+kernels: a fused half-kick + drift (with the pending Nose-Hoover rescale), the
+pair-force kernel, and the second half-kick.
+
+State tensors are updated in place: the state returned by ``apply_fn`` shares
+its buffers with the one passed in (``state.copy()`` gives an independent
+snapshot).  Positions, momenta and forces are [N, d] views over float4 rows.
+The Nose-Hoover chain lives in one f64 device buffer.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import math
+from typing import Callable, Optional
+
+import numpy as np
+import torch
+
+from . import _native as N
+from . import partition, quantity, smap
+from . import space as _space
+
+SUZUKI_YOSHIDA_WEIGHTS = {
+    # Suzuki-Yoshida weights, the values of jax_md/simulate.py:328-347.
+    1: [1.0],
+    3: [0.828981543588751, -0.657963087177502, 0.828981543588751],
+    5: [0.2967324292201065, 0.2967324292201065, -0.186929716880426, 0.2967324292201065,
+        0.2967324292201065],
+    7: [0.784513610477560, 0.235573213359357, -1.17767998417887, 1.31518632068391,
+        -1.17767998417887, 0.235573213359357, 0.784513610477560],
+}
+
+
+class _StateMixin:
+    def set(self, **kwargs):
+        return dataclasses.replace(self, **kwargs)
+
+    def copy(self):
+        def c(v):
+            return v.clone() if isinstance(v, torch.Tensor) else (
+                v.copy() if hasattr(v, 'copy') else v)
+        return dataclasses.replace(self, **{f.name: c(getattr(self, f.name))
+                                            for f in dataclasses.fields(self)})
+
+
+@dataclasses.dataclass
+class NVEState(_StateMixin):
+    """simulate.py:249-276."""
+    position: torch.Tensor
+    momentum: torch.Tensor
+    force: torch.Tensor
+    mass: object
+
+    @property
+    def velocity(self):
+        return self.momentum / _mass_col(self.mass)
+
+
+@dataclasses.dataclass
+class NoseHooverChain(_StateMixin):
+    """simulate.py:350-374, stored as one f64 buffer
+    [xi(16) | p_xi(16) | Q(16) | spare(16) | KE | kT]."""
+    buffer: torch.Tensor
+    chain_length: int
+    tau: float
+    degrees_of_freedom: int
+
+    @property
+    def position(self):
+        return self.buffer[0:self.chain_length]
+
+    @property
+    def momentum(self):
+        return self.buffer[16:16 + self.chain_length]
+
+    @property
+    def mass(self):
+        return self.buffer[32:32 + self.chain_length]
+
+    @property
+    def kinetic_energy(self):
+        return self.buffer[64]
+
+    def copy(self):
+        return dataclasses.replace(self, buffer=self.buffer.clone())
+
+
+@dataclasses.dataclass
+class NVTNoseHooverState(_StateMixin):
+    """simulate.py:538-562."""
+    position: torch.Tensor
+    momentum: torch.Tensor
+    force: torch.Tensor
+    mass: object
+    chain: NoseHooverChain
+
+    @property
+    def velocity(self):
+        return self.momentum / _mass_col(self.mass)
+
+
+def _mass_col(mass):
+    if isinstance(mass, torch.Tensor) and mass.numel() > 1:
+        return mass.reshape(-1, 1)
+    return mass
+
+
+def canonicalize_mass(mass, n, device):
+    """simulate.py:119-138: scalar stays a float, arrays become [N] float32."""
+    if isinstance(mass, (int, float)):
+        return float(mass)
+    m = torch.as_tensor(mass, dtype=torch.float32, device=device)
+    if m.numel() == 1:
+        return float(m)
+    if m.dim() == 2 and m.shape[1] == 1:
+        m = m[:, 0]
+    if m.dim() != 1 or m.shape[0] != n:
+        raise ValueError('Expected mass to be either a floating point number or a one-dimensional '
+                         f'ndarray. Found {tuple(m.shape)}.')
+    return m.contiguous()
+
+
+def _mass_ptr(mass):
+    if isinstance(mass, torch.Tensor):
+        return mass.data_ptr(), 1.0
+    return None, float(mass)
+
+
+def _rows4(t: torch.Tensor) -> torch.Tensor:
+    """Float4-row copy of an [N, d] tensor, returned as an [N, d] view."""
+    return partition.padded_rows(t.detach().to(torch.float32))
+
+
+def _shift_space(shift_fn, dim) -> N.Space:
+    s = N.Space()
+    s.dim = dim
+    periodic = isinstance(shift_fn, _space.Shift) and shift_fn.periodic and shift_fn.wrapped
+    if not isinstance(shift_fn, _space.Shift):
+        raise NotImplementedError('the GB300 integrators need a shift_fn from jax_md_gb300.space')
+    s.periodic = 1 if periodic else 0
+    if periodic:
+        b = partition._box_list(shift_fn.box, dim)
+        for d in range(dim):
+            s.box[d] = b[d]
+    return s
+
+
+def initialize_momenta(R, mass, key, kT):
+    """simulate.py:141-159 with torch's generator (the JAX PRNG is not reproducible here)."""
+    g = key if isinstance(key, torch.Generator) else None
+    if g is None:
+        g = torch.Generator(device=R.device)
+        g.manual_seed(int(key) if key is not None else 0)
+    m = _mass_col(mass)
+    m = m if isinstance(m, torch.Tensor) else torch.tensor(m, device=R.device)
+    P = torch.sqrt(m * kT) * torch.randn(R.shape, generator=g, device=R.device, dtype=R.dtype)
+    if R.shape[0] > 1:
+        P = P - P.mean(0, keepdim=True)
+    return P
+
+
+class _Stepper:
+    """Kernel plumbing shared by nve / nvt_nose_hoover."""
+
+    def __init__(self, energy_or_force_fn, shift_fn, dt):
+        self.energy_fn = energy_or_force_fn
+        self.force_fn = quantity.canonicalize_force(energy_or_force_fn)
+        self.kernel_force = quantity._kernel_energy(energy_or_force_fn)
+        self.shift_fn = shift_fn
+        self.dt = float(np.float32(dt))
+
+    def forces_into(self, R, out, **kwargs):
+        if self.kernel_force:
+            e = self.energy_fn
+            if isinstance(e, smap.PairAllEnergy):
+                e.forces(R, out=out, **kwargs)
+            else:
+                nb = kwargs.pop('neighbor')
+                e.forces(R, nb, out=out, **kwargs)
+        else:
+            out.copy_(self.force_fn(R, **kwargs))
+        return out
+
+    def kick_drift(self, state, dt, p_scale=None):
+        R, P, F = state.position, state.momentum, state.force
+        n, dim = R.shape
+        s = _shift_space(self.shift_fn, dim)
+        mptr, m0 = _mass_ptr(state.mass)
+        N.check(N.lib().jmd_verlet_kick_drift(
+            R.data_ptr(), R.stride(0), P.data_ptr(), P.stride(0), F.data_ptr(), F.stride(0), mptr, m0,
+            n, ctypes.byref(s), dt, N.ptr(p_scale), None, 0, 0.0, None, N.stream_ptr()),
+            'verlet_kick_drift')
+
+    def kick(self, state, dt_half):
+        P, F = state.momentum, state.force
+        n, dim = P.shape
+        N.check(N.lib().jmd_momentum_step(P.data_ptr(), P.stride(0), F.data_ptr(), F.stride(0), n,
+                                          dim, dt_half, N.stream_ptr()), 'momentum_step')
+
+    def velocity_verlet(self, state, dt=None, p_scale=None, **kwargs):
+        """simulate.py:227-243."""
+        dt = self.dt if dt is None else float(np.float32(dt))
+        self.kick_drift(state, dt, p_scale)
+        self.forces_into(state.position, state.force, **kwargs)
+        self.kick(state, float(np.float32(dt / 2)))
+        return state
+
+    def new_state_tensors(self, R, **kwargs):
+        N.require_cuda(R)
+        R4 = _rows4(R)
+        F4 = _rows4(torch.zeros_like(R4))
+        self.forces_into(R4, F4, **kwargs)
+        return R4, F4
+
+
+def momentum_step(state, dt):
+    """simulate.py:168-173 (in place)."""
+    P, F = state.momentum, state.force
+    N.check(N.lib().jmd_momentum_step(P.data_ptr(), P.stride(0), F.data_ptr(), F.stride(0),
+                                      P.shape[0], P.shape[1], float(dt), N.stream_ptr()),
+            'momentum_step')
+    return state
+
+
+def position_step(state, shift_fn, dt, **kwargs):
+    """simulate.py:176-188 (in place)."""
+    R, P = state.position, state.momentum
+    s = _shift_space(shift_fn, R.shape[1])
+    mptr, m0 = _mass_ptr(state.mass)
+    N.check(N.lib().jmd_position_step(R.data_ptr(), R.stride(0), P.data_ptr(), P.stride(0), mptr,
+                                      m0, R.shape[0], ctypes.byref(s), float(dt), N.stream_ptr()),
+            'position_step')
+    return state
+
+
+def velocity_verlet(force_fn, shift_fn, dt, state, **kwargs):
+    """simulate.py:227-243 for any force function (in place)."""
+    st = _Stepper(force_fn, shift_fn, dt)
+    return st.velocity_verlet(state, **kwargs)
+
+
+def nve(energy_or_force_fn, shift_fn, dt=1e-3, **sim_kwargs):
+    """simulate.nve (simulate.py:279-317)."""
+    st = _Stepper(energy_or_force_fn, shift_fn, dt)
+
+    def init_fn(key, R, kT=None, mass=1.0, momenta=None, **kwargs):
+        R4, F4 = st.new_state_tensors(R, **kwargs)
+        m = canonicalize_mass(mass, R.shape[0], R.device)
+        if momenta is None:
+            P = initialize_momenta(R4, m, key, kT)
+        else:
+            P = momenta
+        return NVEState(R4, _rows4(P), F4, m)
+
+    def apply_fn(state, **kwargs):
+        dt_ = kwargs.pop('dt', None)
+        return st.velocity_verlet(state, dt_, **kwargs)
+
+    init_fn.stepper = st
+    apply_fn.stepper = st
+    return init_fn, apply_fn
+
+
+class _Chain:
+    """Device-side Nose-Hoover chain (simulate.py:384-517)."""
+
+    def __init__(self, dt, chain_length, chain_steps, sy_steps, tau):
+        if chain_length < 2 or chain_length > 16:
+            raise ValueError('chain_length must be between 2 and 16')
+        if sy_steps not in SUZUKI_YOSHIDA_WEIGHTS:
+            raise ValueError('sy_steps must be 1, 3, 5 or 7')
+        self.dt = dt
+        self.M1 = chain_length
+        self.chain_steps = chain_steps
+        self.sy_steps = sy_steps
+        self.tau = tau
+
+    def init(self, dof, KE, kT, device):
+        buf = torch.zeros(66, dtype=torch.float64, device=device)
+        buf[32:32 + self.M1] = kT * self.tau ** 2
+        buf[32] = buf[32] * dof
+        buf[64] = KE
+        buf[65] = kT
+        return NoseHooverChain(buf, self.M1, self.tau, dof)
+
+    def half_step(self, chain: NoseHooverChain, p_scale, ke=None, update_mass=False):
+        c = N.Nhc()
+        c.chain_length = self.M1
+        c.chain_steps = self.chain_steps
+        c.sy_steps = self.sy_steps
+        c.dof = chain.degrees_of_freedom
+        c.dt = self.dt
+        c.tau = chain.tau
+        N.check(N.lib().jmd_nhc_half_step(ctypes.byref(c), chain.buffer.data_ptr(), N.ptr(ke),
+                                          1 if update_mass else 0, p_scale.data_ptr(),
+                                          N.stream_ptr()), 'nhc_half_step')
+
+
+def nvt_nose_hoover(energy_or_force_fn, shift_fn, dt, kT, chain_length: int = 5,
+                    chain_steps: int = 2, sy_steps: int = 3, tau: Optional[float] = None,
+                    **sim_kwargs):
+    """simulate.nvt_nose_hoover (simulate.py:565-669)."""
+    st = _Stepper(energy_or_force_fn, shift_fn, dt)
+    dt32 = float(np.float32(dt))
+    if tau is None:
+        tau = dt32 * 100
+    tau = float(np.float32(tau))
+    chain_fns = _Chain(dt32, chain_length, chain_steps, sy_steps, tau)
+
+    def init_fn(key, R, mass=1.0, momenta=None, **kwargs):
+        _kT = kwargs.pop('kT', kT)
+        R4, F4 = st.new_state_tensors(R, **kwargs)
+        m = canonicalize_mass(mass, R.shape[0], R.device)
+        P = initialize_momenta(R4, m, key, _kT) if momenta is None else momenta
+        P4 = _rows4(P)
+        dof = quantity.count_dof(R)
+        KE = float(quantity._ke_f64(P4, m))
+        chain = chain_fns.init(dof, KE, float(_kT), R.device)
+        return NVTNoseHooverState(R4, P4, F4, m, chain)
+
+    def apply_fn(state, **kwargs):
+        chain = state.chain
+        if 'kT' in kwargs:
+            chain.buffer[65] = float(kwargs.pop('kT'))
+        scale = torch.empty((), dtype=torch.float64, device=state.position.device)
+        # update_mass + first half step (simulate.py:653-656); the rescale is
+        # applied inside the fused kick-drift kernel.
+        chain_fns.half_step(chain, scale, update_mass=True)
+        st.velocity_verlet(state, p_scale=scale, **kwargs)
+        ke = quantity._ke_f64(state.momentum, state.mass, out=chain.buffer[64])
+        chain_fns.half_step(chain, scale, ke=None)
+        P = state.momentum
+        N.check(N.lib().jmd_scale_momentum(P.data_ptr(), P.stride(0), P.shape[0], P.shape[1],
+                                           scale.data_ptr(), N.stream_ptr()), 'scale_momentum')
+        return state
+
+    init_fn.stepper = st
+    apply_fn.stepper = st
+    return init_fn, apply_fn
+
+
+def nvt_nose_hoover_invariant(energy_fn, state: NVTNoseHooverState, kT, **kwargs):
+    """simulate.py:672-701 (f64)."""
+    if quantity._kernel_energy(energy_fn):
+        if isinstance(energy_fn, smap.PairAllEnergy):
+            PE = energy_fn.compute(state.position, force=False)[0]
+        else:
+            PE = energy_fn.energy_f64(state.position, kwargs.pop('neighbor'), **kwargs)
+    else:
+        PE = energy_fn(state.position, **kwargs).double()
+    KE = quantity._ke_f64(state.momentum, state.mass)
+    c = state.chain
+    dof = quantity.count_dof(state.position)
+    E = PE + KE
+    E = E + c.momentum[0] ** 2 / (2 * c.mass[0]) + dof * kT * c.position[0]
+    for r, p, m in zip(c.position[1:], c.momentum[1:], c.mass[1:]):
+        E = E + p ** 2 / (2 * m) + kT * r
+    return E

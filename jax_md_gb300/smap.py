@@ -1,0 +1,241 @@
+"""Pair maps over neighbour lists (jax_md/smap.py) backed by the CUDA kernels.
+
+``pair_neighbor_list(fn, displacement, species=None, reduce_axis=None,
+ignore_unused_parameters=False, **kwargs)`` keeps the reference signature
+(smap.py:856-979) and returns ``fn_mapped(R, neighbor, **dynamic_kwargs)``.
+``fn`` must be one of the potentials in ``jax_md_gb300.energy`` (there is
+no kernel for an arbitrary Python function, and no CPU fallback).
+Parameters are scalars or, with ``species``, [S, S] matrices (smap.py:778-823).
+
+The returned energy is float32 like the reference (an f64 sum cast back,
+util.high_precision_sum); it is differentiable with respect to ``R`` (the
+backward pass returns -F from the same kernel launch).  The object also
+exposes ``forces``, ``energy_f64`` and ``compute`` for the integrators.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Tuple
+
+import numpy as np
+import torch
+
+from . import _native as N
+from . import partition
+from . import space as _space
+
+
+def _param_matrix(v, n_species: int, name: str):
+    """Scalar or [S, S] species matrix -> nested list [8][8] of floats."""
+    if isinstance(v, torch.Tensor):
+        v = v.detach().cpu().double().numpy()
+    a = np.asarray(v, np.float64)
+    out = np.zeros((N.MAX_SPECIES, N.MAX_SPECIES))
+    if a.ndim == 0:
+        out[:, :] = float(a)
+        return out
+    if a.ndim == 1:
+        raise NotImplementedError(f'per-particle parameter arrays ({name}) are not supported by the '
+                                  'pair kernels; use scalars or species matrices')
+    if a.ndim == 2:
+        if n_species == 0:
+            raise NotImplementedError(f'an [N, N] parameter matrix ({name}) needs species; per-pair '
+                                      'matrices are not supported by the pair kernels')
+        S = a.shape[0]
+        if S > N.MAX_SPECIES:
+            raise ValueError(f'at most {N.MAX_SPECIES} species are supported')
+        out[:S, :S] = a
+        return out
+    raise ValueError(f'Parameter array must be either a scalar, a vector, or a matrix. '
+                     f'Found ndim={a.ndim}.')
+
+
+def make_pair_struct(fn, params: dict, n_species: int) -> N.Pair:
+    p = N.Pair()
+    p.kind = fn.kind
+    p.n_species = n_species
+    p.per_pair_cutoff = 1 if params.get('per_pair_cutoff', False) else 0
+    rc = fn.r_cutoff
+    p.r_cutoff = float(np.float32(rc)) if np.isfinite(rc) else 3.0e38
+    ro = fn.r_onset
+    p.r_onset = float(np.float32(ro)) if np.isfinite(ro) else p.r_cutoff
+    for key, default in (('sigma', 1.0), ('epsilon', 1.0), ('alpha', 2.0)):
+        m = _param_matrix(params.get(key, default), n_species, key)
+        arr = getattr(p, key)
+        for a in range(N.MAX_SPECIES):
+            for b in range(N.MAX_SPECIES):
+                arr[a][b] = float(m[a, b])
+    return p
+
+
+class _EnergyFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, R, runner):
+        E, F = runner(R)
+        ctx.save_for_backward(F)
+        return E
+
+    @staticmethod
+    def backward(ctx, gE):
+        F, = ctx.saved_tensors
+        return -F * gE.to(F.dtype), None
+
+
+class PairNeighborListEnergy:
+    """fn_mapped of smap.pair_neighbor_list, bound to the CUDA kernels."""
+
+    def __init__(self, fn, displacement_or_metric, species, reduce_axis, ignore_unused_parameters,
+                 params):
+        if not hasattr(fn, 'kind'):
+            raise NotImplementedError('pair_neighbor_list needs a potential from '
+                                      'jax_md_gb300.energy (lennard_jones, soft_sphere or their '
+                                      'multiplicative_isotropic_cutoff); there is no kernel for '
+                                      f'{fn!r}')
+        self.fn = fn
+        self.geometry = _space.geometry_of(displacement_or_metric)
+        self.species = species
+        self.reduce_axis = reduce_axis
+        self.ignore_unused_parameters = ignore_unused_parameters
+        self.params = dict(params)
+        if reduce_axis is not None and tuple(reduce_axis) not in ((1,), (0, 1)):
+            raise NotImplementedError('reduce_axis must be None, (1,) or (0, 1) for the pair kernels')
+
+    # -- plumbing ---------------------------------------------------------
+    def _resolve(self, R, dynamic):
+        species = dynamic.get('species', self.species)
+        params = dict(self.params)
+        for k in ('sigma', 'epsilon', 'alpha'):
+            if k in dynamic:
+                params[k] = dynamic[k]
+        S = 0
+        for k in ('sigma', 'epsilon', 'alpha'):
+            v = params.get(k)
+            if v is not None and np.ndim(v.detach().cpu() if isinstance(v, torch.Tensor) else v) == 2:
+                S = max(S, int(v.shape[0]) if hasattr(v, 'shape') else len(v))
+        if S:
+            if species is None or isinstance(species, int):
+                raise NotImplementedError('species matrices need a per-atom species array')
+            if not isinstance(species, torch.Tensor):
+                species = torch.as_tensor(np.asarray(species))
+            species = species.to(device=R.device, dtype=torch.int32).contiguous()
+        else:
+            species = None
+        return species, make_pair_struct(self.fn, params, S)
+
+    def launch(self, R, neighbor, force=None, energy=None, per_atom=None, virial=None, **dynamic):
+        R, rs = partition._rows(R)
+        n, dim = R.shape
+        species, pair = self._resolve(R, dynamic)
+        sp = self.geometry.space(dim)
+        fmt = {partition.Dense: N.DENSE, partition.Sparse: N.SPARSE,
+               partition.OrderedSparse: N.ORDERED_SPARSE}[neighbor.format]
+        idx = neighbor.idx
+        if idx.dtype != torch.int32:
+            idx = idx.to(torch.int32)
+        if idx.dim() != 2 or idx.stride(1) != 1:
+            idx = idx.contiguous()
+        if fmt == N.DENSE and idx.shape[0] != n:
+            raise ValueError('neighbor list has a different number of atoms than R')
+        width = idx.shape[1]
+        ld = idx.stride(0) if idx.shape[0] > 1 else max(width, 1)
+        cnt = neighbor.nbr_count if (fmt == N.DENSE and hasattr(neighbor, 'nbr_count')
+                                      and neighbor.nbr_count is not None
+                                      and neighbor.idx is idx) else None
+        L = N.lib()
+        ws = N.workspace(L.jmd_pair_workspace_bytes(n), R.device, 'pair')
+        fs = force.stride(0) if force is not None else 0
+        N.check(L.jmd_pair_forces(ctypes.byref(pair), ctypes.byref(sp), fmt, R.data_ptr(), rs,
+                                  N.ptr(species), n, idx.data_ptr(), ld, width, N.ptr(cnt),
+                                  N.ptr(force), fs, N.ptr(energy), N.ptr(per_atom), N.ptr(virial),
+                                  ws.data_ptr(), ws.numel(), N.stream_ptr()), 'pair_forces')
+
+    def forces(self, R, neighbor, out: Optional[torch.Tensor] = None, **dynamic):
+        """-dE/dR as [N, d] (rows of stride 4 when R has them)."""
+        if out is None:
+            out = torch.empty((R.shape[0], 4), dtype=torch.float32, device=R.device)[:, :R.shape[1]]
+        self.launch(R, neighbor, force=out, **dynamic)
+        return out
+
+    def compute(self, R, neighbor, force=True, per_atom=False, virial=False, **dynamic):
+        """(energy f64 0-d, forces or None, per-atom energy or None, virial[6|3] or None)."""
+        dev = R.device
+        e = torch.empty((), dtype=torch.float64, device=dev)
+        f = torch.empty((R.shape[0], 4), dtype=torch.float32, device=dev)[:, :R.shape[1]] if force else None
+        pa = torch.empty(R.shape[0], dtype=torch.float32, device=dev) if per_atom else None
+        dim = R.shape[1]
+        w = torch.empty(6 if dim == 3 else 3, dtype=torch.float64, device=dev) if virial else None
+        self.launch(R, neighbor, force=f, energy=e, per_atom=pa, virial=w, **dynamic)
+        return e, f, pa, w
+
+    def energy_f64(self, R, neighbor, **dynamic):
+        return self.compute(R, neighbor, force=False, **dynamic)[0]
+
+    def __call__(self, R, neighbor, **dynamic):
+        per_particle = self.reduce_axis is not None and tuple(self.reduce_axis) == (1,)
+        if per_particle:
+            if neighbor.format is partition.OrderedSparse:
+                raise ValueError('Cannot report per-particle values with a neighbor list whose '
+                                 'format is `OrderedSparse`. Please use either `Dense` or `Sparse`.')
+            _, _, pa, _ = self.compute(R.detach(), neighbor, force=False, per_atom=True, **dynamic)
+            return pa
+
+        def runner(Rd):
+            e, f, _, _ = self.compute(Rd, neighbor, force=True, **dynamic)
+            return e.to(Rd.dtype), f
+        if R.requires_grad:
+            return _EnergyFn.apply(R, runner)
+        return self.energy_f64(R, neighbor, **dynamic).to(R.dtype)
+
+
+def pair_neighbor_list(fn, displacement_or_metric, species=None, reduce_axis=None,
+                       ignore_unused_parameters: bool = False, **kwargs):
+    """smap.pair_neighbor_list (smap.py:856-979)."""
+    kwargs.pop('fractional_coordinates', None)
+    return PairNeighborListEnergy(fn, displacement_or_metric, species, reduce_axis,
+                                  ignore_unused_parameters, kwargs)
+
+
+class PairAllEnergy:
+    """smap.pair (smap.py:548-691): every pair i != j, through an all-pairs list."""
+
+    def __init__(self, fn, displacement_or_metric, species, reduce_axis, params):
+        self.inner = PairNeighborListEnergy(fn, displacement_or_metric, species, reduce_axis,
+                                            True, params)
+        self.fn = fn
+        self.geometry = self.inner.geometry
+        self._cache = {}
+
+    def _neighbors(self, R):
+        n, dim = R.shape
+        key = (n, dim, R.device)
+        nb = self._cache.get(key)
+        if nb is None:
+            geo = self.geometry
+            box = geo.box if geo.periodic else 1.0e30
+            rc = self.fn.r_cutoff
+            if self.fn.kind == N.SOFT_SPHERE:
+                sig = self.inner.params.get('sigma', 1.0)
+                rc = float(np.max(np.asarray(sig.detach().cpu() if isinstance(sig, torch.Tensor) else sig)))
+            if not np.isfinite(rc):
+                rc = 1.0e18
+            fns = partition.neighbor_list(geo, box, rc, 0.0, capacity_multiplier=1.0,
+                                          disable_cell_list=True)
+            nb = (fns, fns.allocate(R))
+            self._cache = {key: nb}
+            return nb[1]
+        return nb[0].update(R, nb[1])
+
+    def __call__(self, R, **dynamic):
+        return self.inner(R, self._neighbors(R.detach()), **dynamic)
+
+    def compute(self, R, **kw):
+        return self.inner.compute(R, self._neighbors(R), **kw)
+
+    def forces(self, R, **kw):
+        return self.inner.forces(R, self._neighbors(R), **kw)
+
+
+def pair(fn, displacement_or_metric, species=None, reduce_axis=None, **kwargs):
+    """smap.pair (smap.py:548-691) for the kernel potentials."""
+    kwargs.pop('ignore_unused_parameters', None)
+    return PairAllEnergy(fn, displacement_or_metric, species, reduce_axis, kwargs)

@@ -1,0 +1,167 @@
+"""Pins the FP64 oracle to the reference's golden fixtures and known answers.
+
+CPU only.  Each case cites the reference test it restates.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import md_oracle as O
+from tests.helpers import GOLDEN, fcc_system, random_box
+
+
+def test_lammps_lj_energy_and_stress():
+    """tests/quantity_test.py:436-455: truncated LJ at 2.5, tol 5e-5."""
+    g = np.load(GOLDEN / 'lammps_lj_stress.npz')
+    box = float(g['box'])
+    R = g['fractional_position'] * box
+    V = g['velocity']
+    spec = O.PairSpec(kind='lj_truncated', r_cutoff=2.5)
+    E, F, W = O.all_pairs_energy_forces(spec, R, np.full(3, box))
+    assert abs(E / len(R) - g['energy_per_atom']) < 5e-5
+    S = O.stress(W, V, 1.0, box ** 3)
+    np.testing.assert_allclose(S, g['stress'], atol=5e-5, rtol=5e-5)
+
+
+def test_jammed_soft_sphere_pressure_and_energy():
+    """tests/quantity_test.py:134-150 (pressure, f64 tol 1e-7) + the stored energy."""
+    g = np.load(GOLDEN / 'jammed_soft_sphere_2d.npz')
+    L = np.diag(g['box'])
+    spec = O.PairSpec(kind='soft_sphere', sigma=g['sigma'], epsilon=1.0, alpha=2.0,
+                      species=g['species'])
+    E, F, W = O.all_pairs_energy_forces(spec, g['real_position'], L)
+    P = O.pressure(W, 0.0, 2, np.prod(L))
+    assert abs(P - g['pressure']) < 1e-7
+    assert abs(E - g['energy']) < 1e-10
+
+
+def test_lj_minimum():
+    """tests/energy_test.py:325-342: U(2^(1/6) sigma) = -eps, U' = 0."""
+    for sigma, eps in [(1.0, 1.0), (0.5, 2.0), (1.3, 0.7)]:
+        r = np.array([2 ** (1 / 6) * sigma])
+        U, dU, _ = O.lennard_jones(r, sigma, eps)
+        assert abs(U[0] + eps) < 1e-12
+        assert abs(dU[0]) < 1e-10
+
+
+def test_soft_sphere_known_values():
+    """tests/energy_test.py:284-312."""
+    for alpha in (2.0, 2.5, 3.0):
+        sigma, eps = 1.3, 0.8
+        U, dU, _ = O.soft_sphere(np.array([0.0, sigma, 2 * sigma]), sigma, eps, alpha)
+        assert abs(U[0] - eps / alpha) < 1e-12
+        assert U[1] == 0.0 and U[2] == 0.0
+        assert dU[2] == 0.0
+        if alpha > 2:
+            assert abs(dU[1]) < 1e-12
+
+
+def test_multiplicative_cutoff_regions():
+    """tests/energy_test.py:533-562: identity below r_onset, zero beyond r_cutoff, C1."""
+    r = np.linspace(0.5, 3.0, 1001)
+    S, dS, _ = O.multiplicative_cutoff(r, 2.0, 2.5)
+    assert np.all(S[r < 2.0] == 1.0)
+    assert np.all(S[r >= 2.5] == 0.0)
+    # continuity of S and S' at both ends
+    for r0 in (2.0, 2.5):
+        s_l, ds_l, _ = O.multiplicative_cutoff(np.array([r0 - 1e-7]), 2.0, 2.5)
+        s_r, ds_r, _ = O.multiplicative_cutoff(np.array([r0 + 1e-7]), 2.0, 2.5)
+        assert abs(s_l - s_r) < 1e-6 and abs(ds_l - ds_r) < 1e-5
+
+
+def test_oracle_second_derivative_matches_fd():
+    spec = O.PairSpec(kind='lj')
+    r = np.linspace(0.9, 2.6, 301)
+    h = 1e-6
+    _, dU, d2U = O.pair_terms(spec, r)
+    _, dUp, _ = O.pair_terms(spec, r + h)
+    _, dUm, _ = O.pair_terms(spec, r - h)
+    fd = (dUp - dUm) / (2 * h)
+    mask = (np.abs(r - 2.0) > 1e-3) & (np.abs(r - 2.5) > 1e-3)
+    np.testing.assert_allclose(d2U[mask], fd[mask], rtol=1e-5, atol=1e-5)
+
+
+def test_cell_list_emplace_2d():
+    """tests/partition_test.py:61-98: slot rule hash*cap + (rank mod cap)."""
+    R = np.array([[0.25, 0.25], [8.5, 1.95], [8.1, 1.5], [3.7, 7.9]], np.float32)
+    box = np.array([8.65, 8.0], np.float32)
+    cap = O.estimate_cell_capacity(R, box, 1.0, 1.25, 2)
+    cl = O.cell_list(R, box, 1.0, cap)
+    cps = cl.cells_per_side
+    ids = cl.id_buffer.reshape(cps[1], cps[0], cap)
+    assert ids[0, 0, 0] == 0
+    assert ids[1, 7, 1] == 1   # the reference indexes [1, 8, 1] and JAX clamps 8 -> 7
+    assert ids[1, 7, 0] == 2
+    assert ids[7, 3, 1] == 3
+
+
+@pytest.mark.parametrize('dim', [2, 3])
+def test_oracle_neighbor_list_matches_all_pairs(dim):
+    """tests/partition_test.py:203-257: neighbour sets == brute force, rectangular box."""
+    box = np.array([9.0, 3.25] if dim == 2 else [9.0, 4.0, 7.25], np.float32)
+    R = random_box(400, dim, box, seed=3)
+    nl = O.NeighborListOracle(box, 1.23 / 2, 0.0, fmt=O.DENSE)  # 3 cells on the short side
+    nb = nl.allocate(R)
+    assert nb.use_cell_list
+    sets = O.neighbor_sets(nb, len(R))
+    d = O.displacement(R[:, None], R[None], box)
+    r2 = (d * d).sum(-1)
+    for i in range(len(R)):
+        brute = sorted(int(j) for j in np.nonzero(r2[i] < nl.cutoff_sq)[0] if j != i)
+        assert sets[i] == brute
+
+
+@pytest.mark.parametrize('r_cut,dc,cm', [(0.12, True, 1.5), (0.25, False, 1.5),
+                                         (0.31, False, 1.5), (0.31, False, 1.0)])
+@pytest.mark.parametrize('mask_self', [False, True])
+@pytest.mark.parametrize('fmt', [O.DENSE, O.SPARSE, O.ORDERED_SPARSE])
+def test_capacity_shapes(r_cut, dc, cm, mask_self, fmt):
+    """tests/partition_test.py:489-546 (issue 191): 20 atoms at one point."""
+    if fmt == O.DENSE:
+        want = (20, 19) if mask_self else (20, 20)
+    elif fmt == O.SPARSE:
+        want = (2, 20 * 19) if mask_self else (2, 400)
+    else:
+        want = (2, 20 * 19 // 2)
+    R = np.full((20, 3), 0.5, np.float32)
+    nl = O.NeighborListOracle(np.ones(3), r_cut, 0.1 * r_cut, capacity_multiplier=cm,
+                              disable_cell_list=dc, mask_self=mask_self, fmt=fmt)
+    nb = nl.allocate(R)
+    assert not O.did_buffer_overflow(nb.error)
+    assert nb.idx.shape == want
+    nb2 = nl.update(R + np.float32(0.1), nb)
+    assert not O.did_buffer_overflow(nb2.error)
+    assert nb2.idx.shape == want
+
+
+def test_overflow_on_collapse():
+    """tests/partition_test.py:363-401: free space, two points collapse -> overflow."""
+    R = np.array([[20.0, 20.0], [30.0, 30.0], [40.0, 40.0], [50.0, 50.0]], np.float32)
+    nl = O.NeighborListOracle(100.0, 3.0, 0.0, periodic=False)
+    nb = nl.allocate(R)
+    assert not O.did_buffer_overflow(nb.error)
+    R2 = R.copy()
+    R2[1] = R2[0]
+    nb2 = nl.update(R2, nb)
+    assert O.did_buffer_overflow(nb2.error)
+
+
+def test_nhc_invariant_drift_small():
+    """simulate_test.py:264-304 style: NVT invariant conserved (oracle, small system)."""
+    R, P, L = fcc_system(3)
+    box = np.full(3, L)
+    spec = O.PairSpec(kind='lj')
+    nl = O.NeighborListOracle(box, 2.5, 0.3)
+    nb = nl.allocate(R)
+    def fn(X):
+        return O.pair_energy_forces(spec, X, nb.idx, O.DENSE, box)[1]
+    R = R.astype(np.float64)
+    P = P.astype(np.float64)
+    F = fn(R)
+    c = O.nhc_init(R.size, O.kinetic_energy(P), 0.722, 0.5, 5)
+    H0 = O.nvt_invariant(O.pair_energy_forces(spec, R, nb.idx, O.DENSE, box)[0], P, 1.0, c, 0.722)
+    for _ in range(100):
+        R, P, F, c = O.nvt_nose_hoover_step(fn, R, P, F, 1.0, c, 0.005, 0.722, box)
+    H1 = O.nvt_invariant(O.pair_energy_forces(spec, R, nb.idx, O.DENSE, box)[0], P, 1.0, c, 0.722)
+    assert abs(H1 - H0) / len(R) < 5e-4
