@@ -509,14 +509,16 @@ __global__ void k_skin(const float* __restrict__ x, int64_t xs, const float* __r
 }
 
 // ------------------------------------------------------------ host side ----
-int validate(const jmd_nlist* nl, int64_t n) {
+int validate(const jmd_nlist* nl, int64_t n, int min_cells = 3) {
   JMD_REQUIRE(nl != nullptr, "nlist descriptor is null");
   JMD_REQUIRE(nl->space.dim == 2 || nl->space.dim == 3, "dim must be 2 or 3");
   JMD_REQUIRE(n >= 0 && n < (int64_t)INT32_MAX, "atom count out of range");
   JMD_REQUIRE(nl->format >= 0 && nl->format <= 2, "unknown neighbour list format");
   if (nl->use_cell_list) {
     for (int d = 0; d < nl->space.dim; ++d) {
-      JMD_REQUIRE(nl->cells_per_side[d] >= 3, "cell list needs >= 3 cells per side");
+      JMD_REQUIRE(nl->cells_per_side[d] >= min_cells,
+                  min_cells == 3 ? "the neighbour search needs >= 3 cells per side"
+                                 : "cells_per_side must be >= 1");
       JMD_REQUIRE(nl->cell_size[d] > 0.f, "cell size must be positive");
     }
     JMD_REQUIRE(nl->cell_capacity >= 1, "cell capacity must be >= 1");
@@ -627,7 +629,7 @@ size_t jmd_neighbor_list_workspace_bytes(const jmd_nlist* nl, int64_t n) {
 int jmd_cell_max_filling(const float* position, int64_t pos_stride, int64_t n,
                          const jmd_nlist* nl, int32_t* max_filling, void* workspace,
                          size_t workspace_bytes, void* stream) {
-  int e = validate(nl, n);
+  int e = validate(nl, n, 1);
   if (e) return e;
   JMD_REQUIRE(nl->use_cell_list, "cell grid required");
   JMD_REQUIRE(max_filling != nullptr, "max_filling is null");
@@ -658,7 +660,7 @@ int jmd_cell_list_build(const float* position, int64_t pos_stride, int64_t n, co
                         int32_t* id_buffer, float* position_buffer, int32_t* particle_cell_id,
                         uint8_t* error_code, void* workspace, size_t workspace_bytes,
                         void* stream) {
-  int e = validate(nl, n);
+  int e = validate(nl, n, 1);
   if (e) return e;
   JMD_REQUIRE(nl->use_cell_list, "cell grid required");
   JMD_REQUIRE(id_buffer != nullptr, "id_buffer is null");

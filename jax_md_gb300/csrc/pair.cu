@@ -81,6 +81,11 @@ struct DenseArgs {
   Geo geo;
 };
 
+// Species index clamped into the table (JAX clamps out-of-range gathers too).
+__device__ __forceinline__ int sp_clamp(int s, int nsp) {
+  return s < 0 ? 0 : (s >= nsp ? nsp - 1 : s);
+}
+
 template <int TPA, typename T>
 __device__ __forceinline__ T group_sum(T v) {
 #pragma unroll
@@ -104,7 +109,7 @@ __global__ void __launch_bounds__(256) k_pair_dense(DenseArgs a, const __grid_co
   float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f, w4 = 0.f, w5 = 0.f;
   if (active) {
     const float4 xi = load_row<DIM, VEC4>(a.x, a.xs, atom);
-    const int si = SPECIES ? __ldg(a.species + atom) : 0;
+    const int si = SPECIES ? sp_clamp(__ldg(a.species + atom), tab.nsp) : 0;
     const int32_t* row = a.idx + atom * a.ld;
     int64_t end = a.width;
     if (a.cnt) end = min((int64_t)__ldg(a.cnt + atom), a.width);
@@ -119,7 +124,8 @@ __global__ void __launch_bounds__(256) k_pair_dense(DenseArgs a, const __grid_co
       r2 = fmaf(dy, dy, r2);
       if (DIM == 3) r2 = fmaf(dz, dz, r2);
       if (!(r2 < rc2m) || r2 == 0.f) continue;
-      const PairCoef& c = SPECIES ? sc[si * JMD_MAX_SPECIES + __ldg(a.species + j)] : tab.c[0];
+      const PairCoef& c =
+          SPECIES ? sc[si * JMD_MAX_SPECIES + sp_clamp(__ldg(a.species + j), tab.nsp)] : tab.c[0];
       if (SPECIES && !(r2 < c.rc2)) continue;
       float U, g, h;
       pair_eval<KIND, false>(r2, c, U, g, h);
@@ -245,7 +251,8 @@ __global__ void __launch_bounds__(256) k_pair_sparse(SparseArgs a, const __grid_
       float r2 = dx * dx;
       r2 = fmaf(dy, dy, r2);
       if (DIM == 3) r2 = fmaf(dz, dz, r2);
-      const PairCoef& c = SPECIES ? sc[__ldg(a.species + i) * JMD_MAX_SPECIES + __ldg(a.species + j)]
+      const PairCoef& c = SPECIES ? sc[sp_clamp(__ldg(a.species + i), tab.nsp) * JMD_MAX_SPECIES +
+                                       sp_clamp(__ldg(a.species + j), tab.nsp)]
                                   : tab.c[0];
       if (r2 < c.rc2 && r2 > 0.f) {
         float U, g, h;
