@@ -194,26 +194,13 @@ def main():
     init, apply = simulate.nve(efn, shift, DT)
     st = init(0, Rt, momenta=torch.tensor(P, device=dev), neighbor=nb)
 
-    def step():
-        nb.update(st.position)
-        apply(st, neighbor=nb)
-
-    for _ in range(max(3, args.warmup)):
-        step()
+    # warm-up: the engine run (also builds and caches its CUDA graph)
+    simulate.run(apply, st, nb, max(3, args.warmup))
     torch.cuda.synchronize()
-    # capture one step in a CUDA graph; replay it K times
-    s = torch.cuda.Stream(dev)
-    s.wait_stream(torch.cuda.current_stream(dev))
-    with torch.cuda.stream(s):
-        step()
-    torch.cuda.current_stream(dev).wait_stream(s)
-    g = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g):
-        step()
-    torch.cuda.synchronize()
-    g.replay()
+    simulate.run(apply, st, nb, args.steps)     # records the graph for K steps
     torch.cuda.synchronize()
     E0 = float(efn.energy_f64(st.position, nb) + quantity._ke_f64(st.momentum))
+    rebuilds0 = 0
     cur = torch.cuda.current_stream(dev)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if world > 1:
@@ -221,8 +208,7 @@ def main():
     torch.cuda.synchronize()
     with Clocks() as clk:
         ev0.record(cur)
-        for _ in range(args.steps):
-            g.replay()
+        simulate.run(apply, st, nb, args.steps)   # exactly K steps, one graph launch
         ev1.record(cur)
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
@@ -235,24 +221,40 @@ def main():
     E1 = float(efn.energy_f64(st.position, nb) + quantity._ke_f64(st.momentum))
     overflow = bool(nb.did_buffer_overflow)
 
-    # dominant kernel alone: the LJ pair-force kernel
+    # dominant kernel alone: the fused step kernel (force + kicks + drift + skin test)
+    import ctypes as _C
     nbar = float(nb.nbr_count.float().mean())
-    f_out = st.force
+    species, pair = efn._resolve(st.position, {})
+    sp = simulate._shift_space(shift, 3)
+    xa = st.position
+    xb = torch.empty((n, 4), dtype=torch.float32, device=dev)[:, :3]
+    xb.copy_(xa)
+    pm = st.momentum.clone()
+    flag = torch.zeros((), dtype=torch.int32, device=dev)
+    L_ = NAT.lib()
+
+    def fused(src, dst):
+        NAT.check(L_.jmd_nve_fused_step(_C.byref(pair), _C.byref(sp), src.data_ptr(), dst.data_ptr(),
+                                        pm.data_ptr(), None, 1.0, None, n, nb.idx.data_ptr(),
+                                        nb.plan.ld, nb.max_occupancy, nb.nbr_count.data_ptr(),
+                                        DT, nb.reference_position.data_ptr(), nb.plan.threshold_sq,
+                                        flag.data_ptr(), NAT.stream_ptr()), 'fused step')
     for _ in range(3):
-        efn.forces(st.position, nb, out=f_out)
+        fused(xa, xb)
     torch.cuda.synchronize()
     reps = 50
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(cur)
-    for _ in range(reps):
-        efn.forces(st.position, nb, out=f_out)
+    for r in range(reps):
+        fused(xa, xb)      # same input each time: identical work per launch
     e1.record(cur)
     torch.cuda.synchronize()
-    pair_ms = e0.elapsed_time(e1) / reps
-    # algorithmic bytes of one force launch: index rows + counts + own position + force row
-    pair_bytes = n * (4 * nbar + 4 + 16 + 16)
+    kern_ms = e0.elapsed_time(e1) / reps
+    # algorithmic bytes of one fused-step launch: Dense index rows (4 B x mean
+    # neighbours), position read + write, momentum read + write, reference read
+    kern_bytes = n * (4 * nbar + 80)
     hbm, src = peaks()
-    achieved = pair_bytes / (pair_ms / 1e3) / 1e9
+    achieved = kern_bytes / (kern_ms / 1e3) / 1e9
     step_bytes = n * (4 * nbar + 96)
 
     # e2e: host pinned buffers through the public API, every step
@@ -261,19 +263,22 @@ def main():
     xh.copy_(st.position)
     ph.copy_(st.momentum)
     e2e_steps = max(5, min(args.steps, 50))
+    simulate.run(apply, st, nb, 1)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         st.position.copy_(xh, non_blocking=True)
         st.momentum.copy_(ph, non_blocking=True)
-        g.replay()
+        simulate.run(apply, st, nb, 1)
         xh.copy_(st.position, non_blocking=True)
         ph.copy_(st.momentum, non_blocking=True)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_value = n * world * e2e_steps / e2e_s
 
-    launches_per_step = 3 + 1 + 7  # kick-drift, pair, kick, skin test, rebuild chain
+    # per step: the fused step kernel + the conditional-set kernel; the rebuild
+    # chain (6 kernels) runs only on rebuild steps
+    launches_per_step = 2
     line = {
         'metric': METRIC, 'value': value, 'unit': 'atom-steps/s', 'n_gpus': world,
         'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_per_step,
@@ -286,7 +291,8 @@ def main():
                    'energy_drift_per_atom': (E1 - E0) / n, 'overflow': overflow},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
                      'frac': achieved / hbm, 'traffic': None, 'peak_source': src,
-                     'kernel': 'k_pair_dense (LJ, Dense)', 'kernel_ms': pair_ms,
+                     'kernel': 'k_dense2 fused NVE step (LJ, Dense, FP32x2)', 'kernel_ms': kern_ms,
+                     'bytes_per_atom': 4 * nbar + 80,
                      'step_algorithmic_GBps': step_bytes * args.steps / (ms / 1e3) / 1e9},
         'e2e': {'value': e2e_value, 'unit': 'atom-steps/s', 'h2d_bytes_per_step': 2 * n * 12,
                 'd2h_bytes_per_step': 2 * n * 12},

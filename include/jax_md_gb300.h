@@ -236,6 +236,83 @@ int jmd_nhc_half_step(const jmd_nhc* c, double* chain,
 int jmd_scale_momentum(float* momentum, int64_t p_stride, int64_t n,
                        int32_t dim, const double* scale, void* stream);
 
+/* ------------------------------------------------------- fused kernels -- */
+
+/* Threads per atom of the float4 Dense pair kernels (4, 8 or 16; default 8). */
+int jmd_set_dense_threads_per_atom(int tpa);
+/* Threads per atom of the generic-stride Dense pair kernel (4, 8, 16, 32). */
+int jmd_set_pair_threads_per_atom(int tpa);
+/* 1: route Dense pair calls through the generic-stride kernel (testing). */
+int jmd_set_pair_generic(int generic);
+
+/* One fused velocity-Verlet step on float4 rows, starting from the
+ * half-kicked state p' = p + dt/2 f_old (simulate.py:227-243):
+ *   f = F(position); p' += dt/2 f; p' += dt/2 f;
+ *   position_next = shift(position, dt p' / m);
+ * and the skin test of position_next against reference_position (ORs 1 into
+ * *rebuild_flag).  The force is not stored.  Dense lists only. */
+int jmd_nve_fused_step(const jmd_pair* pp, const jmd_space* space,
+                       const float* position, float* position_next,
+                       float* momentum, const float* mass, float mass_scalar,
+                       const int32_t* species, int64_t n, const int32_t* idx,
+                       int64_t idx_ld, int64_t idx_width,
+                       const int32_t* nbr_count, float dt,
+                       const float* reference_position, float threshold_sq,
+                       int32_t* rebuild_flag, void* stream);
+
+/* Closing half of velocity_verlet on float4 rows: force = F(position),
+ * momentum += dt/2 force. */
+int jmd_force_kick(const jmd_pair* pp, const jmd_space* space,
+                   const float* position, float* force, float* momentum,
+                   const int32_t* species, int64_t n, const int32_t* idx,
+                   int64_t idx_ld, int64_t idx_width, const int32_t* nbr_count,
+                   float dt, void* stream);
+
+/* ------------------------------------------------------------- engine ---- */
+
+/* A device-resident NVE system with its Dense neighbour list: the state of
+ * the reference's simulation loop body
+ *   nbrs = nbrs.update(state.position); state = apply_fn(state, neighbor=nbrs)
+ * (partition.py:841-854, simulate.py:279-317).  All buffers are float4 rows
+ * (16-byte aligned) owned by the caller; position_alt is scratch of the same
+ * size used to ping-pong positions between fused steps. */
+typedef struct {
+  int64_t n;
+  jmd_space space;
+  float* position;
+  float* position_alt;
+  float* momentum;
+  float* force;
+  const float* mass;          /* [n] or NULL (mass_scalar) */
+  float mass_scalar;
+  const int32_t* species;     /* [n] or NULL */
+  jmd_pair pair;
+  jmd_nlist nlist;            /* format must be JMD_DENSE */
+  int32_t* idx;
+  int64_t idx_ld;
+  int32_t* nbr_count;
+  float* reference_position;
+  uint8_t* error_code;
+  int64_t* occupancy;
+  int32_t* rebuild_flag;      /* device int32, 0 between calls */
+  void* nl_workspace;
+  size_t nl_workspace_bytes;
+  float dt;
+  float threshold_sq;         /* (dr_threshold / 2)^2; < 0: rebuild every step */
+} jmd_nve_system;
+
+/* Runs n_steps NVE steps.  use_graph != 0 records the whole run once per
+ * (system, n_steps) as a CUDA graph in which each step's rebuild chain sits
+ * in a device-side conditional (IF) node set by the skin test, and replays it
+ * on `stream`; use_graph == 0 launches the kernels directly with the rebuild
+ * kernels gated by the device flag.  Neighbour-list overflow is reported in
+ * error_code exactly as jmd_neighbor_list_build does. */
+int jmd_nve_run(const jmd_nve_system* sys, int64_t n_steps, int32_t use_graph,
+                void* stream);
+
+/* Drops every cached graph of the engine. */
+int jmd_engine_clear_cache(void);
+
 #ifdef __cplusplus
 }
 #endif

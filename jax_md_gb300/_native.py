@@ -49,6 +49,18 @@ class Nhc(C.Structure):
                 ('dof', C.c_int32), ('dt', C.c_double), ('tau', C.c_double)]
 
 
+class NveSystem(C.Structure):
+    _fields_ = [('n', C.c_int64), ('space', Space), ('position', C.c_void_p),
+                ('position_alt', C.c_void_p), ('momentum', C.c_void_p), ('force', C.c_void_p),
+                ('mass', C.c_void_p), ('mass_scalar', C.c_float), ('species', C.c_void_p),
+                ('pair', Pair), ('nlist', NList), ('idx', C.c_void_p), ('idx_ld', C.c_int64),
+                ('nbr_count', C.c_void_p), ('reference_position', C.c_void_p),
+                ('error_code', C.c_void_p), ('occupancy', C.c_void_p),
+                ('rebuild_flag', C.c_void_p), ('nl_workspace', C.c_void_p),
+                ('nl_workspace_bytes', C.c_size_t), ('dt', C.c_float),
+                ('threshold_sq', C.c_float)]
+
+
 P = C.c_void_p
 I64 = C.c_int64
 I32 = C.c_int32
@@ -78,6 +90,14 @@ SIGNATURES = {
     'jmd_kinetic_energy': (C.c_int, [P, I64, P, F32, I64, I32, P, P, SZ, P]),
     'jmd_nhc_half_step': (C.c_int, [C.POINTER(Nhc), P, P, I32, P, P]),
     'jmd_scale_momentum': (C.c_int, [P, I64, I64, I32, P, P]),
+    'jmd_set_dense_threads_per_atom': (C.c_int, [C.c_int]),
+    'jmd_set_pair_generic': (C.c_int, [C.c_int]),
+    'jmd_nve_fused_step': (C.c_int, [C.POINTER(Pair), C.POINTER(Space), P, P, P, P, F32, P, I64, P,
+                                     I64, I64, P, F32, P, F32, P, P]),
+    'jmd_force_kick': (C.c_int, [C.POINTER(Pair), C.POINTER(Space), P, P, P, P, I64, P, I64, I64,
+                                 P, F32, P]),
+    'jmd_nve_run': (C.c_int, [C.POINTER(NveSystem), I64, I32, P]),
+    'jmd_engine_clear_cache': (C.c_int, []),
 }
 
 _lib = None

@@ -1,0 +1,227 @@
+// Device-resident NVE runner: the reference's simulation loop
+//   for s in range(n): nbrs = nbrs.update(x); state = apply_fn(state, neighbor=nbrs)
+// (jax_md/partition.py:841-854, jax_md/simulate.py:279-317) with the host
+// taken out of the loop.
+//
+// Per run of n steps:
+//   skin test (x0)          -> conditional rebuild
+//   kick + drift            (p' = p + dt/2 f, x1)        + skin test (x1)
+//   n-1 times:              conditional rebuild;  fused step  x_s -> x_{s+1}
+//                           (F(x_s), both half kicks, drift, skin test)
+//   conditional rebuild;    force + closing half kick at x_n
+// Positions ping-pong between `position` and `position_alt`; the final
+// positions are copied back into `position` when the run ends in the other
+// buffer.
+//
+// Graph mode records this sequence once per (system, n) into a CUDA graph.
+// Each "conditional rebuild" is a one-thread kernel that copies the device
+// rebuild flag into a graph conditional handle (cudaGraphSetConditional) and
+// an IF node whose body is the rebuild chain, so a step without a rebuild
+// costs nothing for the rebuild kernels; the flag itself is cleared by the
+// rebuild's last kernel.  Direct mode launches the same kernels with the
+// rebuild chain gated by the device flag inside each kernel.
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace jmd {
+namespace {
+
+__global__ void k_set_cond(cudaGraphConditionalHandle h, const int32_t* flag) {
+  cudaGraphSetConditional(h, *flag != 0 ? 1u : 0u);
+}
+
+__global__ void k_set_flag(int32_t* flag) { *flag = 1; }
+
+struct GraphPlan {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+std::mutex g_mu;
+std::map<std::string, GraphPlan> g_cache;
+
+int validate_sys(const jmd_nve_system& s) {
+  JMD_REQUIRE(s.n > 0 && s.n < INT32_MAX, "atom count out of range");
+  JMD_REQUIRE(s.space.dim == 2 || s.space.dim == 3, "dim must be 2 or 3");
+  JMD_REQUIRE(s.nlist.format == JMD_DENSE, "the engine runs Dense neighbour lists");
+  JMD_REQUIRE(s.position && s.position_alt && s.momentum && s.force && s.idx &&
+                  s.reference_position && s.error_code && s.occupancy && s.rebuild_flag,
+              "null buffer in jmd_nve_system");
+  JMD_REQUIRE(s.position != s.position_alt, "position_alt must be a separate buffer");
+  for (const void* p : {(const void*)s.position, (const void*)s.position_alt,
+                        (const void*)s.momentum, (const void*)s.force,
+                        (const void*)s.reference_position})
+    JMD_REQUIRE((reinterpret_cast<uintptr_t>(p) % 16) == 0, "float4 rows must be 16-byte aligned");
+  JMD_REQUIRE(s.idx_ld >= s.nlist.max_occupancy && s.idx_ld % 2 == 0, "idx_ld must be even and >= max_occupancy");
+  return JMD_OK;
+}
+
+// One rebuild of the Dense list at positions x (gated by the device flag).
+int rebuild(const jmd_nve_system& s, const float* x, bool gated, cudaStream_t st) {
+  return jmd_neighbor_list_build(&s.nlist, x, 4, s.n, s.idx, s.idx_ld, s.nbr_count, s.occupancy,
+                                 s.error_code, s.reference_position, 4,
+                                 gated ? s.rebuild_flag : nullptr, s.nl_workspace,
+                                 s.nl_workspace_bytes, st);
+}
+
+// Appends "set conditional from flag; IF { rebuild(x) }" to the capture on st.
+int conditional_rebuild(const jmd_nve_system& s, const float* x, cudaStream_t st,
+                        cudaStream_t body_st) {
+  cudaStreamCaptureStatus status;
+  cudaGraph_t graph;
+  JMD_CUDA(cudaStreamGetCaptureInfo(st, &status, nullptr, &graph, nullptr, nullptr, nullptr));
+  if (status != cudaStreamCaptureStatusActive) return fail(JMD_ERR_CUDA, "stream is not capturing");
+  cudaGraphConditionalHandle h;
+  JMD_CUDA(cudaGraphConditionalHandleCreate(&h, graph, 0, cudaGraphCondAssignDefault));
+  k_set_cond<<<1, 1, 0, st>>>(h, s.rebuild_flag);
+  JMD_CUDA(cudaGetLastError());
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  JMD_CUDA(cudaStreamGetCaptureInfo(st, &status, nullptr, &graph, &deps, nullptr, &ndeps));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  JMD_CUDA(cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  JMD_CUDA(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  JMD_CUDA(cudaStreamBeginCaptureToGraph(body_st, body, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal));
+  int rc = rebuild(s, x, true, body_st);
+  cudaGraph_t out;
+  cudaError_t e = cudaStreamEndCapture(body_st, &out);
+  if (rc) return rc;
+  JMD_CUDA(e);
+  return JMD_OK;
+}
+
+// Enqueues the whole run; `graphed` selects conditional nodes vs gated kernels.
+int enqueue_run(const jmd_nve_system& s, int64_t steps, bool graphed, cudaStream_t st,
+                cudaStream_t body_st) {
+  const bool always = s.threshold_sq < 0.f;
+  auto gate = [&](const float* x) -> int {
+    if (always) return rebuild(s, x, false, st);
+    if (graphed) return conditional_rebuild(s, x, st, body_st);
+    return rebuild(s, x, true, st);
+  };
+  const float4* none = nullptr;
+  (void)none;
+  int rc;
+  // update at x0
+  if (!always) {
+    rc = jmd_skin_check(s.position, 4, s.reference_position, 4, s.n, &s.space, s.threshold_sq,
+                        s.rebuild_flag, st);
+    if (rc) return rc;
+  }
+  if ((rc = gate(s.position))) return rc;
+  // first half of step 0: kick + drift + skin test of x1
+  rc = jmd_verlet_kick_drift(s.position, 4, s.momentum, 4, s.force, 4, s.mass, s.mass_scalar,
+                             s.n, &s.space, s.dt, nullptr,
+                             always ? nullptr : s.reference_position, 4,
+                             s.threshold_sq, always ? nullptr : s.rebuild_flag, st);
+  if (rc) return rc;
+  float* cur = s.position;
+  float* nxt = s.position_alt;
+  const int64_t width = s.nlist.max_occupancy;
+  for (int64_t k = 1; k < steps; ++k) {
+    if ((rc = gate(cur))) return rc;
+    rc = jmd_nve_fused_step(&s.pair, &s.space, cur, nxt, s.momentum, s.mass, s.mass_scalar,
+                            s.species, s.n, s.idx, s.idx_ld, width, s.nbr_count, s.dt,
+                            always ? nullptr : s.reference_position, s.threshold_sq,
+                            always ? nullptr : s.rebuild_flag, st);
+    if (rc) return rc;
+    std::swap(cur, nxt);
+  }
+  if ((rc = gate(cur))) return rc;
+  rc = jmd_force_kick(&s.pair, &s.space, cur, s.force, s.momentum, s.species, s.n, s.idx,
+                      s.idx_ld, width, s.nbr_count, s.dt, st);
+  if (rc) return rc;
+  if (cur != s.position) {
+    JMD_CUDA(cudaMemcpyAsync(s.position, cur, sizeof(float4) * (size_t)s.n,
+                             cudaMemcpyDeviceToDevice, st));
+  }
+  return JMD_OK;
+}
+
+std::string plan_key(const jmd_nve_system& s, int64_t steps, int device) {
+  std::string k(reinterpret_cast<const char*>(&s), sizeof(s));
+  k.append(reinterpret_cast<const char*>(&steps), sizeof(steps));
+  k.append(reinterpret_cast<const char*>(&device), sizeof(device));
+  return k;
+}
+
+}  // namespace
+}  // namespace jmd
+
+using namespace jmd;
+
+extern "C" {
+
+int jmd_nve_run(const jmd_nve_system* sys, int64_t n_steps, int32_t use_graph, void* stream) {
+  JMD_REQUIRE(sys != nullptr, "system is null");
+  int e = validate_sys(*sys);
+  if (e) return e;
+  JMD_REQUIRE(n_steps >= 0, "n_steps must be >= 0");
+  if (n_steps == 0) return JMD_OK;
+  cudaStream_t st = as_stream(stream);
+  cudaStreamCaptureStatus cap;
+  JMD_CUDA(cudaStreamIsCapturing(st, &cap));
+  if (!use_graph || cap != cudaStreamCaptureStatusNone) {
+    int rc = enqueue_run(*sys, n_steps, false, st, nullptr);
+    return rc ? rc : check_launch("jmd_nve_run");
+  }
+  int device;
+  JMD_CUDA(cudaGetDevice(&device));
+  std::lock_guard<std::mutex> lock(g_mu);
+  const std::string key = plan_key(*sys, n_steps, device);
+  auto it = g_cache.find(key);
+  if (it == g_cache.end()) {
+    cudaStream_t cs, bs;
+    JMD_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    JMD_CUDA(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
+    GraphPlan plan;
+    cudaError_t ce = cudaGraphCreate(&plan.graph, 0);
+    int rc = JMD_OK;
+    if (ce == cudaSuccess)
+      ce = cudaStreamBeginCaptureToGraph(cs, plan.graph, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+      rc = enqueue_run(*sys, n_steps, true, cs, bs);
+      cudaGraph_t out;
+      cudaError_t ee = cudaStreamEndCapture(cs, &out);
+      if (!rc && ee != cudaSuccess) ce = ee;
+    }
+    if (!rc && ce == cudaSuccess) ce = cudaGraphInstantiate(&plan.exec, plan.graph, 0);
+    cudaStreamDestroy(cs);
+    cudaStreamDestroy(bs);
+    if (rc || ce != cudaSuccess) {
+      if (plan.exec) cudaGraphExecDestroy(plan.exec);
+      if (plan.graph) cudaGraphDestroy(plan.graph);
+      cudaGetLastError();
+      if (rc) return rc;
+      return fail(JMD_ERR_CUDA, std::string("jmd_nve_run graph build: ") + cudaGetErrorString(ce));
+    }
+    it = g_cache.emplace(key, plan).first;
+  }
+  JMD_CUDA(cudaGraphLaunch(it->second.exec, st));
+  return JMD_OK;
+}
+
+int jmd_engine_clear_cache(void) {
+  std::lock_guard<std::mutex> lock(g_mu);
+  for (auto& kv : g_cache) {
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+  }
+  g_cache.clear();
+  return JMD_OK;
+}
+
+}  // extern "C"

@@ -448,6 +448,172 @@ k_search(const float* __restrict__ x, int64_t stride, Bins b, SearchArgs a, int3
   }
 }
 
+// Cell-staged Dense search: one CTA per cell.  The CTA stages the members
+// of the 3^d neighbour cells into shared memory in the reference's candidate
+// order (shift order, slot rotation within each cell), then every warp takes
+// one atom of the centre cell and scans the whole candidate stream in chunks
+// of 64 (two candidates per lane), so lanes stay busy across cell borders and
+// each candidate position is read from global memory once per cell rather
+// than once per atom.  Cells whose stream exceeds the shared-memory budget read
+// the same stream from global memory instead.
+constexpr int kStageMax = 2048;
+
+template <int DIM>
+struct CellStream {
+  int beg[27], cnt[27], split[27], off[28];
+};
+
+template <int DIM>
+__device__ __forceinline__ int stream_index(const CellStream<DIM>& cs, int ns, int t) {
+  // largest k with off[k] <= t
+  int lo = 0, hi = ns - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (cs.off[mid] <= t) lo = mid; else hi = mid - 1;
+  }
+  const int k = lo;
+  const int r = t - cs.off[k];
+  const int c = cs.cnt[k], sp = cs.split[k];
+  int m;
+  if (c <= sp) {
+    m = r;
+  } else {
+    const int l1 = c - sp;
+    m = r < l1 ? sp + r : r - l1;
+  }
+  return cs.beg[k] + m;
+}
+
+template <int DIM, bool WRAP>
+__device__ __forceinline__ void scan_stream(const CellStream<DIM>& cs, int ns, int total,
+                                            bool staged, const float4* __restrict__ spos,
+                                            const int32_t* __restrict__ sid, const Bins& b,
+                                            float4 xi, int i, const SearchArgs& a, int lane,
+                                            int& count, int32_t* row, int64_t row_cap) {
+  const unsigned lt = (1u << lane) - 1u;
+  for (int base = 0; base < total; base += 64) {
+    const int t0 = base + lane, t1 = t0 + 32;
+    bool ok0 = false, ok1 = false;
+    int j0 = 0, j1 = 0;
+    if (t0 < total) {
+      float4 x0, x1;
+      if (staged) {
+        x0 = spos[t0];
+        j0 = sid[t0];
+        if (t1 < total) { x1 = spos[t1]; j1 = sid[t1]; }
+        else { x1 = x0; j1 = j0; }
+      } else {
+        int s0 = stream_index<DIM>(cs, ns, t0);
+        x0 = __ldg(b.sorted_pos + s0);
+        j0 = __ldg(b.sorted_id + s0);
+        if (t1 < total) {
+          int s1 = stream_index<DIM>(cs, ns, t1);
+          x1 = __ldg(b.sorted_pos + s1);
+          j1 = __ldg(b.sorted_id + s1);
+        } else { x1 = x0; j1 = j0; }
+      }
+      float d0, d1;
+      if (WRAP) {
+        d0 = dist2<DIM>(xi, x0, a.geo);
+        d1 = dist2<DIM>(xi, x1, a.geo);
+      } else {
+        float ax = xi.x - x0.x, ay = xi.y - x0.y, az = DIM == 3 ? xi.z - x0.z : 0.f;
+        float bx = xi.x - x1.x, by = xi.y - x1.y, bz = DIM == 3 ? xi.z - x1.z : 0.f;
+        d0 = fmaf(az, az, fmaf(ay, ay, ax * ax));
+        d1 = fmaf(bz, bz, fmaf(by, by, bx * bx));
+      }
+      ok0 = d0 < a.cut2;
+      ok1 = t1 < total && d1 < a.cut2;
+      if (a.mask_self) { ok0 = ok0 && j0 != i; ok1 = ok1 && j1 != i; }
+      if (a.ordered) { ok0 = ok0 && j0 < i; ok1 = ok1 && j1 < i; }
+    }
+    const unsigned m0 = __ballot_sync(0xffffffffu, ok0);
+    const unsigned m1 = __ballot_sync(0xffffffffu, ok1);
+    if (row) {
+      // candidates base..base+31 come before base+32..base+63
+      const int64_t p0 = (int64_t)count + __popc(m0 & lt);
+      if (ok0 && p0 < row_cap) row[p0] = j0;
+      const int64_t p1 = (int64_t)count + __popc(m0) + __popc(m1 & lt);
+      if (ok1 && p1 < row_cap) row[p1] = j1;
+    }
+    count += __popc(m0) + __popc(m1);
+  }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(128)
+k_search_cells(const float* __restrict__ x, int64_t stride, Bins b, SearchArgs a, int32_t* idx,
+               int64_t ld, int32_t* nbr_count, float* ref, int64_t ref_stride,
+               const int32_t* flag) {
+  if (skip(flag)) return;
+  extern __shared__ float4 smem4[];
+  float4* spos = smem4;
+  int32_t* sid = reinterpret_cast<int32_t*>(smem4 + kStageMax);
+  __shared__ CellStream<DIM> cs;
+  const int c = blockIdx.x;
+  const int ns = DIM == 3 ? 27 : 9;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int c0 = c % a.grid.cps[0];
+  const int c1 = (c / a.grid.cps[0]) % a.grid.cps[1];
+  const int c2 = DIM == 3 ? c / (a.grid.cps[0] * a.grid.cps[1]) : 0;
+  if (threadIdx.x < ns) {
+    const int k = threadIdx.x;
+    int sh0, sh1, sh2;
+    if (DIM == 3) { sh0 = k / 9 - 1; sh1 = (k / 3) % 3 - 1; sh2 = k % 3 - 1; }
+    else { sh0 = k / 3 - 1; sh1 = k % 3 - 1; sh2 = 0; }
+    int q0 = c0 + sh0, q1 = c1 + sh1, q2 = c2 + sh2;
+    q0 = q0 < 0 ? q0 + a.grid.cps[0] : (q0 >= a.grid.cps[0] ? q0 - a.grid.cps[0] : q0);
+    q1 = q1 < 0 ? q1 + a.grid.cps[1] : (q1 >= a.grid.cps[1] ? q1 - a.grid.cps[1] : q1);
+    if (DIM == 3) q2 = q2 < 0 ? q2 + a.grid.cps[2] : (q2 >= a.grid.cps[2] ? q2 - a.grid.cps[2] : q2);
+    const int h = q0 + q1 * a.grid.mult[1] + (DIM == 3 ? q2 * a.grid.mult[2] : 0);
+    const int beg = b.start[h], end = b.start[h + 1];
+    cs.beg[k] = beg;
+    cs.cnt[k] = end - beg;
+    cs.split[k] = a.cap - (beg % a.cap);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int o = 0;
+    for (int k = 0; k < ns; ++k) { cs.off[k] = o; o += cs.cnt[k]; }
+    cs.off[ns] = o;
+  }
+  __syncthreads();
+  const int total = cs.off[ns];
+  const bool staged = total <= kStageMax;
+  if (staged) {
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+      const int s = stream_index<DIM>(cs, ns, t);
+      spos[t] = b.sorted_pos[s];
+      sid[t] = b.sorted_id[s];
+    }
+  }
+  __syncthreads();
+  // periodic wrap can only occur for cells on a face of the grid
+  bool edge = a.geo.periodic && (c0 == 0 || c0 == a.grid.cps[0] - 1 || c1 == 0 ||
+                                 c1 == a.grid.cps[1] - 1 ||
+                                 (DIM == 3 && (c2 == 0 || c2 == a.grid.cps[2] - 1)));
+  const int cb = b.start[c], cn = b.start[c + 1] - cb;
+  for (int q = warp; q < cn; q += nw) {
+    const int i = b.sorted_id[cb + q];
+    const float4 xi = b.sorted_pos[cb + q];
+    int32_t* row = idx ? idx + (int64_t)i * ld : nullptr;
+    int count = 0;
+    if (edge)
+      scan_stream<DIM, true>(cs, ns, total, staged, spos, sid, b, xi, i, a, lane, count, row, a.width);
+    else
+      scan_stream<DIM, false>(cs, ns, total, staged, spos, sid, b, xi, i, a, lane, count, row, a.width);
+    if (row) {
+      for (int64_t p = min((int64_t)count, a.width) + lane; p < a.width; p += 32) row[p] = a.n;
+    }
+    if (lane == 0) {
+      if (nbr_count) nbr_count[i] = count;
+      atomicMax(&b.sc->occupancy, (unsigned long long)count);
+      if (count > a.width) atomicOr(&b.sc->flags, (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
+      if (ref) store_row_full<DIM, false>(ref, ref_stride, i, xi);
+    }
+  }
+}
+
 // Copies the raw positions as float4 rows for the all-pairs path.
 template <int DIM, bool VEC4>
 __global__ void k_pack(const float* __restrict__ x, int64_t stride, int n, float4* out,
@@ -576,8 +742,8 @@ int build_impl(const jmd_nlist* nl, const float* x, int64_t stride, int64_t n64,
   if (nl->format == JMD_DENSE) {
     if (n > 0) {
       if (cells)
-        k_search<DIM, true, VEC4, 0><<<sgrid, 256, 0, st>>>(x, stride, b, a, idx, ld, nbr_count,
-                                                            ref, ref_stride, flag, allpos);
+        k_search_cells<DIM><<<(unsigned)c, 128, kStageMax * (sizeof(float4) + sizeof(int32_t)),
+                              st>>>(x, stride, b, a, idx, ld, nbr_count, ref, ref_stride, flag);
       else
         k_search<DIM, false, VEC4, 0><<<sgrid, 256, 0, st>>>(x, stride, b, a, idx, ld, nbr_count,
                                                              ref, ref_stride, flag, allpos);

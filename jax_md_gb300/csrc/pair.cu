@@ -366,6 +366,7 @@ void sparse_kind(int kind, bool species, bool ev, bool v4, bool fv4, const Spars
 }
 
 int g_default_tpa = 8;
+bool g_force_generic = false;
 
 }  // namespace
 
@@ -388,6 +389,11 @@ using namespace jmd;
 extern "C" {
 
 size_t jmd_pair_workspace_bytes(int64_t n) { return pair_ws_bytes(n); }
+
+int jmd_set_pair_generic(int generic) {
+  g_force_generic = generic != 0;
+  return JMD_OK;
+}
 
 int jmd_set_pair_threads_per_atom(int tpa) {
   JMD_REQUIRE(tpa == 4 || tpa == 8 || tpa == 16 || tpa == 32, "threads per atom must be 4, 8, 16 or 32");
@@ -445,7 +451,14 @@ int jmd_pair_forces(const jmd_pair* pp, const jmd_space* space, int32_t format,
     const int tpa = g_default_tpa;
     if (ev && ceil_div(n * tpa, 256) > kMaxPairBlocks)
       return fail(JMD_ERR_UNSUPPORTED, "system too large for the energy reduction");
-    if (n > 0) {
+    const bool fast = !g_force_generic &&
+                      dense2_applicable(position, pos_stride, idx, idx_ld, force, force_stride);
+    if (fast) {
+      int rc = dense2_forces(pp, space, position, species, n, idx, idx_ld, idx_width, nbr_count,
+                             force, energy, per_atom_energy, virial, w.partials, w.counter,
+                             w.totals, st);
+      if (rc) return rc;
+    } else if (n > 0) {
       const bool fv4 = force == nullptr || is_vec4(force, force_stride);
       if (dim == 3) {
         if (v4 && fv4) dispatch_tpa<3, true>(tpa, pp->kind, sp, ev, a, t, st);

@@ -32,6 +32,15 @@ struct PairTable {
 };
 
 PairTable make_pair_table(const jmd_pair& pp);
+int validate_pair(const jmd_pair* pp);
+
+// Packed float4 Dense path (fused.cu).
+bool dense2_applicable(const float* x, int64_t xs, const int32_t* idx, int64_t ld, const float* f,
+                       int64_t fs);
+int dense2_forces(const jmd_pair* pp, const jmd_space* space, const float* x, const int32_t* species,
+                  int64_t n, const int32_t* idx, int64_t ld, int64_t width, const int32_t* cnt,
+                  float* f, double* energy, float* e_atom, double* virial, double* partials,
+                  unsigned int* counter, double* totals, cudaStream_t st);
 
 // 1/x to ~0.5 ulp: hardware approximation plus one Newton step.
 __device__ __forceinline__ float rcp_nr(float x) {

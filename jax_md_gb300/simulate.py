@@ -362,3 +362,81 @@ def nvt_nose_hoover_invariant(energy_fn, state: NVTNoseHooverState, kT, **kwargs
     for r, p, m in zip(c.position[1:], c.momentum[1:], c.mass[1:]):
         E = E + p ** 2 / (2 * m) + kT * r
     return E
+
+
+# ---------------------------------------------------------------------------
+# Device-resident runner
+def _nve_system(st: '_Stepper', state: NVEState, nbrs, alt: torch.Tensor) -> N.NveSystem:
+    e = st.energy_fn
+    if not isinstance(e, smap.PairNeighborListEnergy):
+        raise NotImplementedError('run() needs a neighbour-list energy from jax_md_gb300.energy')
+    if nbrs.format is not partition.Dense or nbrs.plan is None:
+        raise NotImplementedError('run() needs a Dense NeighborList from jax_md_gb300.partition')
+    R, P, F = state.position, state.momentum, state.force
+    for t, name in ((R, 'position'), (P, 'momentum'), (F, 'force')):
+        if t.stride(0) != 4 or t.data_ptr() % 16:
+            raise ValueError(f'state.{name} must be float4 rows (use init_fn of this module)')
+    n, dim = R.shape
+    plan = nbrs.plan
+    species, pair = e._resolve(R, {})
+    s = N.NveSystem()
+    s.n = n
+    s.space = _shift_space(st.shift_fn, dim)
+    s.position = R.data_ptr()
+    s.position_alt = alt.data_ptr()
+    s.momentum = P.data_ptr()
+    s.force = F.data_ptr()
+    mptr, m0 = _mass_ptr(state.mass)
+    s.mass = mptr
+    s.mass_scalar = m0
+    s.species = N.ptr(species)
+    s.pair = pair
+    s.nlist = plan.nl
+    s.idx = nbrs.idx.data_ptr()
+    s.idx_ld = plan.ld
+    s.nbr_count = plan.count.data_ptr()
+    s.reference_position = nbrs.reference_position.data_ptr()
+    s.error_code = nbrs.error.code.data_ptr()
+    s.occupancy = plan.occupancy.data_ptr()
+    s.rebuild_flag = plan.flag.data_ptr()
+    s.nl_workspace = plan.workspace.data_ptr()
+    s.nl_workspace_bytes = plan.workspace.numel()
+    s.dt = st.dt
+    s.threshold_sq = -1.0 if plan.always_rebuild else plan.threshold_sq
+    return s, species
+
+
+def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bool = True,
+        max_reallocations: int = 4):
+    """Runs the reference loop body ``n_steps`` times on the device:
+
+        nbrs = nbrs.update(state.position); state = apply_fn(state, neighbor=nbrs)
+
+    (jax_md/partition.py:841-854) as fused kernels, replayed from a CUDA graph
+    whose per-step rebuild sits in a device-side conditional node.  With
+    ``neighbor_fn``, overflow is handled as the reference's host loop does:
+    the run is repeated from its starting state with a list re-allocated there.
+    Returns (state, neighbor)."""
+    st = apply_fn.stepper
+    if not isinstance(state, NVEState):
+        raise NotImplementedError('run() drives NVE states')
+    snapshot = state.copy() if neighbor_fn is not None else None
+    for attempt in range(max_reallocations + 1):
+        alt = getattr(state, '_alt', None)
+        if alt is None or alt.shape[0] != state.position.shape[0]:
+            alt = torch.empty((state.position.shape[0], 4), dtype=torch.float32,
+                              device=state.position.device)
+            object.__setattr__(state, '_alt', alt)
+        sysd, _species = _nve_system(st, state, neighbor, alt)
+        N.check(N.lib().jmd_nve_run(ctypes.byref(sysd), int(n_steps), 1 if use_graph else 0,
+                                    N.stream_ptr()), 'nve_run')
+        if neighbor_fn is None or not bool(neighbor.did_buffer_overflow):
+            return state, neighbor
+        # overflow: restore the starting state, re-allocate there (with growing
+        # headroom, so a block whose occupancy peaks above the start's fits), repeat
+        state.position.copy_(snapshot.position)
+        state.momentum.copy_(snapshot.momentum)
+        state.force.copy_(snapshot.force)
+        extra = (attempt + 1) * max(1, neighbor.max_occupancy // 8)
+        neighbor = neighbor_fn.allocate(state.position, extra_capacity=extra)
+    raise RuntimeError('neighbour list kept overflowing after re-allocation')

@@ -385,6 +385,29 @@ def pair_terms(spec: PairSpec, r, si=None, sj=None):
     return U * S, dU * S + U * dS, d2U * S + 2 * dU * dS + U * d2S
 
 
+def pair_force_abs_sum(spec: PairSpec, R, nbrs_idx, fmt, box=None):
+    """Per-atom sum over its pairs of |F_ij|: the scale of the rounding error
+    an fp32 force sum can carry (the condition number of the sum)."""
+    R = np.asarray(R, np.float64)
+    N = R.shape[0]
+    if fmt == DENSE:
+        i = np.repeat(np.arange(N), nbrs_idx.shape[1])
+        j = nbrs_idx.reshape(-1)
+    else:
+        j, i = nbrs_idx[0], nbrs_idx[1]
+    m = j < N
+    i, j = i[m], j[m]
+    dR = displacement(R[j], R[i], box)
+    r = np.sqrt((dR * dR).sum(-1))
+    si = spec.species[i] if spec.species is not None else None
+    sj = spec.species[j] if spec.species is not None else None
+    _, dU, _ = pair_terms(spec, r, si, sj)
+    out = np.zeros(N)
+    np.add.at(out, i, np.abs(dU))
+    np.add.at(out, j, np.abs(dU))
+    return out if fmt != DENSE else out / 2
+
+
 def pair_energy_forces(spec: PairSpec, R, nbrs_idx, fmt, box=None,
                        per_particle=False):
     """smap.pair_neighbor_list (jax_md/smap.py:922-979) + grad (quantity.py:58-60).

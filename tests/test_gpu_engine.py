@@ -1,0 +1,120 @@
+"""The fused, graph-replayed NVE runner against the per-step API and the oracle.
+
+The runner (jmd_nve_run) fuses both half kicks, the drift and the skin test
+into the force kernel and gates each step's rebuild with a device-side
+conditional graph node.  Graph and direct launches must agree bit for bit;
+against the per-step API (which checks the skin one step earlier, as the
+reference loop does) and the FP64 oracle, trajectories agree to fp32 accuracy
+over short runs.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import md_oracle as O
+from tests.helpers import LJ_DT, fcc_system, lj_spec
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(cuda, n_cells=6, skin=0.3):
+    from jax_md_gb300 import energy, partition, simulate, space
+    R, P, L = fcc_system(n_cells)
+    disp, shift = space.periodic(L)
+    nfn, efn = energy.lennard_jones_neighbor_list(disp, L, dr_threshold=skin, format=partition.Dense)
+    Rt = torch.tensor(R, device=cuda)
+    nb = nfn.allocate(Rt)
+    init, apply = simulate.nve(efn, shift, LJ_DT)
+    st = init(0, Rt, momenta=torch.tensor(P, device=cuda), neighbor=nb)
+    return R, P, L, nfn, efn, init, apply, st, nb
+
+
+@pytest.mark.parametrize('steps', [1, 2, 7, 40])
+def test_graph_equals_direct(cuda, steps):
+    from jax_md_gb300 import simulate
+    _, _, _, nfn, efn, init, apply, st_a, nb_a = _setup(cuda)
+    _, _, _, nfn2, _, _, apply2, st_b, nb_b = _setup(cuda)
+    simulate.run(apply, st_a, nb_a, steps, use_graph=True)
+    simulate.run(apply2, st_b, nb_b, steps, use_graph=False)
+    torch.cuda.synchronize()
+    assert torch.equal(st_a.position, st_b.position)
+    assert torch.equal(st_a.momentum, st_b.momentum)
+    assert torch.equal(st_a.force, st_b.force)
+    assert torch.equal(nb_a.idx, nb_b.idx)
+    assert int(nb_a.error.code) == int(nb_b.error.code) == 0
+
+
+def test_graph_replay_repeats(cuda):
+    """A cached graph replayed twice equals one direct run of twice the length."""
+    from jax_md_gb300 import simulate
+    _, _, _, _, _, _, apply, st_a, nb_a = _setup(cuda)
+    _, _, _, _, _, _, apply2, st_b, nb_b = _setup(cuda)
+    simulate.run(apply, st_a, nb_a, 10)
+    simulate.run(apply, st_a, nb_a, 10)
+    for _ in range(2):
+        simulate.run(apply2, st_b, nb_b, 10, use_graph=False)
+    torch.cuda.synchronize()
+    assert torch.equal(st_a.position, st_b.position)
+
+
+def test_runner_matches_per_step_api_and_oracle(cuda):
+    from jax_md_gb300 import simulate
+    R, P, L, nfn, efn, init, apply, st, nb = _setup(cuda)
+    _, _, _, nfn2, efn2, init2, apply2, st2, nb2 = _setup(cuda)
+    steps = 40
+    simulate.run(apply, st, nb, steps)
+    for _ in range(steps):
+        nb2 = nb2.update(st2.position)
+        st2 = apply2(st2, neighbor=nb2)
+    torch.cuda.synchronize()
+    box = np.full(3, L)
+    d = O.displacement(st.position.cpu().numpy(), st2.position.cpu().numpy(), box)
+    assert np.abs(d).max() < 1e-5
+    # oracle trajectory
+    spec = lj_spec()
+    nl = O.NeighborListOracle(box, 2.5, 0.3)
+    h = {'nb': nl.allocate(R)}
+
+    def fn(X):
+        h['nb'] = nl.update(X, h['nb'])
+        return O.pair_energy_forces(spec, X, h['nb'].idx, O.DENSE, box)[1]
+    Rd, Pd = R.astype(np.float64), P.astype(np.float64)
+    F = fn(Rd)
+    for _ in range(steps):
+        Rd, Pd, F = O.velocity_verlet(fn, Rd, Pd, F, 1.0, LJ_DT, box)
+    d = O.displacement(st.position.cpu().numpy(), Rd, box)
+    assert np.abs(d).max() < 1e-4
+    assert np.abs(st.force.cpu().numpy() - F).max() < 1e-3
+
+
+def test_always_rebuild_mode(cuda):
+    """dr_threshold = 0 rebuilds every step (partition.py:1141-1144)."""
+    from jax_md_gb300 import simulate
+    R, P, L, nfn, efn, init, apply, st, nb = _setup(cuda, skin=0.0)
+    _, _, _, _, _, _, apply2, st2, nb2 = _setup(cuda, skin=0.0)
+    simulate.run(apply, st, nb, 5)
+    for _ in range(5):
+        nb2 = nb2.update(st2.position)
+        st2 = apply2(st2, neighbor=nb2)
+    torch.cuda.synchronize()
+    d = O.displacement(st.position.cpu().numpy(), st2.position.cpu().numpy(), np.full(3, L))
+    assert np.abs(d).max() < 1e-5
+
+
+def test_overflow_reallocates(cuda):
+    """A list allocated too small overflows; run(neighbor_fn=...) restores and re-allocates."""
+    from jax_md_gb300 import energy, partition, simulate, space
+    R, P, L = fcc_system(6)
+    disp, shift = space.periodic(L)
+    nfn, efn = energy.lennard_jones_neighbor_list(disp, L, dr_threshold=0.3, format=partition.Dense,
+                                                  capacity_multiplier=1.0)
+    Rt = torch.tensor(R, device=cuda)
+    nb = nfn.allocate(Rt)                      # no headroom over the lattice's occupancy
+    init, apply = simulate.nve(efn, shift, LJ_DT)
+    st = init(0, Rt, momenta=3.0 * torch.tensor(P, device=cuda), neighbor=nb)
+    first = nb.max_occupancy
+    st, nb2 = simulate.run(apply, st, nb, 300, neighbor_fn=nfn)
+    torch.cuda.synchronize()
+    assert not bool(nb2.did_buffer_overflow)
+    assert nb2.max_occupancy > first
+    assert torch.isfinite(st.position).all()

@@ -175,3 +175,15 @@ def test_cell_list_buffers_match_oracle(cuda):
         out = torch.zeros(1001, dim)
         out[idf] = pf
         np.testing.assert_array_equal(out[:-1].numpy(), R)
+
+
+def test_crowded_cells_exceed_shared_stage(cuda):
+    """~110 atoms per cell: each cell's candidate stream (>2048) is read from global memory."""
+    box = np.full(3, 9.0, np.float32)
+    R = random_box(3000, 3, box, seed=11)
+    fns, nb, Rt = _gpu_list(R, box, 2.9, 0.05, 0, cuda)
+    onl = O.NeighborListOracle(box, np.float32(2.9), np.float32(0.05), fmt=O.DENSE)
+    onb = onl.allocate(R)
+    assert onb.use_cell_list and nb.cell_list_capacity == onb.cell_list_capacity
+    skip = near_cutoff_pairs(R, box, float(np.float32(np.float32(2.9) + np.float32(0.05))))
+    assert _strict_equal_rows(nb.idx.cpu().numpy(), onb.idx, len(R), skip) == []
