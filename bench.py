@@ -194,6 +194,9 @@ def main():
     init, apply = simulate.nve(efn, shift, DT)
     st = init(0, Rt, momenta=torch.tensor(P, device=dev), neighbor=nb)
 
+    # launch shape: project autotuner (threads per atom of the fused step)
+    from jax_md_gb300 import tune
+    tpa, tpa_ms = tune.autotune_dense(efn, st, nb, shift, DT, use_cache=False)
     # warm-up: the engine run (also builds and caches its CUDA graph)
     simulate.run(apply, st, nb, max(3, args.warmup))
     torch.cuda.synchronize()
@@ -288,6 +291,7 @@ def main():
                                'r_onset=2.0 skin=0.3 dt=0.005 NVE Dense, replicas only',
                    'l2': 'inputs larger than L2 (neighbour rows ~%d MB)' % int(n * 4 * nbar / 1e6),
                    'mean_neighbors': nbar, 'max_occupancy': nb.max_occupancy,
+                   'threads_per_atom': tpa, 'tpa_ms': {str(k): v for k, v in tpa_ms.items()},
                    'energy_drift_per_atom': (E1 - E0) / n, 'overflow': overflow},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
                      'frac': achieved / hbm, 'traffic': None, 'peak_source': src,

@@ -5,7 +5,8 @@
  * strides and sizes, and a CUDA stream (`cudaStream_t`, passed here as
  * `void*` so this header needs no CUDA include).  All buffers are owned by the
  * caller.  Functions that need scratch memory take a caller-provided workspace
- * and a `*_workspace_bytes` query.  Nothing here synchronises the stream, so
+ * and a `*_workspace_bytes` query; its contents need not be initialised, and
+ * calls that share one workspace must not overlap on the GPU.  Nothing here synchronises the stream, so
  * every call is stream-ordered and may be captured into a CUDA graph.
  *
  * Return value: JMD_OK (0) or a JMD_ERR_* code for argument / launch errors;

@@ -26,7 +26,7 @@
 #include <string>
 #include <vector>
 
-#include "common.cuh"
+#include "pair.cuh"
 
 namespace jmd {
 namespace {
@@ -154,6 +154,8 @@ std::string plan_key(const jmd_nve_system& s, int64_t steps, int device) {
   std::string k(reinterpret_cast<const char*>(&s), sizeof(s));
   k.append(reinterpret_cast<const char*>(&steps), sizeof(steps));
   k.append(reinterpret_cast<const char*>(&device), sizeof(device));
+  const int tpa = dense_tpa();  // the launch shape is baked into the graph
+  k.append(reinterpret_cast<const char*>(&tpa), sizeof(tpa));
   return k;
 }
 

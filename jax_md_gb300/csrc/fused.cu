@@ -66,6 +66,20 @@ __device__ __forceinline__ T gsum(T v) {
 
 __device__ __forceinline__ int spc(int s, int nsp) { return s < 0 ? 0 : (s >= nsp ? nsp - 1 : s); }
 
+// Read-only float4 gather that asks L2 to keep the line (evict_last): the
+// positions are re-gathered ~n_neighbours times per step while the index rows
+// stream through once (those use evict-first loads).
+__device__ __forceinline__ float4 ldg_keep(const float4* p) {
+  float4 r;
+  asm volatile(
+      "{\n\t.reg .b64 pol;\n\t"
+      "createpolicy.fractional.L2::evict_last.b64 pol, 1.0;\n\t"
+      "ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], pol;\n\t}"
+      : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+      : "l"(p));
+  return r;
+}
+
 template <int DIM>
 __device__ __forceinline__ bool interior(const float4& x, const Geo& g, float m) {
   if (!g.periodic) return true;
@@ -99,24 +113,20 @@ k_dense2(D2Args a, const __grid_constant__ PairTable tab) {
     const bool inner = interior<DIM>(xi, a.geo, a.margin);
     const float rc2m = tab.rc2_max;
     const Coef2 c0 = coef2(tab.c[0]);
-    for (int k = 2 * sub; k < end; k += 2 * TPA) {
-      const int2 jj = __ldcs(reinterpret_cast<const int2*>(row + k));
+    // One packed step over the entries k, k+1 whose ids and positions are loaded.
+    auto body = [&](int2 jj, int k, const float4& b0, const float4& b1) {
       const bool v1 = k + 1 < end;
-      int j0 = jj.x, j1 = v1 ? jj.y : jj.x;
       bool ok0 = true, ok1 = v1;
+      int j0 = jj.x, j1 = jj.y;
       if (!CNT) {
         ok0 = (unsigned)j0 < (unsigned)a.n;
         ok1 = ok1 && (unsigned)j1 < (unsigned)a.n;
-        j0 = ok0 ? j0 : atom;
-        j1 = ok1 ? j1 : atom;
       }
-      const float4 b0 = __ldg(a.x + j0);
-      const float4 b1 = __ldg(a.x + j1);
       float2 dx = sub2(xx, f2(b0.x, b1.x));
       float2 dy = sub2(xy, f2(b0.y, b1.y));
       float2 dz = DIM == 3 ? sub2(xz, f2(b0.z, b1.z)) : f2s(0.f);
       if (!inner) {
-        // exact minimum image, element by element (rare path)
+        // exact minimum image, element by element (atoms near a periodic face)
         float ex, ey, ez;
         displacement<DIM>(xi, b0, a.geo, ex, ey, ez);
         dx.x = ex; dy.x = ey; dz.x = ez;
@@ -128,16 +138,16 @@ k_dense2(D2Args a, const __grid_constant__ PairTable tab) {
       if (DIM == 3) r2 = fma2(dz, dz, r2);
       Coef2 c;
       if (SPECIES) {
-        const PairCoef& p0 = sc[si * JMD_MAX_SPECIES + spc(__ldg(a.species + j0), tab.nsp)];
-        const PairCoef& p1 = sc[si * JMD_MAX_SPECIES + spc(__ldg(a.species + j1), tab.nsp)];
-        c = coef2(p0, p1);
+        const int sj0 = ok0 ? spc(__ldg(a.species + j0), tab.nsp) : 0;
+        const int sj1 = ok1 ? spc(__ldg(a.species + j1), tab.nsp) : 0;
+        c = coef2(sc[si * JMD_MAX_SPECIES + sj0], sc[si * JMD_MAX_SPECIES + sj1]);
       } else {
         c = c0;
       }
       const float rc0 = SPECIES ? c.rc2.x : rc2m, rc1 = SPECIES ? c.rc2.y : rc2m;
       const bool m0 = ok0 && r2.x < rc0 && r2.x > 0.f;
       const bool m1 = ok1 && r2.y < rc1 && r2.y > 0.f;
-      if (!(m0 || m1)) continue;
+      if (!(m0 || m1)) return;
       const float2 r2s = f2(m0 ? r2.x : 1.f, m1 ? r2.y : 1.f);
       float2 U, g;
       pair_eval2<KIND, EV>(r2s, c, U, g);
@@ -164,6 +174,52 @@ k_dense2(D2Args a, const __grid_constant__ PairTable tab) {
           w3 = fma2(gx, dy, w3);
         }
       }
+    };
+    // Ids that cannot be gathered (padding, sentinels) are replaced by the atom
+    // itself: its position is at distance 0 and the pair is masked.
+    auto fix = [&](int2 jj, int k) -> int2 {
+      if (!(k + 1 < end)) jj.y = atom;
+      if (!CNT) {
+        if ((unsigned)jj.x >= (unsigned)a.n) jj.x = atom;
+        if ((unsigned)jj.y >= (unsigned)a.n) jj.y = atom;
+      }
+      return jj;
+    };
+    // Software pipeline: every id of this lane's slice (up to IT pairs) is
+    // loaded up front, and the neighbour positions of slot t+1 are in flight
+    // while slot t is evaluated.
+    constexpr int IT = TPA == 4 ? 16 : (TPA == 8 ? 8 : 4);
+    int2 ids[IT];
+#pragma unroll
+    for (int t = 0; t < IT; ++t) {
+      const int k = 2 * sub + t * 2 * TPA;
+      ids[t] = k < end ? fix(__ldcs(reinterpret_cast<const int2*>(row + k)), k)
+                       : make_int2(atom, atom);
+    }
+    float4 c0p = make_float4(0.f, 0.f, 0.f, 0.f), c1p = c0p;
+    if (2 * sub < end) {
+      c0p = ldg_keep(a.x + ids[0].x);
+      c1p = ldg_keep(a.x + ids[0].y);
+    }
+#pragma unroll
+    for (int t = 0; t < IT; ++t) {
+      const int k = 2 * sub + t * 2 * TPA;
+      if (k >= end) break;
+      float4 n0 = c0p, n1 = c1p;
+      if (t + 1 < IT && k + 2 * TPA < end) {
+        n0 = ldg_keep(a.x + ids[t + 1].x);
+        n1 = ldg_keep(a.x + ids[t + 1].y);
+      }
+      body(ids[t], k, c0p, c1p);
+      c0p = n0;
+      c1p = n1;
+    }
+    // rows longer than the prefetched slice
+    for (int k = 2 * sub + IT * 2 * TPA; k < end; k += 2 * TPA) {
+      const int2 jj = fix(__ldcs(reinterpret_cast<const int2*>(row + k)), k);
+      const float4 b0 = ldg_keep(a.x + jj.x);
+      const float4 b1 = ldg_keep(a.x + jj.y);
+      body(jj, k, b0, b1);
     }
   }
   float fx = -gsum<TPA>(ax.x + ax.y);
@@ -274,6 +330,8 @@ void launch_mode(int dim, int tpa, int kind, bool sp, bool cnt, const D2Args& a,
 int g_tpa2 = 8;
 
 }  // namespace
+
+int dense_tpa() { return g_tpa2; }
 
 // Shared with pair.cu: true when the float4 / packed path applies.
 bool dense2_applicable(const float* x, int64_t xs, const int32_t* idx, int64_t ld, const float* f,

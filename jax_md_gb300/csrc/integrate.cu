@@ -295,6 +295,7 @@ int jmd_kinetic_energy(const float* momentum, int64_t p_stride, const float* mas
   }
   int64_t gr = ceil_div(n, 256);
   if (gr > kMaxReduceBlocks) return fail(JMD_ERR_UNSUPPORTED, "system too large");
+  JMD_CUDA(cudaMemsetAsync(w.counter, 0, sizeof(unsigned int), st));
   if (dim == 3) k_ke<3><<<(unsigned)gr, 256, 0, st>>>(momentum, p_stride, mass, mass_scalar, (int)n, w.partials, w.counter, out);
   else k_ke<2><<<(unsigned)gr, 256, 0, st>>>(momentum, p_stride, mass, mass_scalar, (int)n, w.partials, w.counter, out);
   return check_launch("jmd_kinetic_energy");

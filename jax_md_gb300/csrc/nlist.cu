@@ -456,7 +456,7 @@ k_search(const float* __restrict__ x, int64_t stride, Bins b, SearchArgs a, int3
 // each candidate position is read from global memory once per cell rather
 // than once per atom.  Cells whose stream exceeds the shared-memory budget read
 // the same stream from global memory instead.
-constexpr int kStageMax = 2048;
+constexpr int kStageMax = 1024;
 
 template <int DIM>
 struct CellStream {
@@ -484,59 +484,81 @@ __device__ __forceinline__ int stream_index(const CellStream<DIM>& cs, int ns, i
   return cs.beg[k] + m;
 }
 
+// Tests one staged candidate (position, id) against two centre atoms with
+// packed FP32x2 arithmetic; exact minimum image for cells on a periodic face.
 template <int DIM, bool WRAP>
-__device__ __forceinline__ void scan_stream(const CellStream<DIM>& cs, int ns, int total,
-                                            bool staged, const float4* __restrict__ spos,
-                                            const int32_t* __restrict__ sid, const Bins& b,
-                                            float4 xi, int i, const SearchArgs& a, int lane,
-                                            int& count, int32_t* row, int64_t row_cap) {
+__device__ __forceinline__ void test2(const float4& xa, const float4& xb, const float4& c,
+                                      const SearchArgs& a, float& d0, float& d1) {
+  float2 dx = __ffma2_rn(make_float2(c.x, c.x), make_float2(-1.f, -1.f), make_float2(xa.x, xb.x));
+  float2 dy = __ffma2_rn(make_float2(c.y, c.y), make_float2(-1.f, -1.f), make_float2(xa.y, xb.y));
+  float2 dz = make_float2(0.f, 0.f);
+  if (DIM == 3)
+    dz = __ffma2_rn(make_float2(c.z, c.z), make_float2(-1.f, -1.f), make_float2(xa.z, xb.z));
+  if (WRAP) {
+    bool w = fabsf(dx.x) > a.geo.halfL[0] || fabsf(dx.y) > a.geo.halfL[0] ||
+             fabsf(dy.x) > a.geo.halfL[1] || fabsf(dy.y) > a.geo.halfL[1];
+    if (DIM == 3) w = w || fabsf(dz.x) > a.geo.halfL[2] || fabsf(dz.y) > a.geo.halfL[2];
+    if (w) {
+      d0 = dist2<DIM>(xa, c, a.geo);
+      d1 = dist2<DIM>(xb, c, a.geo);
+      return;
+    }
+  }
+  float2 r2 = __fmul2_rn(dx, dx);
+  r2 = __ffma2_rn(dy, dy, r2);
+  if (DIM == 3) r2 = __ffma2_rn(dz, dz, r2);
+  d0 = r2.x;
+  d1 = r2.y;
+}
+
+// Scans the cell's candidate stream for the centre atoms ia / ib (ib < 0: none)
+// and appends hits to their rows in stream order.  Lanes own candidates.
+template <int DIM, bool WRAP, bool ORDERED>
+__device__ __forceinline__ void scan_pair(const CellStream<DIM>& cs, int ns, int total,
+                                          bool staged, const float4* __restrict__ spos,
+                                          const Bins& b, int ia, float4 xa, int ib, float4 xb,
+                                          const SearchArgs& a, int lane, int& ca, int& cb,
+                                          int32_t* ra, int32_t* rb, int64_t row_cap) {
   const unsigned lt = (1u << lane) - 1u;
-  for (int base = 0; base < total; base += 64) {
-    const int t0 = base + lane, t1 = t0 + 32;
-    bool ok0 = false, ok1 = false;
-    int j0 = 0, j1 = 0;
-    if (t0 < total) {
-      float4 x0, x1;
+  for (int base = 0; base < total; base += 32) {
+    const int t = base + lane;
+    bool oka = false, okb = false;
+    int j = 0;
+    if (t < total) {
+      float4 c;
       if (staged) {
-        x0 = spos[t0];
-        j0 = sid[t0];
-        if (t1 < total) { x1 = spos[t1]; j1 = sid[t1]; }
-        else { x1 = x0; j1 = j0; }
+        c = spos[t];
       } else {
-        int s0 = stream_index<DIM>(cs, ns, t0);
-        x0 = __ldg(b.sorted_pos + s0);
-        j0 = __ldg(b.sorted_id + s0);
-        if (t1 < total) {
-          int s1 = stream_index<DIM>(cs, ns, t1);
-          x1 = __ldg(b.sorted_pos + s1);
-          j1 = __ldg(b.sorted_id + s1);
-        } else { x1 = x0; j1 = j0; }
+        const int s = stream_index<DIM>(cs, ns, t);
+        c = __ldg(b.sorted_pos + s);
+        c.w = __int_as_float(__ldg(b.sorted_id + s));
       }
+      j = __float_as_int(c.w);
       float d0, d1;
-      if (WRAP) {
-        d0 = dist2<DIM>(xi, x0, a.geo);
-        d1 = dist2<DIM>(xi, x1, a.geo);
-      } else {
-        float ax = xi.x - x0.x, ay = xi.y - x0.y, az = DIM == 3 ? xi.z - x0.z : 0.f;
-        float bx = xi.x - x1.x, by = xi.y - x1.y, bz = DIM == 3 ? xi.z - x1.z : 0.f;
-        d0 = fmaf(az, az, fmaf(ay, ay, ax * ax));
-        d1 = fmaf(bz, bz, fmaf(by, by, bx * bx));
+      test2<DIM, WRAP>(xa, xb, c, a, d0, d1);
+      oka = d0 < a.cut2;
+      okb = ib >= 0 && d1 < a.cut2;
+      if (a.mask_self) {
+        oka = oka && j != ia;
+        okb = okb && j != ib;
       }
-      ok0 = d0 < a.cut2;
-      ok1 = t1 < total && d1 < a.cut2;
-      if (a.mask_self) { ok0 = ok0 && j0 != i; ok1 = ok1 && j1 != i; }
-      if (a.ordered) { ok0 = ok0 && j0 < i; ok1 = ok1 && j1 < i; }
+      if (ORDERED) {
+        oka = oka && j < ia;
+        okb = okb && j < ib;
+      }
     }
-    const unsigned m0 = __ballot_sync(0xffffffffu, ok0);
-    const unsigned m1 = __ballot_sync(0xffffffffu, ok1);
-    if (row) {
-      // candidates base..base+31 come before base+32..base+63
-      const int64_t p0 = (int64_t)count + __popc(m0 & lt);
-      if (ok0 && p0 < row_cap) row[p0] = j0;
-      const int64_t p1 = (int64_t)count + __popc(m0) + __popc(m1 & lt);
-      if (ok1 && p1 < row_cap) row[p1] = j1;
+    const unsigned ma = __ballot_sync(0xffffffffu, oka);
+    const unsigned mb = __ballot_sync(0xffffffffu, okb);
+    if (ra) {
+      const int64_t pa = (int64_t)ca + __popc(ma & lt);
+      if (oka && pa < row_cap) ra[pa] = j;
     }
-    count += __popc(m0) + __popc(m1);
+    if (rb) {
+      const int64_t pb = (int64_t)cb + __popc(mb & lt);
+      if (okb && pb < row_cap) rb[pb] = j;
+    }
+    ca += __popc(ma);
+    cb += __popc(mb);
   }
 }
 
@@ -546,9 +568,7 @@ k_search_cells(const float* __restrict__ x, int64_t stride, Bins b, SearchArgs a
                int64_t ld, int32_t* nbr_count, float* ref, int64_t ref_stride,
                const int32_t* flag) {
   if (skip(flag)) return;
-  extern __shared__ float4 smem4[];
-  float4* spos = smem4;
-  int32_t* sid = reinterpret_cast<int32_t*>(smem4 + kStageMax);
+  extern __shared__ float4 spos[];  // kStageMax candidates: xyz + id (as the w bits)
   __shared__ CellStream<DIM> cs;
   const int c = blockIdx.x;
   const int ns = DIM == 3 ? 27 : 9;
@@ -583,33 +603,43 @@ k_search_cells(const float* __restrict__ x, int64_t stride, Bins b, SearchArgs a
   if (staged) {
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
       const int s = stream_index<DIM>(cs, ns, t);
-      spos[t] = b.sorted_pos[s];
-      sid[t] = b.sorted_id[s];
+      float4 v = b.sorted_pos[s];
+      v.w = __int_as_float(b.sorted_id[s]);
+      spos[t] = v;
     }
   }
   __syncthreads();
-  // periodic wrap can only occur for cells on a face of the grid
-  bool edge = a.geo.periodic && (c0 == 0 || c0 == a.grid.cps[0] - 1 || c1 == 0 ||
-                                 c1 == a.grid.cps[1] - 1 ||
-                                 (DIM == 3 && (c2 == 0 || c2 == a.grid.cps[2] - 1)));
-  const int cb = b.start[c], cn = b.start[c + 1] - cb;
-  for (int q = warp; q < cn; q += nw) {
-    const int i = b.sorted_id[cb + q];
-    const float4 xi = b.sorted_pos[cb + q];
-    int32_t* row = idx ? idx + (int64_t)i * ld : nullptr;
-    int count = 0;
-    if (edge)
-      scan_stream<DIM, true>(cs, ns, total, staged, spos, sid, b, xi, i, a, lane, count, row, a.width);
+  // Positions inside the box cannot wrap for cells off the faces; the wrap
+  // test still runs there (cheaply) so positions at exactly L stay exact.
+  const int cb0 = b.start[c], cn = b.start[c + 1] - cb0;
+  for (int q = 2 * warp; q < cn; q += 2 * nw) {
+    const int ia = b.sorted_id[cb0 + q];
+    const float4 xa = b.sorted_pos[cb0 + q];
+    const bool two = q + 1 < cn;
+    const int ib = two ? b.sorted_id[cb0 + q + 1] : -1;
+    const float4 xb = two ? b.sorted_pos[cb0 + q + 1] : xa;
+    int32_t* ra = idx ? idx + (int64_t)ia * ld : nullptr;
+    int32_t* rb = (idx && two) ? idx + (int64_t)ib * ld : nullptr;
+    int na = 0, nb = 0;
+    if (a.geo.periodic)
+      scan_pair<DIM, true, false>(cs, ns, total, staged, spos, b, ia, xa, ib, xb, a, lane, na, nb,
+                                  ra, rb, a.width);
     else
-      scan_stream<DIM, false>(cs, ns, total, staged, spos, sid, b, xi, i, a, lane, count, row, a.width);
-    if (row) {
-      for (int64_t p = min((int64_t)count, a.width) + lane; p < a.width; p += 32) row[p] = a.n;
-    }
+      scan_pair<DIM, false, false>(cs, ns, total, staged, spos, b, ia, xa, ib, xb, a, lane, na, nb,
+                                   ra, rb, a.width);
+    if (ra) for (int64_t p = min((int64_t)na, a.width) + lane; p < a.width; p += 32) ra[p] = a.n;
+    if (rb) for (int64_t p = min((int64_t)nb, a.width) + lane; p < a.width; p += 32) rb[p] = a.n;
     if (lane == 0) {
-      if (nbr_count) nbr_count[i] = count;
-      atomicMax(&b.sc->occupancy, (unsigned long long)count);
-      if (count > a.width) atomicOr(&b.sc->flags, (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
-      if (ref) store_row_full<DIM, false>(ref, ref_stride, i, xi);
+      if (nbr_count) nbr_count[ia] = na;
+      atomicMax(&b.sc->occupancy, (unsigned long long)na);
+      if (na > a.width) atomicOr(&b.sc->flags, (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
+      if (ref) store_row_full<DIM, false>(ref, ref_stride, ia, xa);
+      if (two) {
+        if (nbr_count) nbr_count[ib] = nb;
+        atomicMax(&b.sc->occupancy, (unsigned long long)nb);
+        if (nb > a.width) atomicOr(&b.sc->flags, (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
+        if (ref) store_row_full<DIM, false>(ref, ref_stride, ib, xb);
+      }
     }
   }
 }
@@ -742,8 +772,8 @@ int build_impl(const jmd_nlist* nl, const float* x, int64_t stride, int64_t n64,
   if (nl->format == JMD_DENSE) {
     if (n > 0) {
       if (cells)
-        k_search_cells<DIM><<<(unsigned)c, 128, kStageMax * (sizeof(float4) + sizeof(int32_t)),
-                              st>>>(x, stride, b, a, idx, ld, nbr_count, ref, ref_stride, flag);
+        k_search_cells<DIM><<<(unsigned)c, 128, kStageMax * sizeof(float4), st>>>(
+            x, stride, b, a, idx, ld, nbr_count, ref, ref_stride, flag);
       else
         k_search<DIM, false, VEC4, 0><<<sgrid, 256, 0, st>>>(x, stride, b, a, idx, ld, nbr_count,
                                                              ref, ref_stride, flag, allpos);

@@ -424,6 +424,9 @@ int jmd_pair_forces(const jmd_pair* pp, const jmd_space* space, int32_t format,
   w.counter = cv.take<unsigned int>(1);
   w.totals = cv.take<double>(8);
   if (ev && !cv.ok()) return fail(JMD_ERR_WORKSPACE, "pair workspace too small");
+  // the grid reduction needs a zero block counter; the workspace may hold
+  // anything (callers pass uninitialised scratch)
+  if (ev) JMD_CUDA(cudaMemsetAsync(w.counter, 0, sizeof(unsigned int), st));
   PairTable t = make_pair_table(*pp);
   const bool sp = pp->n_species > 0;
   const int dim = space->dim;

@@ -35,6 +35,7 @@ PairTable make_pair_table(const jmd_pair& pp);
 int validate_pair(const jmd_pair* pp);
 
 // Packed float4 Dense path (fused.cu).
+int dense_tpa();
 bool dense2_applicable(const float* x, int64_t xs, const int32_t* idx, int64_t ld, const float* f,
                        int64_t fs);
 int dense2_forces(const jmd_pair* pp, const jmd_space* space, const float* x, const int32_t* species,
