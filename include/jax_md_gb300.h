@@ -311,6 +311,54 @@ typedef struct {
 int jmd_nve_run(const jmd_nve_system* sys, int64_t n_steps, int32_t use_graph,
                 void* stream);
 
+/* Spatial sort (cell order) of float4 per-atom state, the reordering that
+ * keeps neighbour gathers coalesced.  Bins `position` on nl's grid (stable
+ * counting sort, the order of partition.py:425-447) and permutes position,
+ * momentum, optional force and species, and `perm` (which maps sorted index to
+ * the caller's atom id) in place, through the scratch buffers (float4
+ * scratch4a/b, int32 scratch_i_a/b, each [n]).  rebuild_flag gates it like
+ * jmd_neighbor_list_build (and is not cleared). */
+int jmd_sort_by_cell(const jmd_nlist* nl, float* position, float* momentum,
+                     float* force, int32_t* species, int32_t* perm, int64_t n,
+                     float* scratch4a, float* scratch4b, int32_t* scratch_i_a,
+                     int32_t* scratch_i_b, int32_t* rebuild_flag,
+                     void* workspace, size_t workspace_bytes, void* stream);
+
+/* Engine-private state of a spatially sorted run: the system's atoms held in
+ * cell order (re-sorted at every rebuild) with their own Dense list in sorted
+ * ids.  Every buffer is [n] rows (float4 or int32) owned by the caller. */
+typedef struct {
+  float* position_a;
+  float* position_b;
+  float* momentum;
+  float* force;
+  float* reference_position;
+  float* scratch4a;
+  float* scratch4b;
+  int32_t* species;           /* NULL when the system has no species */
+  int32_t* perm;              /* sorted index -> caller atom id */
+  int32_t* scratch_i_a;
+  int32_t* scratch_i_b;
+  int32_t* idx;               /* [n, idx_ld] Dense list in sorted ids */
+  int64_t idx_ld;
+  int32_t* nbr_count;
+  uint8_t* error_code;
+  int64_t* occupancy;
+  int32_t* rebuild_flag;
+  void* workspace;
+  size_t workspace_bytes;
+} jmd_sorted_state;
+
+/* jmd_nve_run with the atoms kept in cell order inside the run: on entry the
+ * caller's state is copied in and sorted, the steps run on the sorted copy
+ * (each rebuild re-sorts it), and on exit positions, momenta, forces and the
+ * reference positions go back to the caller's order and the caller's Dense
+ * list is rebuilt there (in the reference's entry order).  Requires a scalar
+ * mass.  Overflow bits of the private list are OR-ed into the caller's
+ * error_code. */
+int jmd_nve_run_sorted(const jmd_nve_system* sys, const jmd_sorted_state* sorted,
+                       int64_t n_steps, int32_t use_graph, void* stream);
+
 /* Drops every cached graph of the engine. */
 int jmd_engine_clear_cache(void);
 

@@ -61,6 +61,17 @@ class NveSystem(C.Structure):
                 ('threshold_sq', C.c_float)]
 
 
+class SortedState(C.Structure):
+    _fields_ = [('position_a', C.c_void_p), ('position_b', C.c_void_p), ('momentum', C.c_void_p),
+                ('force', C.c_void_p), ('reference_position', C.c_void_p),
+                ('scratch4a', C.c_void_p), ('scratch4b', C.c_void_p), ('species', C.c_void_p),
+                ('perm', C.c_void_p), ('scratch_i_a', C.c_void_p), ('scratch_i_b', C.c_void_p),
+                ('idx', C.c_void_p), ('idx_ld', C.c_int64), ('nbr_count', C.c_void_p),
+                ('error_code', C.c_void_p), ('occupancy', C.c_void_p),
+                ('rebuild_flag', C.c_void_p), ('workspace', C.c_void_p),
+                ('workspace_bytes', C.c_size_t)]
+
+
 P = C.c_void_p
 I64 = C.c_int64
 I32 = C.c_int32
@@ -98,6 +109,8 @@ SIGNATURES = {
                                  P, F32, P]),
     'jmd_nve_run': (C.c_int, [C.POINTER(NveSystem), I64, I32, P]),
     'jmd_engine_clear_cache': (C.c_int, []),
+    'jmd_sort_by_cell': (C.c_int, [C.POINTER(NList), P, P, P, P, P, I64, P, P, P, P, P, P, SZ, P]),
+    'jmd_nve_run_sorted': (C.c_int, [C.POINTER(NveSystem), C.POINTER(SortedState), I64, I32, P]),
 }
 
 _lib = None

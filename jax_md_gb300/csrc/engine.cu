@@ -69,16 +69,16 @@ int rebuild(const jmd_nve_system& s, const float* x, bool gated, cudaStream_t st
                                  s.nl_workspace_bytes, st);
 }
 
-// Appends "set conditional from flag; IF { rebuild(x) }" to the capture on st.
-int conditional_rebuild(const jmd_nve_system& s, const float* x, cudaStream_t st,
-                        cudaStream_t body_st) {
+// Appends "set conditional from flag; IF { body(body_st) }" to the capture on st.
+template <typename Body>
+int conditional(const int32_t* rebuild_flag, Body body, cudaStream_t st, cudaStream_t body_st) {
   cudaStreamCaptureStatus status;
   cudaGraph_t graph;
   JMD_CUDA(cudaStreamGetCaptureInfo(st, &status, nullptr, &graph, nullptr, nullptr, nullptr));
   if (status != cudaStreamCaptureStatusActive) return fail(JMD_ERR_CUDA, "stream is not capturing");
   cudaGraphConditionalHandle h;
   JMD_CUDA(cudaGraphConditionalHandleCreate(&h, graph, 0, cudaGraphCondAssignDefault));
-  k_set_cond<<<1, 1, 0, st>>>(h, s.rebuild_flag);
+  k_set_cond<<<1, 1, 0, st>>>(h, rebuild_flag);
   JMD_CUDA(cudaGetLastError());
   const cudaGraphNode_t* deps = nullptr;
   size_t ndeps = 0;
@@ -90,11 +90,11 @@ int conditional_rebuild(const jmd_nve_system& s, const float* x, cudaStream_t st
   cp.conditional.size = 1;
   cudaGraphNode_t node;
   JMD_CUDA(cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &cp));
-  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  cudaGraph_t body_graph = cp.conditional.phGraph_out[0];
   JMD_CUDA(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
-  JMD_CUDA(cudaStreamBeginCaptureToGraph(body_st, body, nullptr, nullptr, 0,
+  JMD_CUDA(cudaStreamBeginCaptureToGraph(body_st, body_graph, nullptr, nullptr, 0,
                                          cudaStreamCaptureModeThreadLocal));
-  int rc = rebuild(s, x, true, body_st);
+  int rc = body(body_st);
   cudaGraph_t out;
   cudaError_t e = cudaStreamEndCapture(body_st, &out);
   if (rc) return rc;
@@ -108,7 +108,9 @@ int enqueue_run(const jmd_nve_system& s, int64_t steps, bool graphed, cudaStream
   const bool always = s.threshold_sq < 0.f;
   auto gate = [&](const float* x) -> int {
     if (always) return rebuild(s, x, false, st);
-    if (graphed) return conditional_rebuild(s, x, st, body_st);
+    if (graphed)
+      return conditional(s.rebuild_flag, [&](cudaStream_t b) { return rebuild(s, x, true, b); }, st,
+                         body_st);
     return rebuild(s, x, true, st);
   };
   const float4* none = nullptr;
@@ -150,6 +152,128 @@ int enqueue_run(const jmd_nve_system& s, int64_t steps, bool graphed, cudaStream
   return JMD_OK;
 }
 
+// ---------------------------------------------------------- sorted run ----
+__global__ void k_load_user(int n, const float4* x, const float4* p, const float4* f,
+                            const int32_t* species, float4* xs, float4* ps, float4* fs,
+                            int32_t* ss, int32_t* perm, uint8_t* err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *err = 0;
+  if (i >= n) return;
+  float4 r = x[i];
+  r.w = 0.f;
+  xs[i] = r;
+  ps[i] = p[i];
+  fs[i] = f[i];
+  if (species) ss[i] = species[i];
+  perm[i] = i;
+}
+
+__global__ void k_store_user(int n, const int32_t* perm, const float4* xs, const float4* ps,
+                             const float4* fs, const float4* rs, float4* x, float4* p, float4* f,
+                             float4* ref) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int i = perm[s];
+  float4 r = xs[s];
+  r.w = x[i].w;
+  x[i] = r;
+  p[i] = ps[s];
+  f[i] = fs[s];
+  ref[i] = rs[s];
+}
+
+__global__ void k_or_error(uint8_t* dst, const uint8_t* src) { *dst = (uint8_t)(*dst | *src); }
+
+int validate_sorted(const jmd_nve_system& s, const jmd_sorted_state& z) {
+  JMD_REQUIRE(s.mass == nullptr, "the sorted run needs a scalar mass");
+  JMD_REQUIRE(s.nlist.use_cell_list, "the sorted run needs a cell grid");
+  JMD_REQUIRE(z.position_a && z.position_b && z.momentum && z.force && z.reference_position &&
+                  z.scratch4a && z.scratch4b && z.perm && z.scratch_i_a && z.scratch_i_b &&
+                  z.idx && z.nbr_count && z.error_code && z.occupancy && z.rebuild_flag,
+              "null buffer in jmd_sorted_state");
+  JMD_REQUIRE(!s.species || z.species, "sorted species buffer required");
+  JMD_REQUIRE(z.idx_ld >= s.nlist.max_occupancy && z.idx_ld % 2 == 0, "bad sorted idx_ld");
+  for (const void* p : {(const void*)z.position_a, (const void*)z.position_b,
+                        (const void*)z.momentum, (const void*)z.force,
+                        (const void*)z.reference_position, (const void*)z.scratch4a,
+                        (const void*)z.scratch4b})
+    JMD_REQUIRE((reinterpret_cast<uintptr_t>(p) % 16) == 0, "float4 rows must be 16-byte aligned");
+  return JMD_OK;
+}
+
+int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64_t steps,
+                       bool graphed, cudaStream_t st, cudaStream_t body_st) {
+  const bool always = s.threshold_sq < 0.f;
+  const int n = (int)s.n;
+  const unsigned gr = (unsigned)ceil_div(n, 256);
+  // sort + build on the private copy; gated by the flag unless `force_now`
+  auto rebuild_at = [&](float* x, bool gated, bool with_force, cudaStream_t q) -> int {
+    int32_t* flag = gated ? z.rebuild_flag : nullptr;
+    int rc = jmd_sort_by_cell(&s.nlist, x, z.momentum, with_force ? z.force : nullptr, z.species,
+                              z.perm, s.n, z.scratch4a, z.scratch4b, z.scratch_i_a, z.scratch_i_b,
+                              flag, z.workspace, z.workspace_bytes, q);
+    if (rc) return rc;
+    return jmd_neighbor_list_build(&s.nlist, x, 4, s.n, z.idx, z.idx_ld, z.nbr_count, z.occupancy,
+                                   z.error_code, z.reference_position, 4, flag, z.workspace,
+                                   z.workspace_bytes, q);
+  };
+  auto gate = [&](float* x) -> int {
+    if (always) return rebuild_at(x, false, false, st);
+    if (graphed)
+      return conditional(z.rebuild_flag, [&](cudaStream_t b) { return rebuild_at(x, true, false, b); },
+                         st, body_st);
+    return rebuild_at(x, true, false, st);
+  };
+  int rc;
+  k_load_user<<<gr, 256, 0, st>>>(n, reinterpret_cast<const float4*>(s.position),
+                                  reinterpret_cast<const float4*>(s.momentum),
+                                  reinterpret_cast<const float4*>(s.force), s.species,
+                                  reinterpret_cast<float4*>(z.position_a),
+                                  reinterpret_cast<float4*>(z.momentum),
+                                  reinterpret_cast<float4*>(z.force), z.species, z.perm,
+                                  z.error_code);
+  JMD_CUDA(cudaGetLastError());
+  if ((rc = rebuild_at(z.position_a, false, true, st))) return rc;
+  rc = jmd_verlet_kick_drift(z.position_a, 4, z.momentum, 4, z.force, 4, nullptr, s.mass_scalar,
+                             s.n, &s.space, s.dt, nullptr,
+                             always ? nullptr : z.reference_position, 4, s.threshold_sq,
+                             always ? nullptr : z.rebuild_flag, st);
+  if (rc) return rc;
+  float* cur = z.position_a;
+  float* nxt = z.position_b;
+  const int64_t width = s.nlist.max_occupancy;
+  for (int64_t k = 1; k < steps; ++k) {
+    if ((rc = gate(cur))) return rc;
+    rc = jmd_nve_fused_step(&s.pair, &s.space, cur, nxt, z.momentum, nullptr, s.mass_scalar,
+                            z.species, s.n, z.idx, z.idx_ld, width, z.nbr_count, s.dt,
+                            always ? nullptr : z.reference_position, s.threshold_sq,
+                            always ? nullptr : z.rebuild_flag, st);
+    if (rc) return rc;
+    std::swap(cur, nxt);
+  }
+  if ((rc = gate(cur))) return rc;
+  rc = jmd_force_kick(&s.pair, &s.space, cur, z.force, z.momentum, z.species, s.n, z.idx,
+                      z.idx_ld, width, z.nbr_count, s.dt, st);
+  if (rc) return rc;
+  k_store_user<<<gr, 256, 0, st>>>(n, z.perm, reinterpret_cast<const float4*>(cur),
+                                   reinterpret_cast<const float4*>(z.momentum),
+                                   reinterpret_cast<const float4*>(z.force),
+                                   reinterpret_cast<const float4*>(z.reference_position),
+                                   reinterpret_cast<float4*>(s.position),
+                                   reinterpret_cast<float4*>(s.momentum),
+                                   reinterpret_cast<float4*>(s.force),
+                                   reinterpret_cast<float4*>(s.reference_position));
+  JMD_CUDA(cudaGetLastError());
+  // the caller's list, in the reference's order, at the last rebuild's positions
+  rc = jmd_neighbor_list_build(&s.nlist, s.reference_position, 4, s.n, s.idx, s.idx_ld,
+                               s.nbr_count, s.occupancy, s.error_code, s.reference_position, 4,
+                               nullptr, s.nl_workspace, s.nl_workspace_bytes, st);
+  if (rc) return rc;
+  k_or_error<<<1, 1, 0, st>>>(s.error_code, z.error_code);
+  JMD_CUDA(cudaGetLastError());
+  return JMD_OK;
+}
+
 std::string plan_key(const jmd_nve_system& s, int64_t steps, int device) {
   std::string k(reinterpret_cast<const char*>(&s), sizeof(s));
   k.append(reinterpret_cast<const char*>(&steps), sizeof(steps));
@@ -166,6 +290,79 @@ using namespace jmd;
 
 extern "C" {
 
+}  // extern "C"
+
+namespace jmd {
+namespace {
+
+// Records `enq(capture_stream, body_stream)` once per key as a CUDA graph and
+// launches it on st.
+template <typename Enq>
+int launch_graphed(const std::string& key, Enq enq, cudaStream_t st) {
+  std::lock_guard<std::mutex> lock(g_mu);
+  auto it = g_cache.find(key);
+  if (it == g_cache.end()) {
+    cudaStream_t cs, bs;
+    JMD_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    JMD_CUDA(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
+    GraphPlan plan;
+    cudaError_t ce = cudaGraphCreate(&plan.graph, 0);
+    int rc = JMD_OK;
+    if (ce == cudaSuccess)
+      ce = cudaStreamBeginCaptureToGraph(cs, plan.graph, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+      rc = enq(cs, bs);
+      cudaGraph_t out;
+      cudaError_t ee = cudaStreamEndCapture(cs, &out);
+      if (!rc && ee != cudaSuccess) ce = ee;
+    }
+    if (!rc && ce == cudaSuccess) ce = cudaGraphInstantiate(&plan.exec, plan.graph, 0);
+    cudaStreamDestroy(cs);
+    cudaStreamDestroy(bs);
+    if (rc || ce != cudaSuccess) {
+      if (plan.exec) cudaGraphExecDestroy(plan.exec);
+      if (plan.graph) cudaGraphDestroy(plan.graph);
+      cudaGetLastError();
+      if (rc) return rc;
+      return fail(JMD_ERR_CUDA, std::string("engine graph build: ") + cudaGetErrorString(ce));
+    }
+    it = g_cache.emplace(key, plan).first;
+  }
+  JMD_CUDA(cudaGraphLaunch(it->second.exec, st));
+  return JMD_OK;
+}
+
+}  // namespace
+}  // namespace jmd
+
+extern "C" {
+
+int jmd_nve_run_sorted(const jmd_nve_system* sys, const jmd_sorted_state* sorted, int64_t n_steps,
+                       int32_t use_graph, void* stream) {
+  JMD_REQUIRE(sys != nullptr && sorted != nullptr, "null argument");
+  int e = validate_sys(*sys);
+  if (e) return e;
+  e = validate_sorted(*sys, *sorted);
+  if (e) return e;
+  JMD_REQUIRE(n_steps >= 0, "n_steps must be >= 0");
+  if (n_steps == 0) return JMD_OK;
+  cudaStream_t st = as_stream(stream);
+  cudaStreamCaptureStatus cap;
+  JMD_CUDA(cudaStreamIsCapturing(st, &cap));
+  if (!use_graph || cap != cudaStreamCaptureStatusNone) {
+    int rc = enqueue_run_sorted(*sys, *sorted, n_steps, false, st, nullptr);
+    return rc ? rc : check_launch("jmd_nve_run_sorted");
+  }
+  int device;
+  JMD_CUDA(cudaGetDevice(&device));
+  std::string key = "sorted" + plan_key(*sys, n_steps, device);
+  key.append(reinterpret_cast<const char*>(sorted), sizeof(*sorted));
+  return launch_graphed(key, [&](cudaStream_t cs, cudaStream_t bs) {
+    return enqueue_run_sorted(*sys, *sorted, n_steps, true, cs, bs);
+  }, st);
+}
+
 int jmd_nve_run(const jmd_nve_system* sys, int64_t n_steps, int32_t use_graph, void* stream) {
   JMD_REQUIRE(sys != nullptr, "system is null");
   int e = validate_sys(*sys);
@@ -181,39 +378,10 @@ int jmd_nve_run(const jmd_nve_system* sys, int64_t n_steps, int32_t use_graph, v
   }
   int device;
   JMD_CUDA(cudaGetDevice(&device));
-  std::lock_guard<std::mutex> lock(g_mu);
   const std::string key = plan_key(*sys, n_steps, device);
-  auto it = g_cache.find(key);
-  if (it == g_cache.end()) {
-    cudaStream_t cs, bs;
-    JMD_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-    JMD_CUDA(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
-    GraphPlan plan;
-    cudaError_t ce = cudaGraphCreate(&plan.graph, 0);
-    int rc = JMD_OK;
-    if (ce == cudaSuccess)
-      ce = cudaStreamBeginCaptureToGraph(cs, plan.graph, nullptr, nullptr, 0,
-                                         cudaStreamCaptureModeThreadLocal);
-    if (ce == cudaSuccess) {
-      rc = enqueue_run(*sys, n_steps, true, cs, bs);
-      cudaGraph_t out;
-      cudaError_t ee = cudaStreamEndCapture(cs, &out);
-      if (!rc && ee != cudaSuccess) ce = ee;
-    }
-    if (!rc && ce == cudaSuccess) ce = cudaGraphInstantiate(&plan.exec, plan.graph, 0);
-    cudaStreamDestroy(cs);
-    cudaStreamDestroy(bs);
-    if (rc || ce != cudaSuccess) {
-      if (plan.exec) cudaGraphExecDestroy(plan.exec);
-      if (plan.graph) cudaGraphDestroy(plan.graph);
-      cudaGetLastError();
-      if (rc) return rc;
-      return fail(JMD_ERR_CUDA, std::string("jmd_nve_run graph build: ") + cudaGetErrorString(ce));
-    }
-    it = g_cache.emplace(key, plan).first;
-  }
-  JMD_CUDA(cudaGraphLaunch(it->second.exec, st));
-  return JMD_OK;
+  return launch_graphed(key, [&](cudaStream_t cs, cudaStream_t bs) {
+    return enqueue_run(*sys, n_steps, true, cs, bs);
+  }, st);
 }
 
 int jmd_engine_clear_cache(void) {

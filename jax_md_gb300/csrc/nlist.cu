@@ -667,6 +667,38 @@ __global__ void k_sparse_pad(int32_t* idx, int64_t ld, int64_t width, const int3
   }
 }
 
+
+// ------------------------------------------------------- spatial sort -------
+// Gathers every per-atom array into cell order after a binning pass:
+// new position s takes old atom sorted_id[s].  Positions come from the
+// binning's sorted copy; the rest are gathered into scratch and copied back
+// by k_sort_copy_back (both gated by the rebuild flag when one is given).
+__global__ void k_sort_gather(int n, Bins b, const float4* p, const float4* f,
+                              const int32_t* species, const int32_t* perm, float4* tp, float4* tf,
+                              int32_t* tsp, int32_t* tperm, const int32_t* flag) {
+  if (skip(flag)) return;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int i = b.sorted_id[s];
+  tp[s] = p[i];
+  if (f) tf[s] = f[i];
+  if (species) tsp[s] = species[i];
+  tperm[s] = perm[i];
+}
+
+__global__ void k_sort_copy_back(int n, Bins b, float4* x, float4* p, float4* f, int32_t* species,
+                                 int32_t* perm, const float4* tp, const float4* tf,
+                                 const int32_t* tsp, const int32_t* tperm, const int32_t* flag) {
+  if (skip(flag)) return;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  x[s] = b.sorted_pos[s];
+  p[s] = tp[s];
+  if (f) f[s] = tf[s];
+  if (species) species[s] = tsp[s];
+  perm[s] = tperm[s];
+}
+
 // Host-side constants carried into the finalize kernel.
 struct FinalizeArgs {
   int format;
@@ -937,4 +969,41 @@ int jmd_skin_check(const float* position, int64_t pos_stride, const float* refer
   return check_launch("jmd_skin_check");
 }
 
+int jmd_sort_by_cell(const jmd_nlist* nl, float* position, float* momentum, float* force,
+                     int32_t* species, int32_t* perm, int64_t n, float* scratch4a,
+                     float* scratch4b, int32_t* scratch_i_a, int32_t* scratch_i_b,
+                     int32_t* rebuild_flag, void* workspace, size_t workspace_bytes,
+                     void* stream) {
+  int e = validate(nl, n, 1);
+  if (e) return e;
+  JMD_REQUIRE(nl->use_cell_list, "sorting needs a cell grid");
+  JMD_REQUIRE(position && momentum && perm && scratch4a && scratch_i_b, "null buffer");
+  JMD_REQUIRE(!force || scratch4b, "force needs scratch4b");
+  JMD_REQUIRE(!species || scratch_i_a, "species needs scratch_i_a");
+  for (const void* q : {(const void*)position, (const void*)momentum, (const void*)scratch4a})
+    JMD_REQUIRE((reinterpret_cast<uintptr_t>(q) % 16) == 0, "float4 rows must be 16-byte aligned");
+  if (n <= 0) return JMD_OK;
+  cudaStream_t st = as_stream(stream);
+  Grid g = make_grid(*nl);
+  bool ok;
+  Bins b = carve_bins(workspace, workspace_bytes, n, g.count, &ok);
+  if (!ok) return fail(JMD_ERR_WORKSPACE, "sort workspace too small");
+  if (nl->space.dim == 3) run_binning<3, true>(position, 4, (int)n, g, b, nullptr, rebuild_flag, st);
+  else run_binning<2, true>(position, 4, (int)n, g, b, nullptr, rebuild_flag, st);
+  const unsigned gr = (unsigned)ceil_div(n, 256);
+  k_sort_gather<<<gr, 256, 0, st>>>((int)n, b, reinterpret_cast<const float4*>(momentum),
+                                    reinterpret_cast<const float4*>(force), species, perm,
+                                    reinterpret_cast<float4*>(scratch4a),
+                                    reinterpret_cast<float4*>(scratch4b), scratch_i_a, scratch_i_b,
+                                    rebuild_flag);
+  k_sort_copy_back<<<gr, 256, 0, st>>>((int)n, b, reinterpret_cast<float4*>(position),
+                                       reinterpret_cast<float4*>(momentum),
+                                       reinterpret_cast<float4*>(force), species, perm,
+                                       reinterpret_cast<const float4*>(scratch4a),
+                                       reinterpret_cast<const float4*>(scratch4b), scratch_i_a,
+                                       scratch_i_b, rebuild_flag);
+  return check_launch("jmd_sort_by_cell");
+}
+
 }  // extern "C"
+

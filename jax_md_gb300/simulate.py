@@ -406,8 +406,52 @@ def _nve_system(st: '_Stepper', state: NVEState, nbrs, alt: torch.Tensor) -> N.N
     return s, species
 
 
+class _SortedBuffers:
+    """Engine-private, cell-ordered copy of a system (see jmd_nve_run_sorted)."""
+
+    def __init__(self, n, ld, species: bool, workspace_bytes: int, device):
+        f4 = lambda: torch.empty((n, 4), dtype=torch.float32, device=device)
+        i4 = lambda: torch.empty(n, dtype=torch.int32, device=device)
+        self.n, self.ld = n, ld
+        self.xa, self.xb, self.p, self.f, self.ref, self.t4a, self.t4b = (f4() for _ in range(7))
+        self.perm, self.tia, self.tib = i4(), i4(), i4()
+        self.species = i4() if species else None
+        self.idx = torch.empty((n, ld), dtype=torch.int32, device=device)
+        self.cnt = i4()
+        self.err = torch.zeros((), dtype=torch.uint8, device=device)
+        self.occ = torch.zeros((), dtype=torch.int64, device=device)
+        self.flag = torch.zeros((), dtype=torch.int32, device=device)
+        self.ws = torch.empty(workspace_bytes, dtype=torch.uint8, device=device)
+
+    def struct(self) -> N.SortedState:
+        z = N.SortedState()
+        z.position_a, z.position_b = self.xa.data_ptr(), self.xb.data_ptr()
+        z.momentum, z.force = self.p.data_ptr(), self.f.data_ptr()
+        z.reference_position = self.ref.data_ptr()
+        z.scratch4a, z.scratch4b = self.t4a.data_ptr(), self.t4b.data_ptr()
+        z.species = N.ptr(self.species)
+        z.perm, z.scratch_i_a, z.scratch_i_b = self.perm.data_ptr(), self.tia.data_ptr(), self.tib.data_ptr()
+        z.idx, z.idx_ld, z.nbr_count = self.idx.data_ptr(), self.ld, self.cnt.data_ptr()
+        z.error_code, z.occupancy = self.err.data_ptr(), self.occ.data_ptr()
+        z.rebuild_flag = self.flag.data_ptr()
+        z.workspace, z.workspace_bytes = self.ws.data_ptr(), self.ws.numel()
+        return z
+
+
+def _sorted_buffers(state, nbrs, species):
+    plan = nbrs.plan
+    key = (plan.ld, species is not None, plan.workspace.numel())
+    b = getattr(state, '_sorted', None)
+    if b is None or b.n != state.position.shape[0] or getattr(b, 'key', None) != key:
+        b = _SortedBuffers(state.position.shape[0], plan.ld, species is not None,
+                           plan.workspace.numel(), state.position.device)
+        b.key = key
+        object.__setattr__(state, '_sorted', b)
+    return b
+
+
 def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bool = True,
-        max_reallocations: int = 4):
+        max_reallocations: int = 4, sort=None):
     """Runs the reference loop body ``n_steps`` times on the device:
 
         nbrs = nbrs.update(state.position); state = apply_fn(state, neighbor=nbrs)
@@ -416,7 +460,12 @@ def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bo
     whose per-step rebuild sits in a device-side conditional node.  With
     ``neighbor_fn``, overflow is handled as the reference's host loop does:
     the run is repeated from its starting state with a list re-allocated there.
-    Returns (state, neighbor)."""
+
+    ``sort`` (default: when the mass is a scalar and a cell grid exists) keeps
+    the atoms in cell order inside the run so neighbour gathers are
+    coalesced; on return the state is back in the caller's order and the
+    caller's list is rebuilt, in the reference's entry order, at the
+    positions of the last rebuild.  Returns (state, neighbor)."""
     st = apply_fn.stepper
     if not isinstance(state, NVEState):
         raise NotImplementedError('run() drives NVE states')
@@ -427,9 +476,19 @@ def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bo
             alt = torch.empty((state.position.shape[0], 4), dtype=torch.float32,
                               device=state.position.device)
             object.__setattr__(state, '_alt', alt)
-        sysd, _species = _nve_system(st, state, neighbor, alt)
-        N.check(N.lib().jmd_nve_run(ctypes.byref(sysd), int(n_steps), 1 if use_graph else 0,
-                                    N.stream_ptr()), 'nve_run')
+        sysd, species = _nve_system(st, state, neighbor, alt)
+        use_sort = sort
+        if use_sort is None:
+            use_sort = (not isinstance(state.mass, torch.Tensor)) and bool(sysd.nlist.use_cell_list)
+        if use_sort:
+            sb = _sorted_buffers(state, neighbor, species)
+            z = sb.struct()
+            N.check(N.lib().jmd_nve_run_sorted(ctypes.byref(sysd), ctypes.byref(z), int(n_steps),
+                                               1 if use_graph else 0, N.stream_ptr()),
+                    'nve_run_sorted')
+        else:
+            N.check(N.lib().jmd_nve_run(ctypes.byref(sysd), int(n_steps), 1 if use_graph else 0,
+                                        N.stream_ptr()), 'nve_run')
         if neighbor_fn is None or not bool(neighbor.did_buffer_overflow):
             return state, neighbor
         # overflow: restore the starting state, re-allocate there (with growing

@@ -29,13 +29,14 @@ def _setup(cuda, n_cells=6, skin=0.3):
     return R, P, L, nfn, efn, init, apply, st, nb
 
 
+@pytest.mark.parametrize('sort', [False, True])
 @pytest.mark.parametrize('steps', [1, 2, 7, 40])
-def test_graph_equals_direct(cuda, steps):
+def test_graph_equals_direct(cuda, steps, sort):
     from jax_md_gb300 import simulate
     _, _, _, nfn, efn, init, apply, st_a, nb_a = _setup(cuda)
     _, _, _, nfn2, _, _, apply2, st_b, nb_b = _setup(cuda)
-    simulate.run(apply, st_a, nb_a, steps, use_graph=True)
-    simulate.run(apply2, st_b, nb_b, steps, use_graph=False)
+    simulate.run(apply, st_a, nb_a, steps, use_graph=True, sort=sort)
+    simulate.run(apply2, st_b, nb_b, steps, use_graph=False, sort=sort)
     torch.cuda.synchronize()
     assert torch.equal(st_a.position, st_b.position)
     assert torch.equal(st_a.momentum, st_b.momentum)
@@ -57,19 +58,20 @@ def test_graph_replay_repeats(cuda):
     assert torch.equal(st_a.position, st_b.position)
 
 
-def test_runner_matches_per_step_api_and_oracle(cuda):
+@pytest.mark.parametrize('sort', [False, True])
+def test_runner_matches_per_step_api_and_oracle(cuda, sort):
     from jax_md_gb300 import simulate
     R, P, L, nfn, efn, init, apply, st, nb = _setup(cuda)
     _, _, _, nfn2, efn2, init2, apply2, st2, nb2 = _setup(cuda)
     steps = 40
-    simulate.run(apply, st, nb, steps)
+    simulate.run(apply, st, nb, steps, sort=sort)
     for _ in range(steps):
         nb2 = nb2.update(st2.position)
         st2 = apply2(st2, neighbor=nb2)
     torch.cuda.synchronize()
     box = np.full(3, L)
     d = O.displacement(st.position.cpu().numpy(), st2.position.cpu().numpy(), box)
-    assert np.abs(d).max() < 1e-5
+    assert np.abs(d).max() < (1e-4 if sort else 1e-5)
     # oracle trajectory
     spec = lj_spec()
     nl = O.NeighborListOracle(box, 2.5, 0.3)
@@ -121,3 +123,23 @@ def test_overflow_reallocates(cuda):
     assert not bool(nb2.did_buffer_overflow)
     assert nb2.max_occupancy > first
     assert torch.isfinite(st.position).all()
+
+
+def test_sorted_run_returns_reference_order_list(cuda):
+    """After a sorted run the caller's list is the reference's build at its reference positions."""
+    from jax_md_gb300 import simulate
+    R, P, L, nfn, efn, init, apply, st, nb = _setup(cuda, n_cells=8)
+    simulate.run(apply, st, nb, 60, sort=True)
+    torch.cuda.synchronize()
+    box = np.full(3, L, np.float32)
+    ref = nb.reference_position.contiguous().cpu().numpy()
+    onl = O.NeighborListOracle(box, np.float32(2.5), np.float32(0.3))
+    ob = onl.build(ref, nb.max_occupancy, 0, nb.cell_list_capacity)
+    from tests.helpers import near_cutoff_pairs
+    from tests.test_gpu_neighbor import _strict_equal_rows
+    skip = near_cutoff_pairs(ref, box, float(np.float32(2.8)))
+    assert _strict_equal_rows(nb.idx.cpu().numpy(), ob.idx, len(R), skip) == []
+    # the list still covers the current positions (skin not exceeded since the rebuild)
+    d = O.displacement(st.position.contiguous().cpu().numpy(), ref, box)
+    assert ((d * d).sum(-1) <= (0.15 ** 2) * (1 + 1e-5) + 0.3 * 0.005).all()
+    assert int(nb.error.code) == 0
