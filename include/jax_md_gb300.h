@@ -269,6 +269,41 @@ int jmd_force_kick(const jmd_pair* pp, const jmd_space* space,
                    int64_t idx_ld, int64_t idx_width, const int32_t* nbr_count,
                    float dt, void* stream);
 
+/* Tiled Dense layout used inside the engine (atoms in cell order): entry k
+ * of atom i lives at tidx[(i / 32) * depth * 32 + k * 32 + i % 32], columns
+ * are bounded by nbr_count and not padded.  Same pairs and the same entry
+ * order per atom as jmd_neighbor_list_build. */
+int jmd_neighbor_list_build_tiled(const jmd_nlist* nl, const float* position,
+                                  int64_t n, int32_t* tidx, int64_t depth,
+                                  int32_t* nbr_count, int64_t* occupancy,
+                                  uint8_t* error_code, float* reference_position,
+                                  int32_t* rebuild_flag, void* workspace,
+                                  size_t workspace_bytes, void* stream);
+
+/* Forces over a tiled list, one thread per atom (float4 rows). */
+int jmd_pair_forces_tiled(const jmd_pair* pp, const jmd_space* space,
+                          const float* position, const int32_t* species,
+                          int64_t n, const int32_t* tidx, int64_t depth,
+                          int64_t width, const int32_t* nbr_count, float* force,
+                          void* stream);
+
+/* jmd_nve_fused_step over a tiled list (scalar mass). */
+int jmd_nve_fused_step_tiled(const jmd_pair* pp, const jmd_space* space,
+                             const float* position, float* position_next,
+                             float* momentum, float mass_scalar,
+                             const int32_t* species, int64_t n,
+                             const int32_t* tidx, int64_t depth, int64_t width,
+                             const int32_t* nbr_count, float dt,
+                             const float* reference_position, float threshold_sq,
+                             int32_t* rebuild_flag, void* stream);
+
+/* jmd_force_kick over a tiled list. */
+int jmd_force_kick_tiled(const jmd_pair* pp, const jmd_space* space,
+                         const float* position, float* force, float* momentum,
+                         const int32_t* species, int64_t n, const int32_t* tidx,
+                         int64_t depth, int64_t width, const int32_t* nbr_count,
+                         float dt, void* stream);
+
 /* ------------------------------------------------------------- engine ---- */
 
 /* A device-resident NVE system with its Dense neighbour list: the state of
@@ -339,8 +374,8 @@ typedef struct {
   int32_t* perm;              /* sorted index -> caller atom id */
   int32_t* scratch_i_a;
   int32_t* scratch_i_b;
-  int32_t* idx;               /* [n, idx_ld] Dense list in sorted ids */
-  int64_t idx_ld;
+  int32_t* idx;               /* tiled Dense list in sorted ids, ceil(n/32)*32*idx_ld */
+  int64_t idx_ld;             /* tile depth >= max_occupancy */
   int32_t* nbr_count;
   uint8_t* error_code;
   int64_t* occupancy;

@@ -111,6 +111,14 @@ SIGNATURES = {
     'jmd_engine_clear_cache': (C.c_int, []),
     'jmd_sort_by_cell': (C.c_int, [C.POINTER(NList), P, P, P, P, P, I64, P, P, P, P, P, P, SZ, P]),
     'jmd_nve_run_sorted': (C.c_int, [C.POINTER(NveSystem), C.POINTER(SortedState), I64, I32, P]),
+    'jmd_neighbor_list_build_tiled': (C.c_int, [C.POINTER(NList), P, I64, P, I64, P, P, P, P, P, P,
+                                                SZ, P]),
+    'jmd_pair_forces_tiled': (C.c_int, [C.POINTER(Pair), C.POINTER(Space), P, P, I64, P, I64, I64,
+                                        P, P, P]),
+    'jmd_nve_fused_step_tiled': (C.c_int, [C.POINTER(Pair), C.POINTER(Space), P, P, P, F32, P, I64,
+                                           P, I64, I64, P, F32, P, F32, P, P]),
+    'jmd_force_kick_tiled': (C.c_int, [C.POINTER(Pair), C.POINTER(Space), P, P, P, P, I64, P, I64,
+                                       I64, P, F32, P]),
 }
 
 _lib = None

@@ -100,4 +100,31 @@ __device__ __forceinline__ void pair_eval2(float2 r2, const Coef2& c, float2& U,
   }
 }
 
+// L2 policy that asks to keep lines (evict_last): the positions are
+// re-gathered ~n_neighbours times per step while the index rows stream
+// through once (those use evict-first loads).  Created once per thread.
+__device__ __forceinline__ uint64_t policy_keep() {
+  uint64_t pol;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+// Read-only float4 gather under an L2 cache policy (positions do not change
+// while a kernel runs; the step kernels write the next positions elsewhere).
+__device__ __forceinline__ float4 ldg_keep(const float4* p, uint64_t pol) {
+  float4 r;
+  asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+      : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+      : "l"(p), "l"(pol));
+  return r;
+}
+
+template <int DIM>
+__device__ __forceinline__ bool interior(const float4& x, const Geo& g, float m) {
+  if (!g.periodic) return true;
+  bool in = x.x >= m && x.x <= g.L[0] - m && x.y >= m && x.y <= g.L[1] - m;
+  if (DIM == 3) in = in && x.z >= m && x.z <= g.L[2] - m;
+  return in;
+}
+
 }  // namespace jmd

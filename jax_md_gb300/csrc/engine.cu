@@ -192,7 +192,7 @@ int validate_sorted(const jmd_nve_system& s, const jmd_sorted_state& z) {
                   z.idx && z.nbr_count && z.error_code && z.occupancy && z.rebuild_flag,
               "null buffer in jmd_sorted_state");
   JMD_REQUIRE(!s.species || z.species, "sorted species buffer required");
-  JMD_REQUIRE(z.idx_ld >= s.nlist.max_occupancy && z.idx_ld % 2 == 0, "bad sorted idx_ld");
+  JMD_REQUIRE(z.idx_ld >= s.nlist.max_occupancy, "tile depth (idx_ld) < max_occupancy");
   for (const void* p : {(const void*)z.position_a, (const void*)z.position_b,
                         (const void*)z.momentum, (const void*)z.force,
                         (const void*)z.reference_position, (const void*)z.scratch4a,
@@ -213,9 +213,9 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
                               z.perm, s.n, z.scratch4a, z.scratch4b, z.scratch_i_a, z.scratch_i_b,
                               flag, z.workspace, z.workspace_bytes, q);
     if (rc) return rc;
-    return jmd_neighbor_list_build(&s.nlist, x, 4, s.n, z.idx, z.idx_ld, z.nbr_count, z.occupancy,
-                                   z.error_code, z.reference_position, 4, flag, z.workspace,
-                                   z.workspace_bytes, q);
+    return jmd_neighbor_list_build_tiled(&s.nlist, x, s.n, z.idx, z.idx_ld, z.nbr_count,
+                                         z.occupancy, z.error_code, z.reference_position, flag,
+                                         z.workspace, z.workspace_bytes, q);
   };
   auto gate = [&](float* x) -> int {
     if (always) return rebuild_at(x, false, false, st);
@@ -244,16 +244,16 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
   const int64_t width = s.nlist.max_occupancy;
   for (int64_t k = 1; k < steps; ++k) {
     if ((rc = gate(cur))) return rc;
-    rc = jmd_nve_fused_step(&s.pair, &s.space, cur, nxt, z.momentum, nullptr, s.mass_scalar,
-                            z.species, s.n, z.idx, z.idx_ld, width, z.nbr_count, s.dt,
-                            always ? nullptr : z.reference_position, s.threshold_sq,
-                            always ? nullptr : z.rebuild_flag, st);
+    rc = jmd_nve_fused_step_tiled(&s.pair, &s.space, cur, nxt, z.momentum, s.mass_scalar,
+                                  z.species, s.n, z.idx, z.idx_ld, width, z.nbr_count, s.dt,
+                                  always ? nullptr : z.reference_position, s.threshold_sq,
+                                  always ? nullptr : z.rebuild_flag, st);
     if (rc) return rc;
     std::swap(cur, nxt);
   }
   if ((rc = gate(cur))) return rc;
-  rc = jmd_force_kick(&s.pair, &s.space, cur, z.force, z.momentum, z.species, s.n, z.idx,
-                      z.idx_ld, width, z.nbr_count, s.dt, st);
+  rc = jmd_force_kick_tiled(&s.pair, &s.space, cur, z.force, z.momentum, z.species, s.n, z.idx,
+                            z.idx_ld, width, z.nbr_count, s.dt, st);
   if (rc) return rc;
   k_store_user<<<gr, 256, 0, st>>>(n, z.perm, reinterpret_cast<const float4*>(cur),
                                    reinterpret_cast<const float4*>(z.momentum),

@@ -66,28 +66,6 @@ __device__ __forceinline__ T gsum(T v) {
 
 __device__ __forceinline__ int spc(int s, int nsp) { return s < 0 ? 0 : (s >= nsp ? nsp - 1 : s); }
 
-// Read-only float4 gather that asks L2 to keep the line (evict_last): the
-// positions are re-gathered ~n_neighbours times per step while the index rows
-// stream through once (those use evict-first loads).
-__device__ __forceinline__ float4 ldg_keep(const float4* p) {
-  float4 r;
-  asm volatile(
-      "{\n\t.reg .b64 pol;\n\t"
-      "createpolicy.fractional.L2::evict_last.b64 pol, 1.0;\n\t"
-      "ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], pol;\n\t}"
-      : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
-      : "l"(p));
-  return r;
-}
-
-template <int DIM>
-__device__ __forceinline__ bool interior(const float4& x, const Geo& g, float m) {
-  if (!g.periodic) return true;
-  bool in = x.x >= m && x.x <= g.L[0] - m && x.y >= m && x.y <= g.L[1] - m;
-  if (DIM == 3) in = in && x.z >= m && x.z <= g.L[2] - m;
-  return in;
-}
-
 template <int DIM, int TPA, int KIND, bool SPECIES, int MODE, bool CNT>
 __global__ void __launch_bounds__(256)
 k_dense2(D2Args a, const __grid_constant__ PairTable tab) {
@@ -103,6 +81,12 @@ k_dense2(D2Args a, const __grid_constant__ PairTable tab) {
   float2 ax = f2s(0.f), ay = f2s(0.f), az = f2s(0.f), ae = f2s(0.f);
   float2 w0 = f2s(0.f), w1 = f2s(0.f), w2 = f2s(0.f), w3 = f2s(0.f), w4 = f2s(0.f), w5 = f2s(0.f);
   float4 xi = make_float4(0.f, 0.f, 0.f, 0.f);
+  // rows the epilogue needs, loaded now so their latency overlaps the loop
+  float4 q = xi, rf = xi;
+  if (active && sub == 0) {
+    if (MODE == MODE_STEP || MODE == MODE_KICK) q = a.p[atom];
+    if (MODE == MODE_STEP && a.ref) rf = __ldg(a.ref + atom);
+  }
   if (active) {
     xi = __ldg(a.x + atom);
     const int si = SPECIES ? spc(__ldg(a.species + atom), tab.nsp) : 0;
@@ -113,6 +97,7 @@ k_dense2(D2Args a, const __grid_constant__ PairTable tab) {
     const bool inner = interior<DIM>(xi, a.geo, a.margin);
     const float rc2m = tab.rc2_max;
     const Coef2 c0 = coef2(tab.c[0]);
+    const uint64_t pol = policy_keep();
     // One packed step over the entries k, k+1 whose ids and positions are loaded.
     auto body = [&](int2 jj, int k, const float4& b0, const float4& b1) {
       const bool v1 = k + 1 < end;
@@ -198,8 +183,8 @@ k_dense2(D2Args a, const __grid_constant__ PairTable tab) {
     }
     float4 c0p = make_float4(0.f, 0.f, 0.f, 0.f), c1p = c0p;
     if (2 * sub < end) {
-      c0p = ldg_keep(a.x + ids[0].x);
-      c1p = ldg_keep(a.x + ids[0].y);
+      c0p = ldg_keep(a.x + ids[0].x, pol);
+      c1p = ldg_keep(a.x + ids[0].y, pol);
     }
 #pragma unroll
     for (int t = 0; t < IT; ++t) {
@@ -207,8 +192,8 @@ k_dense2(D2Args a, const __grid_constant__ PairTable tab) {
       if (k >= end) break;
       float4 n0 = c0p, n1 = c1p;
       if (t + 1 < IT && k + 2 * TPA < end) {
-        n0 = ldg_keep(a.x + ids[t + 1].x);
-        n1 = ldg_keep(a.x + ids[t + 1].y);
+        n0 = ldg_keep(a.x + ids[t + 1].x, pol);
+        n1 = ldg_keep(a.x + ids[t + 1].y, pol);
       }
       body(ids[t], k, c0p, c1p);
       c0p = n0;
@@ -217,8 +202,8 @@ k_dense2(D2Args a, const __grid_constant__ PairTable tab) {
     // rows longer than the prefetched slice
     for (int k = 2 * sub + IT * 2 * TPA; k < end; k += 2 * TPA) {
       const int2 jj = fix(__ldcs(reinterpret_cast<const int2*>(row + k)), k);
-      const float4 b0 = ldg_keep(a.x + jj.x);
-      const float4 b1 = ldg_keep(a.x + jj.y);
+      const float4 b0 = ldg_keep(a.x + jj.x, pol);
+      const float4 b1 = ldg_keep(a.x + jj.y, pol);
       body(jj, k, b0, b1);
     }
   }
@@ -231,7 +216,6 @@ k_dense2(D2Args a, const __grid_constant__ PairTable tab) {
   }
   if (MODE == MODE_KICK && leader) {
     const float h = 0.5f * a.dt;
-    float4 q = a.p[atom];
     q.x = fmaf(h, fx, q.x);
     q.y = fmaf(h, fy, q.y);
     q.z = fmaf(h, fz, q.z);
@@ -241,7 +225,6 @@ k_dense2(D2Args a, const __grid_constant__ PairTable tab) {
     bool over = false;
     if (leader) {
       const float h = 0.5f * a.dt;
-      float4 q = a.p[atom];
       // closing half kick of the previous step, opening half kick of this one
       q.x = fmaf(h, fx, q.x);
       q.y = fmaf(h, fy, q.y);
@@ -264,9 +247,8 @@ k_dense2(D2Args a, const __grid_constant__ PairTable tab) {
       a.p[atom] = q;
       a.x_next[atom] = r;
       if (a.ref) {
-        const float4 c = __ldg(a.ref + atom);
         float ex, ey, ez;
-        displacement<DIM>(r, c, a.geo, ex, ey, ez);
+        displacement<DIM>(r, rf, a.geo, ex, ey, ez);
         over = ex * ex + ey * ey + ez * ez > a.thr2;
       }
     }

@@ -518,7 +518,7 @@ __device__ __forceinline__ void scan_pair(const CellStream<DIM>& cs, int ns, int
                                           bool staged, const float4* __restrict__ spos,
                                           const Bins& b, int ia, float4 xa, int ib, float4 xb,
                                           const SearchArgs& a, int lane, int& ca, int& cb,
-                                          int32_t* ra, int32_t* rb, int64_t row_cap) {
+                                          int32_t* ra, int32_t* rb, int64_t row_cap, int rs) {
   const unsigned lt = (1u << lane) - 1u;
   for (int base = 0; base < total; base += 32) {
     const int t = base + lane;
@@ -551,18 +551,21 @@ __device__ __forceinline__ void scan_pair(const CellStream<DIM>& cs, int ns, int
     const unsigned mb = __ballot_sync(0xffffffffu, okb);
     if (ra) {
       const int64_t pa = (int64_t)ca + __popc(ma & lt);
-      if (oka && pa < row_cap) ra[pa] = j;
+      if (oka && pa < row_cap) ra[pa * rs] = j;
     }
     if (rb) {
       const int64_t pb = (int64_t)cb + __popc(mb & lt);
-      if (okb && pb < row_cap) rb[pb] = j;
+      if (okb && pb < row_cap) rb[pb * rs] = j;
     }
     ca += __popc(ma);
     cb += __popc(mb);
   }
 }
 
-template <int DIM>
+// TILED: rows go to the engine's tiled layout (entry k of atom i at
+// idx[(i/32)*ld*32 + k*32 + i%32]) without padding; otherwise row-major
+// [n, ld] padded with n up to max_occupancy.
+template <int DIM, bool TILED>
 __global__ void __launch_bounds__(128)
 k_search_cells(const float* __restrict__ x, int64_t stride, Bins b, SearchArgs a, int32_t* idx,
                int64_t ld, int32_t* nbr_count, float* ref, int64_t ref_stride,
@@ -618,17 +621,24 @@ k_search_cells(const float* __restrict__ x, int64_t stride, Bins b, SearchArgs a
     const bool two = q + 1 < cn;
     const int ib = two ? b.sorted_id[cb0 + q + 1] : -1;
     const float4 xb = two ? b.sorted_pos[cb0 + q + 1] : xa;
-    int32_t* ra = idx ? idx + (int64_t)ia * ld : nullptr;
-    int32_t* rb = (idx && two) ? idx + (int64_t)ib * ld : nullptr;
+    auto row_of = [&](int atom) -> int32_t* {
+      if (TILED) return idx + (int64_t)(atom >> 5) * ld * 32 + (atom & 31);
+      return idx + (int64_t)atom * ld;
+    };
+    int32_t* ra = idx ? row_of(ia) : nullptr;
+    int32_t* rb = (idx && two) ? row_of(ib) : nullptr;
+    const int rs = TILED ? 32 : 1;
     int na = 0, nb = 0;
     if (a.geo.periodic)
       scan_pair<DIM, true, false>(cs, ns, total, staged, spos, b, ia, xa, ib, xb, a, lane, na, nb,
-                                  ra, rb, a.width);
+                                  ra, rb, a.width, rs);
     else
       scan_pair<DIM, false, false>(cs, ns, total, staged, spos, b, ia, xa, ib, xb, a, lane, na, nb,
-                                   ra, rb, a.width);
-    if (ra) for (int64_t p = min((int64_t)na, a.width) + lane; p < a.width; p += 32) ra[p] = a.n;
-    if (rb) for (int64_t p = min((int64_t)nb, a.width) + lane; p < a.width; p += 32) rb[p] = a.n;
+                                   ra, rb, a.width, rs);
+    if (!TILED) {
+      if (ra) for (int64_t p = min((int64_t)na, a.width) + lane; p < a.width; p += 32) ra[p] = a.n;
+      if (rb) for (int64_t p = min((int64_t)nb, a.width) + lane; p < a.width; p += 32) rb[p] = a.n;
+    }
     if (lane == 0) {
       if (nbr_count) nbr_count[ia] = na;
       atomicMax(&b.sc->occupancy, (unsigned long long)na);
@@ -774,7 +784,7 @@ template <int DIM, bool VEC4>
 int build_impl(const jmd_nlist* nl, const float* x, int64_t stride, int64_t n64, int32_t* idx,
                int64_t ld, int32_t* nbr_count, int64_t* occupancy, uint8_t* error_code,
                float* ref, int64_t ref_stride, int32_t* flag, void* ws, size_t ws_bytes,
-               cudaStream_t st) {
+               cudaStream_t st, bool tiled = false) {
   const int n = (int)n64;
   const bool cells = nl->use_cell_list != 0;
   Grid g = cells ? make_grid(*nl) : Grid{};
@@ -803,8 +813,11 @@ int build_impl(const jmd_nlist* nl, const float* x, int64_t stride, int64_t n64,
   FinalizeArgs f{nl->format, nl->max_occupancy, cells ? 1 : 0, a.cap, n};
   if (nl->format == JMD_DENSE) {
     if (n > 0) {
-      if (cells)
-        k_search_cells<DIM><<<(unsigned)c, 128, kStageMax * sizeof(float4), st>>>(
+      if (cells && tiled)
+        k_search_cells<DIM, true><<<(unsigned)c, 128, kStageMax * sizeof(float4), st>>>(
+            x, stride, b, a, idx, ld, nbr_count, ref, ref_stride, flag);
+      else if (cells)
+        k_search_cells<DIM, false><<<(unsigned)c, 128, kStageMax * sizeof(float4), st>>>(
             x, stride, b, a, idx, ld, nbr_count, ref, ref_stride, flag);
       else
         k_search<DIM, false, VEC4, 0><<<sgrid, 256, 0, st>>>(x, stride, b, a, idx, ld, nbr_count,
@@ -949,6 +962,25 @@ int jmd_neighbor_list_build(const jmd_nlist* nl, const float* position, int64_t 
             : build_impl<2, false>(nl, position, pos_stride, n, idx, idx_ld, nbr_count, occupancy,
                                    error_code, reference_position, ref_stride, rebuild_flag,
                                    workspace, workspace_bytes, st);
+}
+
+int jmd_neighbor_list_build_tiled(const jmd_nlist* nl, const float* position, int64_t n,
+                                  int32_t* tidx, int64_t depth, int32_t* nbr_count,
+                                  int64_t* occupancy, uint8_t* error_code,
+                                  float* reference_position, int32_t* rebuild_flag,
+                                  void* workspace, size_t workspace_bytes, void* stream) {
+  int e = validate(nl, n);
+  if (e) return e;
+  JMD_REQUIRE(nl->format == JMD_DENSE && nl->use_cell_list, "tiled lists are Dense with a cell grid");
+  JMD_REQUIRE(tidx && nbr_count && depth >= nl->max_occupancy, "tiled list needs depth >= max_occupancy");
+  JMD_REQUIRE(is_vec4(position, 4), "positions must be 16-byte aligned float4 rows");
+  cudaStream_t st = as_stream(stream);
+  if (nl->space.dim == 3)
+    return build_impl<3, true>(nl, position, 4, n, tidx, depth, nbr_count, occupancy, error_code,
+                               reference_position, 4, rebuild_flag, workspace, workspace_bytes, st,
+                               true);
+  return build_impl<2, true>(nl, position, 4, n, tidx, depth, nbr_count, occupancy, error_code,
+                             reference_position, 4, rebuild_flag, workspace, workspace_bytes, st, true);
 }
 
 int jmd_skin_check(const float* position, int64_t pos_stride, const float* reference_position,

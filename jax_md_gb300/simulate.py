@@ -416,7 +416,7 @@ class _SortedBuffers:
         self.xa, self.xb, self.p, self.f, self.ref, self.t4a, self.t4b = (f4() for _ in range(7))
         self.perm, self.tia, self.tib = i4(), i4(), i4()
         self.species = i4() if species else None
-        self.idx = torch.empty((n, ld), dtype=torch.int32, device=device)
+        self.idx = torch.empty(((n + 31) // 32) * 32 * ld, dtype=torch.int32, device=device)
         self.cnt = i4()
         self.err = torch.zeros((), dtype=torch.uint8, device=device)
         self.occ = torch.zeros((), dtype=torch.int64, device=device)

@@ -143,3 +143,43 @@ def test_sorted_run_returns_reference_order_list(cuda):
     d = O.displacement(st.position.contiguous().cpu().numpy(), ref, box)
     assert ((d * d).sum(-1) <= (0.15 ** 2) * (1 + 1e-5) + 0.3 * 0.005).all()
     assert int(nb.error.code) == 0
+
+
+def test_tiled_list_and_forces_match_row_major(cuda):
+    """The engine's tiled layout holds the row-major list's entries in the same order per
+    atom, and the thread-per-atom kernel gives the row-major kernel's forces."""
+    import ctypes
+    from jax_md_gb300 import _native as N, partition
+    R, P, L, nfn, efn, init, apply, st, nb = _setup(cuda, n_cells=8)
+    X = partition.padded_rows(torch.tensor(R, device=cuda))
+    n = X.shape[0]
+    plan = nb.plan
+    depth = plan.ld
+    tidx = torch.full((((n + 31) // 32) * 32 * depth,), -1, dtype=torch.int32, device=cuda)
+    cnt = torch.zeros(n, dtype=torch.int32, device=cuda)
+    occ = torch.zeros((), dtype=torch.int64, device=cuda)
+    err = torch.zeros((), dtype=torch.uint8, device=cuda)
+    ref = torch.zeros((n, 4), device=cuda)
+    ws = torch.empty(plan.workspace.numel(), dtype=torch.uint8, device=cuda)
+    L_ = N.lib()
+    N.check(L_.jmd_neighbor_list_build_tiled(ctypes.byref(plan.nl), X.data_ptr(), n, tidx.data_ptr(),
+                                             depth, cnt.data_ptr(), occ.data_ptr(), err.data_ptr(),
+                                             ref.data_ptr(), None, ws.data_ptr(), ws.numel(),
+                                             N.stream_ptr()))
+    nb2 = nfn.allocate(X)
+    assert torch.equal(cnt, nb2.nbr_count)
+    t = tidx.reshape(-1, depth, 32).permute(0, 2, 1).reshape(-1, depth)[:n]
+    rows = nb2.idx.cpu().numpy()
+    tt = t.cpu().numpy()
+    c = cnt.cpu().numpy()
+    for i in range(0, n, 7):
+        assert np.array_equal(tt[i, :c[i]], rows[i, :c[i]])
+    species, pair = efn._resolve(X, {})
+    sp = efn.geometry.space(3)
+    F = torch.zeros((n, 4), device=cuda)
+    N.check(L_.jmd_pair_forces_tiled(ctypes.byref(pair), ctypes.byref(sp), X.data_ptr(), None, n,
+                                     tidx.data_ptr(), depth, nb2.max_occupancy, cnt.data_ptr(),
+                                     F.data_ptr(), N.stream_ptr()))
+    F0 = efn.forces(X, nb2)
+    torch.cuda.synchronize()
+    assert (F[:, :3] - F0).abs().max().item() < 2e-5
