@@ -484,41 +484,44 @@ __device__ __forceinline__ int stream_index(const CellStream<DIM>& cs, int ns, i
   return cs.beg[k] + m;
 }
 
-// Tests one staged candidate (position, id) against two centre atoms with
-// packed FP32x2 arithmetic; exact minimum image for cells on a periodic face.
-template <int DIM, bool WRAP>
+// Search geometry of one CTA.
+//   PLAIN : free space, raw differences.
+//   FRAME : periodic with >= 4 cells per side.  Every staged coordinate is
+//           moved into the centre cell's frame by subtracting 0 or L (exact,
+//           Sterbenz: only coordinates >= L/2 are shifted), after folding a
+//           coordinate equal to L back to 0; plain differences of the moved
+//           coordinates are then the minimum image with a single rounding.
+//   EXACT : periodic with 3 cells on some side: exact minimum image per test.
+enum { S_PLAIN = 0, S_FRAME = 1, S_EXACT = 2 };
+
+template <int DIM, int GEOM>
 __device__ __forceinline__ void test2(const float4& xa, const float4& xb, const float4& c,
                                       const SearchArgs& a, float& d0, float& d1) {
+  if (GEOM == S_EXACT) {
+    d0 = dist2<DIM>(xa, c, a.geo);
+    d1 = dist2<DIM>(xb, c, a.geo);
+    return;
+  }
   float2 dx = __ffma2_rn(make_float2(c.x, c.x), make_float2(-1.f, -1.f), make_float2(xa.x, xb.x));
   float2 dy = __ffma2_rn(make_float2(c.y, c.y), make_float2(-1.f, -1.f), make_float2(xa.y, xb.y));
-  float2 dz = make_float2(0.f, 0.f);
-  if (DIM == 3)
-    dz = __ffma2_rn(make_float2(c.z, c.z), make_float2(-1.f, -1.f), make_float2(xa.z, xb.z));
-  if (WRAP) {
-    bool w = fabsf(dx.x) > a.geo.halfL[0] || fabsf(dx.y) > a.geo.halfL[0] ||
-             fabsf(dy.x) > a.geo.halfL[1] || fabsf(dy.y) > a.geo.halfL[1];
-    if (DIM == 3) w = w || fabsf(dz.x) > a.geo.halfL[2] || fabsf(dz.y) > a.geo.halfL[2];
-    if (w) {
-      d0 = dist2<DIM>(xa, c, a.geo);
-      d1 = dist2<DIM>(xb, c, a.geo);
-      return;
-    }
-  }
   float2 r2 = __fmul2_rn(dx, dx);
   r2 = __ffma2_rn(dy, dy, r2);
-  if (DIM == 3) r2 = __ffma2_rn(dz, dz, r2);
+  if (DIM == 3) {
+    float2 dz = __ffma2_rn(make_float2(c.z, c.z), make_float2(-1.f, -1.f), make_float2(xa.z, xb.z));
+    r2 = __ffma2_rn(dz, dz, r2);
+  }
   d0 = r2.x;
   d1 = r2.y;
 }
 
 // Scans the cell's candidate stream for the centre atoms ia / ib (ib < 0: none)
 // and appends hits to their rows in stream order.  Lanes own candidates.
-template <int DIM, bool WRAP, bool ORDERED>
+template <int DIM, int GEOM, bool MASK_SELF>
 __device__ __forceinline__ void scan_pair(const CellStream<DIM>& cs, int ns, int total,
                                           bool staged, const float4* __restrict__ spos,
                                           const Bins& b, int ia, float4 xa, int ib, float4 xb,
                                           const SearchArgs& a, int lane, int& ca, int& cb,
-                                          int32_t* ra, int32_t* rb, int64_t row_cap, int rs) {
+                                          int32_t* ra, int32_t* rb, int row_cap, int rs) {
   const unsigned lt = (1u << lane) - 1u;
   for (int base = 0; base < total; base += 32) {
     const int t = base + lane;
@@ -535,28 +538,20 @@ __device__ __forceinline__ void scan_pair(const CellStream<DIM>& cs, int ns, int
       }
       j = __float_as_int(c.w);
       float d0, d1;
-      test2<DIM, WRAP>(xa, xb, c, a, d0, d1);
+      test2<DIM, GEOM>(xa, xb, c, a, d0, d1);
       oka = d0 < a.cut2;
-      okb = ib >= 0 && d1 < a.cut2;
-      if (a.mask_self) {
+      okb = d1 < a.cut2 && ib >= 0;
+      if (MASK_SELF) {
         oka = oka && j != ia;
         okb = okb && j != ib;
-      }
-      if (ORDERED) {
-        oka = oka && j < ia;
-        okb = okb && j < ib;
       }
     }
     const unsigned ma = __ballot_sync(0xffffffffu, oka);
     const unsigned mb = __ballot_sync(0xffffffffu, okb);
-    if (ra) {
-      const int64_t pa = (int64_t)ca + __popc(ma & lt);
-      if (oka && pa < row_cap) ra[pa * rs] = j;
-    }
-    if (rb) {
-      const int64_t pb = (int64_t)cb + __popc(mb & lt);
-      if (okb && pb < row_cap) rb[pb * rs] = j;
-    }
+    const int pa = ca + __popc(ma & lt);
+    const int pb = cb + __popc(mb & lt);
+    if (oka && pa < row_cap) ra[pa * rs] = j;
+    if (okb && pb < row_cap) rb[pb * rs] = j;
     ca += __popc(ma);
     cb += __popc(mb);
   }
@@ -573,26 +568,48 @@ k_search_cells(const float* __restrict__ x, int64_t stride, Bins b, SearchArgs a
   if (skip(flag)) return;
   extern __shared__ float4 spos[];  // kStageMax candidates: xyz + id (as the w bits)
   __shared__ CellStream<DIM> cs;
+  __shared__ float soff[27][3];     // per neighbour cell: amount subtracted (FRAME)
+  __shared__ float coff[3];         // for the centre cell's atoms
   const int c = blockIdx.x;
   const int ns = DIM == 3 ? 27 : 9;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int c0 = c % a.grid.cps[0];
-  const int c1 = (c / a.grid.cps[0]) % a.grid.cps[1];
-  const int c2 = DIM == 3 ? c / (a.grid.cps[0] * a.grid.cps[1]) : 0;
+  int cc[3];
+  cc[0] = c % a.grid.cps[0];
+  cc[1] = (c / a.grid.cps[0]) % a.grid.cps[1];
+  cc[2] = DIM == 3 ? c / (a.grid.cps[0] * a.grid.cps[1]) : 0;
+  bool frame = a.geo.periodic != 0;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) frame = frame && a.grid.cps[d] >= 4;
+  const int geom = !a.geo.periodic ? S_PLAIN : (frame ? S_FRAME : S_EXACT);
   if (threadIdx.x < ns) {
     const int k = threadIdx.x;
-    int sh0, sh1, sh2;
-    if (DIM == 3) { sh0 = k / 9 - 1; sh1 = (k / 3) % 3 - 1; sh2 = k % 3 - 1; }
-    else { sh0 = k / 3 - 1; sh1 = k % 3 - 1; sh2 = 0; }
-    int q0 = c0 + sh0, q1 = c1 + sh1, q2 = c2 + sh2;
-    q0 = q0 < 0 ? q0 + a.grid.cps[0] : (q0 >= a.grid.cps[0] ? q0 - a.grid.cps[0] : q0);
-    q1 = q1 < 0 ? q1 + a.grid.cps[1] : (q1 >= a.grid.cps[1] ? q1 - a.grid.cps[1] : q1);
-    if (DIM == 3) q2 = q2 < 0 ? q2 + a.grid.cps[2] : (q2 >= a.grid.cps[2] ? q2 - a.grid.cps[2] : q2);
-    const int h = q0 + q1 * a.grid.mult[1] + (DIM == 3 ? q2 * a.grid.mult[2] : 0);
+    int sh[3];
+    if (DIM == 3) { sh[0] = k / 9 - 1; sh[1] = (k / 3) % 3 - 1; sh[2] = k % 3 - 1; }
+    else { sh[0] = k / 3 - 1; sh[1] = k % 3 - 1; sh[2] = 0; }
+    int q[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      int v = cc[d] + sh[d];
+      v = v < 0 ? v + a.grid.cps[d] : (v >= a.grid.cps[d] ? v - a.grid.cps[d] : v);
+      q[d] = v;
+      // FRAME: shift by L the coordinates that lie in the upper half of the box
+      // as seen from the centre cell: a wrapped lower neighbour of a centre at
+      // the low face, or every non-wrapped cell of a centre at the high face.
+      float o = 0.f;
+      if (cc[d] == 0 && sh[d] == -1) o = a.geo.L[d];
+      if (cc[d] == a.grid.cps[d] - 1 && sh[d] != 1) o = a.geo.L[d];
+      soff[k][d] = o;
+    }
+    const int h = q[0] + q[1] * a.grid.mult[1] + (DIM == 3 ? q[2] * a.grid.mult[2] : 0);
     const int beg = b.start[h], end = b.start[h + 1];
     cs.beg[k] = beg;
     cs.cnt[k] = end - beg;
     cs.split[k] = a.cap - (beg % a.cap);
+  }
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      coff[d] = (d < DIM && cc[d] == a.grid.cps[d] - 1) ? a.geo.L[d] : 0.f;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -602,39 +619,72 @@ k_search_cells(const float* __restrict__ x, int64_t stride, Bins b, SearchArgs a
   }
   __syncthreads();
   const int total = cs.off[ns];
+  // the shifted frame is applied only to staged streams
   const bool staged = total <= kStageMax;
+  const int g2 = (geom == S_FRAME && !staged) ? S_EXACT : geom;
   if (staged) {
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
       const int s = stream_index<DIM>(cs, ns, t);
       float4 v = b.sorted_pos[s];
+      if (g2 == S_FRAME) {
+        int lo = 0, hi = ns - 1;  // cell of stream position t
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (cs.off[mid] <= t) lo = mid; else hi = mid - 1;
+        }
+        v.x = (v.x >= a.geo.L[0] ? v.x - a.geo.L[0] : v.x) - soff[lo][0];
+        v.y = (v.y >= a.geo.L[1] ? v.y - a.geo.L[1] : v.y) - soff[lo][1];
+        if (DIM == 3) v.z = (v.z >= a.geo.L[2] ? v.z - a.geo.L[2] : v.z) - soff[lo][2];
+      }
       v.w = __int_as_float(b.sorted_id[s]);
       spos[t] = v;
     }
   }
   __syncthreads();
-  // Positions inside the box cannot wrap for cells off the faces; the wrap
-  // test still runs there (cheaply) so positions at exactly L stay exact.
+  auto centre = [&](float4 v) -> float4 {
+    if (g2 == S_FRAME) {
+      v.x = (v.x >= a.geo.L[0] ? v.x - a.geo.L[0] : v.x) - coff[0];
+      v.y = (v.y >= a.geo.L[1] ? v.y - a.geo.L[1] : v.y) - coff[1];
+      if (DIM == 3) v.z = (v.z >= a.geo.L[2] ? v.z - a.geo.L[2] : v.z) - coff[2];
+    }
+    return v;
+  };
   const int cb0 = b.start[c], cn = b.start[c + 1] - cb0;
-  for (int q = 2 * warp; q < cn; q += 2 * nw) {
-    const int ia = b.sorted_id[cb0 + q];
-    const float4 xa = b.sorted_pos[cb0 + q];
-    const bool two = q + 1 < cn;
-    const int ib = two ? b.sorted_id[cb0 + q + 1] : -1;
-    const float4 xb = two ? b.sorted_pos[cb0 + q + 1] : xa;
+  const int row_cap = (int)min(a.width, (int64_t)INT32_MAX);
+  const int rs = TILED ? 32 : 1;
+  for (int qa = 2 * warp; qa < cn; qa += 2 * nw) {
+    const int ia = b.sorted_id[cb0 + qa];
+    const float4 pa = b.sorted_pos[cb0 + qa];
+    const bool two = qa + 1 < cn;
+    const int ib = two ? b.sorted_id[cb0 + qa + 1] : -1;
+    const float4 pb = two ? b.sorted_pos[cb0 + qa + 1] : pa;
+    const float4 xa = centre(pa), xb = centre(pb);
     auto row_of = [&](int atom) -> int32_t* {
+      if (!idx || atom < 0) return nullptr;
       if (TILED) return idx + (int64_t)(atom >> 5) * ld * 32 + (atom & 31);
       return idx + (int64_t)atom * ld;
     };
-    int32_t* ra = idx ? row_of(ia) : nullptr;
-    int32_t* rb = (idx && two) ? row_of(ib) : nullptr;
-    const int rs = TILED ? 32 : 1;
+    int32_t* ra = row_of(ia);
+    int32_t* rb = row_of(ib);
+    // no rows (count pass): capacity 0 suppresses every write; a missing
+    // second atom never matches (ib < 0), so rb is never written
+    const int cap = idx ? row_cap : 0;
     int na = 0, nb = 0;
-    if (a.geo.periodic)
-      scan_pair<DIM, true, false>(cs, ns, total, staged, spos, b, ia, xa, ib, xb, a, lane, na, nb,
-                                  ra, rb, a.width, rs);
-    else
-      scan_pair<DIM, false, false>(cs, ns, total, staged, spos, b, ia, xa, ib, xb, a, lane, na, nb,
-                                   ra, rb, a.width, rs);
+    if (a.mask_self) {
+      if (g2 == S_FRAME)
+        scan_pair<DIM, S_FRAME, true>(cs, ns, total, staged, spos, b, ia, xa, ib, xb, a, lane, na, nb, ra, rb, cap, rs);
+      else if (g2 == S_EXACT)
+        scan_pair<DIM, S_EXACT, true>(cs, ns, total, staged, spos, b, ia, xa, ib, xb, a, lane, na, nb, ra, rb, cap, rs);
+      else
+        scan_pair<DIM, S_PLAIN, true>(cs, ns, total, staged, spos, b, ia, xa, ib, xb, a, lane, na, nb, ra, rb, cap, rs);
+    } else {
+      if (g2 == S_FRAME)
+        scan_pair<DIM, S_FRAME, false>(cs, ns, total, staged, spos, b, ia, xa, ib, xb, a, lane, na, nb, ra, rb, cap, rs);
+      else if (g2 == S_EXACT)
+        scan_pair<DIM, S_EXACT, false>(cs, ns, total, staged, spos, b, ia, xa, ib, xb, a, lane, na, nb, ra, rb, cap, rs);
+      else
+        scan_pair<DIM, S_PLAIN, false>(cs, ns, total, staged, spos, b, ia, xa, ib, xb, a, lane, na, nb, ra, rb, cap, rs);
+    }
     if (!TILED) {
       if (ra) for (int64_t p = min((int64_t)na, a.width) + lane; p < a.width; p += 32) ra[p] = a.n;
       if (rb) for (int64_t p = min((int64_t)nb, a.width) + lane; p < a.width; p += 32) rb[p] = a.n;
@@ -643,12 +693,12 @@ k_search_cells(const float* __restrict__ x, int64_t stride, Bins b, SearchArgs a
       if (nbr_count) nbr_count[ia] = na;
       atomicMax(&b.sc->occupancy, (unsigned long long)na);
       if (na > a.width) atomicOr(&b.sc->flags, (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
-      if (ref) store_row_full<DIM, false>(ref, ref_stride, ia, xa);
+      if (ref) store_row_full<DIM, false>(ref, ref_stride, ia, pa);
       if (two) {
         if (nbr_count) nbr_count[ib] = nb;
         atomicMax(&b.sc->occupancy, (unsigned long long)nb);
         if (nb > a.width) atomicOr(&b.sc->flags, (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
-        if (ref) store_row_full<DIM, false>(ref, ref_stride, ib, xb);
+        if (ref) store_row_full<DIM, false>(ref, ref_stride, ib, pb);
       }
     }
   }

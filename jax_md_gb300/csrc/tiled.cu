@@ -91,9 +91,10 @@ k_tiled(TArgs a, const __grid_constant__ PairTable tab) {
     const float rc0 = SPECIES ? cc.rc2.x : rc2m, rc1 = SPECIES ? cc.rc2.y : rc2m;
     const bool m0 = r2.x < rc0 && r2.x > 0.f;
     const bool m1 = r2.y < rc1 && r2.y > 0.f;
-    const float2 r2s = f2(m0 ? r2.x : 1.f, m1 ? r2.y : 1.f);
+    // masked pairs (beyond the cutoff, or the atom itself at r2 = 0) may give
+    // inf/NaN here; the selects below discard them
     float2 U, g;
-    pair_eval2<KIND, false>(r2s, cc, U, g);
+    pair_eval2<KIND, false>(r2, cc, U, g);
     g.x = m0 ? g.x : 0.f;
     g.y = m1 ? g.y : 0.f;
     ax = fma2(g, dx, ax);
@@ -101,14 +102,22 @@ k_tiled(TArgs a, const __grid_constant__ PairTable tab) {
     if (DIM == 3) az = fma2(g, dz, az);
   };
 
-  // entries past the count point at the atom itself (distance 0: masked)
+  // Entries past the count point at the atom itself (distance 0: masked).
+  // The column indices of the next four entries are loaded while the current
+  // four positions are gathered, so each iteration waits on one memory
+  // latency (the gathers) instead of two.
+  int jn[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) jn[u] = (u < c) ? __ldcs(col + u * 32) : i;
   for (int k0 = 0; k0 < c; k0 += 4) {
     int j[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) j[u] = (k0 + u < c) ? __ldcs(col + (int64_t)(k0 + u) * 32) : i;
+    for (int u = 0; u < 4; ++u) j[u] = jn[u];
     float4 b[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) b[u] = ldg_keep(a.x + j[u], pol);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) jn[u] = (k0 + 4 + u < c) ? __ldcs(col + (k0 + 4 + u) * 32) : i;
     pair2(j[0], j[1], b[0], b[1]);
     if (k0 + 2 < c) pair2(j[2], j[3], b[2], b[3]);
   }
