@@ -233,6 +233,24 @@ int jmd_nhc_half_step(const jmd_nhc* c, double* chain,
                       const double* kinetic_energy, int32_t update_mass,
                       double* p_scale, void* stream);
 
+/* FIRE (minimize.fire_descent, minimize.py:124-226) on float4 rows with the
+ * minimiser's scalars kept on the device: fire_state[6] floats
+ * {dt, alpha, n_pos, keep, alpha_mix, |P|/|F|}, initialised by the caller to
+ * {dt_start, alpha_start, 0, 1, 0, 0}.  One FIRE step is
+ *   jmd_fire_kick_drift (p += dt/2 f; x = shift(x, dt p / m)),
+ *   the force of the new positions (any pair entry point),
+ *   jmd_fire_update (p += dt/2 f; f64 |F|, |P|, F.P; the scalar update of
+ *   dt / alpha / n_pos; P mixing and the reset when F.P < 0). */
+int jmd_fire_kick_drift(float* position, float* momentum, const float* force,
+                        const float* mass, float mass_scalar, int64_t n,
+                        const jmd_space* space, const float* fire_state,
+                        void* stream);
+size_t jmd_fire_workspace_bytes(int64_t n);
+int jmd_fire_update(float* momentum, const float* force, int64_t n, int32_t dim,
+                    float* fire_state, float dt_max, float n_min, float f_inc,
+                    float f_dec, float alpha_start, float f_alpha,
+                    void* workspace, size_t workspace_bytes, void* stream);
+
 /* p *= *scale. */
 int jmd_scale_momentum(float* momentum, int64_t p_stride, int64_t n,
                        int32_t dim, const double* scale, void* stream);

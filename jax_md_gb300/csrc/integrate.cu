@@ -196,6 +196,99 @@ __global__ void k_nhc_half(NhcArgs a, double* chain, const double* ke_in, double
   *p_scale = scale;
 }
 
+// ------------------------------------------------------------- FIRE ------
+// FIRE state on the device (float32 like the reference's scalars):
+//   [0] dt  [1] alpha  [2] n_pos (as float)  [3] keep (F.P >= 0)
+//   [4] alpha used for this step's mixing  [5] |P| / |F|
+struct FireParams {
+  float dt_max, n_min, f_inc, f_dec, alpha_start, f_alpha;
+};
+
+template <int DIM>
+__global__ void k_fire_kick_drift(float4* x, float4* p, const float4* f, const float* mass,
+                                  float m0, int n, Geo g, const float* fs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float dt = fs[0];
+  const float h = dt * 0.5f;
+  float4 q = p[i];
+  const float4 ff = f[i];
+  float4 r = x[i];
+  q.x = fmaf(h, ff.x, q.x);
+  q.y = fmaf(h, ff.y, q.y);
+  q.z = fmaf(h, ff.z, q.z);
+  const float m = mass ? mass[i] : m0;
+  const float dx = dt * q.x / m, dy = dt * q.y / m, dz = dt * q.z / m;
+  if (g.periodic) {
+    r.x = wrap(r.x + dx, g.L[0]);
+    r.y = wrap(r.y + dy, g.L[1]);
+    if (DIM == 3) r.z = wrap(r.z + dz, g.L[2]);
+  } else {
+    r.x += dx;
+    r.y += dy;
+    if (DIM == 3) r.z += dz;
+  }
+  p[i] = q;
+  x[i] = r;
+}
+
+// Closing half kick, then the three FIRE reductions (|F|^2, |P|^2, F.P) in
+// f64; k_fire_scalar then runs the scalar update of minimize.py:190-224.
+template <int DIM>
+__global__ void k_fire_finish(float4* p, const float4* f, int n, const float* fs,
+                              double* partials, unsigned int* counter, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[3] = {0.0, 0.0, 0.0};
+  if (i < n) {
+    const float h = fs[0] * 0.5f;
+    float4 q = p[i];
+    const float4 ff = f[i];
+    q.x = fmaf(h, ff.x, q.x);
+    q.y = fmaf(h, ff.y, q.y);
+    q.z = fmaf(h, ff.z, q.z);
+    p[i] = q;
+    v[0] = (double)ff.x * ff.x + (double)ff.y * ff.y + (DIM == 3 ? (double)ff.z * ff.z : 0.0);
+    v[1] = (double)q.x * q.x + (double)q.y * q.y + (DIM == 3 ? (double)q.z * q.z : 0.0);
+    v[2] = (double)ff.x * q.x + (double)ff.y * q.y + (DIM == 3 ? (double)ff.z * q.z : 0.0);
+  }
+  grid_reduce<3>(v, partials, counter, out, false);
+}
+
+__global__ void k_fire_scalar(float* fs, FireParams fp, const double* red) {
+  if (threadIdx.x != 0) return;
+  const float F_norm = (float)sqrt(red[0] + 1e-6);
+  const float P_norm = (float)sqrt(red[1]);
+  const float F_dot_P = (float)red[2];
+  float dt = fs[0], alpha = fs[1], n_pos = fs[2];
+  fs[4] = alpha;                          // mixing uses the current alpha
+  fs[5] = P_norm / F_norm;
+  n_pos = F_dot_P >= 0.f ? n_pos + 1.f : 0.f;
+  if (F_dot_P > 0.f && n_pos > fp.n_min) {
+    dt = fminf(dt * fp.f_inc, fp.dt_max);
+    alpha = alpha * fp.f_alpha;
+  }
+  if (F_dot_P < 0.f) {
+    dt = dt * fp.f_dec;
+    alpha = fp.alpha_start;
+  }
+  fs[0] = dt;
+  fs[1] = alpha;
+  fs[2] = n_pos;
+  fs[3] = F_dot_P >= 0.f ? 1.f : 0.f;
+}
+
+__global__ void k_fire_mix(float4* p, const float4* f, int n, const float* fs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float alpha = fs[4], ratio = fs[5], keep = fs[3];
+  float4 q = p[i];
+  const float4 ff = f[i];
+  q.x = keep * (q.x + alpha * (ff.x * ratio - q.x));
+  q.y = keep * (q.y + alpha * (ff.y * ratio - q.y));
+  q.z = keep * (q.z + alpha * (ff.z * ratio - q.z));
+  p[i] = q;
+}
+
 struct ReduceWs {
   double* partials;
   unsigned int* counter;
@@ -339,6 +432,62 @@ int jmd_scale_momentum(float* momentum, int64_t p_stride, int64_t n, int32_t dim
   if (dim == 3) k_scale<3><<<gr, 256, 0, as_stream(stream)>>>(momentum, p_stride, (int)n, scale);
   else k_scale<2><<<gr, 256, 0, as_stream(stream)>>>(momentum, p_stride, (int)n, scale);
   return check_launch("jmd_scale_momentum");
+}
+
+int jmd_fire_kick_drift(float* position, float* momentum, const float* force, const float* mass,
+                        float mass_scalar, int64_t n, const jmd_space* space,
+                        const float* fire_state, void* stream) {
+  JMD_REQUIRE(space && (space->dim == 2 || space->dim == 3), "bad space");
+  JMD_REQUIRE(is_vec4(position, 4) && is_vec4(momentum, 4) && is_vec4(force, 4),
+              "FIRE needs 16-byte aligned float4 rows");
+  if (n <= 0) return JMD_OK;
+  const unsigned gr = (unsigned)ceil_div(n, 256);
+  Geo g = make_geo(*space);
+  auto* x4 = reinterpret_cast<float4*>(position);
+  auto* p4 = reinterpret_cast<float4*>(momentum);
+  auto* f4 = reinterpret_cast<const float4*>(force);
+  if (space->dim == 3)
+    k_fire_kick_drift<3><<<gr, 256, 0, as_stream(stream)>>>(x4, p4, f4, mass, mass_scalar, (int)n, g, fire_state);
+  else
+    k_fire_kick_drift<2><<<gr, 256, 0, as_stream(stream)>>>(x4, p4, f4, mass, mass_scalar, (int)n, g, fire_state);
+  return check_launch("jmd_fire_kick_drift");
+}
+
+int jmd_fire_update(float* momentum, const float* force, int64_t n, int32_t dim,
+                    float* fire_state, float dt_max, float n_min, float f_inc, float f_dec,
+                    float alpha_start, float f_alpha, void* workspace, size_t workspace_bytes,
+                    void* stream) {
+  JMD_REQUIRE(dim == 2 || dim == 3, "dim must be 2 or 3");
+  JMD_REQUIRE(is_vec4(momentum, 4) && is_vec4(force, 4), "FIRE needs 16-byte aligned float4 rows");
+  cudaStream_t st = as_stream(stream);
+  Carver cv(workspace, workspace_bytes);
+  double* partials = cv.take<double>(kMaxReduceBlocks * 3);
+  unsigned int* counter = cv.take<unsigned int>(1);
+  double* red = cv.take<double>(4);
+  if (!cv.ok()) return fail(JMD_ERR_WORKSPACE, "FIRE workspace too small");
+  if (n <= 0) return JMD_OK;
+  const int64_t gr = ceil_div(n, 256);
+  if (gr > kMaxReduceBlocks) return fail(JMD_ERR_UNSUPPORTED, "system too large");
+  FireParams fp{dt_max, n_min, f_inc, f_dec, alpha_start, f_alpha};
+  JMD_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), st));
+  auto* p4 = reinterpret_cast<float4*>(momentum);
+  auto* f4 = reinterpret_cast<const float4*>(force);
+  if (dim == 3)
+    k_fire_finish<3><<<(unsigned)gr, 256, 0, st>>>(p4, f4, (int)n, fire_state, partials, counter, red);
+  else
+    k_fire_finish<2><<<(unsigned)gr, 256, 0, st>>>(p4, f4, (int)n, fire_state, partials, counter, red);
+  k_fire_scalar<<<1, 32, 0, st>>>(fire_state, fp, red);
+  k_fire_mix<<<(unsigned)gr, 256, 0, st>>>(p4, f4, (int)n, fire_state);
+  return check_launch("jmd_fire_update");
+}
+
+size_t jmd_fire_workspace_bytes(int64_t n) {
+  (void)n;
+  Carver cv(nullptr, 0);
+  cv.take<double>(kMaxReduceBlocks * 3);
+  cv.take<unsigned int>(1);
+  cv.take<double>(4);
+  return cv.used + 256;
 }
 
 }  // extern "C"
