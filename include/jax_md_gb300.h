@@ -177,6 +177,28 @@ int jmd_pair_forces(const jmd_pair* pp, const jmd_space* space, int32_t format,
                     float* per_atom_energy, double* virial, void* workspace,
                     size_t workspace_bytes, void* stream);
 
+/* --------------------------------------------------------------- adjoint -- */
+
+/* Vector-Jacobian product of the Dense-list pair force F(R; sigma, eps) with a
+ * cotangent lam [n, cot_stride] (the reverse-mode derivative jax.grad takes
+ * through smap.pair_neighbor_list + quantity.force; the LJ cutoff radii follow
+ * sigma as in energy.py:319-320).  Accumulates, scaled by `weight`:
+ *   grad_position [n, grad_stride] += weight * (dF/dR)^T lam   (optional)
+ *   grad_params[130] += weight * d(lam . F)/d theta             (optional)
+ * and, unscaled, grad_energy_params[130] += dE/d theta           (optional),
+ * with bins [a*8+b] = sigma[a][b], [64+a*8+b] = epsilon[a][b] and [128] = the
+ * global cutoff scale max(sigma) (to be credited to the largest sigma entry;
+ * per-pair cutoffs credit sigma[a][b] directly).  Scalar parameters use bin 0
+ * and 64.  Assumes a symmetric list, as built by jmd_neighbor_list_build. */
+int jmd_pair_force_vjp(const jmd_pair* pp, const jmd_space* space,
+                       const float* position, int64_t pos_stride,
+                       const int32_t* species, int64_t n, const int32_t* idx,
+                       int64_t idx_ld, int64_t idx_width,
+                       const int32_t* nbr_count, const float* cotangent,
+                       int64_t cot_stride, float weight, float* grad_position,
+                       int64_t grad_stride, double* grad_params,
+                       double* grad_energy_params, void* stream);
+
 /* ---------------------------------------------------------- integrators -- */
 
 /* momentum_step (simulate.py:168-173): p += dt * f. */
@@ -414,6 +436,39 @@ int jmd_nve_run_sorted(const jmd_nve_system* sys, const jmd_sorted_state* sorted
 
 /* Drops every cached graph of the engine. */
 int jmd_engine_clear_cache(void);
+
+/* ------------------------------------------------------ engine adjoint -- */
+
+/* jmd_nve_run with the positions recorded: `trajectory` (optional) holds
+ * n_steps + 1 blocks of n float4 rows; block k receives x_k (block 0 a copy
+ * of the starting position), and the final position is also left in
+ * sys->position.  force_rebuild != 0 rebuilds the list at x_0 whatever the
+ * skin test says, so a run restarted from the same (position, momentum,
+ * force) repeats bit for bit (every kernel on the path is deterministic).
+ * The reverse-mode derivative of the reference's simulation loop
+ * (simulate.py:227-243 under jax.grad) keeps its trajectory in the same way;
+ * the recording replaces that tape. */
+int jmd_nve_run_recorded(const jmd_nve_system* sys, float* trajectory, int64_t n_steps,
+                         int32_t force_rebuild, int32_t use_graph, void* stream);
+
+/* Reverse pass of velocity Verlet over a recorded segment x_0..x_{n_steps}
+ * (trajectory as written by jmd_nve_run_recorded).  With cotangents
+ * xbar = dL/dx, pbar = dL/dp of the segment's end state (float4 rows, updated
+ * in place to those of its start state):
+ *   closing != 0:  xbar += dt/2 (dF/dR)^T(x_n) pbar    (the closing half kick
+ *                  of the run's last step; set on the last segment only)
+ *   for k = n_steps-1 .. 0:
+ *       q = pbar + (dt/m) xbar;  xbar += w_k (dF/dR)^T(x_k) q;  pbar = q
+ *   with w_k = dt, except dt/2 for k = 0 when opening != 0 (the first segment
+ *   of the run, whose initial force is F(x_0)).
+ * grad_params (optional, [130] doubles) accumulates the matching
+ * d/d(sigma, epsilon, cutoff scale) in the bins of jmd_pair_force_vjp.
+ * The system's list buffers are used (and left valid for some x_k);
+ * record_scratch is 2n float4 rows.  use_graph as for jmd_nve_run. */
+int jmd_nve_adjoint_segment(const jmd_nve_system* sys, const float* trajectory,
+                            int64_t n_steps, int32_t closing, int32_t opening, float* xbar,
+                            float* pbar, float* record_scratch, double* grad_params,
+                            int32_t use_graph, void* stream);
 
 #ifdef __cplusplus
 }

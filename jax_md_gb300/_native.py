@@ -117,6 +117,11 @@ SIGNATURES = {
                                         P, P, P]),
     'jmd_nve_fused_step_tiled': (C.c_int, [C.POINTER(Pair), C.POINTER(Space), P, P, P, F32, P, I64,
                                            P, I64, I64, P, F32, P, F32, P, P]),
+    'jmd_pair_force_vjp': (C.c_int, [C.POINTER(Pair), C.POINTER(Space), P, I64, P, I64, P, I64,
+                                     I64, P, P, I64, F32, P, I64, P, P, P]),
+    'jmd_nve_run_recorded': (C.c_int, [C.POINTER(NveSystem), P, I64, I32, I32, P]),
+    'jmd_nve_adjoint_segment': (C.c_int, [C.POINTER(NveSystem), P, I64, I32, I32, P, P, P, P, I32,
+                                          P]),
     'jmd_fire_kick_drift': (C.c_int, [P, P, P, P, F32, I64, C.POINTER(Space), P, P]),
     'jmd_fire_workspace_bytes': (SZ, [I64]),
     'jmd_fire_update': (C.c_int, [P, P, I64, I32, P, F32, F32, F32, F32, F32, F32, P, SZ, P]),

@@ -1,0 +1,549 @@
+// Adjoint of the pair force and of velocity Verlet.
+//
+// Reference: the forces of jax_md/smap.py:922-979 + quantity.py:58-60 and
+// their derivatives as jax.grad would take them, including the dependence of
+// the LJ cutoff radii on sigma (energy.py:319-320: r_onset = 2 max(sigma),
+// r_cutoff = 2.5 max(sigma)); velocity Verlet of simulate.py:227-243.
+//
+// With d = R_k - R_j, g = U'(r)/r, the force is F_k = -sum_j g d and its
+// Jacobian blocks are J = g I + ((U'' - g)/r^2) d d^T.  For a symmetric
+// (Dense, full) list the VJP with cotangent lam is
+//   gR_k = sum_{j in N(k)} J_kj (lam_j - lam_k)
+// (each atom sums its own row, no atomics on positions).  A Dense entry (k, j)
+// carries half of the pair energy with the parameters of (s_k, s_j), so the
+// parameter gradient of L = lam . F per entry is
+//   dL/d theta[s_k][s_j] += 1/2 (dg/d theta) (lam_j - lam_k) . d.
+#include "pair.cuh"
+
+namespace jmd {
+namespace {
+
+// Bins of the parameter gradient: [a*8+b] sigma, [64 + a*8+b] epsilon,
+// [128] the cutoff scale (max sigma) when the cutoff is global.
+constexpr int kBins = 130;
+
+// Per-pair quantities of the potential and their parameter derivatives.
+struct PairD {
+  float g, hh;              // U'/r and U''
+  float U;                  // energy
+  float dg_s, dg_e, dg_k;   // d g / d sigma, d eps, d cutoff scale
+  float dU_s, dU_e, dU_k;   // d U / ...
+};
+
+template <int KIND>
+__device__ __forceinline__ PairD pair_derivs(float r2, const PairCoef& c, float sigma, float kappa) {
+  PairD o;
+  if (KIND == JMD_SOFT_SPHERE) {
+    const float r = sqrtf(r2);
+    const float is = c.inv_sig;
+    const float b = 1.0f - r * is;
+    const float al = c.alpha;
+    const float pa2 = al == 2.0f ? 1.0f : __powf(b, al - 2.0f);
+    const float pa1 = al == 2.0f ? b : __powf(b, al - 1.0f);
+    const float U = c.eps / al * pa1 * b;
+    const float dU = -c.eps * is * pa1;            // U'
+    const float d2U = c.eps * (al - 1.0f) * is * is * pa2;
+    o.U = U;
+    o.g = dU / r;
+    o.hh = d2U;
+    o.dU_e = U / c.eps;
+    o.dg_e = o.g / c.eps;
+    o.dU_s = c.eps * pa1 * r * is * is;
+    const float dUp_s = c.eps * is * is * pa1 - c.eps * is * (al - 1.0f) * pa2 * r * is * is;
+    o.dg_s = dUp_s / r;
+    o.dg_k = 0.f;
+    o.dU_k = 0.f;
+    return o;
+  }
+  const float ir2 = 1.0f / r2;
+  const float s2 = c.sig2 * ir2;
+  const float s6 = s2 * s2 * s2, s12 = s6 * s6;
+  const float e4 = 4.0f * c.eps;
+  const float U0 = e4 * (s12 - s6);
+  const float U0p_r = e4 * (6.0f * s6 - 12.0f * s12) * ir2;    // U0' / r
+  const float U0pp = e4 * (156.0f * s12 - 42.0f * s6) * ir2;   // U0''
+  const float is = 1.0f / sigma;
+  const float dU0_s = e4 * (12.0f * s12 - 6.0f * s6) * is;
+  const float dU0p_r_s = e4 * (36.0f * s6 - 144.0f * s12) * ir2 * is;  // d(U0'/r)/d sigma
+  float S = 1.f, Su = 0.f, Suu = 0.f, dS_k = 0.f, dSu_k = 0.f;
+  if (KIND == JMD_LJ && r2 > c.ro2) {
+    const float A = c.rc2 - r2;
+    const float B = c.rc2 + 2.0f * r2 - 3.0f * c.ro2;
+    const float idn = c.inv_den;
+    const float w = c.rc2 - c.ro2;
+    S = A * A * B * idn;
+    Su = 6.0f * A * (c.ro2 - r2) * idn;
+    Suu = 6.0f * (2.0f * r2 - c.rc2 - c.ro2) * idn;
+    const float dS_rc = (2.0f * A * B + A * A) * idn - 3.0f * S / w;
+    const float dS_ro = -3.0f * A * A * idn + 3.0f * S / w;
+    const float dSu_rc = 6.0f * (c.ro2 - r2) * idn - 3.0f * Su / w;
+    const float dSu_ro = 6.0f * A * idn + 3.0f * Su / w;
+    const float ik = 2.0f / kappa;  // d(r^2_cut)/d kappa = 2 r^2_cut / kappa
+    dS_k = (dS_ro * c.ro2 + dS_rc * c.rc2) * ik;
+    dSu_k = (dSu_ro * c.ro2 + dSu_rc * c.rc2) * ik;
+  }
+  // U = U0 S ; U'/r = (U0'/r) S + 2 U0 Su ; U'' = U0'' S + 2 U0' S' + U0 S''
+  o.U = U0 * S;
+  o.g = U0p_r * S + 2.0f * U0 * Su;
+  const float Sp_r = 2.0f * Su;                        // S'/r
+  o.hh = U0pp * S + 2.0f * (U0p_r * r2) * Sp_r + U0 * (4.0f * r2 * Suu + 2.0f * Su);
+  o.dU_e = o.U / c.eps;
+  o.dg_e = o.g / c.eps;
+  o.dU_s = dU0_s * S;
+  o.dg_s = dU0p_r_s * S + 2.0f * dU0_s * Su;
+  o.dU_k = U0 * dS_k;
+  o.dg_k = U0p_r * dS_k + 2.0f * U0 * dSu_k;
+  return o;
+}
+
+// Per-thread accumulators of one row of bins (the row is the species of the
+// thread's atom; NB = 8 with species, 1 without).  Entries are picked with
+// unrolled compares so the arrays stay in registers.
+template <int NB>
+struct BinAcc {
+  float s[NB], e[NB], k;
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int b = 0; b < NB; ++b) s[b] = e[b] = 0.f;
+    k = 0.f;
+  }
+  __device__ __forceinline__ void add(int col, float vs, float ve, float vk, bool per_pair) {
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      if (b == col) {
+        s[b] += per_pair ? vs + vk : vs;
+        e[b] += ve;
+      }
+    }
+    if (!per_pair) k += vk;
+  }
+  // Sums over the `width` lanes of a lane group (all of them share a row).
+  // Every lane of the warp must take part (ncol is uniform across the warp).
+  __device__ __forceinline__ void group_sum(int width, int ncol) {
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      if (b < ncol) {
+        for (int o = width / 2; o > 0; o >>= 1) {
+          s[b] += __shfl_xor_sync(0xffffffffu, s[b], o, width);
+          e[b] += __shfl_xor_sync(0xffffffffu, e[b], o, width);
+        }
+      }
+    }
+    for (int o = width / 2; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o, width);
+  }
+  __device__ __forceinline__ void flush(float* bins, int row, int ncol) {
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      if (b < ncol && s[b] != 0.f) atomicAdd(&bins[row * JMD_MAX_SPECIES + b], s[b]);
+      if (b < ncol && e[b] != 0.f) atomicAdd(&bins[64 + row * JMD_MAX_SPECIES + b], e[b]);
+    }
+    if (k != 0.f) atomicAdd(&bins[128], k);
+  }
+};
+
+__device__ __forceinline__ void zero_bins(float* bins) {
+  for (int b = threadIdx.x; b < kBins; b += blockDim.x) bins[b] = 0.f;
+}
+
+__device__ __forceinline__ void publish_bins(const float* bins, double* out, double scale) {
+  for (int b = threadIdx.x; b < kBins; b += blockDim.x)
+    if (out && bins[b] != 0.f) atomicAdd(out + b, scale * (double)bins[b]);
+}
+
+// Shared sigma lookups of the derivative formulas: sigma of each (a, b) in the
+// pad slot of a second table, max sigma (the global cutoff scale) in its pad.
+PairTable sigma_table(const jmd_pair& pp) {
+  PairTable sg;
+  memset(&sg, 0, sizeof(sg));
+  const int S = pp.n_species > 0 ? pp.n_species : 1;
+  float maxs = 0.f;
+  for (int a = 0; a < S; ++a)
+    for (int b = 0; b < S; ++b) {
+      sg.c[a * JMD_MAX_SPECIES + b].pad = pp.sigma[a][b];
+      maxs = std::max(maxs, pp.sigma[a][b]);
+    }
+  sg.pad = maxs;
+  return sg;
+}
+
+// ------------------------------------------------- generic-stride VJP kernel --
+struct VjpArgs {
+  const float* x;
+  int64_t xs;
+  const int32_t* species;
+  int n;
+  const int32_t* idx;
+  int64_t ld;
+  int64_t width;
+  const int32_t* cnt;
+  const float* lam;
+  int64_t ls;
+  float* gx;
+  int64_t gs;
+  float weight;
+  double* gp;      // [kBins] dL/dtheta (accumulated, times weight)
+  double* ge;      // [kBins] dE/dtheta (accumulated), optional
+  Geo geo;
+  int per_pair;    // cutoff scales with sigma_ij
+};
+
+// One thread per atom over a row-major Dense list of any stride.
+template <int DIM, int KIND, bool SPECIES, bool EGRAD>
+__global__ void __launch_bounds__(128) k_force_vjp(VjpArgs a, const __grid_constant__ PairTable tab,
+                                                  const __grid_constant__ PairTable sig) {
+  constexpr int NB = SPECIES ? JMD_MAX_SPECIES : 1;
+  __shared__ float bins[kBins];
+  __shared__ float ebins[EGRAD ? kBins : 1];
+  zero_bins(bins);
+  if (EGRAD) zero_bins(ebins);
+  __syncthreads();
+  BinAcc<NB> acc, eacc;
+  acc.zero();
+  eacc.zero();
+  const bool per_pair = a.per_pair != 0;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int sk = 0;
+  if (k < a.n) {
+    const float4 xk = load_row<DIM, false>(a.x, a.xs, k);
+    const float4 lk = load_row<DIM, false>(a.lam, a.ls, k);
+    sk = SPECIES ? min(max(__ldg(a.species + k), 0), tab.nsp - 1) : 0;
+    const int32_t* row = a.idx + (int64_t)k * a.ld;
+    int end = (int)a.width;
+    if (a.cnt) end = min(__ldg(a.cnt + k), end);
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    for (int e = 0; e < end; ++e) {
+      const int j = __ldg(row + e);
+      if ((unsigned)j >= (unsigned)a.n) continue;
+      const float4 xj = load_row<DIM, false>(a.x, a.xs, j);
+      float dx, dy, dz;
+      displacement<DIM>(xk, xj, a.geo, dx, dy, dz);
+      const float r2 = dx * dx + dy * dy + (DIM == 3 ? dz * dz : 0.f);
+      const int sj = SPECIES ? min(max(__ldg(a.species + j), 0), tab.nsp - 1) : 0;
+      const int bin = sk * JMD_MAX_SPECIES + sj;
+      const PairCoef& c = tab.c[SPECIES ? bin : 0];
+      if (!(r2 < c.rc2) || r2 == 0.f) continue;
+      const float sigma = sig.c[SPECIES ? bin : 0].pad;   // sigma_ij
+      const float kappa = per_pair ? sigma : sig.pad;     // cutoff scale
+      const PairD q = pair_derivs<KIND>(r2, c, sigma, kappa);
+      const float4 lj = load_row<DIM, false>(a.lam, a.ls, j);
+      const float ex = lj.x - lk.x, ey = lj.y - lk.y, ez = DIM == 3 ? lj.z - lk.z : 0.f;
+      const float t = dx * ex + dy * ey + dz * ez;     // (lam_j - lam_k) . d
+      const float cdd = (q.hh - q.g) / r2 * t;
+      gx += q.g * ex + cdd * dx;
+      gy += q.g * ey + cdd * dy;
+      if (DIM == 3) gz += q.g * ez + cdd * dz;
+      const float ht = 0.5f * t;
+      acc.add(sj, q.dg_s * ht, q.dg_e * ht, KIND == JMD_LJ ? q.dg_k * ht : 0.f, per_pair);
+      if (EGRAD)
+        eacc.add(sj, 0.5f * q.dU_s, 0.5f * q.dU_e, KIND == JMD_LJ ? 0.5f * q.dU_k : 0.f, per_pair);
+    }
+    if (a.gx) {
+      float* o = a.gx + (int64_t)k * a.gs;
+      o[0] += a.weight * gx;
+      o[1] += a.weight * gy;
+      if (DIM == 3) o[2] += a.weight * gz;
+    }
+  }
+  const int ncol = SPECIES ? tab.nsp : 1;
+  if (!SPECIES) {
+    acc.group_sum(kWarp, 1);
+    if (EGRAD) eacc.group_sum(kWarp, 1);
+  }
+  if (SPECIES || (threadIdx.x & (kWarp - 1)) == 0) {
+    acc.flush(bins, sk, ncol);
+    if (EGRAD) eacc.flush(ebins, sk, ncol);
+  }
+  __syncthreads();
+  publish_bins(bins, a.gp, (double)a.weight);
+  if (EGRAD) publish_bins(ebins, a.ge, 1.0);
+}
+
+template <int DIM, int KIND>
+void vjp_launch(bool sp, bool eg, const VjpArgs& a, const PairTable& t, const PairTable& s,
+                cudaStream_t st) {
+  const unsigned grid = (unsigned)std::max<int64_t>(1, ceil_div(a.n, 128));
+  if (sp) {
+    if (eg) k_force_vjp<DIM, KIND, true, true><<<grid, 128, 0, st>>>(a, t, s);
+    else k_force_vjp<DIM, KIND, true, false><<<grid, 128, 0, st>>>(a, t, s);
+  } else {
+    if (eg) k_force_vjp<DIM, KIND, false, true><<<grid, 128, 0, st>>>(a, t, s);
+    else k_force_vjp<DIM, KIND, false, false><<<grid, 128, 0, st>>>(a, t, s);
+  }
+}
+
+// ----------------------------------------------- engine reverse-step kernels --
+// A reverse Verlet step at x_s takes two kernels:
+//   pack:  q = pbar + (dt/m) xbar  (pbar <- q), record[i] = (x_i, q_i) in 32
+//          bytes, and the skin test of x_s against the list's reference;
+//   step:  xbar_k += w sum_j J_kj (q_j - q_k) over k's Dense row, TPA lanes
+//          per atom, each neighbour one 32-byte record gather.
+// The closing half kick at the end of a run is a pack without the kick
+// (q = pbar) followed by a step with w = dt/2.
+
+template <int DIM>
+__global__ void __launch_bounds__(256) k_adj_pack(int n, const float4* __restrict__ x,
+                                                  float4* __restrict__ xbar, float4* __restrict__ pbar,
+                                                  const float* __restrict__ mass, float mass_scalar,
+                                                  float dt, int kick, float4* __restrict__ rec,
+                                                  const float4* __restrict__ ref, float thr2,
+                                                  int32_t* flag, Geo geo) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool over = false;
+  if (i < n) {
+    const float4 xi = __ldg(x + i);
+    float4 q = pbar[i];
+    if (kick) {
+      const float4 xb = xbar[i];
+      const float c = dt / (mass ? __ldg(mass + i) : mass_scalar);
+      q.x = fmaf(c, xb.x, q.x);
+      q.y = fmaf(c, xb.y, q.y);
+      if (DIM == 3) q.z = fmaf(c, xb.z, q.z);
+      pbar[i] = q;
+    }
+    rec[2 * i] = make_float4(xi.x, xi.y, DIM == 3 ? xi.z : 0.f, q.x);
+    rec[2 * i + 1] = make_float4(q.y, DIM == 3 ? q.z : 0.f, 0.f, 0.f);
+    if (ref) {
+      float dx, dy, dz;
+      displacement<DIM>(xi, __ldg(ref + i), geo, dx, dy, dz);
+      over = dx * dx + dy * dy + (DIM == 3 ? dz * dz : 0.f) > thr2;
+    }
+  }
+  if (ref && __any_sync(0xffffffffu, over) && (threadIdx.x & (kWarp - 1)) == 0) atomicOr(flag, 1);
+}
+
+struct StepArgs {
+  int n;
+  const float4* rec;
+  float4* xbar;
+  const int32_t* species;
+  const int32_t* idx;
+  int64_t ld;
+  int width;
+  const int32_t* cnt;
+  float weight;
+  double* gp;
+  Geo geo;
+  int per_pair;
+};
+
+template <int DIM, int KIND, bool SPECIES, bool PARAMS, int TPA>
+__global__ void __launch_bounds__(256) k_adj_step(StepArgs a, const __grid_constant__ PairTable tab,
+                                                  const __grid_constant__ PairTable sig) {
+  constexpr int NB = SPECIES ? JMD_MAX_SPECIES : 1;
+  __shared__ float bins[PARAMS ? kBins : 1];
+  if (PARAMS) {
+    zero_bins(bins);
+    __syncthreads();
+  }
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = (int)(t / TPA);
+  const int lane = (int)(t % TPA);
+  const bool active = k < a.n;
+  const bool per_pair = a.per_pair != 0;
+  BinAcc<NB> acc;
+  acc.zero();
+  float gx = 0.f, gy = 0.f, gz = 0.f;
+  int sk = 0;
+  if (active) {
+    const float4 r0 = __ldg(a.rec + 2 * k);
+    const float4 r1 = __ldg(a.rec + 2 * k + 1);
+    const float qx = r0.w, qy = r1.x, qz = r1.y;
+    sk = SPECIES ? min(max(__ldg(a.species + k), 0), tab.nsp - 1) : 0;
+    const int32_t* row = a.idx + (int64_t)k * a.ld;
+    int end = a.width;
+    if (a.cnt) end = min(__ldg(a.cnt + k), end);
+    for (int e = lane; e < end; e += TPA) {
+      const int j = __ldg(row + e);
+      if ((unsigned)j >= (unsigned)a.n) continue;
+      const float4 j0 = __ldg(a.rec + 2 * j);
+      const float4 j1 = __ldg(a.rec + 2 * j + 1);
+      float dx, dy, dz;
+      displacement<DIM>(r0, j0, a.geo, dx, dy, dz);
+      const float r2 = dx * dx + dy * dy + (DIM == 3 ? dz * dz : 0.f);
+      const int sj = SPECIES ? min(max(__ldg(a.species + j), 0), tab.nsp - 1) : 0;
+      const int bin = sk * JMD_MAX_SPECIES + sj;
+      const PairCoef& c = tab.c[SPECIES ? bin : 0];
+      if (!(r2 < c.rc2) || r2 == 0.f) continue;
+      float g, hh;
+      PairD q;
+      if (PARAMS) {
+        const float sigma = sig.c[SPECIES ? bin : 0].pad;
+        q = pair_derivs<KIND>(r2, c, sigma, per_pair ? sigma : sig.pad);
+        g = q.g;
+        hh = q.hh;
+      } else {
+        float U;
+        pair_eval<KIND, true>(r2, c, U, g, hh);
+      }
+      const float ex = j0.w - qx, ey = j1.x - qy, ez = DIM == 3 ? j1.y - qz : 0.f;
+      const float tt = dx * ex + dy * ey + dz * ez;    // (q_j - q_k) . d
+      const float cdd = (hh - g) * rcp_nr(r2) * tt;
+      gx = fmaf(g, ex, fmaf(cdd, dx, gx));
+      gy = fmaf(g, ey, fmaf(cdd, dy, gy));
+      if (DIM == 3) gz = fmaf(g, ez, fmaf(cdd, dz, gz));
+      if (PARAMS) {
+        const float ht = 0.5f * tt;
+        acc.add(sj, q.dg_s * ht, q.dg_e * ht, KIND == JMD_LJ ? q.dg_k * ht : 0.f, per_pair);
+      }
+    }
+  }
+#pragma unroll
+  for (int o = TPA / 2; o > 0; o >>= 1) {
+    gx += __shfl_xor_sync(0xffffffffu, gx, o, TPA);
+    gy += __shfl_xor_sync(0xffffffffu, gy, o, TPA);
+    if (DIM == 3) gz += __shfl_xor_sync(0xffffffffu, gz, o, TPA);
+  }
+  if (active && lane == 0) {
+    float4 b = a.xbar[k];
+    b.x = fmaf(a.weight, gx, b.x);
+    b.y = fmaf(a.weight, gy, b.y);
+    if (DIM == 3) b.z = fmaf(a.weight, gz, b.z);
+    a.xbar[k] = b;
+  }
+  if (PARAMS) {
+    const int ncol = SPECIES ? tab.nsp : 1;
+    if (SPECIES) {
+      acc.group_sum(TPA, ncol);
+      if (active && lane == 0) acc.flush(bins, sk, ncol);
+    } else {
+      acc.group_sum(kWarp, 1);
+      if ((threadIdx.x & (kWarp - 1)) == 0) acc.flush(bins, 0, 1);
+    }
+    __syncthreads();
+    publish_bins(bins, a.gp, (double)a.weight);
+  }
+}
+
+template <int DIM, int KIND, bool SPECIES, bool PARAMS>
+void step_launch_tpa(int tpa, const StepArgs& a, const PairTable& t, const PairTable& s,
+                     cudaStream_t st) {
+  const unsigned grid = (unsigned)std::max<int64_t>(1, ceil_div((int64_t)a.n * tpa, 256));
+  if (tpa == 4) k_adj_step<DIM, KIND, SPECIES, PARAMS, 4><<<grid, 256, 0, st>>>(a, t, s);
+  else if (tpa == 16) k_adj_step<DIM, KIND, SPECIES, PARAMS, 16><<<grid, 256, 0, st>>>(a, t, s);
+  else k_adj_step<DIM, KIND, SPECIES, PARAMS, 8><<<grid, 256, 0, st>>>(a, t, s);
+}
+
+template <int DIM, int KIND>
+void step_launch(int tpa, bool sp, bool params, const StepArgs& a, const PairTable& t,
+                 const PairTable& s, cudaStream_t st) {
+  if (sp) {
+    if (params) step_launch_tpa<DIM, KIND, true, true>(tpa, a, t, s, st);
+    else step_launch_tpa<DIM, KIND, true, false>(tpa, a, t, s, st);
+  } else {
+    if (params) step_launch_tpa<DIM, KIND, false, true>(tpa, a, t, s, st);
+    else step_launch_tpa<DIM, KIND, false, false>(tpa, a, t, s, st);
+  }
+}
+
+}  // namespace
+
+// Host side of the engine's reverse step (declared in pair.cuh).
+int adjoint_pack(const jmd_nve_system& s, const float* x, float* xbar, float* pbar, float* rec,
+                 bool kick, bool skin, cudaStream_t st) {
+  const int n = (int)s.n;
+  const unsigned grid = (unsigned)ceil_div(n, 256);
+  const float4* ref = skin ? reinterpret_cast<const float4*>(s.reference_position) : nullptr;
+  const Geo g = make_geo(s.space);
+  if (s.space.dim == 3)
+    k_adj_pack<3><<<grid, 256, 0, st>>>(n, reinterpret_cast<const float4*>(x),
+                                        reinterpret_cast<float4*>(xbar), reinterpret_cast<float4*>(pbar),
+                                        s.mass, s.mass_scalar, s.dt, kick ? 1 : 0,
+                                        reinterpret_cast<float4*>(rec), ref, s.threshold_sq,
+                                        s.rebuild_flag, g);
+  else
+    k_adj_pack<2><<<grid, 256, 0, st>>>(n, reinterpret_cast<const float4*>(x),
+                                        reinterpret_cast<float4*>(xbar), reinterpret_cast<float4*>(pbar),
+                                        s.mass, s.mass_scalar, s.dt, kick ? 1 : 0,
+                                        reinterpret_cast<float4*>(rec), ref, s.threshold_sq,
+                                        s.rebuild_flag, g);
+  JMD_CUDA(cudaGetLastError());
+  return JMD_OK;
+}
+
+int adjoint_vjp_step(const jmd_nve_system& s, float* xbar, const float* rec, float weight,
+                     double* grad_params, cudaStream_t st) {
+  const PairTable t = make_pair_table(s.pair);
+  const PairTable sg = sigma_table(s.pair);
+  StepArgs a{};
+  a.n = (int)s.n;
+  a.rec = reinterpret_cast<const float4*>(rec);
+  a.xbar = reinterpret_cast<float4*>(xbar);
+  a.species = s.species;
+  a.idx = s.idx;
+  a.ld = s.idx_ld;
+  a.width = (int)s.nlist.max_occupancy;
+  a.cnt = s.nbr_count;
+  a.weight = weight;
+  a.gp = grad_params;
+  a.geo = make_geo(s.space);
+  a.per_pair = s.pair.per_pair_cutoff;
+  const int tpa = dense_tpa();
+  const bool sp = s.pair.n_species > 0 && s.species != nullptr, pr = grad_params != nullptr;
+  if (s.space.dim == 3) {
+    if (s.pair.kind == JMD_LJ) step_launch<3, JMD_LJ>(tpa, sp, pr, a, t, sg, st);
+    else if (s.pair.kind == JMD_LJ_TRUNCATED) step_launch<3, JMD_LJ_TRUNCATED>(tpa, sp, pr, a, t, sg, st);
+    else step_launch<3, JMD_SOFT_SPHERE>(tpa, sp, pr, a, t, sg, st);
+  } else {
+    if (s.pair.kind == JMD_LJ) step_launch<2, JMD_LJ>(tpa, sp, pr, a, t, sg, st);
+    else if (s.pair.kind == JMD_LJ_TRUNCATED) step_launch<2, JMD_LJ_TRUNCATED>(tpa, sp, pr, a, t, sg, st);
+    else step_launch<2, JMD_SOFT_SPHERE>(tpa, sp, pr, a, t, sg, st);
+  }
+  JMD_CUDA(cudaGetLastError());
+  return JMD_OK;
+}
+
+}  // namespace jmd
+
+using namespace jmd;
+
+extern "C" {
+
+int jmd_pair_force_vjp(const jmd_pair* pp, const jmd_space* space, const float* position,
+                       int64_t pos_stride, const int32_t* species, int64_t n, const int32_t* idx,
+                       int64_t idx_ld, int64_t idx_width, const int32_t* nbr_count,
+                       const float* cotangent, int64_t cot_stride, float weight,
+                       float* grad_position, int64_t grad_stride, double* grad_params,
+                       double* grad_energy_params, void* stream) {
+  int e = validate_pair(pp);
+  if (e) return e;
+  JMD_REQUIRE(space && (space->dim == 2 || space->dim == 3), "bad space");
+  JMD_REQUIRE(n >= 0 && n < INT32_MAX, "atom count out of range");
+  JMD_REQUIRE(idx_ld >= idx_width, "idx_ld must be >= idx_width");
+  JMD_REQUIRE(cotangent != nullptr, "cotangent is null");
+  JMD_REQUIRE(pp->n_species == 0 || species != nullptr, "species matrices need a species array");
+  if (n <= 0) return JMD_OK;
+  const PairTable t = make_pair_table(*pp);
+  const PairTable sg = sigma_table(*pp);
+  VjpArgs a{};
+  a.x = position;
+  a.xs = pos_stride;
+  a.species = species;
+  a.n = (int)n;
+  a.idx = idx;
+  a.ld = idx_ld;
+  a.width = idx_width;
+  a.cnt = nbr_count;
+  a.lam = cotangent;
+  a.ls = cot_stride;
+  a.gx = grad_position;
+  a.gs = grad_stride;
+  a.weight = weight;
+  a.gp = grad_params;
+  a.ge = grad_energy_params;
+  a.geo = make_geo(*space);
+  a.per_pair = pp->per_pair_cutoff;
+  const bool sp = pp->n_species > 0, eg = grad_energy_params != nullptr;
+  cudaStream_t st = as_stream(stream);
+  if (space->dim == 3) {
+    if (pp->kind == JMD_LJ) vjp_launch<3, JMD_LJ>(sp, eg, a, t, sg, st);
+    else if (pp->kind == JMD_LJ_TRUNCATED) vjp_launch<3, JMD_LJ_TRUNCATED>(sp, eg, a, t, sg, st);
+    else vjp_launch<3, JMD_SOFT_SPHERE>(sp, eg, a, t, sg, st);
+  } else {
+    if (pp->kind == JMD_LJ) vjp_launch<2, JMD_LJ>(sp, eg, a, t, sg, st);
+    else if (pp->kind == JMD_LJ_TRUNCATED) vjp_launch<2, JMD_LJ_TRUNCATED>(sp, eg, a, t, sg, st);
+    else vjp_launch<2, JMD_SOFT_SPHERE>(sp, eg, a, t, sg, st);
+  }
+  return check_launch("jmd_pair_force_vjp");
+}
+
+}  // extern "C"

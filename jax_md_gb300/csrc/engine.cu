@@ -103,8 +103,11 @@ int conditional(const int32_t* rebuild_flag, Body body, cudaStream_t st, cudaStr
 }
 
 // Enqueues the whole run; `graphed` selects conditional nodes vs gated kernels.
+// With `traj`, positions step through its slots (slot k = x_k, slot 0 a copy
+// of the start) instead of ping-ponging; `force_rebuild` rebuilds at x_0
+// whatever the skin test says.
 int enqueue_run(const jmd_nve_system& s, int64_t steps, bool graphed, cudaStream_t st,
-                cudaStream_t body_st) {
+                cudaStream_t body_st, float* traj = nullptr, bool force_rebuild = false) {
   const bool always = s.threshold_sq < 0.f;
   auto gate = [&](const float* x) -> int {
     if (always) return rebuild(s, x, false, st);
@@ -113,24 +116,31 @@ int enqueue_run(const jmd_nve_system& s, int64_t steps, bool graphed, cudaStream
                          body_st);
     return rebuild(s, x, true, st);
   };
-  const float4* none = nullptr;
-  (void)none;
+  auto slot = [&](int64_t k) { return traj + (size_t)k * 4 * (size_t)s.n; };
+  const size_t rows = sizeof(float4) * (size_t)s.n;
   int rc;
+  if (traj) {
+    JMD_CUDA(cudaMemcpyAsync(slot(0), s.position, rows, cudaMemcpyDeviceToDevice, st));
+    JMD_CUDA(cudaMemcpyAsync(slot(1), s.position, rows, cudaMemcpyDeviceToDevice, st));
+  }
   // update at x0
-  if (!always) {
+  if (force_rebuild && !always) {
+    k_set_flag<<<1, 1, 0, st>>>(s.rebuild_flag);
+    JMD_CUDA(cudaGetLastError());
+  } else if (!always) {
     rc = jmd_skin_check(s.position, 4, s.reference_position, 4, s.n, &s.space, s.threshold_sq,
                         s.rebuild_flag, st);
     if (rc) return rc;
   }
   if ((rc = gate(s.position))) return rc;
   // first half of step 0: kick + drift + skin test of x1
-  rc = jmd_verlet_kick_drift(s.position, 4, s.momentum, 4, s.force, 4, s.mass, s.mass_scalar,
+  float* cur = traj ? slot(1) : s.position;
+  float* nxt = traj ? (steps >= 2 ? slot(2) : nullptr) : s.position_alt;
+  rc = jmd_verlet_kick_drift(cur, 4, s.momentum, 4, s.force, 4, s.mass, s.mass_scalar,
                              s.n, &s.space, s.dt, nullptr,
                              always ? nullptr : s.reference_position, 4,
                              s.threshold_sq, always ? nullptr : s.rebuild_flag, st);
   if (rc) return rc;
-  float* cur = s.position;
-  float* nxt = s.position_alt;
   const int64_t width = s.nlist.max_occupancy;
   for (int64_t k = 1; k < steps; ++k) {
     if ((rc = gate(cur))) return rc;
@@ -139,7 +149,12 @@ int enqueue_run(const jmd_nve_system& s, int64_t steps, bool graphed, cudaStream
                             always ? nullptr : s.reference_position, s.threshold_sq,
                             always ? nullptr : s.rebuild_flag, st);
     if (rc) return rc;
-    std::swap(cur, nxt);
+    if (traj) {
+      cur = slot(k + 1);
+      nxt = k + 2 <= steps ? slot(k + 2) : nullptr;
+    } else {
+      std::swap(cur, nxt);
+    }
   }
   if ((rc = gate(cur))) return rc;
   rc = jmd_force_kick(&s.pair, &s.space, cur, s.force, s.momentum, s.species, s.n, s.idx,
@@ -149,6 +164,40 @@ int enqueue_run(const jmd_nve_system& s, int64_t steps, bool graphed, cudaStream
     JMD_CUDA(cudaMemcpyAsync(s.position, cur, sizeof(float4) * (size_t)s.n,
                              cudaMemcpyDeviceToDevice, st));
   }
+  return JMD_OK;
+}
+
+// Reverse pass of velocity Verlet over positions recorded by enqueue_run's
+// trajectory slots 0..steps (see jmd_nve_adjoint_segment).  The list is
+// rebuilt at the first position visited and then maintained by the skin test
+// as the pass walks back in time.
+int enqueue_adjoint(const jmd_nve_system& s, const float* traj, int64_t steps, bool closing,
+                    bool opening, float* xbar, float* pbar, float* rec, double* gp, bool graphed,
+                    cudaStream_t st, cudaStream_t body_st) {
+  const bool always = s.threshold_sq < 0.f;
+  auto gate = [&](const float* x) -> int {
+    if (always) return rebuild(s, x, false, st);
+    if (graphed)
+      return conditional(s.rebuild_flag, [&](cudaStream_t b) { return rebuild(s, x, true, b); }, st,
+                         body_st);
+    return rebuild(s, x, true, st);
+  };
+  auto slot = [&](int64_t k) { return traj + (size_t)k * 4 * (size_t)s.n; };
+  auto rstep = [&](int64_t k, bool kick, float w) -> int {
+    int rc = adjoint_pack(s, slot(k), xbar, pbar, rec, kick, !always, st);
+    if (rc) return rc;
+    if ((rc = gate(slot(k)))) return rc;
+    return adjoint_vjp_step(s, xbar, rec, w, gp, st);
+  };
+  if (!always) {
+    k_set_flag<<<1, 1, 0, st>>>(s.rebuild_flag);
+    JMD_CUDA(cudaGetLastError());
+  }
+  const float h = 0.5f * s.dt;
+  int rc;
+  if (closing && (rc = rstep(steps, false, h))) return rc;
+  for (int64_t k = steps - 1; k >= 0; --k)
+    if ((rc = rstep(k, true, (opening && k == 0) ? h : s.dt))) return rc;
   return JMD_OK;
 }
 
@@ -381,6 +430,66 @@ int jmd_nve_run(const jmd_nve_system* sys, int64_t n_steps, int32_t use_graph, v
   const std::string key = plan_key(*sys, n_steps, device);
   return launch_graphed(key, [&](cudaStream_t cs, cudaStream_t bs) {
     return enqueue_run(*sys, n_steps, true, cs, bs);
+  }, st);
+}
+
+int jmd_nve_run_recorded(const jmd_nve_system* sys, float* trajectory, int64_t n_steps,
+                         int32_t force_rebuild, int32_t use_graph, void* stream) {
+  JMD_REQUIRE(sys != nullptr, "system is null");
+  int e = validate_sys(*sys);
+  if (e) return e;
+  JMD_REQUIRE(n_steps >= 1, "n_steps must be >= 1");
+  JMD_REQUIRE(trajectory == nullptr || (reinterpret_cast<uintptr_t>(trajectory) % 16) == 0,
+              "trajectory must be 16-byte aligned float4 rows");
+  cudaStream_t st = as_stream(stream);
+  cudaStreamCaptureStatus cap;
+  JMD_CUDA(cudaStreamIsCapturing(st, &cap));
+  if (!use_graph || cap != cudaStreamCaptureStatusNone) {
+    int rc = enqueue_run(*sys, n_steps, false, st, nullptr, trajectory, force_rebuild != 0);
+    return rc ? rc : check_launch("jmd_nve_run_recorded");
+  }
+  int device;
+  JMD_CUDA(cudaGetDevice(&device));
+  std::string key = "rec" + plan_key(*sys, n_steps, device);
+  key.append(reinterpret_cast<const char*>(&trajectory), sizeof(trajectory));
+  key.push_back(force_rebuild ? 'f' : 'g');
+  return launch_graphed(key, [&](cudaStream_t cs, cudaStream_t bs) {
+    return enqueue_run(*sys, n_steps, true, cs, bs, trajectory, force_rebuild != 0);
+  }, st);
+}
+
+int jmd_nve_adjoint_segment(const jmd_nve_system* sys, const float* trajectory, int64_t n_steps,
+                            int32_t closing, int32_t opening, float* xbar, float* pbar,
+                            float* record_scratch, double* grad_params, int32_t use_graph,
+                            void* stream) {
+  JMD_REQUIRE(sys != nullptr, "system is null");
+  int e = validate_sys(*sys);
+  if (e) return e;
+  JMD_REQUIRE(n_steps >= 0, "n_steps must be >= 0");
+  JMD_REQUIRE(trajectory && xbar && pbar && record_scratch, "null buffer");
+  for (const void* p : {(const void*)trajectory, (const void*)xbar, (const void*)pbar,
+                        (const void*)record_scratch})
+    JMD_REQUIRE((reinterpret_cast<uintptr_t>(p) % 16) == 0, "float4 rows must be 16-byte aligned");
+  if (n_steps == 0 && !closing) return JMD_OK;
+  cudaStream_t st = as_stream(stream);
+  cudaStreamCaptureStatus cap;
+  JMD_CUDA(cudaStreamIsCapturing(st, &cap));
+  if (!use_graph || cap != cudaStreamCaptureStatusNone) {
+    int rc = enqueue_adjoint(*sys, trajectory, n_steps, closing != 0, opening != 0, xbar, pbar,
+                             record_scratch, grad_params, false, st, nullptr);
+    return rc ? rc : check_launch("jmd_nve_adjoint_segment");
+  }
+  int device;
+  JMD_CUDA(cudaGetDevice(&device));
+  std::string key = "adj" + plan_key(*sys, n_steps, device);
+  for (const void* p : {(const void*)trajectory, (const void*)xbar, (const void*)pbar,
+                        (const void*)record_scratch, (const void*)grad_params})
+    key.append(reinterpret_cast<const char*>(&p), sizeof(p));
+  key.push_back(closing ? 'c' : '-');
+  key.push_back(opening ? 'o' : '-');
+  return launch_graphed(key, [&](cudaStream_t cs, cudaStream_t bs) {
+    return enqueue_adjoint(*sys, trajectory, n_steps, closing != 0, opening != 0, xbar, pbar,
+                           record_scratch, grad_params, true, cs, bs);
   }, st);
 }
 

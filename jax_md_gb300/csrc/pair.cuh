@@ -130,3 +130,14 @@ __device__ __forceinline__ void displacement(const float4& a, const float4& b, c
 }
 
 }  // namespace jmd
+
+namespace jmd {
+// Reverse Verlet step of the engine (adjoint.cu): pack (x, q) records, with
+// q = pbar + (dt/m) xbar when `kick` (pbar <- q), and the skin test of x when
+// `skin`; then xbar += weight * (dF/dR)^T q over the system's Dense list and,
+// when grad_params is given, weight * d(q . F)/d theta into its 130 bins.
+int adjoint_pack(const jmd_nve_system& s, const float* x, float* xbar, float* pbar, float* rec,
+                 bool kick, bool skin, cudaStream_t st);
+int adjoint_vjp_step(const jmd_nve_system& s, float* xbar, const float* rec, float weight,
+                     double* grad_params, cudaStream_t st);
+}  // namespace jmd

@@ -68,17 +68,83 @@ def make_pair_struct(fn, params: dict, n_species: int) -> N.Pair:
     return p
 
 
-class _EnergyFn(torch.autograd.Function):
+def _param_tensor(v):
+    return v if isinstance(v, torch.Tensor) and v.requires_grad else None
+
+
+def _bins_to_grads(bins, pair, sigma, epsilon):
+    """Maps the kernel's gradient bins onto the shapes of sigma / epsilon.
+
+    bins: [130] f64 = d/d sigma[a][b] (0..63), d/d epsilon[a][b] (64..127) and
+    the global cutoff scale max(sigma) (128), credited to the largest sigma
+    entry as jax.grad does through jnp.max (energy.py:319-320)."""
+    out = []
+    for v, off in ((sigma, 0), (epsilon, 64)):
+        if v is None:
+            out.append(None)
+            continue
+        if v.dim() == 0:
+            g = bins[off:off + 1].sum()
+            if off == 0:
+                g = g + bins[128]
+        else:
+            S = v.shape[0]
+            g = bins[off:off + 64].reshape(8, 8)[:S, :S].clone()
+            if off == 0:
+                flat = torch.argmax(v.detach().reshape(-1))
+                g.reshape(-1)[flat] += bins[128]
+        out.append(g.to(v.dtype))
+    return out
+
+
+class _ForceFn(torch.autograd.Function):
+    """F(R; sigma, epsilon) with a backward pass through the VJP kernel."""
+
     @staticmethod
-    def forward(ctx, R, runner):
-        E, F = runner(R)
-        ctx.save_for_backward(F)
-        return E
+    def forward(ctx, R, sigma, epsilon, owner, neighbor, dynamic):
+        F = owner.forces(R.detach(), neighbor, **dynamic)
+        ctx.save_for_backward(R, sigma if sigma is not None else torch.empty(0),
+                              epsilon if epsilon is not None else torch.empty(0))
+        ctx.owner, ctx.neighbor, ctx.dynamic = owner, neighbor, dynamic
+        ctx.has = (sigma is not None, epsilon is not None)
+        return F
+
+    @staticmethod
+    def backward(ctx, lam):
+        R, sigma, epsilon = ctx.saved_tensors
+        sigma = sigma if ctx.has[0] else None
+        epsilon = epsilon if ctx.has[1] else None
+        gR, bins, _ = ctx.owner.force_vjp(R.detach(), ctx.neighbor, lam.contiguous(), **ctx.dynamic)
+        gs, ge = _bins_to_grads(bins, None, sigma, epsilon)
+        return gR.to(R.dtype), gs, ge, None, None, None
+
+
+class _EnergyFn(torch.autograd.Function):
+    """E(R; sigma, epsilon); dE/dR = -F is itself differentiable (through _ForceFn)."""
+
+    @staticmethod
+    def forward(ctx, R, sigma, epsilon, owner, neighbor, dynamic):
+        E = owner.energy_f64(R.detach(), neighbor, **dynamic)
+        ctx.save_for_backward(R, sigma if sigma is not None else torch.empty(0),
+                              epsilon if epsilon is not None else torch.empty(0))
+        ctx.owner, ctx.neighbor, ctx.dynamic = owner, neighbor, dynamic
+        ctx.has = (sigma is not None, epsilon is not None)
+        return E.to(R.dtype)
 
     @staticmethod
     def backward(ctx, gE):
-        F, = ctx.saved_tensors
-        return -F * gE.to(F.dtype), None
+        R, sigma, epsilon = ctx.saved_tensors
+        sigma = sigma if ctx.has[0] else None
+        epsilon = epsilon if ctx.has[1] else None
+        F = _ForceFn.apply(R, sigma, epsilon, ctx.owner, ctx.neighbor, ctx.dynamic)
+        gR = -F * gE.to(F.dtype)
+        gs = ge = None
+        if sigma is not None or epsilon is not None:
+            bins = ctx.owner.energy_param_grad(R.detach(), ctx.neighbor, **ctx.dynamic)
+            gs, ge = _bins_to_grads(bins, None, sigma, epsilon)
+            gs = gs * gE if gs is not None else None
+            ge = ge * gE if ge is not None else None
+        return gR, gs, ge, None, None, None
 
 
 class PairNeighborListEnergy:
@@ -179,12 +245,56 @@ class PairNeighborListEnergy:
             _, _, pa, _ = self.compute(R.detach(), neighbor, force=False, per_atom=True, **dynamic)
             return pa
 
-        def runner(Rd):
-            e, f, _, _ = self.compute(Rd, neighbor, force=True, **dynamic)
-            return e.to(Rd.dtype), f
-        if R.requires_grad:
-            return _EnergyFn.apply(R, runner)
+        sigma = _param_tensor(dynamic.get('sigma'))
+        epsilon = _param_tensor(dynamic.get('epsilon'))
+        if R.requires_grad or sigma is not None or epsilon is not None:
+            return _EnergyFn.apply(R, sigma, epsilon, self, neighbor, dynamic)
         return self.energy_f64(R, neighbor, **dynamic).to(R.dtype)
+
+    # -- adjoint ------------------------------------------------------------
+    def force_fn_autograd(self, R, neighbor, **dynamic):
+        """-dE/dR as a differentiable function of R and of sigma / epsilon
+        tensors passed in ``dynamic`` (backward through the VJP kernel)."""
+        return _ForceFn.apply(R, _param_tensor(dynamic.get('sigma')),
+                              _param_tensor(dynamic.get('epsilon')), self, neighbor, dynamic)
+
+    def _vjp_launch(self, R, neighbor, lam, weight, gR, gp, ge, **dynamic):
+        if neighbor.format is not partition.Dense:
+            raise NotImplementedError('the force VJP kernel runs on Dense lists')
+        R, rs = partition._rows(R)
+        n, dim = R.shape
+        species, pair = self._resolve(R, dynamic)
+        sp = self.geometry.space(dim)
+        idx = neighbor.idx
+        if lam.stride(-1) != 1:
+            lam = lam.contiguous()
+        cnt = getattr(neighbor, 'nbr_count', None)
+        N.check(N.lib().jmd_pair_force_vjp(
+            ctypes.byref(pair), ctypes.byref(sp), R.data_ptr(), rs, N.ptr(species), n,
+            idx.data_ptr(), idx.stride(0), idx.shape[1], N.ptr(cnt), lam.data_ptr(), lam.stride(0),
+            float(weight), N.ptr(gR), gR.stride(0) if gR is not None else 0, N.ptr(gp), N.ptr(ge),
+            N.stream_ptr()), 'pair_force_vjp')
+
+    def force_vjp(self, R, neighbor, lam, weight=1.0, grad_R=None, grad_params=None, **dynamic):
+        """(dF/dR)^T lam and d(lam . F)/d(sigma, epsilon) bins (accumulated into
+        grad_R / grad_params when given).  Returns (grad_R, grad_params, None)."""
+        dev = R.device
+        n, dim = R.shape
+        if grad_R is None:
+            grad_R = torch.zeros((n, 4), dtype=torch.float32, device=dev)[:, :dim]
+        if grad_params is None:
+            grad_params = torch.zeros(130, dtype=torch.float64, device=dev)
+        self._vjp_launch(R, neighbor, lam, weight, grad_R, grad_params, None, **dynamic)
+        return grad_R, grad_params, None
+
+    def energy_param_grad(self, R, neighbor, out=None, **dynamic):
+        """dE/d(sigma, epsilon) bins [130] (f64)."""
+        dev = R.device
+        if out is None:
+            out = torch.zeros(130, dtype=torch.float64, device=dev)
+        lam = torch.zeros_like(R, dtype=torch.float32)
+        self._vjp_launch(R, neighbor, lam, 0.0, None, None, out, **dynamic)
+        return out
 
 
 def pair_neighbor_list(fn, displacement_or_metric, species=None, reduce_axis=None,

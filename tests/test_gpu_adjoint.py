@@ -1,0 +1,215 @@
+"""The adjoint: force VJPs and trajectory gradients against FP64 finite differences.
+
+Force VJP (jmd_pair_force_vjp): (dF/dR)^T lam against the oracle's analytic
+Hessian-vector product, and d(lam . F)/d(sigma, epsilon) and dE/d(sigma,
+epsilon) against FP64 central differences of the oracle (cutoff radii follow
+max sigma as in energy.py:319-320).  Trajectory gradient (adjoint.nve_trajectory):
+loss = PE/N + 0.1 MSD after a short Kob-Andersen NVE run, against FP64
+central differences of the oracle trajectory (h = 1e-4 for parameters).
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import md_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SIG = np.array([[1.0, 0.8], [0.8, 0.88]])
+EPS = np.array([[1.0, 1.5], [1.5, 0.5]])
+
+
+def _ka(cuda, n_cells=5, seed=0, disorder=0.1):
+    from tests.helpers import fcc_system
+    R, P, _ = fcc_system(n_cells, seed)
+    n = len(R)
+    L = float(np.float32((n / 1.2) ** (1 / 3)))
+    a0 = (4 / 0.8442) ** (1 / 3)
+    R = (R / (a0 * n_cells) * L).astype(np.float32)
+    rng = np.random.default_rng(seed)
+    R = np.mod(R + rng.uniform(-disorder, disorder, R.shape), L).astype(np.float32)
+    species = np.zeros(n, np.int32)
+    species[rng.permutation(n)[: n // 5]] = 1
+    P = (rng.standard_normal((n, 3)) * np.sqrt(0.8)).astype(np.float32)
+    P -= P.mean(0, keepdims=True)
+    return R, P, L, species
+
+
+def _energy(cuda, L, species, fmt='Dense'):
+    from jax_md_gb300 import energy, partition, space
+    disp, shift = space.periodic(L)
+    nfn, efn = energy.lennard_jones_neighbor_list(disp, L, torch.tensor(species, device=cuda),
+                                                  sigma=SIG, epsilon=EPS, dr_threshold=0.3,
+                                                  format=getattr(partition, fmt))
+    return disp, shift, nfn, efn
+
+
+def _spec(species, sig=SIG, eps=EPS):
+    return O.PairSpec(kind='lj', sigma=sig, epsilon=eps, species=species)
+
+
+def test_force_vjp_positions_match_oracle(cuda):
+    R, P, L, species = _ka(cuda)
+    disp, shift, nfn, efn = _energy(cuda, L, species)
+    Rt = torch.tensor(R, device=cuda)
+    nb = nfn.allocate(Rt)
+    lam = np.random.default_rng(1).standard_normal(R.shape).astype(np.float32)
+    gR, _, _ = efn.force_vjp(Rt, nb, torch.tensor(lam, device=cuda))
+    go, _, _ = O.pair_force_vjp(_spec(species), R, nb.idx.cpu().numpy(), O.DENSE,
+                                lam.astype(np.float64), np.full(3, L))
+    scale = np.abs(go).max()
+    assert np.abs(gR.cpu().numpy() - go).max() <= 2e-5 * scale
+
+
+@pytest.mark.parametrize('which', ['sigma', 'epsilon'])
+def test_force_and_energy_param_grads_match_fd(cuda, which):
+    R, P, L, species = _ka(cuda)
+    disp, shift, nfn, efn = _energy(cuda, L, species)
+    Rt = torch.tensor(R, device=cuda)
+    nb = nfn.allocate(Rt)
+    idx = nb.idx.cpu().numpy()
+    lam = np.random.default_rng(2).standard_normal(R.shape)
+    _, bins, _ = efn.force_vjp(Rt, nb, torch.tensor(lam, dtype=torch.float32, device=cuda))
+    ebins = efn.energy_param_grad(Rt, nb)
+    from jax_md_gb300.smap import _bins_to_grads
+    sig_t = torch.tensor(SIG, device=cuda)
+    eps_t = torch.tensor(EPS, device=cuda)
+    gs, ge = _bins_to_grads(bins, None, sig_t, eps_t)
+    es, ee = _bins_to_grads(ebins, None, sig_t, eps_t)
+    g = (gs if which == 'sigma' else ge).cpu().numpy()
+    eg = (es if which == 'sigma' else ee).cpu().numpy()
+    h = 1e-6
+    box = np.full(3, L)
+    for a in range(2):
+        for b in range(2):
+            vals = []
+            for sgn in (1, -1):
+                sig, eps = SIG.copy(), EPS.copy()
+                (sig if which == 'sigma' else eps)[a, b] += sgn * h
+                E, F, _ = O.pair_energy_forces(_spec(species, sig, eps), R, idx, O.DENSE, box)
+                vals.append((float((lam * F).sum()), E))
+            fd = (vals[0][0] - vals[1][0]) / (2 * h)
+            fde = (vals[0][1] - vals[1][1]) / (2 * h)
+            assert abs(g[a, b] - fd) <= 1e-4 * max(1.0, abs(fd)), (a, b, g[a, b], fd)
+            assert abs(eg[a, b] - fde) <= 1e-4 * max(1.0, abs(fde)), (a, b, eg[a, b], fde)
+
+
+def test_autograd_hessian_vector_product(cuda):
+    """torch.autograd double backward through E(R): grad of v . dE/dR is H v."""
+    R, P, L, species = _ka(cuda)
+    disp, shift, nfn, efn = _energy(cuda, L, species)
+    Rt = torch.tensor(R, device=cuda)
+    nb = nfn.allocate(Rt)
+    v = torch.randn(Rt.shape, device=cuda, generator=torch.Generator(device=cuda).manual_seed(3))
+    Rg = Rt.clone().requires_grad_(True)
+    E = efn(Rg, nb)
+    (g,) = torch.autograd.grad(E, Rg, create_graph=True)
+    (hv,) = torch.autograd.grad((g * v).sum(), Rg)
+    go, _, _ = O.pair_force_vjp(_spec(species), R, nb.idx.cpu().numpy(), O.DENSE,
+                                v.cpu().numpy().astype(np.float64), np.full(3, L))
+    # (dF/dR)^T v = -H v
+    assert (hv.cpu().numpy() + go).__abs__().max() <= 2e-5 * np.abs(go).max()
+
+
+def _oracle_loss(R0, P0, L, species, sig, eps, steps, dt=0.005, msd_w=0.1):
+    box = np.full(3, L)
+    spec = _spec(species, sig, eps)
+    nl = O.NeighborListOracle(box, 2.5 * np.max(sig), 0.3)
+    h = {'nb': nl.allocate(R0)}
+
+    def fn(X):
+        h['nb'] = nl.update(X, h['nb'])
+        return O.pair_energy_forces(spec, X, h['nb'].idx, O.DENSE, box)[1]
+    R, P = R0.astype(np.float64), P0.astype(np.float64)
+    F = fn(R)
+    for _ in range(steps):
+        R, P, F = O.velocity_verlet(fn, R, P, F, 1.0, dt, box)
+    nb = nl.build(R, None)
+    E = O.pair_energy_forces(spec, R, nb.idx, O.DENSE, box)[0]
+    d = O.displacement(R, R0.astype(np.float64), box)
+    return E / len(R) + msd_w * float((d * d).sum(-1).mean())
+
+
+@pytest.mark.parametrize('k', [10, None], ids=['checkpointed', 'stored'])
+def test_trajectory_gradient_matches_fd(cuda, k):
+    from jax_md_gb300 import adjoint
+    R, P, L, species = _ka(cuda)
+    disp, shift, nfn, efn = _energy(cuda, L, species)
+    steps = 30
+    Rt = torch.tensor(R, device=cuda)
+    nb = nfn.allocate(Rt)
+    traj = adjoint.nve_trajectory(efn, nfn, shift, 0.005, steps, checkpoint_every=k)
+    sig_t = torch.tensor(SIG, dtype=torch.float32, device=cuda, requires_grad=True)
+    eps_t = torch.tensor(EPS, dtype=torch.float32, device=cuda, requires_grad=True)
+    R0 = Rt.clone().requires_grad_(True)
+    P0 = torch.tensor(P, device=cuda)
+    xn, pn = traj(R0, P0, nb, sigma=sig_t, epsilon=eps_t)
+    nb = nb.update(xn.detach())
+    E = efn(xn, nb, sigma=sig_t, epsilon=eps_t)
+    d = disp(xn, R0)
+    loss = E / len(R) + 0.1 * (d * d).sum(-1).mean()
+    loss.backward()
+    gs = sig_t.grad.cpu().numpy()
+    ge = eps_t.grad.cpu().numpy()
+    L0 = _oracle_loss(R, P, L, species, SIG, EPS, steps)
+    assert abs(float(loss) - L0) <= 1e-4 * abs(L0)
+    hh = 1e-4
+    for mat, g in (('sigma', gs), ('epsilon', ge)):
+        for a in range(2):
+            for b in range(2):
+                lp = []
+                for sgn in (1, -1):
+                    sig, eps = SIG.copy(), EPS.copy()
+                    (sig if mat == 'sigma' else eps)[a, b] += sgn * hh
+                    lp.append(_oracle_loss(R, P, L, species, sig, eps, steps))
+                fd = (lp[0] - lp[1]) / (2 * hh)
+                assert abs(g[a, b] - fd) <= 1e-3 * max(abs(fd), 1e-2), (mat, a, b, g[a, b], fd)
+    # initial positions: directional derivative along a random direction
+    v = np.random.default_rng(5).standard_normal(R.shape)
+    v /= np.linalg.norm(v)
+    eps_r = 1e-4
+    lp = _oracle_loss((R + eps_r * v).astype(np.float64), P, L, species, SIG, EPS, steps)
+    lm = _oracle_loss((R - eps_r * v).astype(np.float64), P, L, species, SIG, EPS, steps)
+    fd = (lp - lm) / (2 * eps_r)
+    ad = float((R0.grad.cpu().numpy() * v).sum())
+    assert abs(ad - fd) <= 1e-3 * max(abs(fd), 1e-2), (ad, fd)
+
+
+@pytest.mark.parametrize('k', [10, None], ids=['checkpointed', 'stored'])
+def test_gradient_cost_ratio(cuda, k):
+    """Forward + backward of a 100-step LJ run (32000 atoms) over the forward
+    alone.  The reverse pass costs one force VJP per step (about one fused
+    step) plus, when checkpointed, a replay of each segment."""
+    import time
+    from jax_md_gb300 import adjoint, energy, partition, space
+    from tests.helpers import fcc_system
+    R, P, L = fcc_system(20, 0)
+    disp, shift = space.periodic(L)
+    nfn, efn = energy.lennard_jones_neighbor_list(disp, L, dr_threshold=0.3, format=partition.Dense)
+    Rt = torch.tensor(R, device=cuda)
+    P0 = torch.tensor(P, device=cuda)
+    nb = nfn.allocate(Rt)
+    traj = adjoint.nve_trajectory(efn, nfn, shift, 0.005, 100, checkpoint_every=k)
+
+    def fwd():
+        with torch.no_grad():
+            return traj(Rt, P0, nb)
+
+    def fwd_bwd():
+        R0 = Rt.clone().requires_grad_(True)
+        xn, pn = traj(R0, P0, nb)
+        (pn * pn).sum().backward()
+        return R0.grad
+
+    def timed(f):
+        f()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(3):
+            f()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / 3
+
+    tf, tb = timed(fwd), timed(fwd_bwd)
+    print(f'forward {tf * 1e3:.1f} ms, forward+backward {tb * 1e3:.1f} ms, ratio {tb / tf:.2f}')
+    assert tb / tf <= 4.0
