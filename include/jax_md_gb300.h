@@ -235,6 +235,27 @@ int jmd_kinetic_energy(const float* momentum, int64_t p_stride,
                        int32_t dim, double* out, void* workspace,
                        size_t workspace_bytes, void* stream);
 
+/* jmd_kinetic_energy without a workspace: the same kernel and result, with
+ * its scratch (block partials and a completion counter) in a fixed device
+ * array built into this library, so the call allocates nothing.  It serves
+ * callers that have no device buffer to lend and may not allocate one at the
+ * point of the call: a host MD code or plugin that measures the temperature
+ * inside its time-step loop, where cudaMalloc/cudaFree would synchronise the
+ * device and break its stream pipelining, or a foreign runtime that hands out
+ * no scratch.  No counterpart in the reference (JAX allocates the reduction's
+ * scratch itself).
+ *   - n <= 4,194,304 atoms; larger n returns JMD_ERR_INVALID_ARGUMENT.
+ *   - The first call on each device looks up the array's device address
+ *     (cudaGetSymbolAddress, with that device current) and caches it; make
+ *     that first call before any stream capture.
+ *   - Every call on a device shares the one array, so calls that overlap on
+ *     the GPU (other streams, other host threads) race: issue them in order
+ *     on one stream.  The counter is cleared by each call. */
+int jmd_kinetic_energy_static_scratch(const float* momentum, int64_t p_stride,
+                                      const float* mass, float mass_scalar,
+                                      int64_t n, int32_t dim, double* out,
+                                      void* stream);
+
 /* Nose-Hoover chain state on the device, f64 (simulate.py:350-374). */
 typedef struct {
   int32_t chain_length;  /* M + 1 <= 16 */

@@ -99,6 +99,7 @@ SIGNATURES = {
                                         P, P, I64, F32, P, P]),
     'jmd_reduce_workspace_bytes': (SZ, [I64]),
     'jmd_kinetic_energy': (C.c_int, [P, I64, P, F32, I64, I32, P, P, SZ, P]),
+    'jmd_kinetic_energy_static_scratch': (C.c_int, [P, I64, P, F32, I64, I32, P, P]),
     'jmd_nhc_half_step': (C.c_int, [C.POINTER(Nhc), P, P, I32, P, P]),
     'jmd_scale_momentum': (C.c_int, [P, I64, I64, I32, P, P]),
     'jmd_set_dense_threads_per_atom': (C.c_int, [C.c_int]),

@@ -5,6 +5,8 @@
 //   velocity_verlet                :227-243
 //   nose_hoover_chain              :384-517  (substep :444-490, half step :492-507)
 // and jax_md/quantity.py:124-159 (kinetic_energy, f64 sum).
+#include <mutex>
+
 #include "common.cuh"
 
 namespace jmd {
@@ -488,6 +490,78 @@ size_t jmd_fire_workspace_bytes(int64_t n) {
   cv.take<unsigned int>(1);
   cv.take<double>(4);
   return cv.used + 256;
+}
+
+}  // extern "C"
+
+// ------------------------------------------- kinetic energy, static scratch --
+// A variant of jmd_kinetic_energy for callers that cannot hand the library a
+// workspace: its block partials and completion counter live in a fixed
+// device array compiled into this library, so a call allocates nothing.
+namespace jmd {
+namespace {
+
+constexpr int64_t kStaticReduceBlocks = 16384;  // 256 atoms per block: 4,194,304 atoms
+constexpr int64_t kStaticMaxAtoms = kStaticReduceBlocks * 256;
+constexpr size_t kStaticCounterOffset = sizeof(double) * kStaticReduceBlocks;
+// 128 KiB of partials + one counter (256 bytes keep the counter aligned).
+static __device__ __align__(256) unsigned char g_reduce_scratch[kStaticCounterOffset + 256];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_reduce_scratch on the current device, looked up once
+// per device (the first call on that device) and cached.
+int static_reduce_scratch(void** out) {
+  int dev = 0;
+  JMD_CUDA(cudaGetDevice(&dev));
+  JMD_REQUIRE(dev >= 0 && dev < kMaxDevices, "device ordinal beyond the static scratch table");
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (g_scratch_ptr[dev] == nullptr) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_reduce_scratch);
+    if (e != cudaSuccess)
+      return fail(JMD_ERR_CUDA, std::string("cudaGetSymbolAddress(static reduce scratch): ") +
+                                    cudaGetErrorString(e));
+    g_scratch_ptr[dev] = ptr;
+  }
+  *out = g_scratch_ptr[dev];
+  return JMD_OK;
+}
+
+}  // namespace
+}  // namespace jmd
+
+extern "C" {
+
+int jmd_kinetic_energy_static_scratch(const float* momentum, int64_t p_stride, const float* mass,
+                                      float mass_scalar, int64_t n, int32_t dim, double* out,
+                                      void* stream) {
+  JMD_REQUIRE(dim == 2 || dim == 3, "dim must be 2 or 3");
+  JMD_REQUIRE(out != nullptr, "out is null");
+  JMD_REQUIRE(n <= kStaticMaxAtoms,
+              "n exceeds the static-scratch limit of 4194304 atoms; use jmd_kinetic_energy with "
+              "a workspace");
+  void* base = nullptr;
+  int rc = static_reduce_scratch(&base);
+  if (rc) return rc;
+  cudaStream_t st = as_stream(stream);
+  if (n <= 0) {
+    JMD_CUDA(cudaMemsetAsync(out, 0, sizeof(double), st));
+    return JMD_OK;
+  }
+  double* partials = static_cast<double*>(base);
+  unsigned int* counter =
+      reinterpret_cast<unsigned int*>(static_cast<char*>(base) + kStaticCounterOffset);
+  // the completion counter must start at zero; the partials are overwritten
+  JMD_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), st));
+  const unsigned gr = (unsigned)ceil_div(n, 256);
+  if (dim == 3)
+    k_ke<3><<<gr, 256, 0, st>>>(momentum, p_stride, mass, mass_scalar, (int)n, partials, counter, out);
+  else
+    k_ke<2><<<gr, 256, 0, st>>>(momentum, p_stride, mass, mass_scalar, (int)n, partials, counter, out);
+  return check_launch("jmd_kinetic_energy_static_scratch");
 }
 
 }  // extern "C"
