@@ -163,6 +163,9 @@ def main():
     ap.add_argument('--impl', default='native')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cells', type=int, default=N_CELLS)
+    ap.add_argument('--direct', action='store_true',
+                    help='launch the engine kernels directly instead of replaying its CUDA '
+                         'graph (profilers list every kernel of the timed region this way)')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
@@ -198,9 +201,10 @@ def main():
     from jax_md_gb300 import tune
     tpa, tpa_ms = tune.autotune_dense(efn, st, nb, shift, DT, use_cache=False)
     # warm-up: the engine run (also builds and caches its CUDA graph)
-    simulate.run(apply, st, nb, max(3, args.warmup))
+    graphed = not args.direct
+    simulate.run(apply, st, nb, max(3, args.warmup), use_graph=graphed)
     torch.cuda.synchronize()
-    simulate.run(apply, st, nb, args.steps)     # records the graph for K steps
+    simulate.run(apply, st, nb, args.steps, use_graph=graphed)  # records the graph for K steps
     torch.cuda.synchronize()
     E0 = float(efn.energy_f64(st.position, nb) + quantity._ke_f64(st.momentum))
     rebuilds0 = 0
@@ -210,10 +214,12 @@ def main():
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with Clocks() as clk:
+        torch.cuda.nvtx.range_push('timed')
         ev0.record(cur)
-        simulate.run(apply, st, nb, args.steps)   # exactly K steps, one graph launch
+        simulate.run(apply, st, nb, args.steps, use_graph=graphed)  # exactly K steps
         ev1.record(cur)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
     ms = ev0.elapsed_time(ev1)
     if world > 1:
         t = torch.tensor([ms], device=dev)
@@ -292,6 +298,7 @@ def main():
                                'r_onset=2.0 skin=0.3 dt=0.005 NVE Dense, replicas only',
                    'l2': 'inputs larger than L2 (neighbour rows ~%d MB)' % int(n * 4 * nbar / 1e6),
                    'mean_neighbors': nbar, 'max_occupancy': nb.max_occupancy,
+                   'launch': 'cuda graph' if graphed else 'direct',
                    'threads_per_atom': tpa, 'tpa_ms': {str(k): v for k, v in tpa_ms.items()},
                    'energy_drift_per_atom': (E1 - E0) / n, 'overflow': overflow},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
