@@ -37,6 +37,9 @@ sys.path.insert(0, str(ROOT))
 METRIC = 'atom-steps/s LJ N=864k NVE fp32'
 N_CELLS = 60
 DENSITY, KT, DT, SKIN = 0.8442, 0.722, 0.005, 0.3
+# DRAM bytes of one fused-step launch per atom, from one ncu capture at
+# N=864,000 (dram__bytes_read.sum + dram__bytes_write.sum = 326.9 MB)
+TILED_DRAM_BYTES_PER_ATOM = 378.35
 
 
 def peaks():
@@ -61,12 +64,17 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(['nvidia-smi', '-i', os.environ.get('CUDA_VISIBLE_DEVICES', '0').split(',')[0],
                                           f'--query-gpu={q}', '--format=csv,noheader,nounits',
-                                          '-lms', '100'], stdout=subprocess.PIPE,
+                                          '-lms', '20'], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # let the sampler start before the timed region; keep only what follows
+            t0 = time.perf_counter()
+            while not self.samples and time.perf_counter() - t0 < 5.0:
+                time.sleep(0.01)
         except (OSError, FileNotFoundError):
             self.proc = None
+        self.mark = len(self.samples)
         return self
 
     def _read(self):
@@ -84,6 +92,8 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self):
+        if len(self.samples) > self.mark:
+            self.samples = self.samples[self.mark:]
         if not self.samples:
             return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unavailable']}
         sm = [float(s[0]) for s in self.samples if s[0].replace('.', '').isdigit()]
@@ -158,7 +168,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=200)
+    ap.add_argument('--steps', type=int, default=1000)
     ap.add_argument('--warmup', type=int, default=20)
     ap.add_argument('--impl', default='native')
     ap.add_argument('--no-cpu', action='store_true')
@@ -302,7 +312,10 @@ def main():
                    'threads_per_atom': tpa, 'tpa_ms': {str(k): v for k, v in tpa_ms.items()},
                    'energy_drift_per_atom': (E1 - E0) / n, 'overflow': overflow},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
-                     'frac': achieved / hbm, 'traffic': None, 'peak_source': src,
+                     'frac': achieved / hbm, 'traffic': TILED_DRAM_BYTES_PER_ATOM * n,
+                     'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one '
+                                       'k_tiled launch at N=864000 (378.35 B/atom), scaled by N',
+                     'peak_source': src,
                      'kernel': 'k_tiled fused NVE step (LJ, Dense tiled, FP32x2)', 'kernel_ms': kern_ms,
                      'bytes_per_atom': 4 * nbar + 80,
                      'step_algorithmic_GBps': step_bytes * args.steps / (ms / 1e3) / 1e9},
