@@ -491,6 +491,120 @@ int jmd_nve_adjoint_segment(const jmd_nve_system* sys, const float* trajectory,
                             float* pbar, float* record_scratch, double* grad_params,
                             int32_t use_graph, void* stream);
 
+/* ---------------------------------------------------------------- batch -- */
+/* Many independent periodic systems of uneven size packed end to end: atoms
+ * of system b are rows sys_offset[b] .. sys_offset[b+1]-1 of every per-atom
+ * array, its cells are global cells cell_offset[b] .. cell_offset[b+1]-1 of
+ * its own grid.  Each phase of a step (binning, search, forces, integration)
+ * is one launch over all systems.  The reference runs one system per call
+ * (jax.vmap needs equal N); a batch gives each system exactly the results of
+ * its own single-system call: the neighbour sets of partition.neighbor_list
+ * (partition.py:1034-1121) with the system's box and cell grid, the forces of
+ * smap.pair_neighbor_list, and the updates of simulate.nve / minimize.fire_descent.
+ * Every array named here is a device array. */
+typedef struct {
+  int32_t dim;                   /* 2 or 3 */
+  int32_t n_systems;             /* B */
+  int64_t n_atoms;               /* sys_offset[B] */
+  int32_t total_cells;           /* cell_offset[B] */
+  int32_t max_cells;             /* largest cell count of one system */
+  const int32_t* sys_offset;     /* [B+1] */
+  const int32_t* atom_sys;       /* [N] system of each atom */
+  const float* box;              /* [B*3] periodic box side per system and axis */
+  const int32_t* cell_offset;    /* [B+1] */
+  const int32_t* cells_per_side; /* [B*3], each >= 3 */
+  const float* cell_size;        /* [B*3] box / cells_per_side (float32, as partition.py:99-132) */
+} jmd_batch;
+
+/* Dense list of a batch in the engine's tiled layout: the entries of atom i
+ * are idx[(i/32)*ld*32 + k*32 + i%32], k < count[i]; entries are global atom
+ * ids (system-local id = id - sys_offset[b]).  Rows hold at most
+ * max_occupancy entries (ld >= max_occupancy); a longer row sets
+ * JMD_NEIGHBOR_LIST_OVERFLOW in error_code, and occupancy[0] receives the
+ * largest row length found (int32). */
+typedef struct {
+  float cutoff_sq;               /* (r_cutoff + dr_threshold)^2, all systems */
+  int32_t max_occupancy;
+  int32_t ld;
+  int32_t mask_self;
+  int32_t* idx;                  /* ((N + 31) / 32) * 32 * ld */
+  int32_t* count;                /* [N] */
+  float* reference_position;     /* [N] float4 rows, positions of the last build */
+  int32_t* occupancy;            /* [1] */
+  uint8_t* error_code;           /* [1] sticky PartitionErrorCode bits */
+  int32_t* rebuild_flag;         /* [1] gate of a conditional build, cleared by it */
+  void* workspace;
+  size_t workspace_bytes;
+} jmd_batch_nlist;
+
+size_t jmd_batch_nlist_workspace_bytes(const jmd_batch* batch);
+
+/* Builds the batch's lists at `position` (float4 rows).  gated != 0: only if
+ * *rebuild_flag != 0 (then clears it). */
+int jmd_batch_neighbor_list_build(const jmd_batch* batch, const jmd_batch_nlist* nl,
+                                  const float* position, int32_t gated, void* stream);
+
+/* Sets *rebuild_flag when any atom moved more than sqrt(threshold_sq) from
+ * its reference position (partition.py:1146-1154, per system box). */
+int jmd_batch_skin_check(const jmd_batch* batch, const jmd_batch_nlist* nl,
+                         const float* position, float threshold_sq, void* stream);
+
+/* Forces of every system (float4 rows) and, optionally, per-system f64
+ * potential energies energy[B] (smap.pair_neighbor_list, Dense /2). */
+int jmd_batch_pair_forces(const jmd_pair* pair, const jmd_batch* batch,
+                          const jmd_batch_nlist* nl, const float* position,
+                          const int32_t* species, float* force, double* energy,
+                          void* stream);
+
+/* Per-system f64 kinetic energy ke[B] (quantity.kinetic_energy) and
+ * largest atom force norm fmax[B] (either may be NULL). */
+int jmd_batch_kinetic_energy(const jmd_batch* batch, const float* momentum,
+                             const float* force, const float* mass, float mass_scalar,
+                             double* ke, float* fmax, void* stream);
+
+/* FIRE constants (minimize.fire_descent, minimize.py:124-226) plus the
+ * convergence tolerance on the largest atom force norm of a system. */
+typedef struct {
+  float dt_start, dt_max, n_min, f_inc, f_dec, alpha_start, f_alpha, f_tol;
+} jmd_fire_params;
+
+/* State of a batched run.  fire_state holds 8 floats per system:
+ * [dt, alpha, n_pos, keep, alpha_mix, |P|/|F|, max |F_i|, -].  done[b]
+ * becomes 1 once system b's largest force norm is below f_tol after a FIRE
+ * step; a done system is frozen (no further updates); n_done[0] counts
+ * them. */
+typedef struct {
+  jmd_batch batch;
+  jmd_batch_nlist nlist;
+  jmd_pair pair;
+  const int32_t* species;        /* [N] or NULL */
+  float* position;               /* [N] float4 rows */
+  float* momentum;
+  float* force;
+  const float* mass;             /* [N] or NULL: mass_scalar */
+  float mass_scalar;
+  float dt;                      /* NVE time step */
+  float threshold_sq;            /* (dr_threshold / 2)^2; < 0: rebuild every step */
+  float* fire_state;             /* [B * 8] */
+  int32_t* done;                 /* [B] */
+  int32_t* n_done;               /* [1] */
+} jmd_batch_system;
+
+/* Sets every system's FIRE scalars to (dt_start, alpha_start, 0, ...) and
+ * clears done / n_done. */
+int jmd_batch_fire_init(const jmd_batch_system* sys, const jmd_fire_params* fp, void* stream);
+
+/* n_steps of batched NVE (velocity Verlet, simulate.py:227-243) or FIRE
+ * (minimize.py:171-226) with the skin-gated list rebuild before every force
+ * evaluation.  The force array must hold F(position) on entry (from
+ * jmd_batch_pair_forces after a build).  use_graph != 0 records the whole run
+ * once per (system, n_steps) as one CUDA graph, each rebuild in a device-side
+ * conditional node, and replays it. */
+int jmd_batch_nve_run(const jmd_batch_system* sys, int64_t n_steps, int32_t use_graph,
+                      void* stream);
+int jmd_batch_fire_run(const jmd_batch_system* sys, const jmd_fire_params* fp,
+                       int64_t n_steps, int32_t use_graph, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,6 +72,35 @@ class SortedState(C.Structure):
                 ('workspace_bytes', C.c_size_t)]
 
 
+class Batch(C.Structure):
+    _fields_ = [('dim', C.c_int32), ('n_systems', C.c_int32), ('n_atoms', C.c_int64),
+                ('total_cells', C.c_int32), ('max_cells', C.c_int32),
+                ('sys_offset', C.c_void_p), ('atom_sys', C.c_void_p), ('box', C.c_void_p),
+                ('cell_offset', C.c_void_p), ('cells_per_side', C.c_void_p),
+                ('cell_size', C.c_void_p)]
+
+
+class BatchNList(C.Structure):
+    _fields_ = [('cutoff_sq', C.c_float), ('max_occupancy', C.c_int32), ('ld', C.c_int32),
+                ('mask_self', C.c_int32), ('idx', C.c_void_p), ('count', C.c_void_p),
+                ('reference_position', C.c_void_p), ('occupancy', C.c_void_p),
+                ('error_code', C.c_void_p), ('rebuild_flag', C.c_void_p),
+                ('workspace', C.c_void_p), ('workspace_bytes', C.c_size_t)]
+
+
+class FireParams(C.Structure):
+    _fields_ = [(k, C.c_float) for k in ('dt_start', 'dt_max', 'n_min', 'f_inc', 'f_dec',
+                                         'alpha_start', 'f_alpha', 'f_tol')]
+
+
+class BatchSystem(C.Structure):
+    _fields_ = [('batch', Batch), ('nlist', BatchNList), ('pair', Pair), ('species', C.c_void_p),
+                ('position', C.c_void_p), ('momentum', C.c_void_p), ('force', C.c_void_p),
+                ('mass', C.c_void_p), ('mass_scalar', C.c_float), ('dt', C.c_float),
+                ('threshold_sq', C.c_float), ('fire_state', C.c_void_p), ('done', C.c_void_p),
+                ('n_done', C.c_void_p)]
+
+
 P = C.c_void_p
 I64 = C.c_int64
 I32 = C.c_int32
@@ -123,6 +152,16 @@ SIGNATURES = {
     'jmd_nve_run_recorded': (C.c_int, [C.POINTER(NveSystem), P, I64, I32, I32, P]),
     'jmd_nve_adjoint_segment': (C.c_int, [C.POINTER(NveSystem), P, I64, I32, I32, P, P, P, P, I32,
                                           P]),
+    'jmd_batch_nlist_workspace_bytes': (SZ, [C.POINTER(Batch)]),
+    'jmd_batch_neighbor_list_build': (C.c_int, [C.POINTER(Batch), C.POINTER(BatchNList), P, I32,
+                                                P]),
+    'jmd_batch_skin_check': (C.c_int, [C.POINTER(Batch), C.POINTER(BatchNList), P, F32, P]),
+    'jmd_batch_pair_forces': (C.c_int, [C.POINTER(Pair), C.POINTER(Batch), C.POINTER(BatchNList),
+                                        P, P, P, P, P]),
+    'jmd_batch_kinetic_energy': (C.c_int, [C.POINTER(Batch), P, P, P, F32, P, P, P]),
+    'jmd_batch_fire_init': (C.c_int, [C.POINTER(BatchSystem), C.POINTER(FireParams), P]),
+    'jmd_batch_nve_run': (C.c_int, [C.POINTER(BatchSystem), I64, I32, P]),
+    'jmd_batch_fire_run': (C.c_int, [C.POINTER(BatchSystem), C.POINTER(FireParams), I64, I32, P]),
     'jmd_fire_kick_drift': (C.c_int, [P, P, P, P, F32, I64, C.POINTER(Space), P, P]),
     'jmd_fire_workspace_bytes': (SZ, [I64]),
     'jmd_fire_update': (C.c_int, [P, P, I64, I32, P, F32, F32, F32, F32, F32, F32, P, SZ, P]),

@@ -1,0 +1,417 @@
+"""Batches of independent periodic systems of uneven size on one GPU.
+
+JAX MD batches systems with ``jax.vmap``, which needs every system to have
+the same number of atoms.  Here systems of any sizes are packed end to end
+(``pack``); every per-atom array of the batch is the concatenation of the
+systems' arrays, ``sys_offset[b]:sys_offset[b+1]`` are system b's rows, and
+each system keeps its own periodic box and its own cell grid.  Each phase of
+a step (binning, neighbour search, forces, integration, the FIRE update) is a
+single launch over all systems, and ``BatchRunner`` replays whole runs of NVE
+(simulate.py:227-243) or FIRE (minimize.py:124-226) from one CUDA graph.
+
+Per system the results are those of the single-system API: the neighbour
+sets of ``partition.neighbor_list`` (partition.py:1034-1121, cell grid from
+``_cell_dimensions`` with the list cutoff), the forces and energies of the
+``smap.pair_neighbor_list`` energy it is given (smap.py:922-979), and the
+updates of ``simulate.nve`` / ``minimize.fire_descent``.  Row order inside a
+neighbour row may differ from the reference's (the sets are equal).
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import math
+from typing import List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _native as N
+from . import smap
+
+
+class Batch:
+    """Systems packed end to end: positions ``[N, 4]`` float4 rows (the
+    ``[N, dim]`` view is ``R``), ``sys_offset`` / ``atom_sys`` / ``box`` on the
+    device, ``species`` (int32 ``[N]``) when given."""
+
+    def __init__(self, positions: Sequence[torch.Tensor], boxes: Sequence, species=None,
+                 device=None):
+        if len(positions) == 0:
+            raise ValueError('a batch needs at least one system')
+        dims = {int(p.shape[1]) for p in positions}
+        if len(dims) != 1 or dims.pop() not in (2, 3):
+            raise ValueError('every system must have the same dimension, 2 or 3')
+        self.dim = int(positions[0].shape[1])
+        dev = torch.device(device) if device is not None else positions[0].device
+        self.device = dev
+        self.sizes = [int(p.shape[0]) for p in positions]
+        self.n_systems = len(positions)
+        off = np.zeros(self.n_systems + 1, np.int64)
+        off[1:] = np.cumsum(self.sizes)
+        if off[-1] >= 2 ** 31 - 1:
+            raise ValueError('a batch holds fewer than 2^31 atoms')
+        self.offsets = off
+        self.n = int(off[-1])
+        box = np.ones((self.n_systems, 3), np.float32)
+        for b, L in enumerate(boxes):
+            Lv = np.broadcast_to(np.asarray(L, np.float32), (self.dim,))
+            if np.any(Lv <= 0):
+                raise ValueError(f'system {b}: box sides must be positive')
+            box[b, :self.dim] = Lv
+        self.box_host = box
+        self.box = torch.tensor(box, device=dev)
+        self.position = torch.zeros((self.n, 4), dtype=torch.float32, device=dev)
+        for b, p in enumerate(positions):
+            pb = torch.as_tensor(p, dtype=torch.float32, device=dev)
+            Lt = self.box[b, :self.dim]
+            self.position[off[b]:off[b + 1], :self.dim] = torch.remainder(pb, Lt)
+        self.sys_offset = torch.tensor(off.astype(np.int32), device=dev)
+        self.atom_sys = torch.repeat_interleave(
+            torch.arange(self.n_systems, dtype=torch.int32, device=dev),
+            torch.tensor(self.sizes, device=dev)).to(torch.int32)
+        self.species = None
+        if species is not None:
+            self.species = torch.cat([torch.as_tensor(s, device=dev).to(torch.int32).reshape(-1)
+                                      for s in species]).contiguous()
+            if self.species.numel() != self.n:
+                raise ValueError('species must give one entry per atom of every system')
+
+    @property
+    def R(self) -> torch.Tensor:
+        return self.position[:, :self.dim]
+
+    def rows(self, b: int) -> slice:
+        return slice(int(self.offsets[b]), int(self.offsets[b + 1]))
+
+    def split(self, t: torch.Tensor) -> List[torch.Tensor]:
+        """Per-system views of a per-atom array."""
+        return [t[self.rows(b)] for b in range(self.n_systems)]
+
+
+def pack(positions, boxes, species=None, device=None) -> Batch:
+    """Packs systems (``[N_b, dim]`` positions, box side(s) per system,
+    optional per-atom species) into one Batch."""
+    return Batch(positions, boxes, species, device)
+
+
+class _Grid:
+    """Per-system cell grids for a list cutoff (partition.py:146-188 per
+    system: cells_per_side = floor(L / cutoff), cell_size = L / cells_per_side)."""
+
+    def __init__(self, batch: Batch, cutoff: float):
+        L = batch.box_host[:, :batch.dim]
+        cps = np.floor(L / np.float32(cutoff)).astype(np.int64)
+        if np.any(cps < 3):
+            b = int(np.argmin(cps.min(1)))
+            raise ValueError(f'system {b}: the box holds fewer than 3 cells of the list cutoff '
+                             f'{cutoff} per side; the batched search needs >= 3')
+        cs = (L / cps.astype(np.float32)).astype(np.float32)
+        ncell = np.prod(cps, axis=1)
+        if int(ncell.max()) > 24576:
+            raise ValueError('a system has more than 24576 cells (the batched binning works in '
+                             'shared memory); raise the cutoff or split the system')
+        coff = np.zeros(batch.n_systems + 1, np.int64)
+        coff[1:] = np.cumsum(ncell)
+        cps3 = np.ones((batch.n_systems, 3), np.int32)
+        cps3[:, :batch.dim] = cps
+        cs3 = np.ones((batch.n_systems, 3), np.float32)
+        cs3[:, :batch.dim] = cs
+        dev = batch.device
+        self.cps = torch.tensor(cps3, device=dev)
+        self.cs = torch.tensor(cs3, device=dev)
+        self.cell_offset = torch.tensor(coff.astype(np.int32), device=dev)
+        self.total_cells = int(coff[-1])
+        self.max_cells = int(ncell.max())
+        s = N.Batch()
+        s.dim = batch.dim
+        s.n_systems = batch.n_systems
+        s.n_atoms = batch.n
+        s.total_cells = self.total_cells
+        s.max_cells = self.max_cells
+        s.sys_offset = batch.sys_offset.data_ptr()
+        s.atom_sys = batch.atom_sys.data_ptr()
+        s.box = batch.box.data_ptr()
+        s.cell_offset = self.cell_offset.data_ptr()
+        s.cells_per_side = self.cps.data_ptr()
+        s.cell_size = self.cs.data_ptr()
+        self.struct = s
+
+
+@dataclasses.dataclass
+class BatchNeighborList:
+    """Dense lists of every system in the engine's tiled layout (see
+    jmd_batch_nlist): entries of atom i (global row) are
+    ``idx[(i//32)*ld*32 + k*32 + i%32]`` for ``k < count[i]``, global ids."""
+    idx: torch.Tensor
+    count: torch.Tensor
+    reference_position: torch.Tensor
+    error: torch.Tensor           # uint8 [1], PartitionErrorCode bits
+    occupancy: torch.Tensor       # int32 [1], largest row found by the last build
+    max_occupancy: int
+    ld: int
+    flag: torch.Tensor
+    workspace: torch.Tensor
+    batch: Batch
+    grid: _Grid
+    cutoff: float
+    threshold_sq: float
+    mask_self: bool
+
+    def struct(self) -> N.BatchNList:
+        s = N.BatchNList()
+        s.cutoff_sq = float(np.float32(np.float32(self.cutoff) * np.float32(self.cutoff)))
+        s.max_occupancy = self.max_occupancy
+        s.ld = self.ld
+        s.mask_self = 1 if self.mask_self else 0
+        s.idx = self.idx.data_ptr()
+        s.count = self.count.data_ptr()
+        s.reference_position = self.reference_position.data_ptr()
+        s.occupancy = self.occupancy.data_ptr()
+        s.error_code = self.error.data_ptr()
+        s.rebuild_flag = self.flag.data_ptr()
+        s.workspace = self.workspace.data_ptr()
+        s.workspace_bytes = self.workspace.numel()
+        return s
+
+    @property
+    def did_buffer_overflow(self) -> bool:
+        return bool(int(self.error.item()) & 3)
+
+    def dense(self, b: int) -> np.ndarray:
+        """System b's list as the reference's Dense ``[N_b, max_occupancy]``
+        array of system-local ids padded with N_b (rows sorted; host copy)."""
+        rows = self.batch.rows(b)
+        n_b = rows.stop - rows.start
+        i = torch.arange(rows.start, rows.stop, device=self.idx.device)
+        k = torch.arange(self.max_occupancy, device=self.idx.device)
+        pos = (i[:, None] // 32) * self.ld * 32 + k[None, :] * 32 + (i[:, None] % 32)
+        ent = self.idx[pos.reshape(-1)].reshape(n_b, self.max_occupancy).long() - rows.start
+        cnt = self.count[rows].long()
+        ent = torch.where(k[None, :] < cnt[:, None], ent, torch.full_like(ent, n_b))
+        out = ent.cpu().numpy()
+        out.sort(axis=1)
+        return out
+
+
+class BatchNeighborListFns:
+    """``allocate(batch)`` / ``update(position, nbrs)`` over a batch, the
+    batched form of partition.neighbor_list (partition.py:801-1164): the list
+    cutoff is r_cutoff + dr_threshold, capacity int(max_occupancy *
+    capacity_multiplier + extra_capacity) (partition.py:1090-1104) shared by
+    all systems, and update rebuilds (every system) when any atom moved more
+    than dr_threshold / 2 since the last build."""
+
+    def __init__(self, r_cutoff, dr_threshold=0.0, capacity_multiplier=1.25, mask_self=True):
+        self.r_cutoff = float(r_cutoff)
+        self.dr_threshold = float(dr_threshold)
+        f32 = np.float32
+        # float32 arithmetic of the reference's run (partition.py:880-884)
+        self.cutoff = float(f32(f32(self.r_cutoff) + f32(self.dr_threshold)))
+        self.capacity_multiplier = float(capacity_multiplier)
+        self.mask_self = bool(mask_self)
+        self.threshold_sq = float(f32((f32(self.dr_threshold) / f32(2)) ** 2)) \
+            if self.dr_threshold > 0 else -1.0
+
+    def _make(self, batch, grid, max_occ):
+        dev = batch.device
+        ld = ((max_occ + 7) // 8) * 8
+        n_pad = ((batch.n + 31) // 32) * 32
+        ws = N.lib().jmd_batch_nlist_workspace_bytes(ctypes.byref(grid.struct))
+        return BatchNeighborList(
+            idx=torch.empty(max(n_pad * ld, 1), dtype=torch.int32, device=dev),
+            count=torch.zeros(max(batch.n, 1), dtype=torch.int32, device=dev),
+            reference_position=torch.zeros((max(batch.n, 1), 4), dtype=torch.float32, device=dev),
+            error=torch.zeros(1, dtype=torch.uint8, device=dev),
+            occupancy=torch.zeros(1, dtype=torch.int32, device=dev),
+            max_occupancy=int(max_occ), ld=int(ld),
+            flag=torch.zeros(1, dtype=torch.int32, device=dev),
+            workspace=torch.empty(ws, dtype=torch.uint8, device=dev),
+            batch=batch, grid=grid, cutoff=self.cutoff, threshold_sq=self.threshold_sq,
+            mask_self=self.mask_self)
+
+    def _build(self, nb, position, gated=False):
+        N.check(N.lib().jmd_batch_neighbor_list_build(ctypes.byref(nb.grid.struct),
+                                                      ctypes.byref(nb.struct()),
+                                                      position.data_ptr(), 1 if gated else 0,
+                                                      N.stream_ptr()), 'batch_neighbor_list_build')
+
+    def allocate(self, batch: Batch, extra_capacity: int = 0) -> BatchNeighborList:
+        N.require_cuda(batch.position)
+        grid = _Grid(batch, self.cutoff)
+        # count pass: a first build at a generous width reports the largest row
+        probe = self._make(batch, grid, 64)
+        self._build(probe, batch.position)
+        occ = int(probe.occupancy.item())
+        if occ > probe.max_occupancy:
+            probe = self._make(batch, grid, occ)
+            self._build(probe, batch.position)
+            occ = int(probe.occupancy.item())
+        cap = int(np.float32(occ) * np.float32(self.capacity_multiplier) + extra_capacity)
+        cap = max(1, min(cap, max(batch.sizes) - (1 if self.mask_self else 0)))
+        nb = self._make(batch, grid, max(cap, 1))
+        self._build(nb, batch.position)
+        return nb
+
+    def update(self, position: torch.Tensor, nbrs: BatchNeighborList) -> BatchNeighborList:
+        L = N.lib()
+        if self.threshold_sq < 0:
+            self._build(nbrs, position)
+            return nbrs
+        N.check(L.jmd_batch_skin_check(ctypes.byref(nbrs.grid.struct), ctypes.byref(nbrs.struct()),
+                                       position.data_ptr(), self.threshold_sq, N.stream_ptr()),
+                'batch_skin_check')
+        self._build(nbrs, position, gated=True)
+        return nbrs
+
+
+def neighbor_list(r_cutoff, dr_threshold=0.0, capacity_multiplier=1.25,
+                  mask_self=True) -> BatchNeighborListFns:
+    return BatchNeighborListFns(r_cutoff, dr_threshold, capacity_multiplier, mask_self)
+
+
+class BatchPairEnergy:
+    """The pair energy of a single-system ``energy.*_neighbor_list`` energy
+    function (smap.PairNeighborListEnergy: its potential and parameters),
+    evaluated on every system of a batch with the batch's species."""
+
+    def __init__(self, energy_fn: smap.PairNeighborListEnergy):
+        if not isinstance(energy_fn, smap.PairNeighborListEnergy):
+            raise NotImplementedError('batched energies come from jax_md_gb300.energy '
+                                      '*_neighbor_list energy functions')
+        self.energy_fn = energy_fn
+
+    def pair(self, batch: Batch):
+        dyn = {'species': batch.species} if batch.species is not None else {}
+        species, pair = self.energy_fn._resolve(batch.R, dyn)
+        return species, pair
+
+    def forces(self, batch: Batch, nbrs: BatchNeighborList, out=None, energies=None):
+        """Forces of every system (``[N, 4]`` float4 rows) and, with
+        ``energies`` (f64 ``[B]``), the per-system potential energies."""
+        species, pair = self.pair(batch)
+        if out is None:
+            out = torch.empty((batch.n, 4), dtype=torch.float32, device=batch.device)
+        N.check(N.lib().jmd_batch_pair_forces(ctypes.byref(pair), ctypes.byref(nbrs.grid.struct),
+                                              ctypes.byref(nbrs.struct()),
+                                              batch.position.data_ptr(), N.ptr(species),
+                                              out.data_ptr(), N.ptr(energies), N.stream_ptr()),
+                'batch_pair_forces')
+        return out
+
+    def energies(self, batch: Batch, nbrs: BatchNeighborList) -> torch.Tensor:
+        e = torch.empty(batch.n_systems, dtype=torch.float64, device=batch.device)
+        scratch = torch.empty((batch.n, 4), dtype=torch.float32, device=batch.device)
+        self.forces(batch, nbrs, out=scratch, energies=e)
+        return e
+
+
+FIRE_DEFAULTS = dict(dt_start=0.1, dt_max=0.4, n_min=5, f_inc=1.1, f_dec=0.5, alpha_start=0.1,
+                     f_alpha=0.99)
+
+
+class BatchRunner:
+    """Device state of a batch (momenta, forces, FIRE scalars per system) and
+    the graph-replayed runners.  Unit mass unless ``mass`` is given (scalar).
+
+    ``fire(n)`` / ``nve(n)`` run n steps of every system as one CUDA graph
+    launch (recorded on first use of each n); ``minimize`` repeats FIRE
+    chunks until every system's largest atom force norm is below f_tol."""
+
+    def __init__(self, batch: Batch, neighbor_fns: BatchNeighborListFns, nbrs: BatchNeighborList,
+                 energy: BatchPairEnergy, dt: float = 1e-3, mass: float = 1.0, **fire):
+        self.batch, self.neighbor_fns, self.nbrs, self.energy = batch, neighbor_fns, nbrs, energy
+        dev = batch.device
+        n = max(batch.n, 1)
+        self.momentum = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+        self.force = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+        self.fire_state = torch.zeros(8 * batch.n_systems, dtype=torch.float32, device=dev)
+        self.done = torch.zeros(batch.n_systems, dtype=torch.int32, device=dev)
+        self.n_done = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.dt = float(np.float32(dt))
+        self.mass = float(mass)
+        params = dict(FIRE_DEFAULTS)
+        params.update({k: v for k, v in fire.items() if k in FIRE_DEFAULTS})
+        self.fire_params = N.FireParams(*[float(np.float32(params[k])) for k in (
+            'dt_start', 'dt_max', 'n_min', 'f_inc', 'f_dec', 'alpha_start', 'f_alpha')], 0.0)
+        self.species, self.pair = energy.pair(batch)
+        self.compute_forces()
+
+    def struct(self) -> N.BatchSystem:
+        s = N.BatchSystem()
+        s.batch = self.nbrs.grid.struct
+        s.nlist = self.nbrs.struct()
+        s.pair = self.pair
+        s.species = N.ptr(self.species)
+        s.position = self.batch.position.data_ptr()
+        s.momentum = self.momentum.data_ptr()
+        s.force = self.force.data_ptr()
+        s.mass = None
+        s.mass_scalar = self.mass
+        s.dt = self.dt
+        s.threshold_sq = self.neighbor_fns.threshold_sq
+        s.fire_state = self.fire_state.data_ptr()
+        s.done = self.done.data_ptr()
+        s.n_done = self.n_done.data_ptr()
+        return s
+
+    def compute_forces(self):
+        self.neighbor_fns.update(self.batch.position, self.nbrs)
+        self.energy.forces(self.batch, self.nbrs, out=self.force)
+        return self.force
+
+    def set_momenta(self, kT: float, seed: int = 0):
+        """Gaussian momenta at temperature kT with each system's net momentum
+        removed (simulate.py:141-165, per system)."""
+        g = torch.Generator(device=self.batch.device).manual_seed(seed)
+        d = self.batch.dim
+        p = torch.randn((self.batch.n, d), generator=g, device=self.batch.device) * math.sqrt(
+            kT * self.mass)
+        for b in range(self.batch.n_systems):
+            r = self.batch.rows(b)
+            p[r] -= p[r].mean(0, keepdim=True)
+        self.momentum.zero_()
+        self.momentum[:, :d] = p
+
+    def fire_init(self, f_tol: float = 0.0):
+        self.fire_params.f_tol = float(np.float32(f_tol))
+        N.check(N.lib().jmd_batch_fire_init(ctypes.byref(self.struct()),
+                                            ctypes.byref(self.fire_params), N.stream_ptr()),
+                'batch_fire_init')
+        self.momentum.zero_()
+
+    def fire(self, n_steps: int, use_graph: bool = True) -> int:
+        N.check(N.lib().jmd_batch_fire_run(ctypes.byref(self.struct()),
+                                           ctypes.byref(self.fire_params), int(n_steps),
+                                           1 if use_graph else 0, N.stream_ptr()), 'batch_fire_run')
+        return int(n_steps)
+
+    def minimize(self, f_tol: float, max_steps: int, chunk: int = 200, use_graph=True) -> int:
+        """FIRE from rest until every system has max |F_i| < f_tol (or
+        max_steps); returns the number of steps run."""
+        self.fire_init(f_tol)
+        steps = 0
+        while steps < max_steps:
+            k = min(chunk, max_steps - steps)
+            self.fire(k, use_graph)
+            steps += k
+            if int(self.n_done.item()) == self.batch.n_systems:
+                break
+        return steps
+
+    def nve(self, n_steps: int, use_graph: bool = True):
+        N.check(N.lib().jmd_batch_nve_run(ctypes.byref(self.struct()), int(n_steps),
+                                          1 if use_graph else 0, N.stream_ptr()), 'batch_nve_run')
+
+    def kinetic(self):
+        """(kinetic energy [B] f64, largest atom force norm [B])."""
+        ke = torch.empty(self.batch.n_systems, dtype=torch.float64, device=self.batch.device)
+        fm = torch.empty(self.batch.n_systems, dtype=torch.float32, device=self.batch.device)
+        N.check(N.lib().jmd_batch_kinetic_energy(ctypes.byref(self.nbrs.grid.struct),
+                                                 self.momentum.data_ptr(), self.force.data_ptr(),
+                                                 None, self.mass, ke.data_ptr(), fm.data_ptr(),
+                                                 N.stream_ptr()), 'batch_kinetic_energy')
+        return ke, fm
+
+    def potential(self):
+        return self.energy.energies(self.batch, self.nbrs)

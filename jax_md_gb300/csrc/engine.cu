@@ -21,6 +21,7 @@
 // rebuild's last kernel.  Direct mode launches the same kernels with the
 // rebuild chain gated by the device flag inside each kernel.
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <string>
@@ -383,6 +384,19 @@ int launch_graphed(const std::string& key, Enq enq, cudaStream_t st) {
 }
 
 }  // namespace
+
+// Shared with the batched runner (declared in pair.cuh).
+int graph_conditional(const int32_t* flag, const std::function<int(cudaStream_t)>& body,
+                      cudaStream_t st, cudaStream_t body_st) {
+  return conditional(flag, body, st, body_st);
+}
+
+int graph_launch_cached(const std::string& key,
+                        const std::function<int(cudaStream_t, cudaStream_t)>& enq,
+                        cudaStream_t st) {
+  return launch_graphed(key, enq, st);
+}
+
 }  // namespace jmd
 
 extern "C" {

@@ -7,6 +7,9 @@
 //   soft_sphere                       :125-173  eps/alpha (1 - r/sigma)^alpha
 #pragma once
 
+#include <functional>
+#include <string>
+
 #include "common.cuh"
 
 namespace jmd {
@@ -140,4 +143,15 @@ int adjoint_pack(const jmd_nve_system& s, const float* x, float* xbar, float* pb
                  bool kick, bool skin, cudaStream_t st);
 int adjoint_vjp_step(const jmd_nve_system& s, float* xbar, const float* rec, float weight,
                      double* grad_params, cudaStream_t st);
+}  // namespace jmd
+
+namespace jmd {
+// CUDA graph helpers of the engine (engine.cu): append "IF (*flag) { body }"
+// to the capture on st (body recorded on body_st); record enq(capture,
+// body stream) once per key as a graph and launch it on st.
+int graph_conditional(const int32_t* flag, const std::function<int(cudaStream_t)>& body,
+                      cudaStream_t st, cudaStream_t body_st);
+int graph_launch_cached(const std::string& key,
+                        const std::function<int(cudaStream_t, cudaStream_t)>& enq,
+                        cudaStream_t st);
 }  // namespace jmd

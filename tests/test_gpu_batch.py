@@ -1,0 +1,196 @@
+"""Batched uneven systems against the FP64 oracle, system by system.
+
+Each system of a batch must get the results of its own single-system call:
+neighbour sets of partition.neighbor_list (sorted rows, pairs within 1e-6 of
+the cutoff excluded), forces and energies of smap.pair_neighbor_list, FIRE
+steps of minimize.fire_descent and velocity-Verlet steps of simulate.nve.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import md_oracle as O
+from tests.helpers import near_cutoff_pairs
+
+pytestmark = pytest.mark.gpu
+
+SS_SIGMA = np.array([[1.0, 1.2], [1.2, 1.4]])
+SIZES_2D = [64, 150, 401, 1000, 97, 2500]
+
+
+def _ss_batch(cuda, sizes=SIZES_2D, seed=0, capacity_multiplier=1.25):
+    from jax_md_gb300 import batch, energy, space
+    systems = [O.bidisperse_2d(n, phi=0.84, seed=seed + k) for k, n in enumerate(sizes)]
+    Rs = [torch.tensor(R, device=cuda) for R, L, s in systems]
+    bt = batch.pack(Rs, [float(L) for R, L, s in systems], species=[s for R, L, s in systems])
+    disp, _ = space.periodic(float(systems[0][1]))
+    _, efn = energy.soft_sphere_neighbor_list(disp, float(systems[0][1]),
+                                              torch.tensor(systems[0][2], device=cuda),
+                                              sigma=SS_SIGMA)
+    fns = batch.neighbor_list(1.4, 0.2, capacity_multiplier=capacity_multiplier)
+    nb = fns.allocate(bt)
+    return systems, bt, fns, nb, batch.BatchPairEnergy(efn)
+
+
+def _lj_batch(cuda, cells=(6, 7, 8), seed=0):
+    from jax_md_gb300 import batch, energy, space
+    systems = [O.fcc_lattice(c, 0.8442, 0.05, seed + k) for k, c in enumerate(cells)]
+    Rs = [torch.tensor(R, device=cuda) for R, L in systems]
+    bt = batch.pack(Rs, [float(L) for R, L in systems])
+    disp, _ = space.periodic(float(systems[0][1]))
+    _, efn = energy.lennard_jones_neighbor_list(disp, float(systems[0][1]), dr_threshold=0.3)
+    fns = batch.neighbor_list(2.5, 0.3)
+    nb = fns.allocate(bt)
+    return systems, bt, fns, nb, batch.BatchPairEnergy(efn)
+
+
+def _check_sets(bt, nb, systems, cutoff, dim):
+    for b, sysb in enumerate(systems):
+        R, L = sysb[0], float(sysb[1])
+        box = np.full(dim, L)
+        got = nb.dense(b)
+        nl = O.NeighborListOracle(box, cutoff, 0.0, fmt=O.DENSE)
+        ref = O.neighbor_sets(nl.build(R), len(R))
+        near = near_cutoff_pairs(R, box, cutoff)
+        for i in range(len(R)):
+            g = {int(j) for j in got[i] if j < len(R)}
+            r = set(ref[i])
+            diff = {(i, j) for j in g ^ r}
+            assert diff <= near, (b, i, sorted(g ^ r))
+
+
+def test_batch_neighbor_sets_2d_uneven(cuda):
+    systems, bt, fns, nb, _ = _ss_batch(cuda)
+    torch.cuda.synchronize()
+    assert not nb.did_buffer_overflow
+    _check_sets(bt, nb, systems, 1.6, 2)
+
+
+def test_batch_neighbor_sets_3d(cuda):
+    systems, bt, fns, nb, _ = _lj_batch(cuda)
+    assert not nb.did_buffer_overflow
+    _check_sets(bt, nb, systems, 2.8, 3)
+
+
+@pytest.mark.parametrize('kind', ['soft_sphere_2d', 'lj_3d'])
+def test_batch_forces_and_energies(cuda, kind):
+    if kind == 'soft_sphere_2d':
+        systems, bt, fns, nb, ef = _ss_batch(cuda)
+        specs = [O.PairSpec(kind='soft_sphere', sigma=SS_SIGMA, species=s) for R, L, s in systems]
+        dim = 2
+    else:
+        systems, bt, fns, nb, ef = _lj_batch(cuda)
+        specs = [O.PairSpec(kind='lj') for _ in systems]
+        dim = 3
+    e = torch.empty(bt.n_systems, dtype=torch.float64, device=cuda)
+    F = ef.forces(bt, nb, energies=e)
+    torch.cuda.synchronize()
+    Fb = bt.split(F[:, :dim])
+    for b, sysb in enumerate(systems):
+        R, L = sysb[0], float(sysb[1])
+        box = np.full(dim, L)
+        idx = nb.dense(b)
+        E0, F0, _ = O.pair_energy_forces(specs[b], R, idx, O.DENSE, box)
+        scale = O.pair_force_abs_sum(specs[b], R, idx, O.DENSE, box)
+        err = np.abs(Fb[b].cpu().numpy() - F0).max(1)
+        assert np.all(err <= 1e-4 + 4e-6 * scale), (b, err.max())
+        assert abs(float(e[b]) - E0) <= 1e-5 * abs(E0) + 1e-6, (b, float(e[b]), E0)
+
+
+def test_batch_fire_matches_oracle_steps(cuda):
+    from jax_md_gb300 import batch
+    systems, bt, fns, nb, ef = _ss_batch(cuda, sizes=[64, 300, 777])
+    run = batch.BatchRunner(bt, fns, nb, ef)
+    run.fire_init(f_tol=0.0)
+    steps = 25
+    run.fire(steps)
+    torch.cuda.synchronize()
+    fs = run.fire_state.view(-1, 8).cpu().numpy()
+    Rb = bt.split(bt.R)
+    for b, (R, L, s) in enumerate(systems):
+        box = np.full(2, float(L))
+        spec = O.PairSpec(kind='soft_sphere', sigma=SS_SIGMA, species=s)
+        nl = O.NeighborListOracle(box, 1.4, 0.2, fmt=O.DENSE)
+        h = {'nb': nl.allocate(R)}
+
+        def fn(X):
+            h['nb'] = nl.update(X, h['nb'])
+            return O.pair_energy_forces(spec, X, h['nb'].idx, O.DENSE, box)[1]
+        Rd = R.astype(np.float64)
+        st = O.FireO(Rd, np.zeros_like(Rd), fn(Rd), 1.0, 0.1, 0.1, 0)
+        for _ in range(steps):
+            st = O.fire_step(fn, st, box)
+        assert abs(fs[b, 0] - st.dt) < 1e-5 * max(1.0, st.dt), (b, fs[b, 0], st.dt)
+        assert abs(fs[b, 1] - st.alpha) < 1e-5, (b, fs[b, 1], st.alpha)
+        assert int(fs[b, 2]) == st.n_pos
+        d = O.displacement(Rb[b].cpu().numpy(), st.R, box)
+        assert np.abs(d).max() < 1e-3, (b, np.abs(d).max())
+
+
+def test_batch_minimize_to_tolerance(cuda):
+    from jax_md_gb300 import batch
+    systems, bt, fns, nb, ef = _ss_batch(cuda, sizes=[64, 200, 512, 128])
+    run = batch.BatchRunner(bt, fns, nb, ef)
+    E0 = run.potential().cpu().numpy()
+    steps = run.minimize(f_tol=1e-4, max_steps=20000, chunk=500)
+    torch.cuda.synchronize()
+    assert int(run.n_done.item()) == bt.n_systems, steps
+    assert not nb.did_buffer_overflow
+    # the stopping test used the forces after each system's last step
+    fmax_stop = run.fire_state.view(-1, 8)[:, 6].cpu().numpy()
+    assert np.all(fmax_stop < 1e-4)
+    E1 = run.potential().cpu().numpy()
+    assert np.all(E1 < E0)
+
+
+def test_batch_nve_matches_oracle(cuda):
+    from jax_md_gb300 import batch
+    systems, bt, fns, nb, ef = _lj_batch(cuda)
+    run = batch.BatchRunner(bt, fns, nb, ef, dt=0.005)
+    P0 = [O.maxwell_boltzmann(len(R), 3, 0.722, 10 + b) for b, (R, L) in enumerate(systems)]
+    run.momentum.zero_()
+    run.momentum[:, :3] = torch.tensor(np.concatenate(P0), device=cuda)
+    steps = 50
+    run.nve(steps)
+    torch.cuda.synchronize()
+    Rb = bt.split(bt.R)
+    Pb = bt.split(run.momentum[:, :3])
+    spec = O.PairSpec(kind='lj')
+    for b, (R, L) in enumerate(systems):
+        box = np.full(3, float(L))
+        nl = O.NeighborListOracle(box, 2.5, 0.3, fmt=O.DENSE)
+        h = {'nb': nl.allocate(R)}
+
+        def fn(X):
+            h['nb'] = nl.update(X, h['nb'])
+            return O.pair_energy_forces(spec, X, h['nb'].idx, O.DENSE, box)[1]
+        X, P = R.astype(np.float64), P0[b].astype(np.float64)
+        F = fn(X)
+        for _ in range(steps):
+            X, P, F = O.velocity_verlet(fn, X, P, F, 1.0, 0.005, box)
+        d = O.displacement(Rb[b].cpu().numpy(), X, box)
+        assert np.abs(d).max() < 1e-3, (b, np.abs(d).max())
+        assert np.abs(Pb[b].cpu().numpy() - P).max() < 1e-2
+
+
+def test_batch_nve_graph_equals_direct(cuda):
+    """The graph-replayed run and direct launches give identical states."""
+    from jax_md_gb300 import batch
+    out = []
+    for use_graph in (True, False):
+        systems, bt, fns, nb, ef = _lj_batch(cuda, cells=(6, 7))
+        run = batch.BatchRunner(bt, fns, nb, ef, dt=0.005)
+        run.set_momenta(0.722, seed=4)
+        run.nve(30, use_graph=use_graph)
+        out.append((bt.position.clone(), run.momentum.clone()))
+    torch.cuda.synchronize()
+    assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
+
+
+def test_batch_overflow_flag(cuda):
+    systems, bt, fns, nb, _ = _ss_batch(cuda, sizes=[64, 150])
+    small = fns._make(bt, nb.grid, 2)
+    fns._build(small, bt.position)
+    torch.cuda.synchronize()
+    assert small.did_buffer_overflow
+    assert int(small.occupancy.item()) == nb.occupancy.item()
