@@ -120,6 +120,182 @@ def cpu_port_run(R, P, L, steps, threads=0):
     return dt, rb, lib.md_cpu_max_threads()
 
 
+def _events(dev):
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def batched_section(dev, n_sys=512, fire_steps=200, nve_steps=200, seed=0):
+    """512 uneven 2D bidisperse soft-sphere systems (N ~ U[64, 4096], phi
+    0.84, sigma_ij = (d_i + d_j) / 2 with d in {1.0, 1.4}): a fixed number of
+    FIRE steps, then NVE at kT = 1e-4, as one graph launch per run over all
+    systems, against the same steps run system by system through the
+    single-system API (FIRE: per-step launches; NVE: one engine graph per
+    system)."""
+    import torch
+    from jax_md_gb300 import batch, energy, minimize, partition, simulate, space
+    from oracle import md_oracle as O
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(64, 4097, n_sys)
+    systems = [O.bidisperse_2d(int(n), 0.84, seed + 1 + k) for k, n in enumerate(sizes)]
+    sigma = np.array([[1.0, 1.2], [1.2, 1.4]])
+    n_tot = int(sizes.sum())
+    Rs = [torch.tensor(R, device=dev) for R, L, sp in systems]
+    bt = batch.pack(Rs, [float(L) for R, L, sp in systems], species=[sp for R, L, sp in systems])
+    disp, _ = space.periodic(float(systems[0][1]))
+    _, efn = energy.soft_sphere_neighbor_list(disp, float(systems[0][1]),
+                                              torch.tensor(systems[0][2], device=dev), sigma=sigma)
+    fns = batch.neighbor_list(1.4, 0.2)
+    nb = fns.allocate(bt, extra_capacity=4)
+    run = batch.BatchRunner(bt, fns, nb, batch.BatchPairEnergy(efn), dt=0.01)
+    x0, f0 = bt.position.clone(), run.force.clone()
+    cur = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        e0, e1 = _events(dev)
+        torch.cuda.synchronize()
+        e0.record(cur)
+        fn()
+        e1.record(cur)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    def restore():
+        bt.position.copy_(x0)
+        run.force.copy_(f0)
+        fns._build(nb, bt.position)
+        run.fire_init(0.0)
+
+    restore()
+    run.fire(fire_steps)                     # records the graph
+    restore()
+    t_bfire = timed(lambda: run.fire(fire_steps))
+    run.set_momenta(1e-4, seed=7)
+    p0 = run.momentum.clone()
+    run.nve(nve_steps)                       # records the graph
+    run.momentum.copy_(p0)
+    t_bnve = timed(lambda: run.nve(nve_steps))
+    overflow = nb.did_buffer_overflow
+
+    # plain: the same systems one at a time through the single-system API
+    plain = []
+    for k, (R, L, sp) in enumerate(systems):
+        d_k, s_k = space.periodic(float(L))
+        nfn_k, efn_k = energy.soft_sphere_neighbor_list(d_k, float(L), torch.tensor(sp, device=dev),
+                                                        sigma=sigma, format=partition.Dense)
+        Rk = torch.tensor(R, device=dev)
+        plain.append((nfn_k, efn_k, s_k, Rk, nfn_k.allocate(Rk, extra_capacity=4)))
+
+    def plain_fire():
+        for nfn_k, efn_k, s_k, Rk, nb_k in plain:
+            init, apply = minimize.fire_descent(efn_k, s_k)
+            st = init(Rk, neighbor=nb_k)
+            for _ in range(fire_steps):
+                nb_k = nb_k.update(st.position)
+                st = apply(st, neighbor=nb_k)
+    t_pfire = timed(plain_fire)
+    states = []
+    for k, (nfn_k, efn_k, s_k, Rk, nb_k) in enumerate(plain):
+        init, apply = simulate.nve(efn_k, s_k, 0.01)
+        pk = p0[bt.rows(k), :2]
+        st = init(0, Rk, momenta=pk, neighbor=nb_k)
+        simulate.run(apply, st, nb_k, nve_steps)      # records each system's graph
+        states.append((apply, st, nb_k))
+
+    def plain_nve():
+        for apply, st, nb_k in states:
+            simulate.run(apply, st, nb_k, nve_steps)
+    t_pnve = timed(plain_nve)
+    return {
+        'workload': f'{n_sys} 2D bidisperse soft-sphere systems, N~U[64,4096] (total {n_tot}), '
+                    'phi=0.84, skin 0.2, FIRE then NVE kT=1e-4 dt=0.01',
+        'fire_steps': fire_steps, 'nve_steps': nve_steps,
+        'batched_fire_atom_steps_per_s': n_tot * fire_steps / t_bfire,
+        'plain_fire_atom_steps_per_s': n_tot * fire_steps / t_pfire,
+        'fire_speedup': t_pfire / t_bfire,
+        'batched_nve_atom_steps_per_s': n_tot * nve_steps / t_bnve,
+        'plain_nve_atom_steps_per_s': n_tot * nve_steps / t_pnve,
+        'nve_speedup': t_pnve / t_bnve,
+        'plain': 'per-system calls of the single-system API on the same GPU (FIRE: per-step '
+                 'launches; NVE: simulate.run, one CUDA graph per system)',
+        'overflow': overflow,
+    }
+
+
+def adjoint_section(dev, steps=2000, checkpoint_every=100, seed=0):
+    """Kob-Andersen 80:20 binary LJ, N = 8000 at rho = 1.2: 200 FIRE steps,
+    momenta at kT = 0.8, then the gradient of PE/N + 0.1 MSD after 2000 NVE
+    steps (dt 0.005) with respect to the species sigma / epsilon matrices and
+    the initial positions, checkpointed every 100 steps; reports the forward
+    time and the forward + backward time."""
+    import torch
+    from jax_md_gb300 import adjoint, energy, minimize, partition, space
+    from oracle import md_oracle as O
+    n_side = 20
+    L = float(np.float32((n_side ** 3 / 1.2) ** (1 / 3)))
+    rng = np.random.default_rng(seed)
+    g = np.stack(np.meshgrid(*[np.arange(n_side)] * 3, indexing='ij'), -1).reshape(-1, 3)
+    R = np.mod((g + 0.5) * (L / n_side) + rng.uniform(-0.05, 0.05, g.shape), L).astype(np.float32)
+    n = len(R)
+    species = np.zeros(n, np.int32)
+    species[rng.permutation(n)[: n // 5]] = 1
+    sig = np.array([[1.0, 0.8], [0.8, 0.88]])
+    eps = np.array([[1.0, 1.5], [1.5, 0.5]])
+    disp, shift = space.periodic(L)
+    sp_t = torch.tensor(species, device=dev)
+    nfn, efn = energy.lennard_jones_neighbor_list(disp, L, sp_t, sigma=sig, epsilon=eps,
+                                                  dr_threshold=0.3, format=partition.Dense)
+    Rt = torch.tensor(R, device=dev)
+    nb = nfn.allocate(Rt, extra_capacity=8)
+    init, apply = minimize.fire_descent(efn, shift)
+    st = init(Rt, neighbor=nb)
+    for _ in range(200):
+        nb = nb.update(st.position)
+        st = apply(st, neighbor=nb)
+    R0 = st.position.contiguous().clone()
+    # the relaxed structure has another occupancy than the lattice start
+    nb = nfn.allocate(R0, extra_capacity=8)
+    P0 = torch.tensor(O.maxwell_boltzmann(n, 3, 0.8, seed + 1), device=dev)
+    traj = adjoint.nve_trajectory(efn, nfn, shift, 0.005, steps, checkpoint_every=checkpoint_every)
+    sig_t = torch.tensor(sig, dtype=torch.float32, device=dev, requires_grad=True)
+    eps_t = torch.tensor(eps, dtype=torch.float32, device=dev, requires_grad=True)
+
+    def forward():
+        with torch.no_grad():
+            return traj(R0, P0, nb, sigma=sig_t.detach(), epsilon=eps_t.detach())
+
+    def forward_backward():
+        Rg = R0.clone().requires_grad_(True)
+        xn, pn = traj(Rg, P0, nb, sigma=sig_t, epsilon=eps_t)
+        nb2 = nb.update(xn.detach())
+        E = efn(xn, nb2, sigma=sig_t, epsilon=eps_t)
+        d = disp(xn, Rg)
+        loss = E / n + 0.1 * (d * d).sum(-1).mean()
+        loss.backward()
+        return loss
+
+    forward()
+    forward_backward()
+    cur = torch.cuda.current_stream(dev)
+    out = {}
+    for name, fn in (('forward_s', forward), ('forward_backward_s', forward_backward)):
+        e0, e1 = _events(dev)
+        torch.cuda.synchronize()
+        e0.record(cur)
+        fn()
+        e1.record(cur)
+        torch.cuda.synchronize()
+        out[name] = e0.elapsed_time(e1) / 1e3
+    out.update({
+        'workload': f'Kob-Andersen N={n} rho=1.2, 200 FIRE steps, kT=0.8, {steps} NVE steps '
+                    f'dt=0.005, checkpoints every {checkpoint_every}, loss PE/N + 0.1 MSD, '
+                    'grad wrt sigma[2x2], epsilon[2x2], R0',
+        'gradient_cost_ratio': out['forward_backward_s'] / out['forward_s'],
+        'forward_atom_steps_per_s': n * steps / out['forward_s'],
+    })
+    return out
+
+
 def cpu_baseline(R, P, L, budget_s=15.0):
     """Times the float32 OpenMP port on a bounded number of steps of the same system."""
     dt1, _, threads = cpu_port_run(R, P, L, 2)
@@ -172,6 +348,8 @@ def main():
     ap.add_argument('--warmup', type=int, default=20)
     ap.add_argument('--impl', default='native')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-extras', action='store_true',
+                    help='skip the batched and adjoint measurements')
     ap.add_argument('--cells', type=int, default=N_CELLS)
     ap.add_argument('--direct', action='store_true',
                     help='launch the engine kernels directly instead of replaying its CUDA '
@@ -324,6 +502,9 @@ def main():
         'gpu_launches': launches_per_step * args.steps,
         'clocks': clk.summary(),
     }
+    if rank == 0 and not args.no_extras:
+        line['batched'] = batched_section(dev)
+        line['adjoint'] = adjoint_section(dev)
     if rank == 0 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline(R, P, L)
     if rank == 0:
