@@ -263,9 +263,9 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
                               z.perm, s.n, z.scratch4a, z.scratch4b, z.scratch_i_a, z.scratch_i_b,
                               flag, z.workspace, z.workspace_bytes, q);
     if (rc) return rc;
-    return jmd_neighbor_list_build_tiled(&s.nlist, x, s.n, z.idx, z.idx_ld, z.nbr_count,
-                                         z.occupancy, z.error_code, z.reference_position, flag,
-                                         z.workspace, z.workspace_bytes, q);
+    return build_tiled_after_sort(&s.nlist, x, s.n, z.idx, z.idx_ld, z.nbr_count, z.occupancy,
+                                  z.error_code, z.reference_position, flag, z.workspace,
+                                  z.workspace_bytes, q);
   };
   auto gate = [&](float* x) -> int {
     if (always) return rebuild_at(x, false, false, st);

@@ -753,6 +753,7 @@ __global__ void k_sort_copy_back(int n, Bins b, float4* x, float4* p, float4* f,
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   x[s] = b.sorted_pos[s];
+  b.sorted_id[s] = s;  // the bins now describe the reordered atoms
   p[s] = tp[s];
   if (f) f[s] = tf[s];
   if (species) species[s] = tsp[s];
@@ -834,7 +835,7 @@ template <int DIM, bool VEC4>
 int build_impl(const jmd_nlist* nl, const float* x, int64_t stride, int64_t n64, int32_t* idx,
                int64_t ld, int32_t* nbr_count, int64_t* occupancy, uint8_t* error_code,
                float* ref, int64_t ref_stride, int32_t* flag, void* ws, size_t ws_bytes,
-               cudaStream_t st, bool tiled = false) {
+               cudaStream_t st, bool tiled = false, bool bins_ready = false) {
   const int n = (int)n64;
   const bool cells = nl->use_cell_list != 0;
   Grid g = cells ? make_grid(*nl) : Grid{};
@@ -852,7 +853,7 @@ int build_impl(const jmd_nlist* nl, const float* x, int64_t stride, int64_t n64,
   a.n = n;
   a.width = nl->max_occupancy;
   if (cells) {
-    run_binning<DIM, VEC4>(x, stride, n, g, b, nullptr, flag, st);
+    if (!bins_ready) run_binning<DIM, VEC4>(x, stride, n, g, b, nullptr, flag, st);
   } else {
     k_zero<<<1, 256, 0, st>>>(b.count, 1, b.sc, flag);
     if (n > 0) k_pack<DIM, VEC4><<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(x, stride, n,
@@ -902,6 +903,27 @@ int build_impl(const jmd_nlist* nl, const float* x, int64_t stride, int64_t n64,
 }
 
 }  // namespace
+
+// The tiled build right after jmd_sort_by_cell on the same positions and
+// workspace: the sort's bins already describe the reordered atoms (its
+// copy-back sets sorted_id to the identity), so the binning is not repeated.
+int build_tiled_after_sort(const jmd_nlist* nl, const float* position, int64_t n, int32_t* tidx,
+                           int64_t depth, int32_t* nbr_count, int64_t* occupancy,
+                           uint8_t* error_code, float* reference_position, int32_t* rebuild_flag,
+                           void* workspace, size_t workspace_bytes, cudaStream_t st) {
+  int e = validate(nl, n);
+  if (e) return e;
+  JMD_REQUIRE(nl->format == JMD_DENSE && nl->use_cell_list, "tiled lists are Dense with a cell grid");
+  JMD_REQUIRE(tidx && nbr_count && depth >= nl->max_occupancy, "tiled list needs depth >= max_occupancy");
+  if (nl->space.dim == 3)
+    return build_impl<3, true>(nl, position, 4, n, tidx, depth, nbr_count, occupancy, error_code,
+                               reference_position, 4, rebuild_flag, workspace, workspace_bytes, st,
+                               true, true);
+  return build_impl<2, true>(nl, position, 4, n, tidx, depth, nbr_count, occupancy, error_code,
+                             reference_position, 4, rebuild_flag, workspace, workspace_bytes, st,
+                             true, true);
+}
+
 }  // namespace jmd
 
 using namespace jmd;

@@ -155,3 +155,12 @@ int graph_launch_cached(const std::string& key,
                         const std::function<int(cudaStream_t, cudaStream_t)>& enq,
                         cudaStream_t st);
 }  // namespace jmd
+
+namespace jmd {
+// Tiled Dense build reusing the bins of a jmd_sort_by_cell just run on the
+// same positions and workspace (nlist.cu).
+int build_tiled_after_sort(const jmd_nlist* nl, const float* position, int64_t n, int32_t* tidx,
+                           int64_t depth, int32_t* nbr_count, int64_t* occupancy,
+                           uint8_t* error_code, float* reference_position, int32_t* rebuild_flag,
+                           void* workspace, size_t workspace_bytes, cudaStream_t st);
+}  // namespace jmd

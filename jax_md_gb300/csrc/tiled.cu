@@ -45,7 +45,7 @@ struct TArgs {
 __device__ __forceinline__ int spc2(int s, int nsp) { return s < 0 ? 0 : (s >= nsp ? nsp - 1 : s); }
 
 template <int DIM, int KIND, bool SPECIES, int MODE>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 8)
 k_tiled(TArgs a, const __grid_constant__ PairTable tab) {
   __shared__ PairCoef sc[SPECIES ? JMD_MAX_SPECIES * JMD_MAX_SPECIES : 1];
   if (SPECIES) {
