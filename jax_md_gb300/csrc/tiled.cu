@@ -12,9 +12,9 @@
 //
 // One thread owns one atom: it loads four column entries, issues their four
 // position gathers back to back (evict-last), and evaluates them as two packed
-// FP32x2 pairs.  No cross-lane reduction is needed.  The momentum and
-// reference rows the epilogue needs are loaded before the neighbour loop, so
-// their latency overlaps the gathers.
+// FP32x2 pairs.  No cross-lane reduction is needed.  The kernel is capped
+// at 56 registers (9 CTAs of 128 threads per SM): it is bound by gather
+// latency, so resident warps matter more than prefetched epilogue rows.
 #include "dense.cuh"
 
 namespace jmd {
@@ -45,7 +45,7 @@ struct TArgs {
 __device__ __forceinline__ int spc2(int s, int nsp) { return s < 0 ? 0 : (s >= nsp ? nsp - 1 : s); }
 
 template <int DIM, int KIND, bool SPECIES, int MODE>
-__global__ void __launch_bounds__(128, 8)
+__global__ void __launch_bounds__(128, 9)
 k_tiled(TArgs a, const __grid_constant__ PairTable tab) {
   __shared__ PairCoef sc[SPECIES ? JMD_MAX_SPECIES * JMD_MAX_SPECIES : 1];
   if (SPECIES) {
@@ -56,8 +56,6 @@ k_tiled(TArgs a, const __grid_constant__ PairTable tab) {
   if (i >= a.n) return;
   const float4 xi = __ldg(a.x + i);
   float4 q = make_float4(0.f, 0.f, 0.f, 0.f), rf = q;
-  if (MODE == T_STEP || MODE == T_KICK) q = a.p[i];
-  if (MODE == T_STEP && a.ref) rf = __ldg(a.ref + i);
   const int c = min(__ldg(a.cnt + i), a.width);
   const int32_t* col = a.tidx + (int64_t)(i >> 5) * a.depth * 32 + (i & 31);
   const int si = SPECIES ? spc2(__ldg(a.species + i), tab.nsp) : 0;
@@ -122,6 +120,10 @@ k_tiled(TArgs a, const __grid_constant__ PairTable tab) {
     if (k0 + 2 < c) pair2(j[2], j[3], b[2], b[3]);
   }
   const float fx = -(ax.x + ax.y), fy = -(ay.x + ay.y), fz = DIM == 3 ? -(az.x + az.y) : 0.f;
+  // epilogue rows are loaded after the loop: keeping them live through it
+  // would cost the registers of a ninth resident CTA
+  if (MODE == T_STEP || MODE == T_KICK) q = a.p[i];
+  if (MODE == T_STEP && a.ref) rf = __ldg(a.ref + i);
   if (MODE == T_FORCE || MODE == T_KICK) a.f[i] = make_float4(fx, fy, fz, 0.f);
   const float h = 0.5f * a.dt;
   if (MODE == T_KICK) {
