@@ -458,6 +458,27 @@ int jmd_nve_run_sorted(const jmd_nve_system* sys, const jmd_sorted_state* sorted
 /* Drops every cached graph of the engine. */
 int jmd_engine_clear_cache(void);
 
+/* Nose-Hoover chain of an NVT run: the chain constants, its device state
+ * (66 doubles, as jmd_nhc_half_step), one double of scratch for the momentum
+ * scale and a reduction workspace of jmd_reduce_workspace_bytes(n) bytes. */
+typedef struct {
+  jmd_nhc chain;
+  double* chain_state;
+  double* p_scale;
+  void* reduce_workspace;
+  size_t reduce_workspace_bytes;
+} jmd_nvt;
+
+/* n_steps of simulate.nvt_nose_hoover's apply_fn (simulate.py:639-669) on the
+ * device, each step: chain half step (with update_mass) -> kick + drift with
+ * the chain's momentum scale -> skin-gated rebuild -> force + kick -> kinetic
+ * energy -> chain half step -> momentum scale.  As jmd_nve_run /
+ * jmd_nve_run_sorted otherwise (the sorted form needs a scalar mass). */
+int jmd_nvt_run(const jmd_nve_system* sys, const jmd_nvt* nvt, int64_t n_steps,
+                int32_t use_graph, void* stream);
+int jmd_nvt_run_sorted(const jmd_nve_system* sys, const jmd_sorted_state* sorted,
+                       const jmd_nvt* nvt, int64_t n_steps, int32_t use_graph, void* stream);
+
 /* ------------------------------------------------------ engine adjoint -- */
 
 /* jmd_nve_run with the positions recorded: `trajectory` (optional) holds

@@ -72,6 +72,11 @@ class SortedState(C.Structure):
                 ('workspace_bytes', C.c_size_t)]
 
 
+class Nvt(C.Structure):
+    _fields_ = [('chain', Nhc), ('chain_state', C.c_void_p), ('p_scale', C.c_void_p),
+                ('reduce_workspace', C.c_void_p), ('reduce_workspace_bytes', C.c_size_t)]
+
+
 class Batch(C.Structure):
     _fields_ = [('dim', C.c_int32), ('n_systems', C.c_int32), ('n_atoms', C.c_int64),
                 ('total_cells', C.c_int32), ('max_cells', C.c_int32),
@@ -149,6 +154,9 @@ SIGNATURES = {
                                            P, I64, I64, P, F32, P, F32, P, P]),
     'jmd_pair_force_vjp': (C.c_int, [C.POINTER(Pair), C.POINTER(Space), P, I64, P, I64, P, I64,
                                      I64, P, P, I64, F32, P, I64, P, P, P]),
+    'jmd_nvt_run': (C.c_int, [C.POINTER(NveSystem), C.POINTER(Nvt), I64, I32, P]),
+    'jmd_nvt_run_sorted': (C.c_int, [C.POINTER(NveSystem), C.POINTER(SortedState), C.POINTER(Nvt),
+                                     I64, I32, P]),
     'jmd_nve_run_recorded': (C.c_int, [C.POINTER(NveSystem), P, I64, I32, I32, P]),
     'jmd_nve_adjoint_segment': (C.c_int, [C.POINTER(NveSystem), P, I64, I32, I32, P, P, P, P, I32,
                                           P]),

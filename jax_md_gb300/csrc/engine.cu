@@ -168,6 +168,58 @@ int enqueue_run(const jmd_nve_system& s, int64_t steps, bool graphed, cudaStream
   return JMD_OK;
 }
 
+// One NVT step on float4 rows x (in place), momentum p, force f:
+// chain half step (update_mass) -> kick + drift scaled by the chain ->
+// gate(x) -> force + kick -> kinetic energy -> chain half step -> scale.
+template <typename Gate, typename ForceKick>
+int nvt_step(const jmd_nve_system& s, const jmd_nvt& v, float* x, float* p, float* f,
+             const float* mass, float* ref, int32_t* flag, bool always, Gate gate,
+             ForceKick force_kick, cudaStream_t st) {
+  int rc = jmd_nhc_half_step(&v.chain, v.chain_state, nullptr, 1, v.p_scale, st);
+  if (rc) return rc;
+  rc = jmd_verlet_kick_drift(x, 4, p, 4, f, 4, mass, s.mass_scalar, s.n, &s.space, s.dt, v.p_scale,
+                             always ? nullptr : ref, 4, s.threshold_sq, always ? nullptr : flag, st);
+  if (rc) return rc;
+  if ((rc = gate(x))) return rc;
+  if ((rc = force_kick(x))) return rc;
+  rc = jmd_kinetic_energy(p, 4, mass, s.mass_scalar, s.n, s.space.dim, v.chain_state + 64,
+                          v.reduce_workspace, v.reduce_workspace_bytes, st);
+  if (rc) return rc;
+  rc = jmd_nhc_half_step(&v.chain, v.chain_state, nullptr, 0, v.p_scale, st);
+  if (rc) return rc;
+  return jmd_scale_momentum(p, 4, s.n, s.space.dim, v.p_scale, st);
+}
+
+int enqueue_nvt(const jmd_nve_system& s, const jmd_nvt& v, int64_t steps, bool graphed,
+                cudaStream_t st, cudaStream_t body_st) {
+  const bool always = s.threshold_sq < 0.f;
+  auto gate = [&](const float* x) -> int {
+    if (always) return rebuild(s, x, false, st);
+    if (graphed)
+      return conditional(s.rebuild_flag, [&](cudaStream_t b) { return rebuild(s, x, true, b); }, st,
+                         body_st);
+    return rebuild(s, x, true, st);
+  };
+  int rc;
+  if (!always) {
+    rc = jmd_skin_check(s.position, 4, s.reference_position, 4, s.n, &s.space, s.threshold_sq,
+                        s.rebuild_flag, st);
+    if (rc) return rc;
+  }
+  if ((rc = gate(s.position))) return rc;
+  const int64_t width = s.nlist.max_occupancy;
+  auto force_kick = [&](const float* x) -> int {
+    return jmd_force_kick(&s.pair, &s.space, x, s.force, s.momentum, s.species, s.n, s.idx,
+                          s.idx_ld, width, s.nbr_count, s.dt, st);
+  };
+  for (int64_t k = 0; k < steps; ++k) {
+    rc = nvt_step(s, v, s.position, s.momentum, s.force, s.mass, s.reference_position,
+                  s.rebuild_flag, always, gate, force_kick, st);
+    if (rc) return rc;
+  }
+  return JMD_OK;
+}
+
 // Reverse pass of velocity Verlet over positions recorded by enqueue_run's
 // trajectory slots 0..steps (see jmd_nve_adjoint_segment).  The list is
 // rebuilt at the first position visited and then maintained by the skin test
@@ -252,7 +304,8 @@ int validate_sorted(const jmd_nve_system& s, const jmd_sorted_state& z) {
 }
 
 int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64_t steps,
-                       bool graphed, cudaStream_t st, cudaStream_t body_st) {
+                       bool graphed, cudaStream_t st, cudaStream_t body_st,
+                       const jmd_nvt* nvt = nullptr) {
   const bool always = s.threshold_sq < 0.f;
   const int n = (int)s.n;
   const unsigned gr = (unsigned)ceil_div(n, 256);
@@ -284,27 +337,39 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
                                   z.error_code);
   JMD_CUDA(cudaGetLastError());
   if ((rc = rebuild_at(z.position_a, false, true, st))) return rc;
-  rc = jmd_verlet_kick_drift(z.position_a, 4, z.momentum, 4, z.force, 4, nullptr, s.mass_scalar,
-                             s.n, &s.space, s.dt, nullptr,
-                             always ? nullptr : z.reference_position, 4, s.threshold_sq,
-                             always ? nullptr : z.rebuild_flag, st);
-  if (rc) return rc;
   float* cur = z.position_a;
   float* nxt = z.position_b;
   const int64_t width = s.nlist.max_occupancy;
-  for (int64_t k = 1; k < steps; ++k) {
-    if ((rc = gate(cur))) return rc;
-    rc = jmd_nve_fused_step_tiled(&s.pair, &s.space, cur, nxt, z.momentum, s.mass_scalar,
-                                  z.species, s.n, z.idx, z.idx_ld, width, z.nbr_count, s.dt,
-                                  always ? nullptr : z.reference_position, s.threshold_sq,
-                                  always ? nullptr : z.rebuild_flag, st);
+  if (nvt) {
+    auto force_kick = [&](const float* x) -> int {
+      return jmd_force_kick_tiled(&s.pair, &s.space, x, z.force, z.momentum, z.species, s.n,
+                                  z.idx, z.idx_ld, width, z.nbr_count, s.dt, st);
+    };
+    for (int64_t k = 0; k < steps; ++k) {
+      rc = nvt_step(s, *nvt, cur, z.momentum, z.force, nullptr, z.reference_position,
+                    z.rebuild_flag, always, gate, force_kick, st);
+      if (rc) return rc;
+    }
+  } else {
+    rc = jmd_verlet_kick_drift(z.position_a, 4, z.momentum, 4, z.force, 4, nullptr, s.mass_scalar,
+                               s.n, &s.space, s.dt, nullptr,
+                               always ? nullptr : z.reference_position, 4, s.threshold_sq,
+                               always ? nullptr : z.rebuild_flag, st);
     if (rc) return rc;
-    std::swap(cur, nxt);
+    for (int64_t k = 1; k < steps; ++k) {
+      if ((rc = gate(cur))) return rc;
+      rc = jmd_nve_fused_step_tiled(&s.pair, &s.space, cur, nxt, z.momentum, s.mass_scalar,
+                                    z.species, s.n, z.idx, z.idx_ld, width, z.nbr_count, s.dt,
+                                    always ? nullptr : z.reference_position, s.threshold_sq,
+                                    always ? nullptr : z.rebuild_flag, st);
+      if (rc) return rc;
+      std::swap(cur, nxt);
+    }
+    if ((rc = gate(cur))) return rc;
+    rc = jmd_force_kick_tiled(&s.pair, &s.space, cur, z.force, z.momentum, z.species, s.n, z.idx,
+                              z.idx_ld, width, z.nbr_count, s.dt, st);
+    if (rc) return rc;
   }
-  if ((rc = gate(cur))) return rc;
-  rc = jmd_force_kick_tiled(&s.pair, &s.space, cur, z.force, z.momentum, z.species, s.n, z.idx,
-                            z.idx_ld, width, z.nbr_count, s.dt, st);
-  if (rc) return rc;
   k_store_user<<<gr, 256, 0, st>>>(n, z.perm, reinterpret_cast<const float4*>(cur),
                                    reinterpret_cast<const float4*>(z.momentum),
                                    reinterpret_cast<const float4*>(z.force),
@@ -504,6 +569,64 @@ int jmd_nve_adjoint_segment(const jmd_nve_system* sys, const float* trajectory, 
   return launch_graphed(key, [&](cudaStream_t cs, cudaStream_t bs) {
     return enqueue_adjoint(*sys, trajectory, n_steps, closing != 0, opening != 0, xbar, pbar,
                            record_scratch, grad_params, true, cs, bs);
+  }, st);
+}
+
+int validate_nvt(const jmd_nvt* v) {
+  JMD_REQUIRE(v != nullptr, "nvt is null");
+  JMD_REQUIRE(v->chain_state && v->p_scale && v->reduce_workspace, "null buffer in jmd_nvt");
+  JMD_REQUIRE(v->reduce_workspace_bytes >= jmd_reduce_workspace_bytes(0),
+              "reduce workspace too small");
+  return JMD_OK;
+}
+
+int jmd_nvt_run(const jmd_nve_system* sys, const jmd_nvt* nvt, int64_t n_steps, int32_t use_graph,
+                void* stream) {
+  JMD_REQUIRE(sys != nullptr, "system is null");
+  int e = validate_sys(*sys);
+  if (e) return e;
+  if ((e = validate_nvt(nvt))) return e;
+  JMD_REQUIRE(n_steps >= 0, "n_steps must be >= 0");
+  if (n_steps == 0) return JMD_OK;
+  cudaStream_t st = as_stream(stream);
+  cudaStreamCaptureStatus cap;
+  JMD_CUDA(cudaStreamIsCapturing(st, &cap));
+  if (!use_graph || cap != cudaStreamCaptureStatusNone) {
+    int rc = enqueue_nvt(*sys, *nvt, n_steps, false, st, nullptr);
+    return rc ? rc : check_launch("jmd_nvt_run");
+  }
+  int device;
+  JMD_CUDA(cudaGetDevice(&device));
+  std::string key = "nvt" + plan_key(*sys, n_steps, device);
+  key.append(reinterpret_cast<const char*>(nvt), sizeof(*nvt));
+  return launch_graphed(key, [&](cudaStream_t cs, cudaStream_t bs) {
+    return enqueue_nvt(*sys, *nvt, n_steps, true, cs, bs);
+  }, st);
+}
+
+int jmd_nvt_run_sorted(const jmd_nve_system* sys, const jmd_sorted_state* sorted,
+                       const jmd_nvt* nvt, int64_t n_steps, int32_t use_graph, void* stream) {
+  JMD_REQUIRE(sys != nullptr && sorted != nullptr, "null argument");
+  int e = validate_sys(*sys);
+  if (e) return e;
+  if ((e = validate_sorted(*sys, *sorted))) return e;
+  if ((e = validate_nvt(nvt))) return e;
+  JMD_REQUIRE(n_steps >= 0, "n_steps must be >= 0");
+  if (n_steps == 0) return JMD_OK;
+  cudaStream_t st = as_stream(stream);
+  cudaStreamCaptureStatus cap;
+  JMD_CUDA(cudaStreamIsCapturing(st, &cap));
+  if (!use_graph || cap != cudaStreamCaptureStatusNone) {
+    int rc = enqueue_run_sorted(*sys, *sorted, n_steps, false, st, nullptr, nvt);
+    return rc ? rc : check_launch("jmd_nvt_run_sorted");
+  }
+  int device;
+  JMD_CUDA(cudaGetDevice(&device));
+  std::string key = "nvtsorted" + plan_key(*sys, n_steps, device);
+  key.append(reinterpret_cast<const char*>(sorted), sizeof(*sorted));
+  key.append(reinterpret_cast<const char*>(nvt), sizeof(*nvt));
+  return launch_graphed(key, [&](cudaStream_t cs, cudaStream_t bs) {
+    return enqueue_run_sorted(*sys, *sorted, n_steps, true, cs, bs, nvt);
   }, st);
 }
 

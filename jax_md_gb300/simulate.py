@@ -342,7 +342,34 @@ def nvt_nose_hoover(energy_or_force_fn, shift_fn, dt, kT, chain_length: int = 5,
 
     init_fn.stepper = st
     apply_fn.stepper = st
+    apply_fn.chain_fns = chain_fns
     return init_fn, apply_fn
+
+
+def _nvt_struct(chain_fns: '_Chain', state: 'NVTNoseHooverState') -> N.Nvt:
+    """jmd_nvt of a state: chain constants, its device buffer, a persistent
+    scale scratch and a reduction workspace (kept on the state so a replayed
+    graph sees the same pointers)."""
+    chain = state.chain
+    dev = state.position.device
+    scratch = getattr(state, '_nvt_scratch', None)
+    n = state.position.shape[0]
+    if scratch is None:
+        ws = torch.empty(N.lib().jmd_reduce_workspace_bytes(n), dtype=torch.uint8, device=dev)
+        scratch = (torch.ones((), dtype=torch.float64, device=dev), ws)
+        object.__setattr__(state, '_nvt_scratch', scratch)
+    v = N.Nvt()
+    v.chain.chain_length = chain_fns.M1
+    v.chain.chain_steps = chain_fns.chain_steps
+    v.chain.sy_steps = chain_fns.sy_steps
+    v.chain.dof = chain.degrees_of_freedom
+    v.chain.dt = chain_fns.dt
+    v.chain.tau = chain.tau
+    v.chain_state = chain.buffer.data_ptr()
+    v.p_scale = scratch[0].data_ptr()
+    v.reduce_workspace = scratch[1].data_ptr()
+    v.reduce_workspace_bytes = scratch[1].numel()
+    return v
 
 
 def nvt_nose_hoover_invariant(energy_fn, state: NVTNoseHooverState, kT, **kwargs):
@@ -467,9 +494,13 @@ def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bo
     caller's list is rebuilt, in the reference's entry order, at the
     positions of the last rebuild.  Returns (state, neighbor)."""
     st = apply_fn.stepper
-    if not isinstance(state, NVEState):
-        raise NotImplementedError('run() drives NVE states')
+    nvt = isinstance(state, NVTNoseHooverState)
+    if not (isinstance(state, NVEState) or nvt):
+        raise NotImplementedError('run() drives NVE and Nose-Hoover NVT states')
+    if nvt and getattr(apply_fn, 'chain_fns', None) is None:
+        raise ValueError('an NVT state needs the apply_fn of simulate.nvt_nose_hoover')
     snapshot = state.copy() if neighbor_fn is not None else None
+    chain0 = state.chain.buffer.clone() if (nvt and neighbor_fn is not None) else None
     for attempt in range(max_reallocations + 1):
         alt = getattr(state, '_alt', None)
         if alt is None or alt.shape[0] != state.position.shape[0]:
@@ -480,12 +511,22 @@ def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bo
         use_sort = sort
         if use_sort is None:
             use_sort = (not isinstance(state.mass, torch.Tensor)) and bool(sysd.nlist.use_cell_list)
+        v = _nvt_struct(apply_fn.chain_fns, state) if nvt else None
         if use_sort:
             sb = _sorted_buffers(state, neighbor, species)
             z = sb.struct()
-            N.check(N.lib().jmd_nve_run_sorted(ctypes.byref(sysd), ctypes.byref(z), int(n_steps),
-                                               1 if use_graph else 0, N.stream_ptr()),
-                    'nve_run_sorted')
+            if nvt:
+                N.check(N.lib().jmd_nvt_run_sorted(ctypes.byref(sysd), ctypes.byref(z),
+                                                   ctypes.byref(v), int(n_steps),
+                                                   1 if use_graph else 0, N.stream_ptr()),
+                        'nvt_run_sorted')
+            else:
+                N.check(N.lib().jmd_nve_run_sorted(ctypes.byref(sysd), ctypes.byref(z),
+                                                   int(n_steps), 1 if use_graph else 0,
+                                                   N.stream_ptr()), 'nve_run_sorted')
+        elif nvt:
+            N.check(N.lib().jmd_nvt_run(ctypes.byref(sysd), ctypes.byref(v), int(n_steps),
+                                        1 if use_graph else 0, N.stream_ptr()), 'nvt_run')
         else:
             N.check(N.lib().jmd_nve_run(ctypes.byref(sysd), int(n_steps), 1 if use_graph else 0,
                                         N.stream_ptr()), 'nve_run')
@@ -496,6 +537,8 @@ def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bo
         state.position.copy_(snapshot.position)
         state.momentum.copy_(snapshot.momentum)
         state.force.copy_(snapshot.force)
+        if chain0 is not None:
+            state.chain.buffer.copy_(chain0)
         extra = (attempt + 1) * max(1, neighbor.max_occupancy // 8)
         neighbor = neighbor_fn.allocate(state.position, extra_capacity=extra)
     raise RuntimeError('neighbour list kept overflowing after re-allocation')
