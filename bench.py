@@ -125,6 +125,35 @@ def _events(dev):
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
+def nvt_section(dev, efn, nfn, shift, R, P, steps, warmup):
+    """The NVT half of the large workload: Nose-Hoover (chain 5, tau = 100 dt,
+    kT = 0.722) on the same N = 864,000 system, K steps as one graph launch."""
+    import torch
+    from jax_md_gb300 import simulate
+    Rt = torch.tensor(R, device=dev)
+    nb = nfn.allocate(Rt)
+    init, apply = simulate.nvt_nose_hoover(efn, shift, DT, KT)
+    st = init(0, Rt, momenta=torch.tensor(P, device=dev), neighbor=nb)
+    simulate.run(apply, st, nb, max(3, warmup))
+    simulate.run(apply, st, nb, steps)          # records the graph of K steps
+    H0 = float(simulate.nvt_nose_hoover_invariant(efn, st, KT, neighbor=nb.update(st.position)))
+    cur = torch.cuda.current_stream(dev)
+    e0, e1 = _events(dev)
+    torch.cuda.synchronize()
+    e0.record(cur)
+    simulate.run(apply, st, nb, steps)
+    e1.record(cur)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    n = len(R)
+    H1 = float(simulate.nvt_nose_hoover_invariant(efn, st, KT, neighbor=nb.update(st.position)))
+    T = float((st.momentum.double() ** 2).sum() / (3 * n))
+    return {'workload': f'Nose-Hoover NVT, same system, chain 5, tau=100 dt, kT={KT}',
+            'steps': steps, 'atom_steps_per_s': n * steps / (ms / 1e3),
+            'ms_per_step': ms / steps, 'invariant_drift_per_atom': (H1 - H0) / n,
+            'temperature': T, 'overflow': bool(nb.did_buffer_overflow)}
+
+
 def batched_section(dev, n_sys=512, fire_steps=200, nve_steps=200, seed=0):
     """512 uneven 2D bidisperse soft-sphere systems (N ~ U[64, 4096], phi
     0.84, sigma_ij = (d_i + d_j) / 2 with d in {1.0, 1.4}): a fixed number of
@@ -503,6 +532,7 @@ def main():
         'clocks': clk.summary(),
     }
     if rank == 0 and not args.no_extras:
+        line['nvt'] = nvt_section(dev, efn, nfn, shift, R, P, args.steps, args.warmup)
         line['batched'] = batched_section(dev)
         line['adjoint'] = adjoint_section(dev)
     if rank == 0 and not args.no_cpu:
