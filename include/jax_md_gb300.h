@@ -626,6 +626,25 @@ int jmd_batch_nve_run(const jmd_batch_system* sys, int64_t n_steps, int32_t use_
 int jmd_batch_fire_run(const jmd_batch_system* sys, const jmd_fire_params* fp,
                        int64_t n_steps, int32_t use_graph, void* stream);
 
+/* Adjoint of a batched NVE run: the batched forms of jmd_nve_run_recorded and
+ * jmd_nve_adjoint_segment (same slot layout, same recurrences; each atom
+ * uses its system's box; grad_params bins are summed over all systems, the
+ * gradient with respect to parameters shared by every system). */
+int jmd_batch_nve_run_recorded(const jmd_batch_system* sys, float* trajectory,
+                               int64_t n_steps, int32_t force_rebuild, int32_t use_graph,
+                               void* stream);
+int jmd_batch_nve_adjoint_segment(const jmd_batch_system* sys, const float* trajectory,
+                                  int64_t n_steps, int32_t closing, int32_t opening,
+                                  float* xbar, float* pbar, float* record_scratch,
+                                  double* grad_params, int32_t use_graph, void* stream);
+
+/* grad_params[130] += sum_b system_weight[b] dE_b/d(sigma, epsilon, cutoff
+ * scale), E_b the potential energy of system b (bins of jmd_pair_force_vjp). */
+int jmd_batch_energy_param_grad(const jmd_pair* pair, const jmd_batch* batch,
+                                const jmd_batch_nlist* nl, const float* position,
+                                const int32_t* species, const double* system_weight,
+                                double* grad_params, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -170,6 +170,11 @@ SIGNATURES = {
     'jmd_batch_fire_init': (C.c_int, [C.POINTER(BatchSystem), C.POINTER(FireParams), P]),
     'jmd_batch_nve_run': (C.c_int, [C.POINTER(BatchSystem), I64, I32, P]),
     'jmd_batch_fire_run': (C.c_int, [C.POINTER(BatchSystem), C.POINTER(FireParams), I64, I32, P]),
+    'jmd_batch_nve_run_recorded': (C.c_int, [C.POINTER(BatchSystem), P, I64, I32, I32, P]),
+    'jmd_batch_nve_adjoint_segment': (C.c_int, [C.POINTER(BatchSystem), P, I64, I32, I32, P, P, P,
+                                                P, I32, P]),
+    'jmd_batch_energy_param_grad': (C.c_int, [C.POINTER(Pair), C.POINTER(Batch),
+                                              C.POINTER(BatchNList), P, P, P, P, P]),
     'jmd_fire_kick_drift': (C.c_int, [P, P, P, P, F32, I64, C.POINTER(Space), P, P]),
     'jmd_fire_workspace_bytes': (SZ, [I64]),
     'jmd_fire_update': (C.c_int, [P, P, I64, I32, P, F32, F32, F32, F32, F32, F32, P, SZ, P]),

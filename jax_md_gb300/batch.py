@@ -28,6 +28,7 @@ import torch
 
 from . import _native as N
 from . import smap
+from .smap import _bins_to_grads, _param_tensor
 
 
 class Batch:
@@ -281,23 +282,43 @@ class BatchPairEnergy:
                                       '*_neighbor_list energy functions')
         self.energy_fn = energy_fn
 
-    def pair(self, batch: Batch):
-        dyn = {'species': batch.species} if batch.species is not None else {}
+    def pair(self, batch: Batch, **dyn):
+        """(species, jmd_pair) with the batch's species and any sigma /
+        epsilon / alpha given as keywords (scalars or species matrices)."""
+        dyn = dict(dyn)
+        if batch.species is not None:
+            dyn['species'] = batch.species
         species, pair = self.energy_fn._resolve(batch.R, dyn)
         return species, pair
 
-    def forces(self, batch: Batch, nbrs: BatchNeighborList, out=None, energies=None):
+    def forces(self, batch: Batch, nbrs: BatchNeighborList, out=None, energies=None,
+               position=None, **dyn):
         """Forces of every system (``[N, 4]`` float4 rows) and, with
-        ``energies`` (f64 ``[B]``), the per-system potential energies."""
-        species, pair = self.pair(batch)
+        ``energies`` (f64 ``[B]``), the per-system potential energies, at
+        ``position`` (float4 rows; default the batch's)."""
+        species, pair = self.pair(batch, **dyn)
+        x = batch.position if position is None else position
         if out is None:
             out = torch.empty((batch.n, 4), dtype=torch.float32, device=batch.device)
         N.check(N.lib().jmd_batch_pair_forces(ctypes.byref(pair), ctypes.byref(nbrs.grid.struct),
-                                              ctypes.byref(nbrs.struct()),
-                                              batch.position.data_ptr(), N.ptr(species),
-                                              out.data_ptr(), N.ptr(energies), N.stream_ptr()),
-                'batch_pair_forces')
+                                              ctypes.byref(nbrs.struct()), x.data_ptr(),
+                                              N.ptr(species), out.data_ptr(), N.ptr(energies),
+                                              N.stream_ptr()), 'batch_pair_forces')
         return out
+
+    def energy_fn_autograd(self, batch: Batch, nbrs: BatchNeighborList):
+        """``E(R, sigma=None, epsilon=None) -> [B]`` per-system potential
+        energies, differentiable with respect to R (``[N, dim]``) and to sigma /
+        epsilon tensors that require grad (shared by every system)."""
+        def fn(R, sigma=None, epsilon=None):
+            dyn = {}
+            if sigma is not None:
+                dyn['sigma'] = sigma
+            if epsilon is not None:
+                dyn['epsilon'] = epsilon
+            return _BatchEnergy.apply(R, _param_tensor(sigma), _param_tensor(epsilon),
+                                      (self, batch, nbrs, dyn))
+        return fn
 
     def energies(self, batch: Batch, nbrs: BatchNeighborList) -> torch.Tensor:
         e = torch.empty(batch.n_systems, dtype=torch.float64, device=batch.device)
@@ -415,3 +436,170 @@ class BatchRunner:
 
     def potential(self):
         return self.energy.energies(self.batch, self.nbrs)
+
+
+def _system_struct(nbrs: BatchNeighborList, pair, species, x, p, f, mass, dt, threshold_sq):
+    s = N.BatchSystem()
+    s.batch = nbrs.grid.struct
+    s.nlist = nbrs.struct()
+    s.pair = pair
+    s.species = N.ptr(species)
+    s.position, s.momentum, s.force = x.data_ptr(), p.data_ptr(), f.data_ptr()
+    s.mass = None
+    s.mass_scalar = float(mass)
+    s.dt = float(np.float32(dt))
+    s.threshold_sq = threshold_sq
+    return s
+
+
+class _BatchEnergy(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, R, sigma, epsilon, cfg):
+        energy, batch, nbrs, dyn = cfg
+        dim = batch.dim
+        x = torch.zeros((batch.n, 4), dtype=torch.float32, device=R.device)
+        x[:, :dim] = R.detach()
+        e = torch.empty(batch.n_systems, dtype=torch.float64, device=R.device)
+        F = energy.forces(batch, nbrs, energies=e, position=x, **dyn)
+        ctx.save_for_backward(sigma if sigma is not None else torch.empty(0),
+                              epsilon if epsilon is not None else torch.empty(0))
+        ctx.has = (sigma is not None, epsilon is not None)
+        ctx.cfg, ctx.x, ctx.F = cfg, x, F
+        return e
+
+    @staticmethod
+    def backward(ctx, gE):
+        energy, batch, nbrs, dyn = ctx.cfg
+        sigma, epsilon = ctx.saved_tensors
+        sigma = sigma if ctx.has[0] else None
+        epsilon = epsilon if ctx.has[1] else None
+        w = gE.to(torch.float64).contiguous()
+        gR = -ctx.F[:, :batch.dim] * w[batch.atom_sys.long()].to(torch.float32)[:, None]
+        gs = ge = None
+        if sigma is not None or epsilon is not None:
+            species, pair = energy.pair(batch, **dyn)
+            bins = torch.zeros(130, dtype=torch.float64, device=gE.device)
+            N.check(N.lib().jmd_batch_energy_param_grad(
+                ctypes.byref(pair), ctypes.byref(nbrs.grid.struct), ctypes.byref(nbrs.struct()),
+                ctx.x.data_ptr(), N.ptr(species), w.data_ptr(), bins.data_ptr(), N.stream_ptr()),
+                'batch_energy_param_grad')
+            gs, ge = _bins_to_grads(bins, None, sigma, epsilon)
+        return gR, gs, ge, None
+
+
+class _BatchTrajectoryFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, R0, P0, sigma, epsilon, cfg):
+        tr, dyn = cfg
+        bt, nb, dim = tr.batch, tr.nbrs, tr.batch.dim
+        buf = tr.buffers()
+        buf['x'].zero_()
+        buf['p'].zero_()
+        buf['x'][:, :dim] = torch.remainder(R0.detach(), bt.box[bt.atom_sys.long(), :dim])
+        buf['p'][:, :dim] = P0.detach()
+        tr.neighbor_fns._build(nb, buf['x'])
+        species, pair = tr.energy.pair(bt, **dyn)
+        tr.energy.forces(bt, nb, out=buf['f'], position=buf['x'], **dyn)
+        sysd = _system_struct(nb, pair, species, buf['x'], buf['p'], buf['f'], tr.mass, tr.dt,
+                              tr.neighbor_fns.threshold_sq)
+        L = N.lib()
+        segs = tr.segments
+        for c, (s0, s1) in enumerate(segs):
+            last = c == len(segs) - 1
+            if not last:
+                buf['ck_x'][c].copy_(buf['x'])
+                buf['ck_p'][c].copy_(buf['p'])
+                buf['ck_f'][c].copy_(buf['f'])
+            N.check(L.jmd_batch_nve_run_recorded(ctypes.byref(sysd),
+                                                 buf['traj'].data_ptr() if last else None,
+                                                 s1 - s0, 1, 1, N.stream_ptr()),
+                    'batch_nve_run_recorded')
+        if nb.did_buffer_overflow:
+            raise RuntimeError('a batched neighbour list overflowed during the trajectory; '
+                               'allocate it with more capacity')
+        ctx.cfg = (tr, sysd, species, buf)
+        ctx.has = (sigma is not None, epsilon is not None)
+        ctx.save_for_backward(sigma if sigma is not None else torch.empty(0),
+                              epsilon if epsilon is not None else torch.empty(0))
+        return buf['x'][:, :dim].clone(), buf['p'][:, :dim].clone()
+
+    @staticmethod
+    def backward(ctx, gx, gp):
+        tr, sysd, species, buf = ctx.cfg
+        sigma, epsilon = ctx.saved_tensors
+        sigma = sigma if ctx.has[0] else None
+        epsilon = epsilon if ctx.has[1] else None
+        dim = tr.batch.dim
+        buf['xbar'].zero_()
+        buf['pbar'].zero_()
+        if gx is not None:
+            buf['xbar'][:, :dim] = gx
+        if gp is not None:
+            buf['pbar'][:, :dim] = gp
+        want = sigma is not None or epsilon is not None
+        bins = torch.zeros(130, dtype=torch.float64, device=buf['x'].device)
+        L = N.lib()
+        segs = tr.segments
+        for c in reversed(range(len(segs))):
+            s0, s1 = segs[c]
+            last = c == len(segs) - 1
+            if not last:
+                buf['x'].copy_(buf['ck_x'][c])
+                buf['p'].copy_(buf['ck_p'][c])
+                buf['f'].copy_(buf['ck_f'][c])
+                N.check(L.jmd_batch_nve_run_recorded(ctypes.byref(sysd), buf['traj'].data_ptr(),
+                                                     s1 - s0, 1, 1, N.stream_ptr()),
+                        'batch_nve_run_recorded')
+            N.check(L.jmd_batch_nve_adjoint_segment(
+                ctypes.byref(sysd), buf['traj'].data_ptr(), s1 - s0, 1 if last else 0,
+                1 if c == 0 else 0, buf['xbar'].data_ptr(), buf['pbar'].data_ptr(),
+                buf['rec'].data_ptr(), bins.data_ptr() if want else None, 1, N.stream_ptr()),
+                'batch_nve_adjoint_segment')
+        gs, ge = _bins_to_grads(bins, None, sigma, epsilon) if want else (None, None)
+        return buf['xbar'][:, :dim].clone(), buf['pbar'][:, :dim].clone(), gs, ge, None
+
+
+class BatchTrajectory:
+    """``traj(R0, P0, sigma=None, epsilon=None) -> (x_n, p_n)``: n_steps of NVE
+    of every system of a batch (``[N, dim]`` packed arrays), differentiable with
+    respect to R0, P0 and sigma / epsilon shared by all systems, through the
+    batched reverse Verlet pass (checkpointed every ``checkpoint_every`` steps;
+    None keeps the whole trajectory when it fits a quarter of free memory).
+    ``nbrs`` is rebuilt in place.  Unit mass unless ``mass`` is given."""
+
+    def __init__(self, batch: Batch, neighbor_fns: BatchNeighborListFns, nbrs: BatchNeighborList,
+                 energy: BatchPairEnergy, dt: float, n_steps: int, checkpoint_every=None,
+                 mass: float = 1.0):
+        if int(n_steps) < 1:
+            raise ValueError('n_steps must be >= 1')
+        self.batch, self.neighbor_fns, self.nbrs, self.energy = batch, neighbor_fns, nbrs, energy
+        self.dt, self.n_steps, self.mass = float(dt), int(n_steps), float(mass)
+        n = max(batch.n, 1)
+        if checkpoint_every is None:
+            free, _ = torch.cuda.mem_get_info()
+            k = int(free // 4 // (16 * n)) - 1
+        else:
+            k = int(checkpoint_every)
+        k = max(1, min(k, self.n_steps))
+        self.segments = [(s0, min(s0 + k, self.n_steps)) for s0 in range(0, self.n_steps, k)]
+        self.k = k
+        self._buf = None
+
+    def buffers(self):
+        if self._buf is None:
+            n, dev = max(self.batch.n, 1), self.batch.device
+            f4 = lambda *s: torch.zeros(s + (n, 4), dtype=torch.float32, device=dev)
+            ns = len(self.segments)
+            self._buf = dict(x=f4(), p=f4(), f=f4(), traj=f4(self.k + 1), ck_x=f4(ns), ck_p=f4(ns),
+                             ck_f=f4(ns), xbar=f4(), pbar=f4(),
+                             rec=torch.zeros((2 * n, 4), dtype=torch.float32, device=dev))
+        return self._buf
+
+    def __call__(self, R0, P0, sigma=None, epsilon=None):
+        dyn = {}
+        if sigma is not None:
+            dyn['sigma'] = sigma
+        if epsilon is not None:
+            dyn['epsilon'] = epsilon
+        return _BatchTrajectoryFn.apply(R0, P0, _param_tensor(sigma), _param_tensor(epsilon),
+                                        (self, dyn))

@@ -19,9 +19,11 @@
 //   k_bfinal  error bits and occupancy, clears the rebuild flag.
 #include <algorithm>
 #include <cstring>
+#include <functional>
 #include <string>
+#include <type_traits>
 
-#include "pair.cuh"
+#include "adjoint.cuh"
 
 namespace jmd {
 namespace {
@@ -549,6 +551,187 @@ __global__ void k_bfire_init(int nsys, float* fs, int32_t* done, int32_t* n_done
   done[b] = 0;
 }
 
+// ------------------------------------------------------------ adjoint ----
+// Reverse velocity Verlet over a batch (the single-system form is in
+// adjoint.cu): pack writes (x, q) records with q = pbar + (dt/m) xbar and runs
+// the skin test with each atom's own box; the step accumulates
+// xbar_k += w sum_j J_kj (q_j - q_k) over k's tiled row and, with PARAMS, the
+// shared sigma / epsilon / cutoff-scale bins summed over every system.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_badj_pack(BatchView v, const float4* __restrict__ x,
+                                                   float4* xbar, float4* pbar, const float* mass,
+                                                   float m0, float dt, int kick, float4* rec,
+                                                   const float4* ref, float thr2, int32_t* flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool over = false;
+  if (i < v.n) {
+    const float4 xi = __ldg(x + i);
+    float4 q = pbar[i];
+    if (kick) {
+      const float4 xb = xbar[i];
+      const float c = dt / (mass ? __ldg(mass + i) : m0);
+      q.x = fmaf(c, xb.x, q.x);
+      q.y = fmaf(c, xb.y, q.y);
+      if (DIM == 3) q.z = fmaf(c, xb.z, q.z);
+      pbar[i] = q;
+    }
+    rec[2 * i] = make_float4(xi.x, xi.y, DIM == 3 ? xi.z : 0.f, q.x);
+    rec[2 * i + 1] = make_float4(q.y, DIM == 3 ? q.z : 0.f, 0.f, 0.f);
+    if (ref) {
+      const SysGeo g = sys_geo(v, __ldg(v.atom_sys + i));
+      float dx, dy, dz;
+      bdisp<DIM>(xi, __ldg(ref + i), g, dx, dy, dz);
+      over = dx * dx + dy * dy + (DIM == 3 ? dz * dz : 0.f) > thr2;
+    }
+  }
+  if (ref && __any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+struct BAdjArgs {
+  const float4* rec;        // step: (x, q) records; energy mode: positions in rec[i] (float4 rows)
+  float4* xbar;
+  const int32_t* species;
+  const int32_t* idx;
+  const int32_t* count;
+  int ld;
+  float weight;
+  const double* sys_weight; // energy mode: per-system weight of dE_b/dtheta
+  double* gp;
+  int per_pair;
+};
+
+// MODE 0: reverse step (records, xbar, optional bins); MODE 1: bins of
+// sum_b sys_weight[b] dE_b/dtheta only.
+template <int DIM, int KIND, bool SPECIES, bool PARAMS, int MODE>
+__global__ void __launch_bounds__(128) k_badj_step(BatchView v, BAdjArgs a,
+                                                   const __grid_constant__ PairTable tab,
+                                                   const __grid_constant__ PairTable sig) {
+  constexpr int NB = SPECIES ? JMD_MAX_SPECIES : 1;
+  __shared__ float bins[PARAMS ? kBins : 1];
+  if (PARAMS) {
+    zero_bins(bins);
+    __syncthreads();
+  }
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < v.n;
+  const bool per_pair = a.per_pair != 0;
+  BinAcc<NB> acc;
+  acc.zero();
+  int si = 0;
+  if (active) {
+    const int b = __ldg(v.atom_sys + i);
+    const SysGeo g = sys_geo(v, b);
+    const float ew = MODE == 1 ? (float)__ldg(a.sys_weight + b) : 1.f;
+    const float4 r0 = MODE == 0 ? __ldg(a.rec + 2 * i) : __ldg(a.rec + i);
+    const float4 r1 = MODE == 0 ? __ldg(a.rec + 2 * i + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float qx = r0.w, qy = r1.x, qz = r1.y;
+    si = SPECIES ? min(max(__ldg(a.species + i), 0), tab.nsp - 1) : 0;
+    const int m = __ldg(a.count + i);
+    const int32_t* col = a.idx + (int64_t)(i >> 5) * a.ld * 32 + (i & 31);
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    for (int e = 0; e < m; ++e) {
+      const int j = __ldcs(col + (int64_t)e * 32);
+      const float4 j0 = MODE == 0 ? __ldg(a.rec + 2 * j) : __ldg(a.rec + j);
+      float dx, dy, dz;
+      bdisp<DIM>(r0, j0, g, dx, dy, dz);
+      const float r2 = dx * dx + dy * dy + (DIM == 3 ? dz * dz : 0.f);
+      const int sj = SPECIES ? min(max(__ldg(a.species + j), 0), tab.nsp - 1) : 0;
+      const int bin = si * JMD_MAX_SPECIES + sj;
+      const PairCoef& c = tab.c[SPECIES ? bin : 0];
+      if (!(r2 < c.rc2) || r2 == 0.f) continue;
+      if (MODE == 1) {
+        const float sigma = sig.c[SPECIES ? bin : 0].pad;
+        const PairD q = pair_derivs<KIND>(r2, c, sigma, per_pair ? sigma : sig.pad);
+        const float h = 0.5f * ew;
+        acc.add(sj, h * q.dU_s, h * q.dU_e, KIND == JMD_LJ ? h * q.dU_k : 0.f, per_pair);
+        continue;
+      }
+      const float4 j1 = __ldg(a.rec + 2 * j + 1);
+      float gg, hh;
+      PairD q;
+      if (PARAMS) {
+        const float sigma = sig.c[SPECIES ? bin : 0].pad;
+        q = pair_derivs<KIND>(r2, c, sigma, per_pair ? sigma : sig.pad);
+        gg = q.g;
+        hh = q.hh;
+      } else {
+        float U;
+        pair_eval<KIND, true>(r2, c, U, gg, hh);
+      }
+      const float ex = j0.w - qx, ey = j1.x - qy, ez = DIM == 3 ? j1.y - qz : 0.f;
+      const float tt = dx * ex + dy * ey + dz * ez;
+      const float cdd = (hh - gg) * rcp_nr(r2) * tt;
+      gx = fmaf(gg, ex, fmaf(cdd, dx, gx));
+      gy = fmaf(gg, ey, fmaf(cdd, dy, gy));
+      if (DIM == 3) gz = fmaf(gg, ez, fmaf(cdd, dz, gz));
+      if (PARAMS) {
+        const float ht = 0.5f * tt;
+        acc.add(sj, q.dg_s * ht, q.dg_e * ht, KIND == JMD_LJ ? q.dg_k * ht : 0.f, per_pair);
+      }
+    }
+    if (MODE == 0) {
+      float4 xb = a.xbar[i];
+      xb.x = fmaf(a.weight, gx, xb.x);
+      xb.y = fmaf(a.weight, gy, xb.y);
+      if (DIM == 3) xb.z = fmaf(a.weight, gz, xb.z);
+      a.xbar[i] = xb;
+    }
+  }
+  if (PARAMS) {
+    const int ncol = SPECIES ? tab.nsp : 1;
+    if (SPECIES) {
+      if (active) acc.flush(bins, si, ncol);
+    } else {
+      acc.group_sum(kWarp, 1);
+      if ((threadIdx.x & (kWarp - 1)) == 0) acc.flush(bins, 0, 1);
+    }
+    __syncthreads();
+    publish_bins(bins, a.gp, MODE == 0 ? (double)a.weight : 1.0);
+  }
+}
+
+template <int DIM, int KIND, bool SP>
+void badj_launch3(int mode, bool params, const BatchView& v, const BAdjArgs& a,
+                  const PairTable& t, const PairTable& s, cudaStream_t st) {
+  const unsigned gr = (unsigned)std::max<int64_t>(1, ceil_div(v.n, 128));
+  if (mode == 1) k_badj_step<DIM, KIND, SP, true, 1><<<gr, 128, 0, st>>>(v, a, t, s);
+  else if (params) k_badj_step<DIM, KIND, SP, true, 0><<<gr, 128, 0, st>>>(v, a, t, s);
+  else k_badj_step<DIM, KIND, SP, false, 0><<<gr, 128, 0, st>>>(v, a, t, s);
+}
+
+int badj_launch(int mode, const jmd_pair& pp, const jmd_batch& bt, const jmd_batch_nlist& nl,
+                const float* rec, float* xbar, const int32_t* species, float weight,
+                const double* sys_weight, double* gp, cudaStream_t st) {
+  if (bt.n_atoms <= 0) return JMD_OK;
+  const PairTable t = make_pair_table(pp);
+  const PairTable sg = sigma_table(pp);
+  const BatchView v = view_of(bt);
+  BAdjArgs a{reinterpret_cast<const float4*>(rec), reinterpret_cast<float4*>(xbar), species,
+             nl.idx, nl.count, nl.ld, weight, sys_weight, gp, pp.per_pair_cutoff};
+  const bool sp = pp.n_species > 0 && species != nullptr, pr = gp != nullptr;
+  auto go = [&](auto dimc, auto kindc) {
+    constexpr int D = decltype(dimc)::value, K = decltype(kindc)::value;
+    if (sp) badj_launch3<D, K, true>(mode, pr, v, a, t, sg, st);
+    else badj_launch3<D, K, false>(mode, pr, v, a, t, sg, st);
+  };
+  using I3 = std::integral_constant<int, 3>;
+  using I2 = std::integral_constant<int, 2>;
+  using KL = std::integral_constant<int, JMD_LJ>;
+  using KT = std::integral_constant<int, JMD_LJ_TRUNCATED>;
+  using KS = std::integral_constant<int, JMD_SOFT_SPHERE>;
+  if (bt.dim == 3) {
+    if (pp.kind == JMD_LJ) go(I3{}, KL{});
+    else if (pp.kind == JMD_LJ_TRUNCATED) go(I3{}, KT{});
+    else go(I3{}, KS{});
+  } else {
+    if (pp.kind == JMD_LJ) go(I2{}, KL{});
+    else if (pp.kind == JMD_LJ_TRUNCATED) go(I2{}, KT{});
+    else go(I2{}, KS{});
+  }
+  JMD_CUDA(cudaGetLastError());
+  return JMD_OK;
+}
+
 // ----------------------------------------------------------------- host ----
 int validate_batch(const jmd_batch* b) {
   JMD_REQUIRE(b != nullptr, "batch is null");
@@ -679,7 +862,8 @@ int validate_system(const jmd_batch_system* s, bool fire) {
 // One step: kick + drift (+ skin test) -> conditional rebuild -> force (+ the
 // closing half kick for NVE, the FIRE update for FIRE).
 int enqueue_batch_run(const jmd_batch_system& s, const jmd_fire_params* fp, int64_t steps,
-                      bool graphed, cudaStream_t st, cudaStream_t body_st) {
+                      bool graphed, cudaStream_t st, cudaStream_t body_st, float* traj = nullptr,
+                      bool force_rebuild = false) {
   const jmd_batch& b = s.batch;
   const BatchView v = view_of(b);
   const bool always = s.threshold_sq < 0.f;
@@ -697,6 +881,14 @@ int enqueue_batch_run(const jmd_batch_system& s, const jmd_fire_params* fp, int6
       }, st, body_st);
     return build_impl(b, s.nlist, s.position, s.nlist.rebuild_flag, st);
   };
+  const size_t rows = sizeof(float4) * (size_t)b.n_atoms;
+  auto slot = [&](int64_t k) { return traj + (size_t)k * 4 * (size_t)b.n_atoms; };
+  if (traj) JMD_CUDA(cudaMemcpyAsync(slot(0), s.position, rows, cudaMemcpyDeviceToDevice, st));
+  if (force_rebuild) {
+    if (!always) JMD_CUDA(cudaMemsetAsync(s.nlist.rebuild_flag, 1, sizeof(int32_t), st));
+    int rc0 = gate();
+    if (rc0) return rc0;
+  }
   for (int64_t k = 0; k < steps; ++k) {
     if (b.dim == 3) {
       if (fire)
@@ -726,7 +918,53 @@ int enqueue_batch_run(const jmd_batch_system& s, const jmd_fire_params* fp, int6
         k_bfire_update<2><<<b.n_systems, 256, 0, st>>>(v, p, f, s.fire_state, s.done, s.n_done, *fp);
       JMD_CUDA(cudaGetLastError());
     }
+    if (traj) JMD_CUDA(cudaMemcpyAsync(slot(k + 1), s.position, rows, cudaMemcpyDeviceToDevice, st));
   }
+  return JMD_OK;
+}
+
+// Reverse pass over a recorded segment (slots 0..steps of traj), as
+// enqueue_adjoint of the single-system engine.
+int enqueue_batch_adjoint(const jmd_batch_system& s, const float* traj, int64_t steps,
+                          bool closing, bool opening, float* xbar, float* pbar, float* rec,
+                          double* gp, bool graphed, cudaStream_t st, cudaStream_t body_st) {
+  const jmd_batch& b = s.batch;
+  const BatchView v = view_of(b);
+  const bool always = s.threshold_sq < 0.f;
+  auto slot = [&](int64_t k) { return traj + (size_t)k * 4 * (size_t)b.n_atoms; };
+  auto gate = [&](const float* x) -> int {
+    if (always) return build_impl(b, s.nlist, x, nullptr, st);
+    if (graphed)
+      return graph_conditional(s.nlist.rebuild_flag, [&](cudaStream_t q) {
+        return build_impl(b, s.nlist, x, s.nlist.rebuild_flag, q);
+      }, st, body_st);
+    return build_impl(b, s.nlist, x, s.nlist.rebuild_flag, st);
+  };
+  const unsigned gr = (unsigned)std::max<int64_t>(1, ceil_div(b.n_atoms, 256));
+  const float4* ref = always ? nullptr : reinterpret_cast<const float4*>(s.nlist.reference_position);
+  auto rstep = [&](int64_t k, bool kick, float w) -> int {
+    const float4* x = reinterpret_cast<const float4*>(slot(k));
+    if (b.dim == 3)
+      k_badj_pack<3><<<gr, 256, 0, st>>>(v, x, reinterpret_cast<float4*>(xbar),
+                                         reinterpret_cast<float4*>(pbar), s.mass, s.mass_scalar,
+                                         s.dt, kick ? 1 : 0, reinterpret_cast<float4*>(rec), ref,
+                                         s.threshold_sq, s.nlist.rebuild_flag);
+    else
+      k_badj_pack<2><<<gr, 256, 0, st>>>(v, x, reinterpret_cast<float4*>(xbar),
+                                         reinterpret_cast<float4*>(pbar), s.mass, s.mass_scalar,
+                                         s.dt, kick ? 1 : 0, reinterpret_cast<float4*>(rec), ref,
+                                         s.threshold_sq, s.nlist.rebuild_flag);
+    JMD_CUDA(cudaGetLastError());
+    int rc = gate(slot(k));
+    if (rc) return rc;
+    return badj_launch(0, s.pair, b, s.nlist, rec, xbar, s.species, w, nullptr, gp, st);
+  };
+  if (!always) JMD_CUDA(cudaMemsetAsync(s.nlist.rebuild_flag, 1, sizeof(int32_t), st));
+  const float h = 0.5f * s.dt;
+  int rc;
+  if (closing && (rc = rstep(steps, false, h))) return rc;
+  for (int64_t k = steps - 1; k >= 0; --k)
+    if ((rc = rstep(k, true, (opening && k == 0) ? h : s.dt))) return rc;
   return JMD_OK;
 }
 
@@ -755,12 +993,89 @@ int run_impl(const jmd_batch_system* sys, const jmd_fire_params* fp, int64_t n_s
   }, st);
 }
 
+int graph_or_direct(const std::string& key, const std::function<int(cudaStream_t, cudaStream_t, bool)>& enq,
+                    int32_t use_graph, void* stream, const char* what) {
+  cudaStream_t st = as_stream(stream);
+  cudaStreamCaptureStatus cap;
+  JMD_CUDA(cudaStreamIsCapturing(st, &cap));
+  if (!use_graph || cap != cudaStreamCaptureStatusNone) {
+    int rc = enq(st, nullptr, false);
+    return rc ? rc : check_launch(what);
+  }
+  int device;
+  JMD_CUDA(cudaGetDevice(&device));
+  std::string k = key;
+  k.append(reinterpret_cast<const char*>(&device), sizeof(device));
+  return graph_launch_cached(k, [&](cudaStream_t cs, cudaStream_t bs) { return enq(cs, bs, true); },
+                             st);
+}
+
 }  // namespace
 }  // namespace jmd
 
 using namespace jmd;
 
 extern "C" {
+
+int jmd_batch_nve_run_recorded(const jmd_batch_system* sys, float* trajectory, int64_t n_steps,
+                               int32_t force_rebuild, int32_t use_graph, void* stream) {
+  int e = validate_system(sys, false);
+  if (e) return e;
+  JMD_REQUIRE(n_steps >= 0, "n_steps must be >= 0");
+  JMD_REQUIRE(trajectory == nullptr || (reinterpret_cast<uintptr_t>(trajectory) % 16) == 0,
+              "trajectory must be 16-byte aligned float4 rows");
+  if (sys->batch.n_atoms == 0) return JMD_OK;
+  std::string key("brec");
+  key.append(reinterpret_cast<const char*>(sys), sizeof(*sys));
+  key.append(reinterpret_cast<const char*>(&trajectory), sizeof(trajectory));
+  key.append(reinterpret_cast<const char*>(&n_steps), sizeof(n_steps));
+  key.push_back(force_rebuild ? 'f' : '-');
+  return graph_or_direct(key, [&](cudaStream_t cs, cudaStream_t bs, bool g) {
+    return enqueue_batch_run(*sys, nullptr, n_steps, g, cs, bs, trajectory, force_rebuild != 0);
+  }, use_graph, stream, "jmd_batch_nve_run_recorded");
+}
+
+int jmd_batch_nve_adjoint_segment(const jmd_batch_system* sys, const float* trajectory,
+                                  int64_t n_steps, int32_t closing, int32_t opening, float* xbar,
+                                  float* pbar, float* record_scratch, double* grad_params,
+                                  int32_t use_graph, void* stream) {
+  int e = validate_system(sys, false);
+  if (e) return e;
+  JMD_REQUIRE(n_steps >= 0, "n_steps must be >= 0");
+  JMD_REQUIRE(trajectory && xbar && pbar && record_scratch, "null buffer");
+  for (const void* q : {(const void*)trajectory, (const void*)xbar, (const void*)pbar,
+                        (const void*)record_scratch})
+    JMD_REQUIRE((reinterpret_cast<uintptr_t>(q) % 16) == 0, "float4 rows must be 16-byte aligned");
+  if (sys->batch.n_atoms == 0 || (n_steps == 0 && !closing)) return JMD_OK;
+  std::string key("badj");
+  key.append(reinterpret_cast<const char*>(sys), sizeof(*sys));
+  for (const void* q : {(const void*)trajectory, (const void*)xbar, (const void*)pbar,
+                        (const void*)record_scratch, (const void*)grad_params})
+    key.append(reinterpret_cast<const char*>(&q), sizeof(q));
+  key.append(reinterpret_cast<const char*>(&n_steps), sizeof(n_steps));
+  key.push_back(closing ? 'c' : '-');
+  key.push_back(opening ? 'o' : '-');
+  return graph_or_direct(key, [&](cudaStream_t cs, cudaStream_t bs, bool g) {
+    return enqueue_batch_adjoint(*sys, trajectory, n_steps, closing != 0, opening != 0, xbar,
+                                 pbar, record_scratch, grad_params, g, cs, bs);
+  }, use_graph, stream, "jmd_batch_nve_adjoint_segment");
+}
+
+int jmd_batch_energy_param_grad(const jmd_pair* pair, const jmd_batch* batch,
+                                const jmd_batch_nlist* nl, const float* position,
+                                const int32_t* species, const double* system_weight,
+                                double* grad_params, void* stream) {
+  int e = validate_pair(pair);
+  if (e) return e;
+  if ((e = validate_batch(batch))) return e;
+  if ((e = validate_nl(nl, batch->n_atoms))) return e;
+  JMD_REQUIRE(position && system_weight && grad_params, "null buffer");
+  JMD_REQUIRE((reinterpret_cast<uintptr_t>(position) % 16) == 0, "float4 rows must be 16-byte aligned");
+  JMD_REQUIRE(pair->n_species == 0 || species != nullptr, "species matrices need species");
+  int rc = badj_launch(1, *pair, *batch, *nl, position, nullptr, species, 1.f, system_weight,
+                       grad_params, as_stream(stream));
+  return rc ? rc : check_launch("jmd_batch_energy_param_grad");
+}
 
 size_t jmd_batch_nlist_workspace_bytes(const jmd_batch* batch) {
   if (!batch) return 0;

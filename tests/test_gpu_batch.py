@@ -194,3 +194,128 @@ def test_batch_overflow_flag(cuda):
     torch.cuda.synchronize()
     assert small.did_buffer_overflow
     assert int(small.occupancy.item()) == nb.occupancy.item()
+
+
+KA_SIG = np.array([[1.0, 0.8], [0.8, 0.88]])
+KA_EPS = np.array([[1.0, 1.5], [1.5, 0.5]])
+
+
+def _ka_system(n_cells, seed):
+    R, L = O.fcc_lattice(n_cells, 0.8442, 0.05, seed)
+    n = len(R)
+    Lk = float(np.float32((n / 1.2) ** (1 / 3)))
+    R = np.mod(R / float(L) * Lk, Lk).astype(np.float32)
+    rng = np.random.default_rng(seed)
+    species = np.zeros(n, np.int32)
+    species[rng.permutation(n)[: n // 5]] = 1
+    P = (rng.standard_normal((n, 3)) * np.sqrt(0.8)).astype(np.float32)
+    P -= P.mean(0, keepdims=True)
+    return R, P, Lk, species
+
+
+def _ka_batch(cuda, cells=(6, 7, 6)):
+    from jax_md_gb300 import batch, energy, space
+    systems = [_ka_system(c, 20 + k) for k, c in enumerate(cells)]
+    bt = batch.pack([torch.tensor(R, device=cuda) for R, P, L, s in systems],
+                    [L for R, P, L, s in systems], species=[s for R, P, L, s in systems])
+    disp, _ = space.periodic(systems[0][2])
+    _, efn = energy.lennard_jones_neighbor_list(disp, systems[0][2],
+                                                torch.tensor(systems[0][3], device=cuda),
+                                                sigma=KA_SIG, epsilon=KA_EPS, dr_threshold=0.3)
+    fns = batch.neighbor_list(2.5, 0.3)
+    nb = fns.allocate(bt, extra_capacity=8)
+    return systems, bt, fns, nb, batch.BatchPairEnergy(efn)
+
+
+def _ka_oracle_final_energies(systems, sig, eps, steps, dt=0.005):
+    out = []
+    for R, P, L, s in systems:
+        box = np.full(3, L)
+        spec = O.PairSpec(kind='lj', sigma=sig, epsilon=eps, species=s)
+        nl = O.NeighborListOracle(box, 2.5 * np.max(sig), 0.3)
+        h = {'nb': nl.allocate(R)}
+
+        def fn(X):
+            h['nb'] = nl.update(X, h['nb'])
+            return O.pair_energy_forces(spec, X, h['nb'].idx, O.DENSE, box)[1]
+        X, Pd = R.astype(np.float64), P.astype(np.float64)
+        F = fn(X)
+        for _ in range(steps):
+            X, Pd, F = O.velocity_verlet(fn, X, Pd, F, 1.0, dt, box)
+        out.append(O.pair_energy_forces(spec, X, nl.build(X).idx, O.DENSE, box)[0] / len(R))
+    return np.array(out)
+
+
+def test_batch_energy_gradients(cuda):
+    systems, bt, fns, nb, ef = _ka_batch(cuda)
+    sig = torch.tensor(KA_SIG, dtype=torch.float32, device=cuda, requires_grad=True)
+    eps = torch.tensor(KA_EPS, dtype=torch.float32, device=cuda, requires_grad=True)
+    R = bt.R.clone().requires_grad_(True)
+    E = ef.energy_fn_autograd(bt, nb)(R, sigma=sig, epsilon=eps)
+    w = torch.tensor([0.5, -1.0, 2.0], dtype=torch.float64, device=cuda)
+    (E * w).sum().backward()
+    F = ef.forces(bt, nb)[:, :3]
+    wa = w[bt.atom_sys.long()].to(torch.float32)[:, None]
+    assert torch.allclose(R.grad, -F * wa, atol=1e-6)
+    h = 1e-6
+    for mat, g in (('sigma', sig.grad), ('epsilon', eps.grad)):
+        for a, b in ((0, 1), (1, 1)):
+            vals = []
+            for sgn in (1, -1):
+                sm, em = KA_SIG.copy(), KA_EPS.copy()
+                (sm if mat == 'sigma' else em)[a, b] += sgn * h
+                tot = 0.0
+                for k, (Rk, Pk, Lk, sk) in enumerate(systems):
+                    spec = O.PairSpec(kind='lj', sigma=sm, epsilon=em, species=sk)
+                    tot += float(w[k]) * O.pair_energy_forces(spec, Rk, nb.dense(k), O.DENSE,
+                                                              np.full(3, Lk))[0]
+                vals.append(tot)
+            fd = (vals[0] - vals[1]) / (2 * h)
+            assert abs(float(g[a, b]) - fd) <= 1e-4 * max(1.0, abs(fd)), (mat, a, b, float(g[a, b]), fd)
+
+
+@pytest.mark.parametrize('k', [7, None], ids=['checkpointed', 'stored'])
+def test_batch_trajectory_gradient_matches_fd(cuda, k):
+    """Gradient of mean_b PE_b(x_n)/N_b after 20 NVE steps of an uneven KA
+    batch with respect to the shared sigma_AB, epsilon_AB (and R0 along a
+    direction), against FP64 central differences of the oracle."""
+    from jax_md_gb300 import batch
+    systems, bt, fns, nb, ef = _ka_batch(cuda)
+    steps = 20
+    traj = batch.BatchTrajectory(bt, fns, nb, ef, 0.005, steps, checkpoint_every=k)
+    sig = torch.tensor(KA_SIG, dtype=torch.float32, device=cuda, requires_grad=True)
+    eps = torch.tensor(KA_EPS, dtype=torch.float32, device=cuda, requires_grad=True)
+    R0 = bt.R.clone().requires_grad_(True)
+    P0 = torch.tensor(np.concatenate([P for R, P, L, s in systems]), device=cuda)
+    xn, pn = traj(R0, P0, sigma=sig, epsilon=eps)
+    x4 = torch.nn.functional.pad(xn.detach(), (0, 1)).contiguous()
+    nb = fns.update(x4, nb)
+    E = ef.energy_fn_autograd(bt, nb)(xn, sigma=sig, epsilon=eps)
+    sizes = torch.tensor(bt.sizes, dtype=torch.float64, device=cuda)
+    loss = (E / sizes).mean()
+    loss.backward()
+    L0 = _ka_oracle_final_energies(systems, KA_SIG, KA_EPS, steps).mean()
+    assert abs(float(loss) - L0) <= 1e-4 * abs(L0)
+    hh = 1e-4
+    for mat, g in (('sigma', sig.grad), ('epsilon', eps.grad)):
+        for a, b in ((0, 1), (0, 0)):
+            lp = []
+            for sgn in (1, -1):
+                sm, em = KA_SIG.copy(), KA_EPS.copy()
+                (sm if mat == 'sigma' else em)[a, b] += sgn * hh
+                lp.append(_ka_oracle_final_energies(systems, sm, em, steps).mean())
+            fd = (lp[0] - lp[1]) / (2 * hh)
+            assert abs(float(g[a, b]) - fd) <= 1e-3 * max(abs(fd), 1e-2), (mat, a, b, float(g[a, b]), fd)
+    v = np.random.default_rng(9).standard_normal((bt.n, 3))
+    v /= np.linalg.norm(v)
+    e_r = 1e-4
+    sp = []
+    for sgn in (1, -1):
+        shifted = []
+        for kk, (R, P, L, s) in enumerate(systems):
+            r = bt.rows(kk)
+            shifted.append(((R + sgn * e_r * v[r]).astype(np.float64), P, L, s))
+        sp.append(_ka_oracle_final_energies(shifted, KA_SIG, KA_EPS, steps).mean())
+    fd = (sp[0] - sp[1]) / (2 * e_r)
+    ad = float((R0.grad.cpu().numpy() * v).sum())
+    assert abs(ad - fd) <= 1e-3 * max(abs(fd), 1e-2), (ad, fd)
