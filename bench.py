@@ -251,6 +251,112 @@ def batched_section(dev, n_sys=512, fire_steps=200, nve_steps=200, seed=0):
     }
 
 
+def batched_adjoint_section(dev, n_sys=128, steps=500, seed=0):
+    """128 Kob-Andersen replicas (80:20, rho = 1.2, N from U[500, 20000]
+    rounded to a cubic lattice n^3, jittered, momenta at kT = 0.6): gradient of
+    the ensemble-mean PE/N after 500 NVE steps with respect to the shared
+    sigma / epsilon matrices, by the batched adjoint, against the cost of
+    finite differences with plain per-replica forward runs (one ensemble pass
+    timed; central differences of the two AB parameters need five)."""
+    import torch
+    from jax_md_gb300 import batch, energy, partition, simulate, space
+    rng = np.random.default_rng(seed)
+    sig = np.array([[1.0, 0.8], [0.8, 0.88]])
+    eps = np.array([[1.0, 1.5], [1.5, 0.5]])
+    systems = []
+    for k in range(n_sys):
+        m = int(round(rng.uniform(500, 20000) ** (1 / 3)))
+        L = float(np.float32((m ** 3 / 1.2) ** (1 / 3)))
+        g = np.stack(np.meshgrid(*[np.arange(m)] * 3, indexing='ij'), -1).reshape(-1, 3)
+        R = np.mod((g + 0.5) * (L / m) + rng.uniform(-0.05, 0.05, g.shape), L).astype(np.float32)
+        sp = np.zeros(len(R), np.int32)
+        sp[rng.permutation(len(R))[: len(R) // 5]] = 1
+        P = (rng.standard_normal(R.shape) * np.sqrt(0.6)).astype(np.float32)
+        P -= P.mean(0, keepdims=True)
+        systems.append((R, P, L, sp))
+    n_tot = sum(len(x[0]) for x in systems)
+    bt = batch.pack([torch.tensor(R, device=dev) for R, P, L, sp in systems],
+                    [L for R, P, L, sp in systems], species=[sp for R, P, L, sp in systems])
+    disp, shift = space.periodic(systems[0][2])
+    _, efn = energy.lennard_jones_neighbor_list(disp, systems[0][2],
+                                                torch.tensor(systems[0][3], device=dev),
+                                                sigma=sig, epsilon=eps, dr_threshold=0.3)
+    fns = batch.neighbor_list(2.5, 0.3)
+    nb = fns.allocate(bt, extra_capacity=12)
+    ef = batch.BatchPairEnergy(efn)
+    traj = batch.BatchTrajectory(bt, fns, nb, ef, 0.005, steps)
+    R0 = bt.R.clone()
+    P0 = torch.tensor(np.concatenate([P for R, P, L, sp in systems]), device=dev)
+    sizes = torch.tensor(bt.sizes, dtype=torch.float64, device=dev)
+    sig_t = torch.tensor(sig, dtype=torch.float32, device=dev, requires_grad=True)
+    eps_t = torch.tensor(eps, dtype=torch.float32, device=dev, requires_grad=True)
+
+    def forward():
+        with torch.no_grad():
+            return traj(R0, P0, sigma=sig_t.detach(), epsilon=eps_t.detach())
+
+    def forward_backward():
+        sig_t.grad = None
+        eps_t.grad = None
+        xn, pn = traj(R0, P0, sigma=sig_t, epsilon=eps_t)
+        fns.update(torch.nn.functional.pad(xn.detach(), (0, 1)).contiguous(), nb)
+        E = ef.energy_fn_autograd(bt, nb)(xn, sigma=sig_t, epsilon=eps_t)
+        loss = (E / sizes).mean()
+        loss.backward()
+        return loss
+
+    def timed(fn):
+        e0, e1 = _events(dev)
+        torch.cuda.synchronize()
+        e0.record(torch.cuda.current_stream(dev))
+        out = fn()
+        e1.record(torch.cuda.current_stream(dev))
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3, out
+
+    forward()
+    forward_backward()
+    t_f, _ = timed(forward)
+    t_fb, loss = timed(forward_backward)
+    g_sab = float((sig_t.grad[0, 1] + sig_t.grad[1, 0]).detach())
+    g_eab = float((eps_t.grad[0, 1] + eps_t.grad[1, 0]).detach())
+    overflow = nb.did_buffer_overflow
+    # plain: the same replicas one at a time, single-system API, direct launches
+    runs = []
+    for R, P, L, sp in systems:
+        d_k, s_k = space.periodic(L)
+        nfn_k, efn_k = energy.lennard_jones_neighbor_list(d_k, L, torch.tensor(sp, device=dev),
+                                                          sigma=sig, epsilon=eps, dr_threshold=0.3,
+                                                          format=partition.Dense)
+        Rk = torch.tensor(R, device=dev)
+        nb_k = nfn_k.allocate(Rk, extra_capacity=12)
+        init, apply = simulate.nve(efn_k, s_k, 0.005)
+        runs.append((apply, init(0, Rk, momenta=torch.tensor(P, device=dev), neighbor=nb_k), nb_k))
+
+    def plain():
+        for apply, st, nb_k in runs:
+            simulate.run(apply, st, nb_k, steps, use_graph=False)
+    t_plain, _ = timed(plain)
+    return {
+        'workload': f'{n_sys} Kob-Andersen replicas, N=n^3 from U[500,20000] (total {n_tot}), '
+                    f'rho=1.2, kT=0.6, {steps} NVE steps dt=0.005, loss mean_b PE_b/N_b, '
+                    'grad wrt shared sigma[2x2], epsilon[2x2]',
+        'forward_s': t_f, 'forward_backward_s': t_fb,
+        'gradient_cost_ratio': t_fb / t_f,
+        'batched_forward_atom_steps_per_s': n_tot * steps / t_f,
+        'plain_forward_ensemble_s': t_plain,
+        'plain_finite_difference_s': 5 * t_plain,
+        'speedup_vs_finite_differences': 5 * t_plain / t_fb,
+        'dloss_dsigma_AB': g_sab, 'dloss_depsilon_AB': g_eab, 'loss': float(loss.detach()),
+        'note': 'over 500 steps the gradient of a chaotic trajectory is large; the FP64 '
+                'finite-difference checks run 20 steps (tests)',
+        'plain': 'per-replica simulate.run with direct launches; central differences of the two '
+                 'AB parameters = 5 ensemble passes (one timed)',
+        'dynamics': 'NVE (the Nose-Hoover adjoint is not built)',
+        'overflow': overflow,
+    }
+
+
 def adjoint_section(dev, steps=2000, checkpoint_every=100, seed=0):
     """Kob-Andersen 80:20 binary LJ, N = 8000 at rho = 1.2: 200 FIRE steps,
     momenta at kT = 0.8, then the gradient of PE/N + 0.1 MSD after 2000 NVE
@@ -535,6 +641,7 @@ def main():
         line['nvt'] = nvt_section(dev, efn, nfn, shift, R, P, args.steps, args.warmup)
         line['batched'] = batched_section(dev)
         line['adjoint'] = adjoint_section(dev)
+        line['batched_adjoint'] = batched_adjoint_section(dev)
     if rank == 0 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline(R, P, L)
     if rank == 0:

@@ -533,7 +533,7 @@ typedef struct {
   const int32_t* atom_sys;       /* [N] system of each atom */
   const float* box;              /* [B*3] periodic box side per system and axis */
   const int32_t* cell_offset;    /* [B+1] */
-  const int32_t* cells_per_side; /* [B*3], each >= 3 */
+  const int32_t* cells_per_side; /* [B*3], each >= 1 (1 or 2: every cell is searched once) */
   const float* cell_size;        /* [B*3] box / cells_per_side (float32, as partition.py:99-132) */
 } jmd_batch;
 

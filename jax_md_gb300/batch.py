@@ -102,11 +102,10 @@ class _Grid:
 
     def __init__(self, batch: Batch, cutoff: float):
         L = batch.box_host[:, :batch.dim]
-        cps = np.floor(L / np.float32(cutoff)).astype(np.int64)
-        if np.any(cps < 3):
-            b = int(np.argmin(cps.min(1)))
-            raise ValueError(f'system {b}: the box holds fewer than 3 cells of the list cutoff '
-                             f'{cutoff} per side; the batched search needs >= 3')
+        # a box shorter than three cutoffs gets one or two cells along that axis,
+        # where the search visits each distinct cell once (the pair set of the
+        # reference's all-pairs candidates, partition.py:893-898)
+        cps = np.maximum(np.floor(L / np.float32(cutoff)).astype(np.int64), 1)
         cs = (L / cps.astype(np.float32)).astype(np.float32)
         ncell = np.prod(cps, axis=1)
         if int(ncell.max()) > 24576:

@@ -235,11 +235,17 @@ __global__ void __launch_bounds__(128) k_bsearch(BatchView v, BWs w, SearchArgs 
   const int nx = __ldg(v.cps + 3 * b), ny = __ldg(v.cps + 3 * b + 1);
   const int nz = DIM == 3 ? __ldg(v.cps + 3 * b + 2) : 1;
   int cnt = 0;
-  for (int oz = (DIM == 3 ? -1 : 0); oz <= (DIM == 3 ? 1 : 0); ++oz) {
+  // neighbour cells along an axis: -1..1 with >= 3 cells, the two cells with
+  // 2, the one cell with 1 (each distinct cell visited once; the minimum
+  // image then gives the pair set of an all-pairs search)
+  const int lz = DIM == 3 ? (nz >= 3 ? -1 : 0) : 0, hz = DIM == 3 ? (nz >= 2 ? 1 : 0) : 0;
+  const int ly = ny >= 3 ? -1 : 0, hy = ny >= 2 ? 1 : 0;
+  const int lx = nx >= 3 ? -1 : 0, hx = nx >= 2 ? 1 : 0;
+  for (int oz = lz; oz <= hz; ++oz) {
     const int z = DIM == 3 ? (cc[2] + oz + nz) % nz : 0;
-    for (int oy = -1; oy <= 1; ++oy) {
+    for (int oy = ly; oy <= hy; ++oy) {
       const int y = (cc[1] + oy + ny) % ny;
-      for (int ox = -1; ox <= 1; ++ox) {
+      for (int ox = lx; ox <= hx; ++ox) {
         const int xcell = (cc[0] + ox + nx) % nx;
         const int gc = c0 + xcell + nx * (y + ny * z);
         const int s = w.cstart[gc], e = s + w.ccount[gc];

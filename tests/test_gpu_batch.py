@@ -72,6 +72,20 @@ def test_batch_neighbor_sets_3d(cuda):
     _check_sets(bt, nb, systems, 2.8, 3)
 
 
+def test_batch_neighbor_sets_small_boxes(cuda):
+    """Boxes of 1, 2 and 3 list cutoffs per side (the reference's all-pairs
+    candidates below three cells) give the oracle's sets."""
+    systems, bt, fns, nb, ef = _lj_batch(cuda, cells=(3, 4, 6))
+    assert nb.grid.cps[:, 0].tolist() == [1, 2, 3]
+    assert not nb.did_buffer_overflow
+    _check_sets(bt, nb, systems, 2.8, 3)
+    F = ef.forces(bt, nb)
+    torch.cuda.synchronize()
+    for b, (R, L) in enumerate(systems):
+        F0 = O.pair_energy_forces(O.PairSpec(kind='lj'), R, nb.dense(b), O.DENSE, np.full(3, L))[1]
+        assert np.abs(bt.split(F[:, :3])[b].cpu().numpy() - F0).max() < 1e-4
+
+
 @pytest.mark.parametrize('kind', ['soft_sphere_2d', 'lj_3d'])
 def test_batch_forces_and_energies(cuda, kind):
     if kind == 'soft_sphere_2d':
