@@ -537,12 +537,9 @@ typedef struct {
   const float* cell_size;        /* [B*3] box / cells_per_side (float32, as partition.py:99-132) */
 } jmd_batch;
 
-/* Dense list of a batch in a tiled layout over cell-order slots: the build
- * orders each system's atoms by cell (slots sys_offset[b] .. sys_offset[b+1]-1
- * stay the system's), slot_atom[s] is the atom of slot s, and the entries of
- * that atom are idx[(s/32)*ld*32 + k*32 + s%32], k < count[s], as global atom
- * ids (system-local id = id - sys_offset[b]).  Kernels walk slots, so
- * neighbouring threads share neighbours in cache.  Rows hold at most
+/* Dense list of a batch in the engine's tiled layout: the entries of atom i
+ * are idx[(i/32)*ld*32 + k*32 + i%32], k < count[i]; entries are global atom
+ * ids (system-local id = id - sys_offset[b]).  Rows hold at most
  * max_occupancy entries (ld >= max_occupancy); a longer row sets
  * JMD_NEIGHBOR_LIST_OVERFLOW in error_code, and occupancy[0] receives the
  * largest row length found (int32). */
@@ -552,8 +549,7 @@ typedef struct {
   int32_t ld;
   int32_t mask_self;
   int32_t* idx;                  /* ((N + 31) / 32) * 32 * ld */
-  int32_t* count;                /* [N] per slot */
-  int32_t* slot_atom;            /* [N] atom of each slot */
+  int32_t* count;                /* [N] */
   float* reference_position;     /* [N] float4 rows, positions of the last build */
   int32_t* occupancy;            /* [1] */
   uint8_t* error_code;           /* [1] sticky PartitionErrorCode bits */

@@ -88,7 +88,6 @@ class Batch(C.Structure):
 class BatchNList(C.Structure):
     _fields_ = [('cutoff_sq', C.c_float), ('max_occupancy', C.c_int32), ('ld', C.c_int32),
                 ('mask_self', C.c_int32), ('idx', C.c_void_p), ('count', C.c_void_p),
-                ('slot_atom', C.c_void_p),
                 ('reference_position', C.c_void_p), ('occupancy', C.c_void_p),
                 ('error_code', C.c_void_p), ('rebuild_flag', C.c_void_p),
                 ('workspace', C.c_void_p), ('workspace_bytes', C.c_size_t)]

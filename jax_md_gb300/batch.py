@@ -140,12 +140,11 @@ class _Grid:
 
 @dataclasses.dataclass
 class BatchNeighborList:
-    """Dense lists of every system in a tiled layout over cell-order slots
-    (see jmd_batch_nlist): slot s holds atom ``slot_atom[s]``, whose entries
-    are ``idx[(s//32)*ld*32 + k*32 + s%32]`` for ``k < count[s]``, global ids."""
+    """Dense lists of every system in the engine's tiled layout (see
+    jmd_batch_nlist): entries of atom i (global row) are
+    ``idx[(i//32)*ld*32 + k*32 + i%32]`` for ``k < count[i]``, global ids."""
     idx: torch.Tensor
     count: torch.Tensor
-    slot_atom: torch.Tensor
     reference_position: torch.Tensor
     error: torch.Tensor           # uint8 [1], PartitionErrorCode bits
     occupancy: torch.Tensor       # int32 [1], largest row found by the last build
@@ -167,7 +166,6 @@ class BatchNeighborList:
         s.mask_self = 1 if self.mask_self else 0
         s.idx = self.idx.data_ptr()
         s.count = self.count.data_ptr()
-        s.slot_atom = self.slot_atom.data_ptr()
         s.reference_position = self.reference_position.data_ptr()
         s.occupancy = self.occupancy.data_ptr()
         s.error_code = self.error.data_ptr()
@@ -185,15 +183,11 @@ class BatchNeighborList:
         array of system-local ids padded with N_b (rows sorted; host copy)."""
         rows = self.batch.rows(b)
         n_b = rows.stop - rows.start
-        dev = self.idx.device
-        slot_of = torch.empty_like(self.slot_atom)
-        slot_of[self.slot_atom.long()] = torch.arange(self.slot_atom.numel(), dtype=torch.int32,
-                                                      device=dev)
-        i = slot_of[rows].long()                      # slots of the system's atoms, in atom order
-        k = torch.arange(self.max_occupancy, device=dev)
+        i = torch.arange(rows.start, rows.stop, device=self.idx.device)
+        k = torch.arange(self.max_occupancy, device=self.idx.device)
         pos = (i[:, None] // 32) * self.ld * 32 + k[None, :] * 32 + (i[:, None] % 32)
         ent = self.idx[pos.reshape(-1)].reshape(n_b, self.max_occupancy).long() - rows.start
-        cnt = self.count[i].long()
+        cnt = self.count[rows].long()
         ent = torch.where(k[None, :] < cnt[:, None], ent, torch.full_like(ent, n_b))
         out = ent.cpu().numpy()
         out.sort(axis=1)
@@ -227,7 +221,6 @@ class BatchNeighborListFns:
         return BatchNeighborList(
             idx=torch.empty(max(n_pad * ld, 1), dtype=torch.int32, device=dev),
             count=torch.zeros(max(batch.n, 1), dtype=torch.int32, device=dev),
-            slot_atom=torch.arange(max(batch.n, 1), dtype=torch.int32, device=dev),
             reference_position=torch.zeros((max(batch.n, 1), 4), dtype=torch.float32, device=dev),
             error=torch.zeros(1, dtype=torch.uint8, device=dev),
             occupancy=torch.zeros(1, dtype=torch.int32, device=dev),

@@ -212,7 +212,6 @@ struct SearchArgs {
   int width, ld, mask_self;
   int32_t* idx;
   int32_t* count;
-  int32_t* slot_atom;
   float4* ref;
 };
 
@@ -257,15 +256,14 @@ __global__ void __launch_bounds__(128) k_bsearch(BatchView v, BWs w, SearchArgs 
           bdisp<DIM>(xi, w.xs[m], g, dx, dy, dz);
           const float d2 = dx * dx + dy * dy + (DIM == 3 ? dz * dz : 0.f);
           if (d2 < a.cutoff_sq) {
-            if (cnt < a.width) a.idx[tile_at(k, cnt, a.ld)] = j;
+            if (cnt < a.width) a.idx[tile_at(i, cnt, a.ld)] = j;
             ++cnt;
           }
         }
       }
     }
   }
-  a.count[k] = min(cnt, a.width);
-  a.slot_atom[k] = i;
+  a.count[i] = min(cnt, a.width);
   a.ref[i] = xi;
   if (cnt > a.width) atomicOr(&w.sc[0], (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
   atomicMax(&w.sc[1], (unsigned)cnt);
@@ -300,9 +298,8 @@ struct BForceArgs {
   float4* f;
   float4* p;
   const int32_t* species;
-  const int32_t* idx;       // tiled by cell-order slot
-  const int32_t* count;     // per slot
-  const int32_t* slot_atom; // atom of each slot
+  const int32_t* idx;
+  const int32_t* count;
   int ld;
   float h;                  // B_KICK: p += h F
   const int32_t* done;      // B_FIRE: frozen systems are skipped
@@ -312,16 +309,15 @@ struct BForceArgs {
 template <int DIM, int KIND, bool SPECIES, int MODE>
 __global__ void __launch_bounds__(128) k_bforce(BatchView v, BForceArgs a,
                                                 const __grid_constant__ PairTable tab) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;  // cell-order slot
-  if (k >= v.n) return;
-  const int i = __ldg(a.slot_atom + k);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n) return;
   const int b = __ldg(v.atom_sys + i);
   if (MODE == B_FIRE && __ldg(a.done + b)) return;
   const SysGeo g = sys_geo(v, b);
   const float4 xi = __ldg(a.x + i);
   const int si = SPECIES ? min(max(__ldg(a.species + i), 0), tab.nsp - 1) : 0;
-  const int m = __ldg(a.count + k);
-  const int32_t* col = a.idx + (int64_t)(k >> 5) * a.ld * 32 + (k & 31);
+  const int m = __ldg(a.count + i);
+  const int32_t* col = a.idx + (int64_t)(i >> 5) * a.ld * 32 + (i & 31);
   float fx = 0.f, fy = 0.f, fz = 0.f;
   for (int e = 0; e < m; ++e) {
     const int j = __ldcs(col + (int64_t)e * 32);
@@ -386,12 +382,11 @@ __global__ void __launch_bounds__(256) k_bsys_energy(BatchView v, BForceArgs a,
   const int a0 = __ldg(v.sys_offset + b), a1 = __ldg(v.sys_offset + b + 1);
   const SysGeo g = sys_geo(v, b);
   double acc = 0.0;
-  for (int k = a0 + threadIdx.x; k < a1; k += blockDim.x) {  // the system's slots
-    const int i = __ldg(a.slot_atom + k);
+  for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
     const float4 xi = __ldg(a.x + i);
     const int si = SPECIES ? min(max(__ldg(a.species + i), 0), tab.nsp - 1) : 0;
-    const int m = __ldg(a.count + k);
-    const int32_t* col = a.idx + (int64_t)(k >> 5) * a.ld * 32 + (k & 31);
+    const int m = __ldg(a.count + i);
+    const int32_t* col = a.idx + (int64_t)(i >> 5) * a.ld * 32 + (i & 31);
     float e_i = 0.f;
     for (int e = 0; e < m; ++e) {
       const int j = __ldg(col + (int64_t)e * 32);
@@ -609,7 +604,6 @@ struct BAdjArgs {
   const int32_t* species;
   const int32_t* idx;
   const int32_t* count;
-  const int32_t* slot_atom;
   int ld;
   float weight;
   const double* sys_weight; // energy mode: per-system weight of dE_b/dtheta
@@ -629,14 +623,13 @@ __global__ void __launch_bounds__(128) k_badj_step(BatchView v, BAdjArgs a,
     zero_bins(bins);
     __syncthreads();
   }
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;  // cell-order slot
-  const bool active = k < v.n;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < v.n;
   const bool per_pair = a.per_pair != 0;
   BinAcc<NB> acc;
   acc.zero();
   int si = 0;
   if (active) {
-    const int i = __ldg(a.slot_atom + k);
     const int b = __ldg(v.atom_sys + i);
     const SysGeo g = sys_geo(v, b);
     const float ew = MODE == 1 ? (float)__ldg(a.sys_weight + b) : 1.f;
@@ -644,8 +637,8 @@ __global__ void __launch_bounds__(128) k_badj_step(BatchView v, BAdjArgs a,
     const float4 r1 = MODE == 0 ? __ldg(a.rec + 2 * i + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float qx = r0.w, qy = r1.x, qz = r1.y;
     si = SPECIES ? min(max(__ldg(a.species + i), 0), tab.nsp - 1) : 0;
-    const int m = __ldg(a.count + k);
-    const int32_t* col = a.idx + (int64_t)(k >> 5) * a.ld * 32 + (k & 31);
+    const int m = __ldg(a.count + i);
+    const int32_t* col = a.idx + (int64_t)(i >> 5) * a.ld * 32 + (i & 31);
     float gx = 0.f, gy = 0.f, gz = 0.f;
     for (int e = 0; e < m; ++e) {
       const int j = __ldcs(col + (int64_t)e * 32);
@@ -725,7 +718,7 @@ int badj_launch(int mode, const jmd_pair& pp, const jmd_batch& bt, const jmd_bat
   const PairTable sg = sigma_table(pp);
   const BatchView v = view_of(bt);
   BAdjArgs a{reinterpret_cast<const float4*>(rec), reinterpret_cast<float4*>(xbar), species,
-             nl.idx, nl.count, nl.slot_atom, nl.ld, weight, sys_weight, gp, pp.per_pair_cutoff};
+             nl.idx, nl.count, nl.ld, weight, sys_weight, gp, pp.per_pair_cutoff};
   const bool sp = pp.n_species > 0 && species != nullptr, pr = gp != nullptr;
   auto go = [&](auto dimc, auto kindc) {
     constexpr int D = decltype(dimc)::value, K = decltype(kindc)::value;
@@ -767,8 +760,7 @@ int validate_batch(const jmd_batch* b) {
 int validate_nl(const jmd_batch_nlist* nl, int64_t n) {
   JMD_REQUIRE(nl != nullptr, "nlist is null");
   JMD_REQUIRE(nl->max_occupancy >= 1 && nl->ld >= nl->max_occupancy, "ld must be >= max_occupancy >= 1");
-  JMD_REQUIRE(nl->idx && nl->count && nl->slot_atom && nl->reference_position && nl->occupancy &&
-                  nl->error_code,
+  JMD_REQUIRE(nl->idx && nl->count && nl->reference_position && nl->occupancy && nl->error_code,
               "null buffer in jmd_batch_nlist");
   JMD_REQUIRE((reinterpret_cast<uintptr_t>(nl->reference_position) % 16) == 0,
               "reference_position must be float4 rows");
@@ -792,7 +784,7 @@ int build_impl(const jmd_batch& b, const jmd_batch_nlist& nl, const float* x, in
     k_bbin<2><<<b.n_systems, kBinThreads, smem, st>>>(v, w, x4, flag);
   }
   JMD_CUDA(cudaGetLastError());
-  SearchArgs a{nl.cutoff_sq, nl.max_occupancy, nl.ld, nl.mask_self, nl.idx, nl.count, nl.slot_atom,
+  SearchArgs a{nl.cutoff_sq, nl.max_occupancy, nl.ld, nl.mask_self, nl.idx, nl.count,
                reinterpret_cast<float4*>(nl.reference_position)};
   const unsigned gr = (unsigned)std::max<int64_t>(1, ceil_div(b.n_atoms, 128));
   if (b.n_atoms > 0) {
@@ -844,8 +836,7 @@ int force_impl(const jmd_pair& pp, const jmd_batch& b, const jmd_batch_nlist& nl
   const PairTable t = make_pair_table(pp);
   const BatchView v = view_of(b);
   BForceArgs a{reinterpret_cast<const float4*>(x), reinterpret_cast<float4*>(f),
-               reinterpret_cast<float4*>(p), species, nl.idx, nl.count, nl.slot_atom, nl.ld, h,
-               done};
+               reinterpret_cast<float4*>(p), species, nl.idx, nl.count, nl.ld, h, done};
   const bool sp = pp.n_species > 0 && species != nullptr;
   const unsigned gr = (unsigned)ceil_div(b.n_atoms, 128);
   const int ns = b.n_systems;
