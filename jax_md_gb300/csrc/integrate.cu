@@ -145,30 +145,34 @@ struct NhcArgs {
   int update_mass;
 };
 
-// Chain layout: xi[16] p[16] Q[16] spare[16] KE kT
-__device__ void nhc_substep(double delta, double* xi, double* p, const double* Q, double& KE,
-                            double& scale_total, int M1, double dof, double kT) {
+// Chain layout: xi[16] p[16] Q[16] spare[16] KE kT (f64 in memory).  The
+// substeps run in float32, the arithmetic of the reference's default float32
+// state (simulate.py:444-507): a single thread walks a long serial chain of
+// exp / divide steps, and float32 keeps it on the fast pipes.
+template <typename T>
+__device__ void nhc_substep(T delta, T* xi, T* p, const T* Q, T& KE, T& scale_total, int M1, T dof,
+                            T kT) {
   const int M = M1 - 1;
-  const double d2 = delta / 2.0, d4 = d2 / 2.0, d8 = d4 / 2.0;
-  double G = p[M - 1] * p[M - 1] / Q[M - 1] - kT;
+  const T d2 = delta / T(2), d4 = d2 / T(2), d8 = d4 / T(2);
+  T G = p[M - 1] * p[M - 1] / Q[M - 1] - kT;
   p[M] += d4 * G;
-  double pnew = p[M];
+  T pnew = p[M];
   for (int m = M - 1; m > 0; --m) {
     G = p[m - 1] * p[m - 1] / Q[m - 1] - kT;
-    double s = exp(-d8 * pnew / Q[m + 1]);
+    T s = exp(-d8 * pnew / Q[m + 1]);
     pnew = s * (s * p[m] + d4 * G);
     p[m] = pnew;
   }
-  G = 2.0 * KE - dof * kT;
-  double s = exp(-d8 * p[1] / Q[1]);
+  G = T(2) * KE - dof * kT;
+  T s = exp(-d8 * p[1] / Q[1]);
   p[0] = s * (s * p[0] + d4 * G);
   s = exp(-d2 * p[0] / Q[0]);
   KE = KE * s * s;
   scale_total *= s;
   for (int m = 0; m <= M; ++m) xi[m] += d2 * p[m] / Q[m];
-  G = 2.0 * KE - dof * kT;
+  G = T(2) * KE - dof * kT;
   for (int m = 0; m < M; ++m) {
-    double sc = exp(-d8 * p[m + 1] / Q[m + 1]);
+    T sc = exp(-d8 * p[m + 1] / Q[m + 1]);
     p[m] = sc * (sc * p[m] + d4 * G);
     G = p[m] * p[m] / Q[m] - kT;
   }
@@ -177,24 +181,37 @@ __device__ void nhc_substep(double delta, double* xi, double* p, const double* Q
 
 __global__ void k_nhc_half(NhcArgs a, double* chain, const double* ke_in, double* p_scale) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double* xi = chain;
-  double* p = chain + 16;
-  double* Q = chain + 32;
-  double& KE = chain[64];
-  const double kT = chain[65];
-  if (ke_in) KE = *ke_in;
+  // the chain is worked on in thread-local copies (L1) and written back once:
+  // the substeps are a long serial dependency chain
+  float xi[16], p[16], Q[16];
+  const int M1 = a.M1;
+  for (int m = 0; m < M1; ++m) {
+    xi[m] = (float)chain[m];
+    p[m] = (float)chain[16 + m];
+    Q[m] = (float)chain[32 + m];
+  }
+  float KE = (float)(ke_in ? *ke_in : chain[64]);
+  const float kT = (float)chain[65];
+  const float dof = (float)a.dof;
   if (a.update_mass) {
-    for (int m = 0; m < a.M1; ++m) Q[m] = kT * a.tau * a.tau;
-    Q[0] *= a.dof;
+    const float tau = (float)a.tau;
+    for (int m = 0; m < M1; ++m) Q[m] = kT * tau * tau;
+    Q[0] *= dof;
   }
-  double scale = 1.0;
+  float scale = 1.f;
   if (a.chain_steps == 1 && a.sy_steps == 1) {
-    nhc_substep(a.dt, xi, p, Q, KE, scale, a.M1, a.dof, kT);
+    nhc_substep<float>((float)a.dt, xi, p, Q, KE, scale, M1, dof, kT);
   } else {
-    const double delta = a.dt / a.chain_steps;
+    const float delta = (float)a.dt / (float)a.chain_steps;
     for (int k = 0; k < a.chain_steps * a.sy_steps; ++k)
-      nhc_substep(delta * a.w[k % a.sy_steps], xi, p, Q, KE, scale, a.M1, a.dof, kT);
+      nhc_substep<float>(delta * (float)a.w[k % a.sy_steps], xi, p, Q, KE, scale, M1, dof, kT);
   }
+  for (int m = 0; m < M1; ++m) {
+    chain[m] = xi[m];
+    chain[16 + m] = p[m];
+    chain[32 + m] = Q[m];
+  }
+  chain[64] = KE;
   *p_scale = scale;
 }
 
