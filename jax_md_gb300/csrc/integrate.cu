@@ -108,19 +108,25 @@ __global__ void k_kick_drift(KickDriftArgs a) {
   if (a.flag && __any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(a.flag, 1);
 }
 
+// Grid-stride: each thread sums its atoms' p^2 / 2m in fp32 (a few terms;
+// the FP64 pipe is narrow on this part), the threads' partial sums are then
+// reduced in f64 in a fixed order.
 template <int DIM>
 __global__ void k_ke(const float* p, int64_t ps, const float* mass, float m0, int n,
                      double* partials, unsigned int* counter, double* out) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double v[1] = {0.0};
-  if (i < n) {
+  float acc = 0.f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float4 q = load_row<DIM, false>(p, ps, i);
     float m = mass ? mass[i] : m0;
     float s = q.x * q.x + q.y * q.y + (DIM == 3 ? q.z * q.z : 0.f);
-    v[0] = 0.5 * (double)s / (double)m;
+    acc += 0.5f * s / m;
   }
+  double v[1] = {(double)acc};
   grid_reduce<1>(v, partials, counter, out, false);
 }
+
+// Blocks of a grid-stride reduction over n atoms: 8 atoms per thread at most.
+inline unsigned ke_blocks(int64_t n) { return (unsigned)std::max<int64_t>(1, ceil_div(n, 256 * 8)); }
 
 template <int DIM>
 __global__ void k_scale(float* p, int64_t ps, int n, const double* scale) {
@@ -405,7 +411,7 @@ int jmd_kinetic_energy(const float* momentum, int64_t p_stride, const float* mas
     JMD_CUDA(cudaMemsetAsync(out, 0, sizeof(double), st));
     return JMD_OK;
   }
-  int64_t gr = ceil_div(n, 256);
+  const int64_t gr = ke_blocks(n);
   if (gr > kMaxReduceBlocks) return fail(JMD_ERR_UNSUPPORTED, "system too large");
   JMD_CUDA(cudaMemsetAsync(w.counter, 0, sizeof(unsigned int), st));
   if (dim == 3) k_ke<3><<<(unsigned)gr, 256, 0, st>>>(momentum, p_stride, mass, mass_scalar, (int)n, w.partials, w.counter, out);
@@ -573,7 +579,7 @@ int jmd_kinetic_energy_static_scratch(const float* momentum, int64_t p_stride, c
       reinterpret_cast<unsigned int*>(static_cast<char*>(base) + kStaticCounterOffset);
   // the completion counter must start at zero; the partials are overwritten
   JMD_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), st));
-  const unsigned gr = (unsigned)ceil_div(n, 256);
+  const unsigned gr = ke_blocks(n);
   if (dim == 3)
     k_ke<3><<<gr, 256, 0, st>>>(momentum, p_stride, mass, mass_scalar, (int)n, partials, counter, out);
   else
