@@ -490,6 +490,10 @@ class _BatchTrajectoryFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, R0, P0, sigma, epsilon, cfg):
         tr, dyn = cfg
+        if tr.busy:
+            raise RuntimeError('this BatchTrajectory holds a recorded run whose backward has not '
+                               'run yet (one buffer set per BatchTrajectory): call backward first '
+                               'or use a second BatchTrajectory')
         bt, nb, dim = tr.batch, tr.nbrs, tr.batch.dim
         buf = tr.buffers()
         buf['x'].zero_()
@@ -516,6 +520,8 @@ class _BatchTrajectoryFn(torch.autograd.Function):
         if nb.did_buffer_overflow:
             raise RuntimeError('a batched neighbour list overflowed during the trajectory; '
                                'allocate it with more capacity')
+        if any(ctx.needs_input_grad[:4]):
+            tr.busy = True   # the recorded trajectory must survive until backward
         ctx.cfg = (tr, sysd, species, buf)
         ctx.has = (sigma is not None, epsilon is not None)
         ctx.save_for_backward(sigma if sigma is not None else torch.empty(0),
@@ -555,6 +561,7 @@ class _BatchTrajectoryFn(torch.autograd.Function):
                 buf['rec'].data_ptr(), bins.data_ptr() if want else None, 1, N.stream_ptr()),
                 'batch_nve_adjoint_segment')
         gs, ge = _bins_to_grads(bins, None, sigma, epsilon) if want else (None, None)
+        tr.busy = False
         return buf['xbar'][:, :dim].clone(), buf['pbar'][:, :dim].clone(), gs, ge, None
 
 
@@ -564,7 +571,9 @@ class BatchTrajectory:
     respect to R0, P0 and sigma / epsilon shared by all systems, through the
     batched reverse Verlet pass (checkpointed every ``checkpoint_every`` steps;
     None keeps the whole trajectory when it fits a quarter of free memory).
-    ``nbrs`` is rebuilt in place.  Unit mass unless ``mass`` is given."""
+    ``nbrs`` is rebuilt in place.  Unit mass unless ``mass`` is given.  One
+    set of device buffers: a forward pass that records for backward must be
+    followed by its backward before the next one (a second call raises)."""
 
     def __init__(self, batch: Batch, neighbor_fns: BatchNeighborListFns, nbrs: BatchNeighborList,
                  energy: BatchPairEnergy, dt: float, n_steps: int, checkpoint_every=None,
@@ -583,6 +592,7 @@ class BatchTrajectory:
         self.segments = [(s0, min(s0 + k, self.n_steps)) for s0 in range(0, self.n_steps, k)]
         self.k = k
         self._buf = None
+        self.busy = False
 
     def buffers(self):
         if self._buf is None:
