@@ -486,6 +486,17 @@ class _BatchEnergy(torch.autograd.Function):
         return gR, gs, ge, None
 
 
+class _Busy:
+    """Marks a BatchTrajectory's buffers as holding a run awaiting backward."""
+
+    def __init__(self, tr):
+        self.tr = tr
+        tr.busy = True
+
+    def __del__(self):
+        self.tr.busy = False
+
+
 class _BatchTrajectoryFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, R0, P0, sigma, epsilon, cfg):
@@ -521,7 +532,9 @@ class _BatchTrajectoryFn(torch.autograd.Function):
             raise RuntimeError('a batched neighbour list overflowed during the trajectory; '
                                'allocate it with more capacity')
         if any(ctx.needs_input_grad[:4]):
-            tr.busy = True   # the recorded trajectory must survive until backward
+            # the recorded trajectory must survive until backward; the lease is
+            # released by backward or when the autograd graph is freed
+            ctx.lease = _Busy(tr)
         ctx.cfg = (tr, sysd, species, buf)
         ctx.has = (sigma is not None, epsilon is not None)
         ctx.save_for_backward(sigma if sigma is not None else torch.empty(0),
@@ -561,7 +574,7 @@ class _BatchTrajectoryFn(torch.autograd.Function):
                 buf['rec'].data_ptr(), bins.data_ptr() if want else None, 1, N.stream_ptr()),
                 'batch_nve_adjoint_segment')
         gs, ge = _bins_to_grads(bins, None, sigma, epsilon) if want else (None, None)
-        tr.busy = False
+        ctx.lease = None
         return buf['xbar'][:, :dim].clone(), buf['pbar'][:, :dim].clone(), gs, ge, None
 
 
