@@ -479,6 +479,17 @@ int jmd_nvt_run(const jmd_nve_system* sys, const jmd_nvt* nvt, int64_t n_steps,
 int jmd_nvt_run_sorted(const jmd_nve_system* sys, const jmd_sorted_state* sorted,
                        const jmd_nvt* nvt, int64_t n_steps, int32_t use_graph, void* stream);
 
+/* jmd_pair_force_vjp for Sparse / OrderedSparse lists (idx [2, idx_ld]:
+ * row 0 receivers, row 1 senders; padding entries >= n are skipped).  Same
+ * outputs and bins; grad_position is accumulated with atomics. */
+int jmd_pair_force_vjp_sparse(const jmd_pair* pp, const jmd_space* space, int32_t format,
+                              const float* position, int64_t pos_stride,
+                              const int32_t* species, int64_t n, const int32_t* idx,
+                              int64_t idx_ld, int64_t idx_width, const float* cotangent,
+                              int64_t cot_stride, float weight, float* grad_position,
+                              int64_t grad_stride, double* grad_params,
+                              double* grad_energy_params, void* stream);
+
 /* ------------------------------------------------------ engine adjoint -- */
 
 /* jmd_nve_run with the positions recorded: `trajectory` (optional) holds

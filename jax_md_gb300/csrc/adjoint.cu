@@ -287,6 +287,118 @@ void step_launch(int tpa, bool sp, bool params, const StepArgs& a, const PairTab
   }
 }
 
+// ------------------------------------------------------ Sparse-list VJP --
+// One thread per entry of a Sparse / OrderedSparse list (idx[0] receivers j,
+// idx[1] senders i, smap.py:967-977): the entry carries c = 1/2 (Sparse) or
+// 1 (OrderedSparse) of the pair energy with the parameters of (s_i, s_j), so
+//   gR_i += c J (lam_j - lam_i),  gR_j -= c J (lam_j - lam_i)   (atomics)
+//   dL/d theta[s_i][s_j] += c (dg/d theta) (lam_j - lam_i) . (R_i - R_j).
+struct SparseVjpArgs {
+  const float* x;
+  int64_t xs;
+  const int32_t* species;
+  int n;
+  const int32_t* idx;
+  int64_t ld;
+  int64_t width;
+  const float* lam;
+  int64_t ls;
+  float* gx;
+  int64_t gs;
+  float weight;
+  float c;
+  double* gp;
+  double* ge;
+  Geo geo;
+  int per_pair;
+};
+
+template <int DIM, int KIND, bool SPECIES, bool EGRAD>
+__global__ void __launch_bounds__(256) k_force_vjp_sparse(SparseVjpArgs a,
+                                                          const __grid_constant__ PairTable tab,
+                                                          const __grid_constant__ PairTable sig) {
+  constexpr int NB = SPECIES ? JMD_MAX_SPECIES : 1;
+  __shared__ float bins[kBins];
+  __shared__ float ebins[EGRAD ? kBins : 1];
+  zero_bins(bins);
+  if (EGRAD) zero_bins(ebins);
+  __syncthreads();
+  BinAcc<NB> acc, eacc;
+  acc.zero();
+  eacc.zero();
+  const bool per_pair = a.per_pair != 0;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int si = 0;
+  if (e < a.width) {
+    const int j = __ldg(a.idx + e);
+    const int i = __ldg(a.idx + a.ld + e);
+    if ((unsigned)j < (unsigned)a.n && (unsigned)i < (unsigned)a.n) {
+      const float4 xi = load_row<DIM, false>(a.x, a.xs, i);
+      const float4 xj = load_row<DIM, false>(a.x, a.xs, j);
+      float dx, dy, dz;
+      displacement<DIM>(xi, xj, a.geo, dx, dy, dz);   // R_i - R_j
+      const float r2 = dx * dx + dy * dy + (DIM == 3 ? dz * dz : 0.f);
+      si = SPECIES ? min(max(__ldg(a.species + i), 0), tab.nsp - 1) : 0;
+      const int sj = SPECIES ? min(max(__ldg(a.species + j), 0), tab.nsp - 1) : 0;
+      const int bin = si * JMD_MAX_SPECIES + sj;
+      const PairCoef& c = tab.c[SPECIES ? bin : 0];
+      if (r2 < c.rc2 && r2 > 0.f) {
+        const float sigma = sig.c[SPECIES ? bin : 0].pad;
+        const PairD q = pair_derivs<KIND>(r2, c, sigma, per_pair ? sigma : sig.pad);
+        const float4 li = load_row<DIM, false>(a.lam, a.ls, i);
+        const float4 lj = load_row<DIM, false>(a.lam, a.ls, j);
+        const float ex = lj.x - li.x, ey = lj.y - li.y, ez = DIM == 3 ? lj.z - li.z : 0.f;
+        const float t = dx * ex + dy * ey + dz * ez;
+        const float cdd = (q.hh - q.g) / r2 * t;
+        if (a.gx) {
+          const float w = a.weight * a.c;
+          const float gx = w * (q.g * ex + cdd * dx), gy = w * (q.g * ey + cdd * dy);
+          const float gz = DIM == 3 ? w * (q.g * ez + cdd * dz) : 0.f;
+          float* oi = a.gx + (int64_t)i * a.gs;
+          float* oj = a.gx + (int64_t)j * a.gs;
+          atomicAdd(oi, gx);
+          atomicAdd(oi + 1, gy);
+          atomicAdd(oj, -gx);
+          atomicAdd(oj + 1, -gy);
+          if (DIM == 3) {
+            atomicAdd(oi + 2, gz);
+            atomicAdd(oj + 2, -gz);
+          }
+        }
+        const float ct = a.c * t;
+        acc.add(sj, q.dg_s * ct, q.dg_e * ct, KIND == JMD_LJ ? q.dg_k * ct : 0.f, per_pair);
+        if (EGRAD)
+          eacc.add(sj, a.c * q.dU_s, a.c * q.dU_e, KIND == JMD_LJ ? a.c * q.dU_k : 0.f, per_pair);
+      }
+    }
+  }
+  const int ncol = SPECIES ? tab.nsp : 1;
+  if (!SPECIES) {
+    acc.group_sum(kWarp, 1);
+    if (EGRAD) eacc.group_sum(kWarp, 1);
+  }
+  if (SPECIES || (threadIdx.x & (kWarp - 1)) == 0) {
+    acc.flush(bins, si, ncol);
+    if (EGRAD) eacc.flush(ebins, si, ncol);
+  }
+  __syncthreads();
+  publish_bins(bins, a.gp, (double)a.weight);
+  if (EGRAD) publish_bins(ebins, a.ge, 1.0);
+}
+
+template <int DIM, int KIND>
+void svjp_launch(bool sp, bool eg, const SparseVjpArgs& a, const PairTable& t,
+                 const PairTable& s, cudaStream_t st) {
+  const unsigned grid = (unsigned)std::max<int64_t>(1, ceil_div(a.width, 256));
+  if (sp) {
+    if (eg) k_force_vjp_sparse<DIM, KIND, true, true><<<grid, 256, 0, st>>>(a, t, s);
+    else k_force_vjp_sparse<DIM, KIND, true, false><<<grid, 256, 0, st>>>(a, t, s);
+  } else {
+    if (eg) k_force_vjp_sparse<DIM, KIND, false, true><<<grid, 256, 0, st>>>(a, t, s);
+    else k_force_vjp_sparse<DIM, KIND, false, false><<<grid, 256, 0, st>>>(a, t, s);
+  }
+}
+
 }  // namespace
 
 // Host side of the engine's reverse step (declared in pair.cuh).
@@ -396,6 +508,55 @@ int jmd_pair_force_vjp(const jmd_pair* pp, const jmd_space* space, const float* 
     else vjp_launch<2, JMD_SOFT_SPHERE>(sp, eg, a, t, sg, st);
   }
   return check_launch("jmd_pair_force_vjp");
+}
+
+int jmd_pair_force_vjp_sparse(const jmd_pair* pp, const jmd_space* space, int32_t format,
+                              const float* position, int64_t pos_stride, const int32_t* species,
+                              int64_t n, const int32_t* idx, int64_t idx_ld, int64_t idx_width,
+                              const float* cotangent, int64_t cot_stride, float weight,
+                              float* grad_position, int64_t grad_stride, double* grad_params,
+                              double* grad_energy_params, void* stream) {
+  int e = validate_pair(pp);
+  if (e) return e;
+  JMD_REQUIRE(space && (space->dim == 2 || space->dim == 3), "bad space");
+  JMD_REQUIRE(format == JMD_SPARSE || format == JMD_ORDERED_SPARSE, "format must be Sparse or OrderedSparse");
+  JMD_REQUIRE(n >= 0 && n < INT32_MAX, "atom count out of range");
+  JMD_REQUIRE(idx_ld >= idx_width, "idx_ld must be >= idx_width");
+  JMD_REQUIRE(cotangent != nullptr, "cotangent is null");
+  JMD_REQUIRE(pp->n_species == 0 || species != nullptr, "species matrices need a species array");
+  if (n <= 0 || idx_width <= 0) return JMD_OK;
+  const PairTable t = make_pair_table(*pp);
+  const PairTable sg = sigma_table(*pp);
+  SparseVjpArgs a{};
+  a.x = position;
+  a.xs = pos_stride;
+  a.species = species;
+  a.n = (int)n;
+  a.idx = idx;
+  a.ld = idx_ld;
+  a.width = idx_width;
+  a.lam = cotangent;
+  a.ls = cot_stride;
+  a.gx = grad_position;
+  a.gs = grad_stride;
+  a.weight = weight;
+  a.c = format == JMD_ORDERED_SPARSE ? 1.f : 0.5f;
+  a.gp = grad_params;
+  a.ge = grad_energy_params;
+  a.geo = make_geo(*space);
+  a.per_pair = pp->per_pair_cutoff;
+  const bool sp = pp->n_species > 0, eg = grad_energy_params != nullptr;
+  cudaStream_t st = as_stream(stream);
+  if (space->dim == 3) {
+    if (pp->kind == JMD_LJ) svjp_launch<3, JMD_LJ>(sp, eg, a, t, sg, st);
+    else if (pp->kind == JMD_LJ_TRUNCATED) svjp_launch<3, JMD_LJ_TRUNCATED>(sp, eg, a, t, sg, st);
+    else svjp_launch<3, JMD_SOFT_SPHERE>(sp, eg, a, t, sg, st);
+  } else {
+    if (pp->kind == JMD_LJ) svjp_launch<2, JMD_LJ>(sp, eg, a, t, sg, st);
+    else if (pp->kind == JMD_LJ_TRUNCATED) svjp_launch<2, JMD_LJ_TRUNCATED>(sp, eg, a, t, sg, st);
+    else svjp_launch<2, JMD_SOFT_SPHERE>(sp, eg, a, t, sg, st);
+  }
+  return check_launch("jmd_pair_force_vjp_sparse");
 }
 
 }  // extern "C"

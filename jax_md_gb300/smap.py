@@ -259,8 +259,6 @@ class PairNeighborListEnergy:
                               _param_tensor(dynamic.get('epsilon')), self, neighbor, dynamic)
 
     def _vjp_launch(self, R, neighbor, lam, weight, gR, gp, ge, **dynamic):
-        if neighbor.format is not partition.Dense:
-            raise NotImplementedError('the force VJP kernel runs on Dense lists')
         R, rs = partition._rows(R)
         n, dim = R.shape
         species, pair = self._resolve(R, dynamic)
@@ -268,6 +266,16 @@ class PairNeighborListEnergy:
         idx = neighbor.idx
         if lam.stride(-1) != 1:
             lam = lam.contiguous()
+        if neighbor.format is not partition.Dense:
+            fmt = N.SPARSE if neighbor.format is partition.Sparse else N.ORDERED_SPARSE
+            if idx.dtype != torch.int32 or idx.stride(1) != 1:
+                idx = idx.to(torch.int32).contiguous()
+            N.check(N.lib().jmd_pair_force_vjp_sparse(
+                ctypes.byref(pair), ctypes.byref(sp), fmt, R.data_ptr(), rs, N.ptr(species), n,
+                idx.data_ptr(), idx.stride(0), idx.shape[1], lam.data_ptr(), lam.stride(0),
+                float(weight), N.ptr(gR), gR.stride(0) if gR is not None else 0, N.ptr(gp),
+                N.ptr(ge), N.stream_ptr()), 'pair_force_vjp_sparse')
+            return
         cnt = getattr(neighbor, 'nbr_count', None)
         N.check(N.lib().jmd_pair_force_vjp(
             ctypes.byref(pair), ctypes.byref(sp), R.data_ptr(), rs, N.ptr(species), n,
