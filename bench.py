@@ -178,6 +178,8 @@ def batched_section(dev, n_sys=512, fire_steps=200, nve_steps=200, seed=0, use_g
     fns = batch.neighbor_list(1.4, 0.2)
     nb = fns.allocate(bt, extra_capacity=4)
     run = batch.BatchRunner(bt, fns, nb, batch.BatchPairEnergy(efn), dt=0.01)
+    run.fire_init(0.0)
+    tuned = batch.autotune(run, steps=20)      # launch shapes of the batched kernels
     x0, f0 = bt.position.clone(), run.force.clone()
     cur = torch.cuda.current_stream(dev)
 
@@ -208,6 +210,7 @@ def batched_section(dev, n_sys=512, fire_steps=200, nve_steps=200, seed=0, use_g
     overflow = nb.did_buffer_overflow
     if not with_plain:
         return {'workload': f'{n_sys} 2D bidisperse soft-sphere systems (total {n_tot})',
+                'autotune': tuned,
                 'batched_fire_atom_steps_per_s': n_tot * fire_steps / t_bfire,
                 'batched_nve_atom_steps_per_s': n_tot * nve_steps / t_bnve,
                 'launch': 'cuda graph' if use_graph else 'direct', 'overflow': overflow}
@@ -244,7 +247,7 @@ def batched_section(dev, n_sys=512, fire_steps=200, nve_steps=200, seed=0, use_g
     return {
         'workload': f'{n_sys} 2D bidisperse soft-sphere systems, N~U[64,4096] (total {n_tot}), '
                     'phi=0.84, skin 0.2, FIRE then NVE kT=1e-4 dt=0.01',
-        'fire_steps': fire_steps, 'nve_steps': nve_steps,
+        'fire_steps': fire_steps, 'nve_steps': nve_steps, 'autotune': tuned,
         'batched_fire_atom_steps_per_s': n_tot * fire_steps / t_bfire,
         'plain_fire_atom_steps_per_s': n_tot * fire_steps / t_pfire,
         'fire_speedup': t_pfire / t_bfire,

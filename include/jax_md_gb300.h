@@ -637,6 +637,12 @@ int jmd_batch_nve_run(const jmd_batch_system* sys, int64_t n_steps, int32_t use_
 int jmd_batch_fire_run(const jmd_batch_system* sys, const jmd_fire_params* fp,
                        int64_t n_steps, int32_t use_graph, void* stream);
 
+/* Launch shapes of the batched kernels (the batch autotuner's choice):
+ * threads per CTA of the force kernels (64, 128, 256; default 128) and
+ * threads per system of the FIRE update (256, 512, 1024; default 1024).
+ * Library-wide; cached graphs are keyed by them. */
+int jmd_batch_set_launch(int force_block, int fire_threads);
+
 /* Adjoint of a batched NVE run: the batched forms of jmd_nve_run_recorded and
  * jmd_nve_adjoint_segment (same slot layout, same recurrences; each atom
  * uses its system's box; grad_params bins are summed over all systems, the

@@ -172,6 +172,7 @@ SIGNATURES = {
     'jmd_batch_fire_init': (C.c_int, [C.POINTER(BatchSystem), C.POINTER(FireParams), P]),
     'jmd_batch_nve_run': (C.c_int, [C.POINTER(BatchSystem), I64, I32, P]),
     'jmd_batch_fire_run': (C.c_int, [C.POINTER(BatchSystem), C.POINTER(FireParams), I64, I32, P]),
+    'jmd_batch_set_launch': (C.c_int, [C.c_int, C.c_int]),
     'jmd_batch_nve_run_recorded': (C.c_int, [C.POINTER(BatchSystem), P, I64, I32, I32, P]),
     'jmd_batch_nve_adjoint_segment': (C.c_int, [C.POINTER(BatchSystem), P, I64, I32, I32, P, P, P,
                                                 P, I32, P]),

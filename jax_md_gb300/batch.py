@@ -625,3 +625,48 @@ class BatchTrajectory:
             dyn['epsilon'] = epsilon
         return _BatchTrajectoryFn.apply(R0, P0, _param_tensor(sigma), _param_tensor(epsilon),
                                         (self, dyn))
+
+
+FORCE_BLOCKS = (64, 128, 256)
+FIRE_THREADS = (256, 512, 1024)
+
+
+def set_launch(force_block: int = 128, fire_threads: int = 1024):
+    """Launch shapes of the batched kernels (jmd_batch_set_launch)."""
+    N.check(N.lib().jmd_batch_set_launch(int(force_block), int(fire_threads)), 'batch_set_launch')
+
+
+def autotune(runner: BatchRunner, steps: int = 20) -> dict:
+    """Times ``steps`` graph-replayed FIRE steps of the runner's batch for every
+    launch shape (force CTA size x FIRE-update threads per system), each from
+    the same starting state, keeps the fastest and returns the timings (ms).
+    The runner's state is restored afterwards."""
+    bt, nb = runner.batch, runner.nbrs
+    saved = [t.clone() for t in (bt.position, runner.momentum, runner.force, runner.fire_state,
+                                 runner.done, runner.n_done)]
+
+    def restore():
+        for t, v in zip((bt.position, runner.momentum, runner.force, runner.fire_state,
+                         runner.done, runner.n_done), saved):
+            t.copy_(v)
+        runner.neighbor_fns._build(nb, bt.position)
+
+    times = {}
+    stream = torch.cuda.current_stream(bt.device)
+    for fb in FORCE_BLOCKS:
+        for ft in FIRE_THREADS:
+            set_launch(fb, ft)
+            restore()
+            runner.fire(steps)                      # records this shape's graph
+            restore()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            runner.fire(steps)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times[(fb, ft)] = e0.elapsed_time(e1)
+    best = min(times, key=times.get)
+    set_launch(*best)
+    restore()
+    return {'best': best, 'ms': {f'{k[0]}x{k[1]}': v for k, v in times.items()}}

@@ -307,7 +307,7 @@ struct BForceArgs {
 
 // One thread per atom over the tiled list; each atom uses its system's box.
 template <int DIM, int KIND, bool SPECIES, int MODE>
-__global__ void __launch_bounds__(128) k_bforce(BatchView v, BForceArgs a,
+__global__ void __launch_bounds__(256) k_bforce(BatchView v, BForceArgs a,
                                                 const __grid_constant__ PairTable tab) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= v.n) return;
@@ -476,7 +476,11 @@ __global__ void __launch_bounds__(256) k_bkick_drift(BatchView v, float4* x, flo
 // FIRE after the force: closing half kick, the three f64 reductions, the
 // scalar update of minimize.py:190-224, the mixing, and the convergence test
 // on the largest atom force norm.  One CTA per system.
-constexpr int kFireThreads = 1024;
+constexpr int kFireThreads = 1024;  // upper bound; the launch uses g_fire_threads
+
+// Launch shapes chosen by the batch autotuner (jmd_batch_set_launch).
+int g_force_block = 128;
+int g_fire_threads = 1024;
 
 template <int DIM>
 __global__ void __launch_bounds__(kFireThreads) k_bfire_update(BatchView v, float4* p, const float4* __restrict__ f,
@@ -813,9 +817,10 @@ int skin_impl(const jmd_batch& b, const jmd_batch_nlist& nl, const float* x, flo
 template <int DIM, int KIND, bool SP>
 void force_launch3(int mode, const BatchView& v, const BForceArgs& a, const PairTable& t,
                    unsigned gr, cudaStream_t st) {
-  if (mode == B_KICK) k_bforce<DIM, KIND, SP, B_KICK><<<gr, 128, 0, st>>>(v, a, t);
-  else if (mode == B_FIRE) k_bforce<DIM, KIND, SP, B_FIRE><<<gr, 128, 0, st>>>(v, a, t);
-  else k_bforce<DIM, KIND, SP, B_FORCE><<<gr, 128, 0, st>>>(v, a, t);
+  const int bs = g_force_block;
+  if (mode == B_KICK) k_bforce<DIM, KIND, SP, B_KICK><<<gr, bs, 0, st>>>(v, a, t);
+  else if (mode == B_FIRE) k_bforce<DIM, KIND, SP, B_FIRE><<<gr, bs, 0, st>>>(v, a, t);
+  else k_bforce<DIM, KIND, SP, B_FORCE><<<gr, bs, 0, st>>>(v, a, t);
 }
 
 template <int DIM, int KIND>
@@ -838,7 +843,7 @@ int force_impl(const jmd_pair& pp, const jmd_batch& b, const jmd_batch_nlist& nl
   BForceArgs a{reinterpret_cast<const float4*>(x), reinterpret_cast<float4*>(f),
                reinterpret_cast<float4*>(p), species, nl.idx, nl.count, nl.ld, h, done};
   const bool sp = pp.n_species > 0 && species != nullptr;
-  const unsigned gr = (unsigned)ceil_div(b.n_atoms, 128);
+  const unsigned gr = (unsigned)ceil_div(b.n_atoms, g_force_block);
   const int ns = b.n_systems;
   if (b.dim == 3) {
     if (pp.kind == JMD_LJ) force_launch2<3, JMD_LJ>(mode, sp, v, a, t, gr, energy, ns, st);
@@ -924,9 +929,9 @@ int enqueue_batch_run(const jmd_batch_system& s, const jmd_fire_params* fp, int6
     if (rc) return rc;
     if (fire) {
       if (b.dim == 3)
-        k_bfire_update<3><<<b.n_systems, kFireThreads, 0, st>>>(v, p, f, s.fire_state, s.done, s.n_done, *fp);
+        k_bfire_update<3><<<b.n_systems, g_fire_threads, 0, st>>>(v, p, f, s.fire_state, s.done, s.n_done, *fp);
       else
-        k_bfire_update<2><<<b.n_systems, kFireThreads, 0, st>>>(v, p, f, s.fire_state, s.done, s.n_done, *fp);
+        k_bfire_update<2><<<b.n_systems, g_fire_threads, 0, st>>>(v, p, f, s.fire_state, s.done, s.n_done, *fp);
       JMD_CUDA(cudaGetLastError());
     }
     if (traj) JMD_CUDA(cudaMemcpyAsync(slot(k + 1), s.position, rows, cudaMemcpyDeviceToDevice, st));
@@ -996,6 +1001,8 @@ int run_impl(const jmd_batch_system* sys, const jmd_fire_params* fp, int64_t n_s
   JMD_CUDA(cudaGetDevice(&device));
   std::string key(what);
   key.append(reinterpret_cast<const char*>(sys), sizeof(*sys));
+  const int shape[2] = {g_force_block, g_fire_threads};   // baked into the graph
+  key.append(reinterpret_cast<const char*>(shape), sizeof(shape));
   if (fp) key.append(reinterpret_cast<const char*>(fp), sizeof(*fp));
   key.append(reinterpret_cast<const char*>(&n_steps), sizeof(n_steps));
   key.append(reinterpret_cast<const char*>(&device), sizeof(device));
@@ -1017,6 +1024,8 @@ int graph_or_direct(const std::string& key, const std::function<int(cudaStream_t
   JMD_CUDA(cudaGetDevice(&device));
   std::string k = key;
   k.append(reinterpret_cast<const char*>(&device), sizeof(device));
+  const int shape[2] = {g_force_block, g_fire_threads};
+  k.append(reinterpret_cast<const char*>(shape), sizeof(shape));
   return graph_launch_cached(k, [&](cudaStream_t cs, cudaStream_t bs) { return enq(cs, bs, true); },
                              st);
 }
@@ -1027,6 +1036,16 @@ int graph_or_direct(const std::string& key, const std::function<int(cudaStream_t
 using namespace jmd;
 
 extern "C" {
+
+int jmd_batch_set_launch(int force_block, int fire_threads) {
+  JMD_REQUIRE(force_block == 64 || force_block == 128 || force_block == 256,
+              "force_block must be 64, 128 or 256");
+  JMD_REQUIRE(fire_threads == 256 || fire_threads == 512 || fire_threads == 1024,
+              "fire_threads must be 256, 512 or 1024");
+  g_force_block = force_block;
+  g_fire_threads = fire_threads;
+  return JMD_OK;
+}
 
 int jmd_batch_nve_run_recorded(const jmd_batch_system* sys, float* trajectory, int64_t n_steps,
                                int32_t force_rebuild, int32_t use_graph, void* stream) {

@@ -333,3 +333,24 @@ def test_batch_trajectory_gradient_matches_fd(cuda, k):
     fd = (sp[0] - sp[1]) / (2 * e_r)
     ad = float((R0.grad.cpu().numpy() * v).sum())
     assert abs(ad - fd) <= 1e-3 * max(abs(fd), 1e-2), (ad, fd)
+
+
+def test_batch_autotune(cuda):
+    """The batch autotuner times every launch shape, leaves the runner's state
+    as it found it, and the forces do not depend on the force CTA size."""
+    from jax_md_gb300 import batch
+    systems, bt, fns, nb, ef = _ss_batch(cuda, sizes=[64, 300, 777])
+    run = batch.BatchRunner(bt, fns, nb, ef)
+    run.fire_init(0.0)
+    x0 = bt.position.clone()
+    r = batch.autotune(run, steps=5)
+    assert len(r['ms']) == len(batch.FORCE_BLOCKS) * len(batch.FIRE_THREADS)
+    assert r['best'][0] in batch.FORCE_BLOCKS and r['best'][1] in batch.FIRE_THREADS
+    assert torch.equal(bt.position, x0)
+    F = {}
+    for fb in batch.FORCE_BLOCKS:
+        batch.set_launch(fb, 1024)
+        F[fb] = ef.forces(bt, nb).clone()
+    torch.cuda.synchronize()
+    assert torch.equal(F[64], F[128]) and torch.equal(F[128], F[256])
+    batch.set_launch(*r['best'])
