@@ -2,7 +2,8 @@
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the product (``jax_md_gb300``) imports
 this module; only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline
-leg of ``bench.py`` may use it, and only as the checker.
+leg of ``bench.py`` may use it, and only to check results or as the timed CPU
+baseline, never in place of a kernel.
 
 Every function restates the reference algorithm in plain NumPy and cites the
 reference file:line it follows (paths relative to the jax_md project root).
