@@ -276,6 +276,18 @@ int jmd_nhc_half_step(const jmd_nhc* c, double* chain,
                       const double* kinetic_energy, int32_t update_mass,
                       double* p_scale, void* stream);
 
+/* Reverse of jmd_nhc_half_step (the adjoint of simulate.nvt_nose_hoover's
+ * chain, simulate.py:444-507): from the chain state before the half step
+ * (chain, 66 doubles, unchanged), the kinetic energy it used and the
+ * cotangents of its outputs (cot_p_xi [chain_length] of the chain momenta
+ * after it, cot_scale of the momentum scale), writes grad_p_xi
+ * [chain_length] and grad_kinetic_energy.  Forward-mode dual numbers in one
+ * thread; chain_length <= 7. */
+int jmd_nhc_half_step_vjp(const jmd_nhc* c, const double* chain,
+                          const double* kinetic_energy, int32_t update_mass,
+                          const double* cot_p_xi, const double* cot_scale,
+                          double* grad_p_xi, double* grad_kinetic_energy, void* stream);
+
 /* FIRE (minimize.fire_descent, minimize.py:124-226) on float4 rows with the
  * minimiser's scalars kept on the device: fire_state[6] floats
  * {dt, alpha, n_pos, keep, alpha_mix, |P|/|F|}, initialised by the caller to

@@ -31,10 +31,11 @@ from __future__ import annotations
 import ctypes
 from typing import Optional
 
+import numpy as np
 import torch
 
 from . import _native as N
-from . import partition, simulate, smap
+from . import partition, quantity, simulate, smap
 from .smap import _bins_to_grads, _param_tensor
 
 
@@ -221,3 +222,165 @@ def nve_trajectory(energy_fn, neighbor_fn, shift_fn, dt: float, n_steps: int,
     the whole trajectory on the device when it fits in a quarter of free memory
     and otherwise splits the run into the longest segments that do."""
     return Trajectory(energy_fn, neighbor_fn, shift_fn, dt, n_steps, checkpoint_every, mass)
+
+
+# ---------------------------------------------------------------------------
+# Nose-Hoover NVT (simulate.py:565-669)
+#
+# Forward step k from (x_k, p_k, chain_k), H the chain half step:
+#     (chain', s1) = H(chain_k, KE(p_k))          update_mass, as apply_fn
+#     q = s1 p_k + h F(x_k);  x_{k+1} = shift(x_k, dt q / m);  r = q + h F(x_{k+1})
+#     (chain_{k+1}, s2) = H(chain', KE(r));  p_{k+1} = s2 r
+# Reverse, with the chain cotangent pxibar (the chain momenta) and
+# J_H^T from jmd_nhc_half_step_vjp:
+#     sbar2 = pbar . r;  rbar = s2 pbar;  (pxibar', kebar) = J_H^T(pxibar, sbar2)
+#     rbar += kebar r / m
+#     xbar += VJP(x_{k+1}, h (rbar + qbar_{k+1}))      both kicks at x_{k+1}
+#     qbar = rbar + (dt/m) xbar;  sbar1 = qbar . p_k;  pbar = s1 qbar
+#     (pxibar, kebar) = J_H^T(pxibar', sbar1);  pbar += kebar p_k / m
+# and finally xbar += VJP(x_0, h qbar_0).
+
+
+class _NvtTrajectoryFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, R0, P0, sigma, epsilon, cfg):
+        tf, nbrs, dyn = cfg
+        init, apply = tf.integrator
+        stepper, chain_fns = apply.stepper, apply.chain_fns
+        R0d, P0d = R0.detach(), P0.detach()
+        dim = R0d.shape[1]
+        nb = rebuild_now(tf.neighbor_fn, nbrs, simulate._rows4(R0d))
+        st = init(0, R0d, mass=tf.mass, momenta=P0d.clone(), neighbor=nb, **dyn)
+        scale = torch.empty((), dtype=torch.float64, device=R0d.device)
+        P = st.momentum
+        tape = []
+        for _ in range(tf.n_steps):
+            nb = nb.update(st.position)
+            x_k, p_k = st.position.clone(), st.momentum.clone()
+            chain_a = st.chain.buffer.clone()
+            chain_fns.half_step(st.chain, scale, update_mass=True)
+            s1 = scale.clone()
+            stepper.velocity_verlet(st, p_scale=scale, neighbor=nb, **dyn)
+            r = st.momentum.clone()
+            quantity._ke_f64(st.momentum, st.mass, out=st.chain.buffer[64])
+            chain_b = st.chain.buffer.clone()
+            chain_fns.half_step(st.chain, scale, ke=None)
+            s2 = scale.clone()
+            N.check(N.lib().jmd_scale_momentum(P.data_ptr(), P.stride(0), P.shape[0], dim,
+                                               scale.data_ptr(), N.stream_ptr()), 'scale_momentum')
+            tape.append((x_k, p_k, chain_a, s1, r, chain_b, s2))
+        if bool(nb.did_buffer_overflow):
+            raise RuntimeError('neighbour list overflowed during the trajectory; allocate it '
+                               'with more capacity')
+        ctx.cfg = (tf, nb, dyn, tape, st.position.clone(), st.chain, st.mass)
+        ctx.has = (sigma is not None, epsilon is not None)
+        ctx.save_for_backward(sigma if sigma is not None else torch.empty(0),
+                              epsilon if epsilon is not None else torch.empty(0))
+        return st.position.clone(), st.momentum.clone()
+
+    @staticmethod
+    def backward(ctx, gx, gp):
+        tf, nb, dyn, tape, x_n, chain, mass = ctx.cfg
+        sigma, epsilon = ctx.saved_tensors
+        sigma = sigma if ctx.has[0] else None
+        epsilon = epsilon if ctx.has[1] else None
+        n, dim = x_n.shape
+        dev = x_n.device
+        dt = float(np.float32(tf.dt))
+        h = float(np.float32(dt / 2))
+        inv_m = (1.0 / mass[:, None]) if isinstance(mass, torch.Tensor) else 1.0 / float(mass)
+        xbar = torch.zeros((n, 4), dtype=torch.float32, device=dev)[:, :dim]
+        if gx is not None:
+            xbar += gx
+        pbar = torch.zeros((n, dim), dtype=torch.float32, device=dev)
+        if gp is not None:
+            pbar += gp
+        bins = torch.zeros(130, dtype=torch.float64, device=dev)
+        c = N.Nhc()
+        c.chain_length, c.chain_steps, c.sy_steps = (tf.chain_length, tf.chain_steps,
+                                                      tf.sy_steps)
+        c.dof, c.dt, c.tau = chain.degrees_of_freedom, tf.dt32, chain.tau
+        pxibar = torch.zeros(16, dtype=torch.float64, device=dev)
+        pxibar1 = torch.zeros(16, dtype=torch.float64, device=dev)
+        kebar = torch.zeros((), dtype=torch.float64, device=dev)
+        L = N.lib()
+
+        def chain_vjp(chain_in, update_mass, cot_p, cot_s, out_p):
+            N.check(L.jmd_nhc_half_step_vjp(ctypes.byref(c), chain_in.data_ptr(),
+                                            chain_in[64:].data_ptr(), update_mass,
+                                            cot_p.data_ptr(), cot_s.data_ptr(), out_p.data_ptr(),
+                                            kebar.data_ptr(), N.stream_ptr()),
+                    'nhc_half_step_vjp')
+
+        def vjp_at(x, lam):
+            nonlocal nb
+            nb = nb.update(x)
+            tf.energy_fn.force_vjp(x, nb, lam.contiguous(), 1.0, grad_R=xbar, grad_params=bins,
+                                   **dyn)
+
+        pending = None
+        for k in range(len(tape) - 1, -1, -1):
+            x_k, p_k, chain_a, s1, r, chain_b, s2 = tape[k]
+            x1 = tape[k + 1][0] if k + 1 < len(tape) else x_n
+            sbar2 = (pbar.double() * r.double()).sum()
+            rbar = pbar * s2.float()
+            chain_vjp(chain_b, 0, pxibar, sbar2, pxibar1)
+            rbar = rbar + (kebar.float() * r) * inv_m
+            lam = h * (rbar if pending is None else rbar + pending)
+            vjp_at(x1, lam)
+            qbar = rbar + (dt * inv_m) * xbar
+            sbar1 = (qbar.double() * p_k.double()).sum()
+            pbar = qbar * s1.float()
+            chain_vjp(chain_a, 1, pxibar1, sbar1, pxibar)
+            pbar = pbar + (kebar.float() * p_k) * inv_m
+            pending = qbar
+        vjp_at(tape[0][0] if tape else x_n, h * pending if pending is not None else
+               torch.zeros((n, dim), dtype=torch.float32, device=dev))
+        gs, ge = _bins_to_grads(bins, None, sigma, epsilon)
+        return xbar.contiguous(), pbar.contiguous(), gs, ge, None
+
+
+class NvtTrajectory:
+    """``traj(R0, P0, nbrs, sigma=None, epsilon=None) -> (x_n, p_n)``: n_steps
+    of simulate.nvt_nose_hoover from (R0, P0) with a fresh chain, differentiable
+    with respect to R0, P0 and sigma / epsilon tensors that require grad,
+    through the reverse pass of the chain (jmd_nhc_half_step_vjp) and of the
+    Verlet step (jmd_pair_force_vjp).  Every step is recorded (positions,
+    momenta and the chain), so memory grows with n_steps."""
+
+    def __init__(self, energy_fn, neighbor_fn, shift_fn, dt, kT, n_steps, chain_length=5,
+                 chain_steps=2, sy_steps=3, tau=None, mass=1.0):
+        if not isinstance(energy_fn, smap.PairNeighborListEnergy):
+            raise NotImplementedError('nvt_trajectory needs a neighbour-list energy from '
+                                      'jax_md_gb300.energy')
+        if not 2 <= int(chain_length) <= 7:
+            raise NotImplementedError('the chain adjoint supports chain_length 2..7')
+        if int(n_steps) < 1:
+            raise ValueError('n_steps must be >= 1')
+        self.energy_fn, self.neighbor_fn, self.shift_fn = energy_fn, neighbor_fn, shift_fn
+        self.dt, self.kT, self.n_steps = dt, kT, int(n_steps)
+        self.dt32 = float(np.float32(dt))
+        self.chain_length, self.chain_steps, self.sy_steps = (int(chain_length), int(chain_steps),
+                                                              int(sy_steps))
+        self.mass = mass
+        self.integrator = simulate.nvt_nose_hoover(energy_fn, shift_fn, dt, kT, chain_length,
+                                                   chain_steps, sy_steps, tau)
+
+    def __call__(self, R0, P0, nbrs, sigma=None, epsilon=None):
+        if nbrs.format is not partition.Dense:
+            raise NotImplementedError('the trajectory adjoint runs on Dense neighbour lists')
+        dyn = {}
+        if sigma is not None:
+            dyn['sigma'] = sigma
+        if epsilon is not None:
+            dyn['epsilon'] = epsilon
+        return _NvtTrajectoryFn.apply(R0, P0, _param_tensor(sigma), _param_tensor(epsilon),
+                                      (self, nbrs, dyn))
+
+
+def nvt_trajectory(energy_fn, neighbor_fn, shift_fn, dt: float, kT: float, n_steps: int,
+                   chain_length: int = 5, chain_steps: int = 2, sy_steps: int = 3, tau=None,
+                   mass=1.0) -> NvtTrajectory:
+    """Differentiable Nose-Hoover NVT run (see NvtTrajectory)."""
+    return NvtTrajectory(energy_fn, neighbor_fn, shift_fn, dt, kT, n_steps, chain_length,
+                         chain_steps, sy_steps, tau, mass)

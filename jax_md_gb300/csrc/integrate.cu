@@ -185,6 +185,94 @@ __device__ void nhc_substep(T delta, T* xi, T* p, const T* Q, T& KE, T& scale_to
   p[M] += d4 * G;
 }
 
+// Forward-mode dual number with 8 tangents: the chain half step run on it
+// gives the Jacobian of (p_xi', scale) with respect to (p_xi, KE) in one
+// pass (chains of up to 7 thermostats).
+struct Dual8 {
+  float v;
+  float d[8];
+  __device__ Dual8() : v(0.f) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) d[i] = 0.f;
+  }
+  __device__ Dual8(float x) : v(x) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) d[i] = 0.f;
+  }
+  __device__ Dual8& operator+=(const Dual8& b) {
+    v += b.v;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) d[i] += b.d[i];
+    return *this;
+  }
+  __device__ Dual8& operator*=(const Dual8& b) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) d[i] = d[i] * b.v + v * b.d[i];
+    v *= b.v;
+    return *this;
+  }
+};
+__device__ inline Dual8 operator+(Dual8 a, const Dual8& b) { return a += b; }
+__device__ inline Dual8 operator-(const Dual8& a) {
+  Dual8 r(-a.v);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.d[i] = -a.d[i];
+  return r;
+}
+__device__ inline Dual8 operator-(const Dual8& a, const Dual8& b) { return a + (-b); }
+__device__ inline Dual8 operator*(Dual8 a, const Dual8& b) { return a *= b; }
+__device__ inline Dual8 operator/(const Dual8& a, const Dual8& b) {
+  Dual8 r(a.v / b.v);
+  const float ib = 1.f / b.v;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+  return r;
+}
+__device__ inline Dual8 exp(const Dual8& a) {
+  Dual8 r(expf(a.v));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.d[i] = r.v * a.d[i];
+  return r;
+}
+
+// Reverse of one chain half step (k_nhc_half): given the chain state before
+// it, the kinetic energy it used and the cotangents of its outputs (p_xi',
+// scale), writes the cotangents of p_xi and of the kinetic energy.
+__global__ void k_nhc_half_vjp(NhcArgs a, const double* chain, const double* ke,
+                               const double* cot_pxi, const double* cot_scale, double* out_pxi,
+                               double* out_ke) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int M1 = a.M1;
+  Dual8 xi[8], p[8], Q[8];
+  const float kT = (float)chain[65];
+  const float dof = (float)a.dof;
+  for (int m = 0; m < M1; ++m) {
+    xi[m] = Dual8((float)chain[m]);
+    p[m] = Dual8((float)chain[16 + m]);
+    p[m].d[m] = 1.f;
+    Q[m] = Dual8(a.update_mass ? kT * (float)a.tau * (float)a.tau : (float)chain[32 + m]);
+  }
+  if (a.update_mass) Q[0] = Q[0] * Dual8(dof);
+  Dual8 KE((float)*ke);
+  KE.d[M1] = 1.f;
+  Dual8 scale(1.f);
+  if (a.chain_steps == 1 && a.sy_steps == 1) {
+    nhc_substep<Dual8>(Dual8((float)a.dt), xi, p, Q, KE, scale, M1, Dual8(dof), Dual8(kT));
+  } else {
+    const float delta = (float)a.dt / (float)a.chain_steps;
+    for (int k = 0; k < a.chain_steps * a.sy_steps; ++k)
+      nhc_substep<Dual8>(Dual8(delta * (float)a.w[k % a.sy_steps]), xi, p, Q, KE, scale, M1,
+                         Dual8(dof), Dual8(kT));
+  }
+  const double cs = *cot_scale;
+  for (int j = 0; j <= M1; ++j) {
+    double g = cs * (double)scale.d[j];
+    for (int m = 0; m < M1; ++m) g += cot_pxi[m] * (double)p[m].d[j];
+    if (j < M1) out_pxi[j] = g;
+    else *out_ke = g;
+  }
+}
+
 __global__ void k_nhc_half(NhcArgs a, double* chain, const double* ke_in, double* p_scale) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   // the chain is worked on in thread-local copies (L1) and written back once:
@@ -314,6 +402,30 @@ __global__ void k_fire_mix(float4* p, const float4* f, int n, const float* fs) {
   p[i] = q;
 }
 
+// Arguments of the chain kernels; Suzuki-Yoshida weights (Yoshida 1990): the
+// values simulate.py:328-347 uses.
+NhcArgs nhc_args(const jmd_nhc& c, int32_t update_mass) {
+  static const double w3[3] = {0.828981543588751, -0.657963087177502, 0.828981543588751};
+  static const double w5[5] = {0.2967324292201065, 0.2967324292201065, -0.186929716880426,
+                               0.2967324292201065, 0.2967324292201065};
+  static const double w7[7] = {0.784513610477560, 0.235573213359357, -1.17767998417887,
+                               1.31518632068391, -1.17767998417887, 0.235573213359357,
+                               0.784513610477560};
+  NhcArgs a;
+  a.M1 = c.chain_length;
+  a.chain_steps = c.chain_steps;
+  a.sy_steps = c.sy_steps;
+  a.dof = (double)c.dof;
+  a.dt = c.dt;
+  a.tau = c.tau;
+  a.update_mass = update_mass;
+  for (int k = 0; k < 7; ++k) a.w[k] = 0.0;
+  const double* src = c.sy_steps == 3 ? w3 : c.sy_steps == 5 ? w5 : c.sy_steps == 7 ? w7 : nullptr;
+  if (src) for (int k = 0; k < c.sy_steps; ++k) a.w[k] = src[k];
+  else a.w[0] = 1.0;
+  return a;
+}
+
 struct ReduceWs {
   double* partials;
   unsigned int* counter;
@@ -426,27 +538,26 @@ int jmd_nhc_half_step(const jmd_nhc* c, double* chain, const double* kinetic_ene
   JMD_REQUIRE(c->chain_steps >= 1, "chain_steps must be >= 1");
   JMD_REQUIRE(c->sy_steps == 1 || c->sy_steps == 3 || c->sy_steps == 5 || c->sy_steps == 7,
               "sy_steps must be 1, 3, 5 or 7");
-  // Suzuki-Yoshida weights (Yoshida 1990): the values simulate.py:328-347 uses.
-  static const double w3[3] = {0.828981543588751, -0.657963087177502, 0.828981543588751};
-  static const double w5[5] = {0.2967324292201065, 0.2967324292201065, -0.186929716880426,
-                               0.2967324292201065, 0.2967324292201065};
-  static const double w7[7] = {0.784513610477560, 0.235573213359357, -1.17767998417887,
-                               1.31518632068391, -1.17767998417887, 0.235573213359357,
-                               0.784513610477560};
-  NhcArgs a;
-  a.M1 = c->chain_length;
-  a.chain_steps = c->chain_steps;
-  a.sy_steps = c->sy_steps;
-  a.dof = (double)c->dof;
-  a.dt = c->dt;
-  a.tau = c->tau;
-  a.update_mass = update_mass;
-  for (int k = 0; k < 7; ++k) a.w[k] = 0.0;
-  const double* src = c->sy_steps == 3 ? w3 : c->sy_steps == 5 ? w5 : c->sy_steps == 7 ? w7 : nullptr;
-  if (src) for (int k = 0; k < c->sy_steps; ++k) a.w[k] = src[k];
-  else a.w[0] = 1.0;
+  const NhcArgs a = nhc_args(*c, update_mass);
   k_nhc_half<<<1, 32, 0, as_stream(stream)>>>(a, chain, kinetic_energy, p_scale);
   return check_launch("jmd_nhc_half_step");
+}
+
+int jmd_nhc_half_step_vjp(const jmd_nhc* c, const double* chain, const double* kinetic_energy,
+                          int32_t update_mass, const double* cot_p_xi, const double* cot_scale,
+                          double* grad_p_xi, double* grad_kinetic_energy, void* stream) {
+  JMD_REQUIRE(c != nullptr && chain && kinetic_energy && cot_p_xi && cot_scale && grad_p_xi &&
+                  grad_kinetic_energy,
+              "null argument");
+  JMD_REQUIRE(c->chain_length >= 2 && c->chain_length <= 7,
+              "the chain VJP supports chain_length 2..7");
+  JMD_REQUIRE(c->chain_steps >= 1, "chain_steps must be >= 1");
+  JMD_REQUIRE(c->sy_steps == 1 || c->sy_steps == 3 || c->sy_steps == 5 || c->sy_steps == 7,
+              "sy_steps must be 1, 3, 5 or 7");
+  const NhcArgs a = nhc_args(*c, update_mass);
+  k_nhc_half_vjp<<<1, 32, 0, as_stream(stream)>>>(a, chain, kinetic_energy, cot_p_xi, cot_scale,
+                                                  grad_p_xi, grad_kinetic_energy);
+  return check_launch("jmd_nhc_half_step_vjp");
 }
 
 int jmd_scale_momentum(float* momentum, int64_t p_stride, int64_t n, int32_t dim,

@@ -257,3 +257,62 @@ def test_sparse_list_vjp(cuda, fmt):
     (gE,) = torch.autograd.grad(E, Rg)
     F = efn_d.forces(Rt, nb_d)
     assert (gE + F).abs().max().item() <= 1e-4 * max(1.0, F.abs().max().item())
+
+
+def _oracle_nvt_loss(R0, P0, L, sig, steps, dt=0.005, kT=0.722):
+    box = np.full(3, L)
+    spec = O.PairSpec(kind='lj', sigma=sig)
+    nl = O.NeighborListOracle(box, 2.5 * sig, 0.3)
+    h = {'nb': nl.allocate(R0)}
+
+    def fn(X):
+        h['nb'] = nl.update(X, h['nb'])
+        return O.pair_energy_forces(spec, X, h['nb'].idx, O.DENSE, box)[1]
+    R, P = R0.astype(np.float64), P0.astype(np.float64)
+    n = len(R)
+    F = fn(R)
+    c = O.nhc_init(3 * n, O.kinetic_energy(P), kT, 100 * dt, 5)
+    for _ in range(steps):
+        R, P, F, c = O.nvt_nose_hoover_step(fn, R, P, F, 1.0, c, dt, kT, box)
+    return O.pair_energy_forces(spec, R, nl.build(R).idx, O.DENSE, box)[0] / n
+
+
+def test_nvt_trajectory_gradient_matches_fd(cuda):
+    """Gradient of PE/N after 12 Nose-Hoover steps (chain 5, tau = 100 dt)
+    with respect to sigma and along random directions of R0 and P0, against
+    FP64 central differences of the oracle's NVT step (simulate.py:649-667)."""
+    from jax_md_gb300 import adjoint, energy, partition, space
+    from tests.helpers import fcc_system
+    R, P, L = fcc_system(5)
+    disp, shift = space.periodic(L)
+    nfn, efn = energy.lennard_jones_neighbor_list(disp, L, dr_threshold=0.3, format=partition.Dense)
+    Rt = torch.tensor(R, device=cuda)
+    nb = nfn.allocate(Rt)
+    steps = 12
+    traj = adjoint.nvt_trajectory(efn, nfn, shift, 0.005, 0.722, steps)
+    sig = torch.tensor(1.0, device=cuda, requires_grad=True)
+    R0 = Rt.clone().requires_grad_(True)
+    P0 = torch.tensor(P, device=cuda).requires_grad_(True)
+    xn, pn = traj(R0, P0, nb, sigma=sig)
+    nb = nb.update(xn.detach())
+    loss = efn(xn, nb, sigma=sig) / len(R)
+    loss.backward()
+    L0 = _oracle_nvt_loss(R, P, L, 1.0, steps)
+    assert abs(float(loss) - L0) <= 1e-4 * abs(L0)
+    hh = 1e-4
+    fd = (_oracle_nvt_loss(R, P, L, 1 + hh, steps) - _oracle_nvt_loss(R, P, L, 1 - hh, steps)) / (2 * hh)
+    assert abs(float(sig.grad) - fd) <= 1e-3 * max(abs(fd), 1e-2), (float(sig.grad), fd)
+    rng = np.random.default_rng(6)
+    e = 1e-4
+    for which, grad in (('R', R0.grad), ('P', P0.grad)):
+        v = rng.standard_normal(R.shape)
+        v /= np.linalg.norm(v)
+        if which == 'R':
+            lp = _oracle_nvt_loss(R + e * v, P, L, 1.0, steps)
+            lm = _oracle_nvt_loss(R - e * v, P, L, 1.0, steps)
+        else:
+            lp = _oracle_nvt_loss(R, P + e * v, L, 1.0, steps)
+            lm = _oracle_nvt_loss(R, P - e * v, L, 1.0, steps)
+        fdv = (lp - lm) / (2 * e)
+        ad = float((grad.cpu().numpy() * v).sum())
+        assert abs(ad - fdv) <= 1e-3 * max(abs(fdv), 1e-2), (which, ad, fdv)
