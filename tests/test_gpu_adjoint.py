@@ -152,7 +152,7 @@ def test_trajectory_gradient_matches_fd(cuda, k):
     gs = sig_t.grad.cpu().numpy()
     ge = eps_t.grad.cpu().numpy()
     L0 = _oracle_loss(R, P, L, species, SIG, EPS, steps)
-    assert abs(float(loss) - L0) <= 1e-4 * abs(L0)
+    assert abs(float(loss.detach()) - L0) <= 1e-4 * abs(L0)
     hh = 1e-4
     for mat, g in (('sigma', gs), ('epsilon', ge)):
         for a in range(2):
@@ -298,7 +298,7 @@ def test_nvt_trajectory_gradient_matches_fd(cuda):
     loss = efn(xn, nb, sigma=sig) / len(R)
     loss.backward()
     L0 = _oracle_nvt_loss(R, P, L, 1.0, steps)
-    assert abs(float(loss) - L0) <= 1e-4 * abs(L0)
+    assert abs(float(loss.detach()) - L0) <= 1e-4 * abs(L0)
     hh = 1e-4
     fd = (_oracle_nvt_loss(R, P, L, 1 + hh, steps) - _oracle_nvt_loss(R, P, L, 1 - hh, steps)) / (2 * hh)
     assert abs(float(sig.grad) - fd) <= 1e-3 * max(abs(fd), 1e-2), (float(sig.grad), fd)
