@@ -361,7 +361,7 @@ def batched_adjoint_section(dev, n_sys=128, steps=500, seed=0):
                 'finite-difference checks run 20 steps (tests)',
         'plain': 'per-replica simulate.run with direct launches; central differences of the two '
                  'AB parameters = 5 ensemble passes (one timed)',
-        'dynamics': 'NVE (the Nose-Hoover adjoint is not built)',
+        'dynamics': 'NVE (the batched Nose-Hoover adjoint is not built; the single-system one is adjoint.nvt_trajectory)',
         'overflow': overflow,
     }
 
