@@ -674,6 +674,58 @@ int jmd_batch_energy_param_grad(const jmd_pair* pair, const jmd_batch* batch,
                                 const int32_t* species, const double* system_weight,
                                 double* grad_params, void* stream);
 
+/* Nose-Hoover chains of a batch, one per system (simulate.nvt_nose_hoover,
+ * simulate.py:565-669, run on every system with its own chain).  The chain
+ * constants are shared; chain.dof is not used: system b has
+ * (sys_offset[b+1] - sys_offset[b]) * dim degrees of freedom
+ * (quantity.count_dof).  chain_state holds 66 doubles per system in the
+ * layout of jmd_nhc_half_step (kT per system at [65]); p_scale [2 B]
+ * receives the two momentum scales of each system's last step (first half
+ * step at [b], second at [B + b]). */
+typedef struct {
+  jmd_nhc chain;
+  double* chain_state;
+  double* p_scale;
+} jmd_batch_nvt;
+
+/* n_steps of batched Nose-Hoover NVT, each step: chain half step with
+ * update_mass on the stored kinetic energy -> kick (after the chain's
+ * momentum scale) + drift -> skin-gated rebuild -> force + kick -> kinetic
+ * energy -> chain half step -> momentum scale (simulate.py:649-667 per
+ * system).  Graphs and forces as jmd_batch_nve_run.  chain_length 2..16. */
+int jmd_batch_nvt_run(const jmd_batch_system* sys, const jmd_batch_nvt* nvt, int64_t n_steps,
+                      int32_t use_graph, void* stream);
+
+/* One chain half step of every system (update_mass first when update_mass
+ * != 0).  measure_ke != 0: the kinetic energy is summed from momentum (f64)
+ * and stored in the chain first, else the chain's stored one is used.
+ * momentum != NULL: each system's momenta are multiplied by its scale.
+ * scale_out[B] / ke_out[B] (either may be NULL) receive each system's scale
+ * and the kinetic energy the step used. */
+int jmd_batch_nhc_half_step(const jmd_batch* batch, const jmd_batch_nvt* nvt, float* momentum,
+                            const float* mass, float mass_scalar, int32_t update_mass,
+                            int32_t measure_ke, double* scale_out, double* ke_out, void* stream);
+
+/* Batched jmd_nhc_half_step_vjp, one thread per system: chain [66 B] the
+ * states before the half step, kinetic_energy [B] the energies they used,
+ * cot_p_xi [16 B] / cot_scale [B] the cotangents of the outputs; writes
+ * grad_p_xi [16 B] and grad_kinetic_energy [B].  chain_length 2..7. */
+int jmd_batch_nhc_half_step_vjp(const jmd_batch* batch, const jmd_nhc* c, const double* chain,
+                                const double* kinetic_energy, int32_t update_mass,
+                                const double* cot_p_xi, const double* cot_scale,
+                                double* grad_p_xi, double* grad_kinetic_energy, void* stream);
+
+/* Force VJP of a batch (the batched jmd_pair_force_vjp, Dense tiled list
+ * built at `position`): grad_position += weight (dF/dR)^T cotangent and,
+ * when grad_params is given, grad_params[130] += weight d(cotangent . F)/d
+ * (sigma, epsilon, cutoff scale) summed over systems.  position, cotangent
+ * and grad_position are float4 rows; record_scratch holds 2 N float4. */
+int jmd_batch_pair_force_vjp(const jmd_pair* pair, const jmd_batch* batch,
+                             const jmd_batch_nlist* nl, const float* position,
+                             const float* cotangent, const int32_t* species, float weight,
+                             float* grad_position, double* grad_params, float* record_scratch,
+                             void* stream);
+
 #ifdef __cplusplus
 }
 #endif

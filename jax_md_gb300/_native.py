@@ -106,6 +106,10 @@ class BatchSystem(C.Structure):
                 ('n_done', C.c_void_p)]
 
 
+class BatchNvt(C.Structure):
+    _fields_ = [('chain', Nhc), ('chain_state', C.c_void_p), ('p_scale', C.c_void_p)]
+
+
 P = C.c_void_p
 I64 = C.c_int64
 I32 = C.c_int32
@@ -179,6 +183,13 @@ SIGNATURES = {
                                                 P, I32, P]),
     'jmd_batch_energy_param_grad': (C.c_int, [C.POINTER(Pair), C.POINTER(Batch),
                                               C.POINTER(BatchNList), P, P, P, P, P]),
+    'jmd_batch_nvt_run': (C.c_int, [C.POINTER(BatchSystem), C.POINTER(BatchNvt), I64, I32, P]),
+    'jmd_batch_nhc_half_step': (C.c_int, [C.POINTER(Batch), C.POINTER(BatchNvt), P, P, F32, I32,
+                                          I32, P, P, P]),
+    'jmd_batch_nhc_half_step_vjp': (C.c_int, [C.POINTER(Batch), C.POINTER(Nhc), P, P, I32, P, P,
+                                              P, P, P]),
+    'jmd_batch_pair_force_vjp': (C.c_int, [C.POINTER(Pair), C.POINTER(Batch),
+                                           C.POINTER(BatchNList), P, P, P, F32, P, P, P, P]),
     'jmd_fire_kick_drift': (C.c_int, [P, P, P, P, F32, I64, C.POINTER(Space), P, P]),
     'jmd_fire_workspace_bytes': (SZ, [I64]),
     'jmd_fire_update': (C.c_int, [P, P, I64, I32, P, F32, F32, F32, F32, F32, F32, P, SZ, P]),

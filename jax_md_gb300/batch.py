@@ -436,6 +436,80 @@ class BatchRunner:
     def potential(self):
         return self.energy.energies(self.batch, self.nbrs)
 
+    # ---------------------------------------------------------- Nose-Hoover
+    def nvt_init(self, kT, chain_length: int = 5, chain_steps: int = 2, sy_steps: int = 3,
+                 tau=None):
+        """One Nose-Hoover chain per system at temperature kT (a scalar or one
+        value per system), as simulate.nvt_nose_hoover's init_fn
+        (simulate.py:625-637) for each system: chain masses kT tau^2, the first
+        times the system's degrees of freedom, zero chain positions and
+        momenta, the system's kinetic energy.  tau defaults to 100 dt."""
+        self.nhc = _nhc_constants(self.dt, chain_length, chain_steps, sy_steps, tau)
+        ke, _ = self.kinetic()
+        self.chain = _chain_init(self.batch, ke, kT, self.nhc)
+        self.p_scale = torch.ones(2 * self.batch.n_systems, dtype=torch.float64,
+                                  device=self.batch.device)
+
+    def nvt_struct(self) -> N.BatchNvt:
+        if getattr(self, 'chain', None) is None:
+            raise RuntimeError('call nvt_init first')
+        v = N.BatchNvt()
+        v.chain = self.nhc
+        v.chain_state = self.chain.data_ptr()
+        v.p_scale = self.p_scale.data_ptr()
+        return v
+
+    def nvt(self, n_steps: int, use_graph: bool = True):
+        """n_steps of Nose-Hoover NVT of every system (simulate.py:649-667)."""
+        N.check(N.lib().jmd_batch_nvt_run(ctypes.byref(self.struct()),
+                                          ctypes.byref(self.nvt_struct()), int(n_steps),
+                                          1 if use_graph else 0, N.stream_ptr()), 'batch_nvt_run')
+
+    def nvt_invariant(self) -> torch.Tensor:
+        """Per-system conserved quantity of the NVT run
+        (simulate.nvt_nose_hoover_invariant, simulate.py:672-701), f64 [B]."""
+        self.compute_forces()
+        ke, _ = self.kinetic()
+        c = self.chain
+        M1 = self.nhc.chain_length
+        dof = torch.tensor(self.batch.sizes, dtype=torch.float64,
+                           device=c.device) * self.batch.dim
+        kT = c[:, 65]
+        xi, pxi, Q = c[:, :M1], c[:, 16:16 + M1], c[:, 32:32 + M1]
+        E = self.potential() + ke
+        E = E + pxi[:, 0] ** 2 / (2 * Q[:, 0]) + dof * kT * xi[:, 0]
+        E = E + (pxi[:, 1:] ** 2 / (2 * Q[:, 1:])).sum(1) + kT * xi[:, 1:].sum(1)
+        return E
+
+
+def _nhc_constants(dt, chain_length, chain_steps, sy_steps, tau) -> N.Nhc:
+    if not 2 <= int(chain_length) <= 16:
+        raise ValueError('chain_length must be between 2 and 16')
+    if int(sy_steps) not in (1, 3, 5, 7):
+        raise ValueError('sy_steps must be 1, 3, 5 or 7')
+    if int(chain_steps) < 1:
+        raise ValueError('chain_steps must be >= 1')
+    dt32 = float(np.float32(dt))
+    c = N.Nhc()
+    c.chain_length, c.chain_steps, c.sy_steps = int(chain_length), int(chain_steps), int(sy_steps)
+    c.dof = 0
+    c.dt = dt32
+    c.tau = float(np.float32(dt32 * 100 if tau is None else tau))
+    return c
+
+
+def _chain_init(batch: 'Batch', ke: torch.Tensor, kT, nhc: N.Nhc) -> torch.Tensor:
+    """[B, 66] f64 chain states (the layout of jmd_nhc_half_step) of a batch."""
+    B, dev = batch.n_systems, batch.device
+    kTs = torch.as_tensor(kT, dtype=torch.float64, device=dev).reshape(-1).expand(B)
+    dof = torch.tensor(batch.sizes, dtype=torch.float64, device=dev) * batch.dim
+    chain = torch.zeros((B, 66), dtype=torch.float64, device=dev)
+    chain[:, 32:32 + nhc.chain_length] = (kTs * nhc.tau ** 2)[:, None]
+    chain[:, 32] *= dof
+    chain[:, 64] = ke
+    chain[:, 65] = kTs
+    return chain
+
 
 def _system_struct(nbrs: BatchNeighborList, pair, species, x, p, f, mass, dt, threshold_sq):
     s = N.BatchSystem()
@@ -625,6 +699,165 @@ class BatchTrajectory:
             dyn['epsilon'] = epsilon
         return _BatchTrajectoryFn.apply(R0, P0, _param_tensor(sigma), _param_tensor(epsilon),
                                         (self, dyn))
+
+
+# Reverse pass of batched Nose-Hoover NVT: the single-system recurrence
+# (adjoint._NvtTrajectoryFn) with every scalar of it per system.  Step k
+# records x_k, p_k, the chain before each half step, the scales s1, s2 and
+# r = p after the Verlet step; backward, with p-bar, chain-momentum and KE
+# cotangents per system:
+#     sbar2_b = sum_{i in b} pbar_i . r_i;  rbar = s2 pbar;
+#     (pxibar', kebar) = J_H^T(pxibar, sbar2);  rbar += kebar r / m
+#     xbar += VJP(x_{k+1}, h (rbar + qbar_{k+1}))
+#     qbar = rbar + (dt/m) xbar;  sbar1_b = sum qbar . p_k;  pbar = s1 qbar
+#     (pxibar, kebar) = J_H^T(pxibar', sbar1);  pbar += kebar p_k / m
+# and finally xbar += VJP(x_0, h qbar_0).
+class _BatchNvtTrajectoryFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, R0, P0, sigma, epsilon, cfg):
+        tr, dyn = cfg
+        bt, nb, dim = tr.batch, tr.nbrs, tr.batch.dim
+        n, dev, B = max(bt.n, 1), bt.device, bt.n_systems
+        f4 = lambda: torch.zeros((n, 4), dtype=torch.float32, device=dev)
+        x, p, f = f4(), f4(), f4()
+        x[:, :dim] = torch.remainder(R0.detach(), bt.box[bt.atom_sys.long(), :dim])
+        p[:, :dim] = P0.detach()
+        tr.neighbor_fns._build(nb, x)
+        species, pair = tr.energy.pair(bt, **dyn)
+        tr.energy.forces(bt, nb, out=f, position=x, **dyn)
+        sysd = _system_struct(nb, pair, species, x, p, f, tr.mass, tr.dt,
+                              tr.neighbor_fns.threshold_sq)
+        L = N.lib()
+        ke = torch.empty(B, dtype=torch.float64, device=dev)
+        N.check(L.jmd_batch_kinetic_energy(ctypes.byref(nb.grid.struct), p.data_ptr(), None, None,
+                                           tr.mass, ke.data_ptr(), None, N.stream_ptr()),
+                'batch_kinetic_energy')
+        chain = _chain_init(bt, ke, tr.kT, tr.nhc)
+        nvt = N.BatchNvt()
+        nvt.chain, nvt.chain_state, nvt.p_scale = tr.nhc, chain.data_ptr(), None
+        steps = tr.n_steps
+        s1 = torch.empty((steps, B), dtype=torch.float64, device=dev)
+        s2 = torch.empty_like(s1)
+        ke2 = torch.empty_like(s1)
+
+        def half(update_mass, measure, scale, ke_out):
+            N.check(L.jmd_batch_nhc_half_step(ctypes.byref(nb.grid.struct), ctypes.byref(nvt),
+                                              p.data_ptr(), None, tr.mass, update_mass, measure,
+                                              scale.data_ptr(), N.ptr(ke_out), N.stream_ptr()),
+                    'batch_nhc_half_step')
+        tape = []
+        for k in range(steps):
+            x_k, p_k, chain_a = x[:, :dim].clone(), p[:, :dim].clone(), chain.clone()
+            half(1, 0, s1[k], None)
+            N.check(L.jmd_batch_nve_run(ctypes.byref(sysd), 1, 0, N.stream_ptr()), 'batch_nve_run')
+            r, chain_b = p[:, :dim].clone(), chain.clone()
+            half(0, 1, s2[k], ke2[k])
+            tape.append((x_k, p_k, chain_a, r, chain_b))
+        if nb.did_buffer_overflow:
+            raise RuntimeError('a batched neighbour list overflowed during the trajectory; '
+                               'allocate it with more capacity')
+        ctx.cfg = (tr, species, pair, tape, x[:, :dim].clone(), s1, s2, ke2)
+        ctx.has = (sigma is not None, epsilon is not None)
+        ctx.save_for_backward(sigma if sigma is not None else torch.empty(0),
+                              epsilon if epsilon is not None else torch.empty(0))
+        return x[:, :dim].clone(), p[:, :dim].clone()
+
+    @staticmethod
+    def backward(ctx, gx, gp):
+        tr, species, pair, tape, x_n, s1, s2, ke2 = ctx.cfg
+        sigma, epsilon = ctx.saved_tensors
+        sigma = sigma if ctx.has[0] else None
+        epsilon = epsilon if ctx.has[1] else None
+        bt, nb, dim = tr.batch, tr.nbrs, tr.batch.dim
+        n, dev, B = max(bt.n, 1), bt.device, bt.n_systems
+        sys_of = bt.atom_sys.long()
+        dt = float(np.float32(tr.dt))
+        h = float(np.float32(dt / 2))
+        inv_m = 1.0 / tr.mass
+        xbar = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+        if gx is not None:
+            xbar[:, :dim] += gx
+        pbar = torch.zeros((n, dim), dtype=torch.float32, device=dev)
+        if gp is not None:
+            pbar += gp
+        want = sigma is not None or epsilon is not None
+        bins = torch.zeros(130, dtype=torch.float64, device=dev)
+        pxi = torch.zeros((B, 16), dtype=torch.float64, device=dev)
+        pxi1 = torch.zeros_like(pxi)
+        kebar = torch.zeros(B, dtype=torch.float64, device=dev)
+        x4 = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+        lam4 = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+        rec = torch.zeros((2 * n, 4), dtype=torch.float32, device=dev)
+        L = N.lib()
+
+        def per_system(v):
+            return torch.zeros(B, dtype=torch.float64, device=dev).index_add_(
+                0, sys_of, v.double().sum(1))
+
+        def chain_vjp(chain_in, ke, update_mass, cot_p, cot_s, out_p):
+            N.check(L.jmd_batch_nhc_half_step_vjp(
+                ctypes.byref(nb.grid.struct), ctypes.byref(tr.nhc), chain_in.data_ptr(),
+                ke.data_ptr(), update_mass, cot_p.data_ptr(), cot_s.data_ptr(), out_p.data_ptr(),
+                kebar.data_ptr(), N.stream_ptr()), 'batch_nhc_half_step_vjp')
+
+        def vjp_at(x, lam):
+            x4[:, :dim] = x
+            tr.neighbor_fns.update(x4, nb)
+            lam4[:, :dim] = lam
+            N.check(L.jmd_batch_pair_force_vjp(
+                ctypes.byref(pair), ctypes.byref(nb.grid.struct), ctypes.byref(nb.struct()),
+                x4.data_ptr(), lam4.data_ptr(), N.ptr(species), 1.0, xbar.data_ptr(),
+                bins.data_ptr() if want else None, rec.data_ptr(), N.stream_ptr()),
+                'batch_pair_force_vjp')
+
+        pending = None
+        for k in range(len(tape) - 1, -1, -1):
+            x_k, p_k, chain_a, r, chain_b = tape[k]
+            x1 = tape[k + 1][0] if k + 1 < len(tape) else x_n
+            sbar2 = per_system(pbar * r)
+            rbar = pbar * s2[k][sys_of].float()[:, None]
+            chain_vjp(chain_b, ke2[k], 0, pxi, sbar2, pxi1)
+            rbar = rbar + (kebar[sys_of].float()[:, None] * r) * inv_m
+            lam = h * (rbar if pending is None else rbar + pending)
+            vjp_at(x1, lam)
+            qbar = rbar + (dt * inv_m) * xbar[:, :dim]
+            sbar1 = per_system(qbar * p_k)
+            pbar = qbar * s1[k][sys_of].float()[:, None]
+            chain_vjp(chain_a, chain_a[:, 64].contiguous(), 1, pxi1, sbar1, pxi)
+            pbar = pbar + (kebar[sys_of].float()[:, None] * p_k) * inv_m
+            pending = qbar
+        vjp_at(tape[0][0], h * pending)
+        gs, ge = _bins_to_grads(bins, None, sigma, epsilon) if want else (None, None)
+        return xbar[:, :dim].clone(), pbar.contiguous(), gs, ge, None
+
+
+class BatchNvtTrajectory:
+    """``traj(R0, P0, sigma=None, epsilon=None) -> (x_n, p_n)``: n_steps of
+    Nose-Hoover NVT of every system of a batch (a fresh chain per system at
+    kT, simulate.nvt_nose_hoover), differentiable with respect to R0, P0 and
+    sigma / epsilon shared by all systems.  Every step is recorded (positions,
+    momenta and the chains), so memory grows with n_steps; ``nbrs`` is
+    rebuilt in place.  Unit mass unless ``mass`` is given."""
+
+    def __init__(self, batch: Batch, neighbor_fns: BatchNeighborListFns, nbrs: BatchNeighborList,
+                 energy: BatchPairEnergy, dt: float, kT, n_steps: int, chain_length: int = 5,
+                 chain_steps: int = 2, sy_steps: int = 3, tau=None, mass: float = 1.0):
+        if int(n_steps) < 1:
+            raise ValueError('n_steps must be >= 1')
+        if not 2 <= int(chain_length) <= 7:
+            raise NotImplementedError('the chain adjoint supports chain_length 2..7')
+        self.batch, self.neighbor_fns, self.nbrs, self.energy = batch, neighbor_fns, nbrs, energy
+        self.dt, self.kT, self.n_steps, self.mass = float(dt), kT, int(n_steps), float(mass)
+        self.nhc = _nhc_constants(dt, chain_length, chain_steps, sy_steps, tau)
+
+    def __call__(self, R0, P0, sigma=None, epsilon=None):
+        dyn = {}
+        if sigma is not None:
+            dyn['sigma'] = sigma
+        if epsilon is not None:
+            dyn['epsilon'] = epsilon
+        return _BatchNvtTrajectoryFn.apply(R0, P0, _param_tensor(sigma), _param_tensor(epsilon),
+                                           (self, dyn))
 
 
 FORCE_BLOCKS = (64, 128, 256)

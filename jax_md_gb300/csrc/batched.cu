@@ -24,6 +24,7 @@
 #include <type_traits>
 
 #include "adjoint.cuh"
+#include "nhc.cuh"
 
 namespace jmd {
 namespace {
@@ -442,7 +443,8 @@ __global__ void __launch_bounds__(256) k_bkick_drift(BatchView v, float4* x, flo
                                                      const float4* __restrict__ f,
                                                      const float* mass, float m0, float dt,
                                                      const float* fs, const int32_t* done,
-                                                     const float4* ref, float thr2, int32_t* flag) {
+                                                     const float4* ref, float thr2, int32_t* flag,
+                                                     const double* pscale) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool over = false;
   if (i < v.n) {
@@ -452,6 +454,12 @@ __global__ void __launch_bounds__(256) k_bkick_drift(BatchView v, float4* x, flo
       const float h = 0.5f * dts;
       const SysGeo g = sys_geo(v, b);
       float4 q = p[i];
+      if (pscale) {  // the Nose-Hoover chain's momentum rescale before the kick
+        const float sc = (float)__ldg(pscale + b);
+        q.x *= sc;
+        q.y *= sc;
+        q.z *= sc;
+      }
       const float4 ff = __ldg(f + i);
       q.x = fmaf(h, ff.x, q.x);
       q.y = fmaf(h, ff.y, q.y);
@@ -471,6 +479,76 @@ __global__ void __launch_bounds__(256) k_bkick_drift(BatchView v, float4* x, flo
     }
   }
   if (ref && __any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+// Nose-Hoover chain half step of every system, one CTA per system
+// (simulate.py:492-517 with update_mass :509-515; the chain of system b is
+// chain[66 b ..], its degrees of freedom n_b * DIM as quantity.count_dof).
+// MEASURE: the kinetic energy is summed from p (FP32 per thread, f64 across
+// threads) and written to the chain first, else the chain's stored one is
+// used.  With p, the system's momenta are multiplied by its scale.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bnhc(BatchView v, NhcArgs a, double* chain, float4* p,
+                                              const float* mass, float m0, int measure,
+                                              double* scale_out, double* ke_out) {
+  const int b = blockIdx.x;
+  const int a0 = __ldg(v.sys_offset + b), a1 = __ldg(v.sys_offset + b + 1);
+  __shared__ float s_scale;
+  double ke = 0.0;
+  if (measure) {
+    float acc = 0.f;
+    for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+      const float4 q = p[i];
+      const float m = mass ? __ldg(mass + i) : m0;
+      acc += (q.x * q.x + q.y * q.y + (DIM == 3 ? q.z * q.z : 0.f)) / m;
+    }
+    ke = 0.5 * block_sum((double)acc);
+  }
+  if (threadIdx.x == 0) {
+    double* c = chain + 66 * (size_t)b;
+    if (measure) c[64] = ke;
+    else ke = c[64];
+    if (ke_out) ke_out[b] = ke;
+    const float sc = nhc_half_chain(a, c, (float)ke, (float)((a1 - a0) * DIM));
+    if (scale_out) scale_out[b] = sc;
+    s_scale = sc;
+  }
+  __syncthreads();
+  if (p) {
+    const float sc = s_scale;
+    for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+      float4 q = p[i];
+      q.x *= sc;
+      q.y *= sc;
+      if (DIM == 3) q.z *= sc;
+      p[i] = q;
+    }
+  }
+}
+
+// Reverse of k_bnhc's chain half step, one thread per system: chain[66 b ..]
+// the state before it, ke[b] the kinetic energy it used, cot_pxi[16 b ..] and
+// cot_scale[b] the cotangents of its outputs; writes grad_pxi[16 b ..] and
+// grad_ke[b].
+__global__ void k_bnhc_vjp(NhcArgs a, int nsys, const int32_t* sys_offset, int dim,
+                           const double* chain, const double* ke, const double* cot_pxi,
+                           const double* cot_scale, double* grad_pxi, double* grad_ke) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nsys) return;
+  const float dof = (float)((sys_offset[b + 1] - sys_offset[b]) * dim);
+  nhc_half_chain_vjp(a, chain + 66 * (size_t)b, (float)ke[b], dof, cot_pxi + 16 * (size_t)b,
+                     cot_scale[b], grad_pxi + 16 * (size_t)b, grad_ke + b);
+}
+
+// (x, lambda) records of the batched force VJP (the layout k_badj_step reads).
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bvjp_pack(int n, const float4* __restrict__ x,
+                                                   const float4* __restrict__ lam, float4* rec) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 xi = __ldg(x + i), q = __ldg(lam + i);
+  rec[2 * i] = make_float4(xi.x, xi.y, DIM == 3 ? xi.z : 0.f, q.x);
+  rec[2 * i + 1] = make_float4(q.y, DIM == 3 ? q.z : 0.f, 0.f, 0.f);
 }
 
 // FIRE after the force: closing half kick, the three f64 reductions, the
@@ -879,7 +957,7 @@ int validate_system(const jmd_batch_system* s, bool fire) {
 // closing half kick for NVE, the FIRE update for FIRE).
 int enqueue_batch_run(const jmd_batch_system& s, const jmd_fire_params* fp, int64_t steps,
                       bool graphed, cudaStream_t st, cudaStream_t body_st, float* traj = nullptr,
-                      bool force_rebuild = false) {
+                      bool force_rebuild = false, const jmd_batch_nvt* nvt = nullptr) {
   const jmd_batch& b = s.batch;
   const BatchView v = view_of(b);
   const bool always = s.threshold_sq < 0.f;
@@ -905,21 +983,39 @@ int enqueue_batch_run(const jmd_batch_system& s, const jmd_fire_params* fp, int6
     int rc0 = gate();
     if (rc0) return rc0;
   }
+  // Nose-Hoover (simulate.py:649-667): chain half step with update_mass on the
+  // stored kinetic energy (its scale applied inside the kick) -> velocity
+  // Verlet -> chain half step on the measured kinetic energy + rescale.
+  const NhcArgs na1 = nvt ? nhc_args(nvt->chain, 1) : NhcArgs{};
+  const NhcArgs na0 = nvt ? nhc_args(nvt->chain, 0) : NhcArgs{};
+  const double* pscale = nvt ? nvt->p_scale : nullptr;
+  auto chain_half = [&](const NhcArgs& na, bool second) {
+    if (b.dim == 3)
+      k_bnhc<3><<<b.n_systems, second ? 256 : 32, 0, st>>>(
+          v, na, nvt->chain_state, second ? p : nullptr, s.mass, s.mass_scalar, second ? 1 : 0,
+          nvt->p_scale + (second ? b.n_systems : 0), nullptr);
+    else
+      k_bnhc<2><<<b.n_systems, second ? 256 : 32, 0, st>>>(
+          v, na, nvt->chain_state, second ? p : nullptr, s.mass, s.mass_scalar, second ? 1 : 0,
+          nvt->p_scale + (second ? b.n_systems : 0), nullptr);
+    return cudaGetLastError();
+  };
   for (int64_t k = 0; k < steps; ++k) {
+    if (nvt) JMD_CUDA(chain_half(na1, false));
     if (b.dim == 3) {
       if (fire)
         k_bkick_drift<3, true><<<gr, 256, 0, st>>>(v, x, p, f, s.mass, s.mass_scalar, s.dt, s.fire_state,
-                                                   s.done, ref, s.threshold_sq, s.nlist.rebuild_flag);
+                                                   s.done, ref, s.threshold_sq, s.nlist.rebuild_flag, nullptr);
       else
         k_bkick_drift<3, false><<<gr, 256, 0, st>>>(v, x, p, f, s.mass, s.mass_scalar, s.dt, nullptr,
-                                                    nullptr, ref, s.threshold_sq, s.nlist.rebuild_flag);
+                                                    nullptr, ref, s.threshold_sq, s.nlist.rebuild_flag, pscale);
     } else {
       if (fire)
         k_bkick_drift<2, true><<<gr, 256, 0, st>>>(v, x, p, f, s.mass, s.mass_scalar, s.dt, s.fire_state,
-                                                   s.done, ref, s.threshold_sq, s.nlist.rebuild_flag);
+                                                   s.done, ref, s.threshold_sq, s.nlist.rebuild_flag, nullptr);
       else
         k_bkick_drift<2, false><<<gr, 256, 0, st>>>(v, x, p, f, s.mass, s.mass_scalar, s.dt, nullptr,
-                                                    nullptr, ref, s.threshold_sq, s.nlist.rebuild_flag);
+                                                    nullptr, ref, s.threshold_sq, s.nlist.rebuild_flag, pscale);
     }
     JMD_CUDA(cudaGetLastError());
     int rc = gate();
@@ -934,6 +1030,7 @@ int enqueue_batch_run(const jmd_batch_system& s, const jmd_fire_params* fp, int6
         k_bfire_update<2><<<b.n_systems, g_fire_threads, 0, st>>>(v, p, f, s.fire_state, s.done, s.n_done, *fp);
       JMD_CUDA(cudaGetLastError());
     }
+    if (nvt) JMD_CUDA(chain_half(na0, true));
     if (traj) JMD_CUDA(cudaMemcpyAsync(slot(k + 1), s.position, rows, cudaMemcpyDeviceToDevice, st));
   }
   return JMD_OK;
@@ -985,7 +1082,8 @@ int enqueue_batch_adjoint(const jmd_batch_system& s, const float* traj, int64_t 
 }
 
 int run_impl(const jmd_batch_system* sys, const jmd_fire_params* fp, int64_t n_steps,
-             int32_t use_graph, void* stream, const char* what) {
+             int32_t use_graph, void* stream, const char* what,
+             const jmd_batch_nvt* nvt = nullptr) {
   int e = validate_system(sys, fp != nullptr);
   if (e) return e;
   JMD_REQUIRE(n_steps >= 0, "n_steps must be >= 0");
@@ -994,7 +1092,7 @@ int run_impl(const jmd_batch_system* sys, const jmd_fire_params* fp, int64_t n_s
   cudaStreamCaptureStatus cap;
   JMD_CUDA(cudaStreamIsCapturing(st, &cap));
   if (!use_graph || cap != cudaStreamCaptureStatusNone) {
-    int rc = enqueue_batch_run(*sys, fp, n_steps, false, st, nullptr);
+    int rc = enqueue_batch_run(*sys, fp, n_steps, false, st, nullptr, nullptr, false, nvt);
     return rc ? rc : check_launch(what);
   }
   int device;
@@ -1004,10 +1102,11 @@ int run_impl(const jmd_batch_system* sys, const jmd_fire_params* fp, int64_t n_s
   const int shape[2] = {g_force_block, g_fire_threads};   // baked into the graph
   key.append(reinterpret_cast<const char*>(shape), sizeof(shape));
   if (fp) key.append(reinterpret_cast<const char*>(fp), sizeof(*fp));
+  if (nvt) key.append(reinterpret_cast<const char*>(nvt), sizeof(*nvt));
   key.append(reinterpret_cast<const char*>(&n_steps), sizeof(n_steps));
   key.append(reinterpret_cast<const char*>(&device), sizeof(device));
   return graph_launch_cached(key, [&](cudaStream_t cs, cudaStream_t bs) {
-    return enqueue_batch_run(*sys, fp, n_steps, true, cs, bs);
+    return enqueue_batch_run(*sys, fp, n_steps, true, cs, bs, nullptr, false, nvt);
   }, st);
 }
 
@@ -1028,6 +1127,15 @@ int graph_or_direct(const std::string& key, const std::function<int(cudaStream_t
   k.append(reinterpret_cast<const char*>(shape), sizeof(shape));
   return graph_launch_cached(k, [&](cudaStream_t cs, cudaStream_t bs) { return enq(cs, bs, true); },
                              st);
+}
+
+int validate_chain(const jmd_nhc& c, int max_length) {
+  JMD_REQUIRE(c.chain_length >= 2 && c.chain_length <= max_length,
+              max_length == 16 ? "chain_length must be in 2..16" : "the chain VJP supports chain_length 2..7");
+  JMD_REQUIRE(c.chain_steps >= 1, "chain_steps must be >= 1");
+  JMD_REQUIRE(c.sy_steps == 1 || c.sy_steps == 3 || c.sy_steps == 5 || c.sy_steps == 7,
+              "sy_steps must be 1, 3, 5 or 7");
+  return JMD_OK;
 }
 
 }  // namespace
@@ -1196,6 +1304,91 @@ int jmd_batch_fire_run(const jmd_batch_system* sys, const jmd_fire_params* fp, i
                        int32_t use_graph, void* stream) {
   JMD_REQUIRE(fp != nullptr, "fire params are null");
   return run_impl(sys, fp, n_steps, use_graph, stream, "jmd_batch_fire_run");
+}
+
+int jmd_batch_nvt_run(const jmd_batch_system* sys, const jmd_batch_nvt* nvt, int64_t n_steps,
+                      int32_t use_graph, void* stream) {
+  JMD_REQUIRE(nvt != nullptr && nvt->chain_state && nvt->p_scale, "null chain buffer");
+  int e = validate_chain(nvt->chain, 16);
+  if (e) return e;
+  return run_impl(sys, nullptr, n_steps, use_graph, stream, "jmd_batch_nvt_run", nvt);
+}
+
+int jmd_batch_nhc_half_step(const jmd_batch* batch, const jmd_batch_nvt* nvt, float* momentum,
+                            const float* mass, float mass_scalar, int32_t update_mass,
+                            int32_t measure_ke, double* scale_out, double* ke_out, void* stream) {
+  int e = validate_batch(batch);
+  if (e) return e;
+  JMD_REQUIRE(nvt != nullptr && nvt->chain_state, "null chain buffer");
+  e = validate_chain(nvt->chain, 16);
+  if (e) return e;
+  JMD_REQUIRE(!measure_ke || momentum, "measuring the kinetic energy needs the momenta");
+  JMD_REQUIRE(!momentum || (reinterpret_cast<uintptr_t>(momentum) % 16) == 0,
+              "float4 rows must be 16-byte aligned");
+  const BatchView v = view_of(*batch);
+  const NhcArgs a = nhc_args(nvt->chain, update_mass);
+  float4* p = reinterpret_cast<float4*>(momentum);
+  const unsigned th = (p || measure_ke) ? 256 : 32;
+  if (batch->dim == 3)
+    k_bnhc<3><<<batch->n_systems, th, 0, as_stream(stream)>>>(v, a, nvt->chain_state, p, mass,
+                                                             mass_scalar, measure_ke ? 1 : 0,
+                                                             scale_out, ke_out);
+  else
+    k_bnhc<2><<<batch->n_systems, th, 0, as_stream(stream)>>>(v, a, nvt->chain_state, p, mass,
+                                                             mass_scalar, measure_ke ? 1 : 0,
+                                                             scale_out, ke_out);
+  return check_launch("jmd_batch_nhc_half_step");
+}
+
+int jmd_batch_nhc_half_step_vjp(const jmd_batch* batch, const jmd_nhc* c, const double* chain,
+                                const double* kinetic_energy, int32_t update_mass,
+                                const double* cot_p_xi, const double* cot_scale,
+                                double* grad_p_xi, double* grad_kinetic_energy, void* stream) {
+  int e = validate_batch(batch);
+  if (e) return e;
+  JMD_REQUIRE(c != nullptr, "chain constants are null");
+  e = validate_chain(*c, 7);
+  if (e) return e;
+  JMD_REQUIRE(chain && kinetic_energy && cot_p_xi && cot_scale && grad_p_xi && grad_kinetic_energy,
+              "null buffer");
+  const NhcArgs a = nhc_args(*c, update_mass);
+  const int ns = batch->n_systems;
+  k_bnhc_vjp<<<(unsigned)ceil_div(ns, 64), 64, 0, as_stream(stream)>>>(
+      a, ns, batch->sys_offset, batch->dim, chain, kinetic_energy, cot_p_xi, cot_scale, grad_p_xi,
+      grad_kinetic_energy);
+  return check_launch("jmd_batch_nhc_half_step_vjp");
+}
+
+int jmd_batch_pair_force_vjp(const jmd_pair* pair, const jmd_batch* batch,
+                             const jmd_batch_nlist* nl, const float* position,
+                             const float* cotangent, const int32_t* species, float weight,
+                             float* grad_position, double* grad_params, float* record_scratch,
+                             void* stream) {
+  JMD_REQUIRE(pair != nullptr, "pair is null");
+  int e = validate_batch(batch);
+  if (e) return e;
+  e = validate_nl(nl, batch->n_atoms);
+  if (e) return e;
+  e = validate_pair(pair);
+  if (e) return e;
+  JMD_REQUIRE(position && cotangent && grad_position && record_scratch, "null buffer");
+  for (const void* q : {(const void*)position, (const void*)cotangent, (const void*)grad_position,
+                        (const void*)record_scratch})
+    JMD_REQUIRE((reinterpret_cast<uintptr_t>(q) % 16) == 0, "float4 rows must be 16-byte aligned");
+  JMD_REQUIRE(pair->n_species == 0 || species != nullptr, "species matrices need species");
+  if (batch->n_atoms == 0) return JMD_OK;
+  cudaStream_t st = as_stream(stream);
+  const int n = (int)batch->n_atoms;
+  const unsigned gr = (unsigned)ceil_div(n, 256);
+  const float4* x = reinterpret_cast<const float4*>(position);
+  const float4* lam = reinterpret_cast<const float4*>(cotangent);
+  float4* rec = reinterpret_cast<float4*>(record_scratch);
+  if (batch->dim == 3) k_bvjp_pack<3><<<gr, 256, 0, st>>>(n, x, lam, rec);
+  else k_bvjp_pack<2><<<gr, 256, 0, st>>>(n, x, lam, rec);
+  JMD_CUDA(cudaGetLastError());
+  int rc = badj_launch(0, *pair, *batch, *nl, record_scratch, grad_position, species, weight,
+                       nullptr, grad_params, st);
+  return rc ? rc : check_launch("jmd_batch_pair_force_vjp");
 }
 
 }  // extern "C"

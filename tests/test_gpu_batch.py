@@ -241,7 +241,9 @@ def _ka_batch(cuda, cells=(6, 7, 6)):
     return systems, bt, fns, nb, batch.BatchPairEnergy(efn)
 
 
-def _ka_oracle_final_energies(systems, sig, eps, steps, dt=0.005):
+def _ka_oracle_final_energies(systems, sig, eps, steps, dt=0.005, kT=None):
+    """PE_b / N_b of each system after `steps` NVE steps, or
+    Nose-Hoover steps (chain 5, tau = 100 dt) at kT when kT is given."""
     out = []
     for R, P, L, s in systems:
         box = np.full(3, L)
@@ -254,8 +256,12 @@ def _ka_oracle_final_energies(systems, sig, eps, steps, dt=0.005):
             return O.pair_energy_forces(spec, X, h['nb'].idx, O.DENSE, box)[1]
         X, Pd = R.astype(np.float64), P.astype(np.float64)
         F = fn(X)
+        c = O.nhc_init(3 * len(R), O.kinetic_energy(Pd), kT, 100 * dt, 5) if kT else None
         for _ in range(steps):
-            X, Pd, F = O.velocity_verlet(fn, X, Pd, F, 1.0, dt, box)
+            if kT:
+                X, Pd, F, c = O.nvt_nose_hoover_step(fn, X, Pd, F, 1.0, c, dt, kT, box)
+            else:
+                X, Pd, F = O.velocity_verlet(fn, X, Pd, F, 1.0, dt, box)
         out.append(O.pair_energy_forces(spec, X, nl.build(X).idx, O.DENSE, box)[0] / len(R))
     return np.array(out)
 
@@ -354,3 +360,118 @@ def test_batch_autotune(cuda):
     torch.cuda.synchronize()
     assert torch.equal(F[64], F[128]) and torch.equal(F[128], F[256])
     batch.set_launch(*r['best'])
+
+
+def _lj_oracle_nvt(R, P0, L, steps, kT=0.722, dt=0.005):
+    box = np.full(3, float(L))
+    spec = O.PairSpec(kind='lj')
+    nl = O.NeighborListOracle(box, 2.5, 0.3, fmt=O.DENSE)
+    h = {'nb': nl.allocate(R)}
+
+    def fn(X):
+        h['nb'] = nl.update(X, h['nb'])
+        return O.pair_energy_forces(spec, X, h['nb'].idx, O.DENSE, box)[1]
+    X, P = R.astype(np.float64), P0.astype(np.float64)
+    F = fn(X)
+    c = O.nhc_init(3 * len(R), O.kinetic_energy(P), kT, 100 * dt, 5)
+    for _ in range(steps):
+        X, P, F, c = O.nvt_nose_hoover_step(fn, X, P, F, 1.0, c, dt, kT, box)
+    return X, P, c
+
+
+def test_batch_nvt_matches_oracle(cuda):
+    """Every system of a batched Nose-Hoover run, each with its own chain,
+    against the oracle's NVT step (simulate.py:649-667) over 50 steps
+    (positions, momenta, chain momenta), and each system's invariant
+    (simulate.py:672-701) conserved."""
+    from jax_md_gb300 import batch
+    systems, bt, fns, nb, ef = _lj_batch(cuda, cells=(4, 5, 6))
+    run = batch.BatchRunner(bt, fns, nb, ef, dt=0.005)
+    P0 = [O.maxwell_boltzmann(len(R), 3, 0.722, 30 + b) for b, (R, L) in enumerate(systems)]
+    run.momentum.zero_()
+    run.momentum[:, :3] = torch.tensor(np.concatenate(P0), device=cuda)
+    run.nvt_init(0.722)
+    H0 = run.nvt_invariant()
+    steps = 50
+    run.nvt(steps)
+    H1 = run.nvt_invariant()
+    torch.cuda.synchronize()
+    Rb = bt.split(bt.R)
+    Pb = bt.split(run.momentum[:, :3])
+    chain = run.chain.cpu().numpy()
+    for b, (R, L) in enumerate(systems):
+        X, P, c = _lj_oracle_nvt(R, P0[b], L, steps)
+        d = O.displacement(Rb[b].cpu().numpy(), X, np.full(3, float(L)))
+        assert np.abs(d).max() < 1e-3, (b, np.abs(d).max())
+        assert np.abs(Pb[b].cpu().numpy() - P).max() < 1e-2
+        err = np.abs(chain[b, 16:21] - c.p_xi).max()
+        assert err <= 1e-2 * max(1.0, np.abs(c.p_xi).max()), (b, chain[b, 16:21], c.p_xi)
+    sizes = torch.tensor(bt.sizes, dtype=torch.float64, device=cuda)
+    assert float(((H1 - H0).abs() / sizes).max()) < 1e-3, (H0, H1)
+
+
+def test_batch_nvt_graph_equals_direct(cuda):
+    """The graph-replayed batched NVT run and direct launches give identical
+    positions, momenta and chains."""
+    from jax_md_gb300 import batch
+    out = []
+    for use_graph in (True, False):
+        systems, bt, fns, nb, ef = _lj_batch(cuda, cells=(5, 6))
+        run = batch.BatchRunner(bt, fns, nb, ef, dt=0.005)
+        run.set_momenta(0.722, seed=4)
+        run.nvt_init(0.722)
+        run.nvt(30, use_graph=use_graph)
+        out.append((bt.position.clone(), run.momentum.clone(), run.chain.clone()))
+    torch.cuda.synchronize()
+    assert all(torch.equal(a, b) for a, b in zip(*out))
+
+
+def test_batch_nvt_trajectory_gradient_matches_fd(cuda):
+    """Gradient of mean_b PE_b(x_n)/N_b after 12 batched Nose-Hoover steps (a
+    chain per system, kT = 0.6) with respect to the shared sigma_AB,
+    epsilon_AB and along random directions of R0 and P0, against FP64 central
+    differences of the oracle's NVT step."""
+    from jax_md_gb300 import batch
+    systems, bt, fns, nb, ef = _ka_batch(cuda)
+    steps, kT = 12, 0.6
+    traj = batch.BatchNvtTrajectory(bt, fns, nb, ef, 0.005, kT, steps)
+    sig = torch.tensor(KA_SIG, dtype=torch.float32, device=cuda, requires_grad=True)
+    eps = torch.tensor(KA_EPS, dtype=torch.float32, device=cuda, requires_grad=True)
+    R0 = bt.R.clone().requires_grad_(True)
+    P0 = torch.tensor(np.concatenate([P for R, P, L, s in systems]), device=cuda).requires_grad_(True)
+    xn, pn = traj(R0, P0, sigma=sig, epsilon=eps)
+    x4 = torch.nn.functional.pad(xn.detach(), (0, 1)).contiguous()
+    nb = fns.update(x4, nb)
+    E = ef.energy_fn_autograd(bt, nb)(xn, sigma=sig, epsilon=eps)
+    sizes = torch.tensor(bt.sizes, dtype=torch.float64, device=cuda)
+    loss = (E / sizes).mean()
+    loss.backward()
+    L0 = _ka_oracle_final_energies(systems, KA_SIG, KA_EPS, steps, kT=kT).mean()
+    assert abs(float(loss.detach()) - L0) <= 1e-4 * abs(L0)
+    hh = 1e-4
+    for mat, g in (('sigma', sig.grad), ('epsilon', eps.grad)):
+        lp = []
+        for sgn in (1, -1):
+            sm, em = KA_SIG.copy(), KA_EPS.copy()
+            (sm if mat == 'sigma' else em)[0, 1] += sgn * hh
+            lp.append(_ka_oracle_final_energies(systems, sm, em, steps, kT=kT).mean())
+        fd = (lp[0] - lp[1]) / (2 * hh)
+        assert abs(float(g[0, 1]) - fd) <= 1e-3 * max(abs(fd), 1e-2), (mat, float(g[0, 1]), fd)
+    rng = np.random.default_rng(11)
+    e = 1e-4
+    for which, grad in (('R', R0.grad), ('P', P0.grad)):
+        v = rng.standard_normal((bt.n, 3))
+        v /= np.linalg.norm(v)
+        sp = []
+        for sgn in (1, -1):
+            shifted = []
+            for kk, (R, P, L, s) in enumerate(systems):
+                r = bt.rows(kk)
+                if which == 'R':
+                    shifted.append(((R + sgn * e * v[r]).astype(np.float64), P, L, s))
+                else:
+                    shifted.append((R, (P + sgn * e * v[r]).astype(np.float64), L, s))
+            sp.append(_ka_oracle_final_energies(shifted, KA_SIG, KA_EPS, steps, kT=kT).mean())
+        fd = (sp[0] - sp[1]) / (2 * e)
+        ad = float((grad.cpu().numpy() * v).sum())
+        assert abs(ad - fd) <= 1e-3 * max(abs(fd), 1e-2), (which, ad, fd)
