@@ -76,6 +76,36 @@ def test_invalid_arguments_are_reported(lib):
     assert b'dim' in L.jmd_last_error()
 
 
+def test_batched_nose_hoover_arguments_are_checked(lib):
+    """The batched chain entries reject bad arguments before any launch."""
+    import numpy as np
+    from jax_md_gb300 import _native as N
+    L = N.lib()
+    assert L.jmd_batch_nvt_run(None, None, 1, 0, None) != 0
+    dummy = np.zeros(16, np.int64)
+    b = N.Batch()
+    b.dim, b.n_systems, b.n_atoms, b.total_cells, b.max_cells = 3, 1, 4, 1, 1
+    for f in ('sys_offset', 'atom_sys', 'box', 'cell_offset', 'cells_per_side', 'cell_size'):
+        setattr(b, f, dummy.ctypes.data)
+    c = N.Nhc()
+    c.chain_length, c.chain_steps, c.sy_steps, c.dt, c.tau = 9, 2, 3, 0.005, 0.5
+    ptr = dummy.ctypes.data
+    rc = L.jmd_batch_nhc_half_step_vjp(ctypes.byref(b), ctypes.byref(c), ptr, ptr, 1, ptr, ptr,
+                                       ptr, ptr, None)
+    assert rc != 0 and b'chain_length 2..7' in L.jmd_last_error()
+    v = N.BatchNvt()
+    v.chain = c
+    v.chain.chain_length, v.chain.sy_steps = 5, 4
+    v.chain_state = ptr
+    rc = L.jmd_batch_nhc_half_step(ctypes.byref(b), ctypes.byref(v), None, None, 1.0, 1, 0, None,
+                                   None, None)
+    assert rc != 0 and b'sy_steps' in L.jmd_last_error()
+    b.dim = 4
+    rc = L.jmd_batch_nhc_half_step(ctypes.byref(b), ctypes.byref(v), None, None, 1.0, 1, 0, None,
+                                   None, None)
+    assert rc != 0 and b'dim' in L.jmd_last_error()
+
+
 def test_compute_without_gpu_fails_loudly():
     import torch
     if torch.cuda.is_available():

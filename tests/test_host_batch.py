@@ -78,3 +78,40 @@ def test_trajectory_segments():
     assert buf_segments[-1] == (20, 23) and sum(b - a for a, b in buf_segments) == 23
     with pytest.raises(ValueError):
         adjoint.nve_trajectory(efn, nfn, shift, 0.005, 0)
+
+
+def test_chain_init_matches_oracle():
+    """Per-system Nose-Hoover chains of a batch: the layout of
+    jmd_nhc_half_step (xi[16] p[16] Q[16] spare[16] KE kT) holding each
+    system's own simulate.py:436-442 initial chain (dof = n_b * dim)."""
+    from oracle import md_oracle as O
+    Rs = [_pos(5, 3, 10.0, 0), _pos(3, 3, 7.0, 1), _pos(8, 3, 12.0, 2)]
+    bt = batch.pack(Rs, [10.0, 7.0, 12.0], device='cpu')
+    c = batch._nhc_constants(0.005, 4, 2, 3, None)
+    assert c.tau == float(np.float32(np.float32(0.005) * 100))
+    ke = torch.tensor([1.5, 2.0, 0.25], dtype=torch.float64)
+    kT = [0.6, 0.7, 0.8]
+    chain = batch._chain_init(bt, ke, torch.tensor(kT, dtype=torch.float64), c).numpy()
+    assert chain.shape == (3, 66)
+    for b, n in enumerate(bt.sizes):
+        ref = O.nhc_init(3 * n, float(ke[b]), kT[b], c.tau, 4)
+        assert np.allclose(chain[b, 32:36], ref.Q)
+        assert np.all(chain[b, 36:48] == 0) and np.all(chain[b, :32] == 0)
+        assert chain[b, 64] == float(ke[b]) and chain[b, 65] == kT[b]
+    # a scalar kT is shared by every system
+    same = batch._chain_init(bt, ke, 0.5, c).numpy()
+    assert np.all(same[:, 65] == 0.5)
+
+
+def test_nose_hoover_argument_checks():
+    with pytest.raises(ValueError):
+        batch._nhc_constants(0.005, 1, 2, 3, None)
+    with pytest.raises(ValueError):
+        batch._nhc_constants(0.005, 5, 2, 4, None)
+    with pytest.raises(ValueError):
+        batch._nhc_constants(0.005, 5, 0, 3, None)
+    bt = batch.pack([_pos(4, 3, 10.0, 0)], [10.0], device='cpu')
+    with pytest.raises(NotImplementedError):
+        batch.BatchNvtTrajectory(bt, None, None, None, 0.005, 1.0, 10, chain_length=8)
+    with pytest.raises(ValueError):
+        batch.BatchNvtTrajectory(bt, None, None, None, 0.005, 1.0, 0)
