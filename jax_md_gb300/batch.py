@@ -903,3 +903,53 @@ def autotune(runner: BatchRunner, steps: int = 20) -> dict:
     set_launch(*best)
     restore()
     return {'best': best, 'ms': {f'{k[0]}x{k[1]}': v for k, v in times.items()}}
+
+
+# ------------------------------------------------------------------ ranks --
+def partition_systems(sizes: Sequence[int], n_ranks: int) -> List[List[int]]:
+    """Systems of an ensemble split across ``n_ranks`` processes, one GPU
+    each.  The systems are independent units: each rank packs and runs its
+    own share with no exchange during the run (weak scaling).  Largest
+    system first onto the least-loaded rank (load = atoms; ties to the lower
+    rank); each rank's list is in ascending system order.  Deterministic, so
+    every rank computes the same split from the same sizes."""
+    if int(n_ranks) < 1:
+        raise ValueError('n_ranks must be >= 1')
+    sizes = [int(s) for s in sizes]
+    if any(s < 0 for s in sizes):
+        raise ValueError('system sizes must be >= 0')
+    load = [0] * int(n_ranks)
+    out: List[List[int]] = [[] for _ in range(int(n_ranks))]
+    for b in sorted(range(len(sizes)), key=lambda k: (-sizes[k], k)):
+        r = min(range(len(load)), key=lambda k: (load[k], k))
+        out[r].append(b)
+        load[r] += sizes[b]
+    return [sorted(x) for x in out]
+
+
+def reduce_ensemble(local_sum: torch.Tensor, n_local: int, grads: Sequence[torch.Tensor] = (),
+                    group=None):
+    """Mean over every rank's systems of a per-system quantity, and of its
+    gradients with respect to parameters shared by all systems.  Each rank
+    passes the sum over its own systems (a scalar tensor), how many systems
+    that is, and the gradients of that sum; one all-reduce (SUM) of
+    [sum, count, grads...] in f64 gives (mean, [gradient of the mean]) on
+    every rank.  Without an initialised process group it is the
+    single-process mean."""
+    dev = local_sum.device
+    parts = [local_sum.detach().reshape(1).to(torch.float64),
+             torch.tensor([float(n_local)], dtype=torch.float64, device=dev)]
+    parts += [g.detach().reshape(-1).to(device=dev, dtype=torch.float64) for g in grads]
+    buf = torch.cat(parts)
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.all_reduce(buf, op=dist.ReduceOp.SUM, group=group)
+    count = buf[1]
+    if float(count) <= 0:
+        raise ValueError('the ensemble has no systems')
+    out, off = [], 2
+    for g in grads:
+        k = g.numel()
+        out.append((buf[off:off + k] / count).reshape(g.shape).to(g.dtype))
+        off += k
+    return buf[0] / count, out
