@@ -343,10 +343,22 @@ def soft_sphere(r, sigma=1.0, epsilon=1.0, alpha=2.0):
     return U, dU, d2U
 
 
+def morse(r, sigma=1.0, epsilon=5.0, alpha=5.0):
+    """jax_md/energy.py:346-371: eps (1 - exp(-alpha (r - sigma)))^2 - eps, the
+    minimum -eps at r = sigma; with U', U''."""
+    e = np.exp(-alpha * (r - sigma))
+    U = epsilon * (1.0 - e) ** 2 - epsilon
+    dU = 2.0 * epsilon * alpha * e * (1.0 - e)
+    d2U = 2.0 * epsilon * alpha ** 2 * e * (2.0 * e - 1.0)
+    return U, dU, d2U
+
+
 @dataclass
 class PairSpec:
-    """Which potential and its parameters (scalar or [S,S] species matrices)."""
-    kind: str = 'lj'                 # 'lj' | 'lj_truncated' | 'soft_sphere'
+    """Which potential and its parameters (scalar or [S,S] species matrices).
+    For 'morse' the radii are absolute (energy.py:374-440), not multiples of
+    max sigma."""
+    kind: str = 'lj'                 # 'lj' | 'lj_truncated' | 'soft_sphere' | 'morse'
     sigma: object = 1.0
     epsilon: object = 1.0
     alpha: object = 2.0
@@ -372,6 +384,12 @@ def pair_terms(spec: PairSpec, r, si=None, sj=None):
     sig, eps, alp = spec.params(si, sj)
     if spec.kind == 'soft_sphere':
         return soft_sphere(r, sig, eps, alp)
+    if spec.kind == 'morse':
+        # morse_pair / morse_neighbor_list: multiplicative_isotropic_cutoff
+        # with the radii as given (energy.py:388-389, 434-435)
+        U, dU, d2U = morse(r, sig, eps, alp)
+        S, dS, d2S = multiplicative_cutoff(r, spec.r_onset, spec.r_cutoff)
+        return U * S, dU * S + U * dS, d2U * S + 2 * dU * dS + U * d2S
     U, dU, d2U = lennard_jones(r, sig, eps)
     if spec.kind == 'lj_truncated':
         ms = spec.max_sigma()

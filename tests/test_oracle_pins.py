@@ -165,3 +165,51 @@ def test_nhc_invariant_drift_small():
         R, P, F, c = O.nvt_nose_hoover_step(fn, R, P, F, 1.0, c, 0.005, 0.722, box)
     H1 = O.nvt_invariant(O.pair_energy_forces(spec, R, nb.idx, O.DENSE, box)[0], P, 1.0, c, 0.722)
     assert abs(H1 - H0) / len(R) < 5e-4
+
+
+def test_morse_minimum_and_scaled_form():
+    """tests/energy_test.py:479-520: U(sigma) = -eps with zero slope for random
+    (sigma, eps, alpha); at r = a / alpha + sigma, U / eps = (1 - e^-a)^2 - 1
+    whatever sigma, eps and alpha are."""
+    rng = np.random.default_rng(17)
+    for _ in range(16):
+        sig, eps, alp = rng.uniform(0.0, 3.0), rng.uniform(0.0, 4.0), rng.uniform(1.0, 30.0)
+        U, dU, _ = O.morse(np.array([sig]), sig, eps, alp)
+        assert abs(U[0] + eps) <= 1e-12 * max(1.0, eps) and abs(dU[0]) <= 1e-12
+    for _ in range(16):
+        sig, eps, alp = rng.uniform(0.0, 3.0), rng.uniform(0.1, 4.0), rng.uniform(1.0, 30.0)
+        a = np.linspace(max(-2.5, -alp * sig), 8.0, 100)
+        U, _, _ = O.morse(a / alp + sig, sig, eps, alp)
+        np.testing.assert_allclose(U / eps, (1.0 - np.exp(-a)) ** 2 - 1.0, rtol=1e-10, atol=1e-12)
+
+
+def test_morse_derivatives_match_fd():
+    """U' and U'' of the cut-off Morse pair (absolute radii 2.0 / 2.5) against
+    central differences, away from the two switch radii."""
+    spec = O.PairSpec(kind='morse', sigma=1.1, epsilon=5.0, alpha=5.0)
+    r = np.linspace(0.8, 2.6, 361)
+    h = 1e-6
+    U, dU, d2U = O.pair_terms(spec, r)
+    Up, dUp, _ = O.pair_terms(spec, r + h)
+    Um, dUm, _ = O.pair_terms(spec, r - h)
+    mask = (np.abs(r - 2.0) > 1e-3) & (np.abs(r - 2.5) > 1e-3)
+    np.testing.assert_allclose(dU[mask], ((Up - Um) / (2 * h))[mask], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(d2U[mask], ((dUp - dUm) / (2 * h))[mask], rtol=1e-5, atol=1e-5)
+    assert np.all(U[r >= 2.5] == 0.0) and np.all(dU[r >= 2.5] == 0.0)
+    bare, _, _ = O.morse(r, 1.1, 5.0, 5.0)
+    np.testing.assert_array_equal(U[r < 2.0], bare[r < 2.0])
+
+
+@pytest.mark.parametrize('fmt', [O.DENSE, O.SPARSE, O.ORDERED_SPARSE])
+def test_morse_neighbor_list_matches_all_pairs(fmt):
+    """tests/energy_test.py:647-700, 852-875: the Morse neighbour-list energy
+    and forces equal the all-pairs ones (morse_pair) in every format."""
+    box = np.array([6.0, 6.0, 6.0], np.float32)
+    R = random_box(150, 3, box, seed=5)
+    spec = O.PairSpec(kind='morse', sigma=1.0, epsilon=5.0, alpha=5.0)
+    E0, F0, W0 = O.all_pairs_energy_forces(spec, R, box)
+    nl = O.NeighborListOracle(box, 2.5, 0.5, fmt=fmt)
+    E, F, W = O.pair_energy_forces(spec, R, nl.allocate(R).idx, fmt, box)
+    assert abs(E - E0) <= 1e-10 * max(1.0, abs(E0))
+    np.testing.assert_allclose(F, F0, rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(W, W0, rtol=1e-10, atol=1e-10)
