@@ -16,7 +16,9 @@ Parity pins for this oracle (see ``tests/test_oracle_pins.py``):
     atom and the 6-component stress, tolerance 5e-5 (tests/quantity_test.py:436-455);
   * jammed soft-sphere fixture (tests/data/simulation_test_state.npy): pressure
     0.06307342 (tests/quantity_test.py:134-150) and its stored energy;
-  * closed forms of tests/energy_test.py:284-342,533-562;
+  * closed forms of tests/energy_test.py:284-342,479-520,533-562 (LJ, soft
+    sphere, Morse, the cutoff);
+  * periodic_general identities of tests/space_test.py:302-350,456-600;
   * capacity / overflow shapes of tests/partition_test.py:363-401,489-546.
 """
 from __future__ import annotations
@@ -51,11 +53,78 @@ def periodic_shift(side, R, dR):
 
 
 def displacement(Ra, Rb, box=None):
-    """Displacement Ra - Rb (free) or wrapped (periodic), space.py:275-329."""
+    """Displacement Ra - Rb (free) or wrapped (periodic), space.py:275-329;
+    `box` may also be a space object with a displacement method
+    (PeriodicGeneral)."""
+    if hasattr(box, 'displacement'):
+        return box.displacement(Ra, Rb)
     dR = np.asarray(Ra, np.float64) - np.asarray(Rb, np.float64)
     if box is None:
         return dR
     return periodic_displacement(box, dR)
+
+
+def transform(box, R):
+    """space.py:125-148 (raw_transform): R * box for a scalar or a vector of
+    sides, R @ box^T for a matrix (x = T u row by row)."""
+    b = np.asarray(box, np.float64)
+    R = np.asarray(R, np.float64)
+    if b.size == 1 or b.ndim == 1:
+        return R * b.reshape(-1) if b.ndim == 1 else R * b.item()
+    return np.einsum('ij,...j->...i', b, R)
+
+
+def inverse(box):
+    """space.py:109-119."""
+    b = np.asarray(box, np.float64)
+    return np.linalg.inv(b) if b.ndim == 2 else 1.0 / b
+
+
+@dataclass
+class PeriodicGeneral:
+    """space.periodic_general (space.py:332-468): periodic parallelepiped
+    X = T [0, 1]^d.  With fractional_coordinates positions live in the unit
+    cube and displacements are T d_U(u, v); otherwise positions live in X and
+    are mapped to the cube by T^-1 first.  d_U wraps each component with
+    mod(d + 1/2, 1) - 1/2 (space.py:205-216).  The keyword `box` replaces T
+    (and, for real coordinates, T^-1); `new_box` replaces T only, which
+    deforms real-coordinate displacements (space.py:417-429)."""
+    box: object
+    fractional_coordinates: bool = True
+    wrapped: bool = True
+
+    def displacement(self, Ra, Rb, box=None, new_box=None):
+        T, Ti = self.box, inverse(self.box)
+        if box is not None:
+            T = box
+            if not self.fractional_coordinates:
+                Ti = inverse(box)
+        if new_box is not None:
+            T = new_box
+        Ra = np.asarray(Ra, np.float64)
+        Rb = np.asarray(Rb, np.float64)
+        if not self.fractional_coordinates:
+            Ra, Rb = transform(Ti, Ra), transform(Ti, Rb)
+        return transform(T, periodic_displacement(1.0, Ra - Rb))
+
+    def shift(self, R, dR, box=None, new_box=None):
+        """space.py:439-466: dR lives in X; R in U (fractional) or X."""
+        R = np.asarray(R, np.float64)
+        dR = np.asarray(dR, np.float64)
+        if not self.fractional_coordinates and not self.wrapped:
+            return R + dR
+        T, Ti = self.box, inverse(self.box)
+        if box is not None:
+            T, Ti = box, inverse(box)
+        if new_box is not None:
+            T = new_box
+        dR = transform(Ti, dR)
+        if not self.fractional_coordinates:
+            R = transform(Ti, R)
+        R = np.mod(R + dR, 1.0) if self.wrapped else R + dR
+        if not self.fractional_coordinates:
+            R = transform(T, R)
+        return R
 
 
 # ---------------------------------------------------------------------------

@@ -213,3 +213,117 @@ def test_morse_neighbor_list_matches_all_pairs(fmt):
     assert abs(E - E0) <= 1e-10 * max(1.0, abs(E0))
     np.testing.assert_allclose(F, F0, rtol=1e-10, atol=1e-10)
     np.testing.assert_allclose(W, W0, rtol=1e-10, atol=1e-10)
+
+
+class _WithKwargs:
+    """A space whose displacement always passes box= / new_box= keywords."""
+
+    def __init__(self, sp, **kw):
+        self.sp, self.kw = sp, kw
+
+    def displacement(self, Ra, Rb):
+        return self.sp.displacement(Ra, Rb, **self.kw)
+
+
+@pytest.mark.parametrize('dim', [2, 3])
+def test_periodic_general_diagonal_matches_periodic(dim):
+    """tests/space_test.py:302-350: a diagonal periodic_general box gives the
+    displacements of space.periodic on scaled positions, and its shift
+    times the sides gives periodic's shift."""
+    rng = np.random.default_rng(21)
+    for _ in range(10):
+        sides = 10.0 * rng.uniform(0.05, 1.0, dim)
+        R = rng.uniform(0.0, 1.0, (10, dim))
+        dR = rng.standard_normal((10, dim))
+        g = O.PeriodicGeneral(np.diag(sides))
+        d_per = O.displacement(R[:, None] * sides, R[None] * sides, sides)
+        np.testing.assert_allclose(g.displacement(R[:, None], R[None]), d_per, atol=1e-13)
+        np.testing.assert_allclose(O.periodic_shift(sides, R * sides, dR), g.shift(R, dR) * sides,
+                                   atol=1e-12)
+
+
+@pytest.mark.parametrize('dim', [2, 3])
+def test_periodic_general_wrapped_vs_unwrapped(dim):
+    """tests/space_test.py:456-500: wrapping positions back into the cell does
+    not change displacements (T = I + dT + dT^T)."""
+    rng = np.random.default_rng(22)
+    for _ in range(10):
+        dT = rng.standard_normal((dim, dim))
+        T = np.eye(dim) + dT + dT.T
+        if abs(np.linalg.det(T)) < 0.1:
+            continue
+        R0 = rng.uniform(0.0, 1.0, (10, dim))
+        R, Ru = R0.copy(), R0.copy()
+        g, gu = O.PeriodicGeneral(T), O.PeriodicGeneral(T, wrapped=False)
+        for _ in range(10):
+            dR = rng.standard_normal((10, dim))
+            R, Ru = g.shift(R, dR), gu.shift(Ru, dR)
+            np.testing.assert_allclose(g.displacement(R[:, None], R0[None]),
+                                       g.displacement(Ru[:, None], R0[None]), atol=1e-9)
+        assert np.all((R >= 0) & (R < 1)) and not np.all((Ru > 0) & (Ru < 1))
+
+
+def _general_systems(dim, box_format, seed=0):
+    """tests/space_test.py:48-71: 16 soft spheres at unit density in a
+    periodic box given as a scalar, a vector or a matrix, in the three
+    parameterisations (periodic, periodic_general fractional and real)."""
+    n = 16
+    L = n ** (1.0 / dim)
+    box = {'scalar': L, 'vector': np.full(dim, L), 'matrix': np.eye(dim) * L}[box_format]
+    R_f = np.random.default_rng(seed).uniform(0.0, 1.0, (n, dim))
+    R = O.transform(box, R_f)
+    side = np.diag(box) if box_format == 'matrix' else box
+    return R_f, R, box, side
+
+
+@pytest.mark.parametrize('box_format', ['scalar', 'vector', 'matrix'])
+@pytest.mark.parametrize('dim', [2, 3])
+def test_periodic_general_energy_force_shift(dim, box_format):
+    """tests/space_test.py:509-575: the three parameterisations give the same
+    soft-sphere energy and the same real-space forces (the reference's
+    transform JVP keeps gradients in real space), and shifting by those
+    forces gives the same positions."""
+    R_f, R, box, side = _general_systems(dim, box_format)
+    spec = O.PairSpec(kind='soft_sphere')
+    gf = O.PeriodicGeneral(box)
+    gr = O.PeriodicGeneral(box, fractional_coordinates=False)
+    E, F, _ = O.all_pairs_energy_forces(spec, R, np.broadcast_to(side, (dim,)))
+    E_f, F_f, _ = O.all_pairs_energy_forces(spec, R_f, gf)
+    E_r, F_r, _ = O.all_pairs_energy_forces(spec, R, gr)
+    assert E > 0 and abs(E - E_f) < 1e-12 and abs(E - E_r) < 1e-12
+    np.testing.assert_allclose(F, F_f, atol=1e-12)
+    np.testing.assert_allclose(F, F_r, atol=1e-12)
+    new = O.periodic_shift(np.broadcast_to(side, (dim,)), R, F)
+    np.testing.assert_allclose(new, O.transform(box, gf.shift(R_f, F_f)), atol=1e-12)
+    np.testing.assert_allclose(new, gr.shift(R, F_r), atol=1e-12)
+
+
+@pytest.mark.parametrize('box_format', ['scalar', 'vector', 'matrix'])
+@pytest.mark.parametrize('dim', [2, 3])
+def test_periodic_general_deform(dim, box_format):
+    """tests/space_test.py:577-598: a deformed box passed as box= to the
+    fractional space equals new_box= to the real-coordinate space."""
+    R_f, R, box, _ = _general_systems(dim, box_format)
+    spec = O.PairSpec(kind='soft_sphere')
+    deformed = np.asarray(box) * 0.9
+    E_f = O.all_pairs_energy_forces(spec, R_f, _WithKwargs(O.PeriodicGeneral(box), box=deformed))[0]
+    E_r = O.all_pairs_energy_forces(
+        spec, R, _WithKwargs(O.PeriodicGeneral(box, fractional_coordinates=False),
+                             new_box=deformed))[0]
+    assert E_f > 0 and abs(E_f - E_r) < 1e-12
+
+
+def test_periodic_general_triclinic_parameterisations_agree():
+    """An upper-triangular (triclinic) cell: fractional and real coordinates
+    give the same LJ energy and forces, and a pure shear of the cell changes
+    the energy (the tilt enters the displacement)."""
+    T = np.array([[6.0, 1.2, 0.7], [0.0, 5.5, -0.9], [0.0, 0.0, 6.5]])
+    R_f = np.random.default_rng(4).uniform(0.0, 1.0, (60, 3))
+    spec = O.PairSpec(kind='lj_truncated', r_cutoff=2.5)
+    E_f, F_f, _ = O.all_pairs_energy_forces(spec, R_f, O.PeriodicGeneral(T))
+    E_r, F_r, _ = O.all_pairs_energy_forces(spec, O.transform(T, R_f),
+                                            O.PeriodicGeneral(T, fractional_coordinates=False))
+    assert abs(E_f - E_r) <= 1e-10 * abs(E_f)
+    np.testing.assert_allclose(F_f, F_r, rtol=1e-9, atol=1e-9)
+    E_0 = O.all_pairs_energy_forces(spec, R_f, O.PeriodicGeneral(np.diag(np.diag(T))))[0]
+    assert abs(E_f - E_0) > 1e-6 * abs(E_0)
