@@ -19,6 +19,8 @@ Parity pins for this oracle (see ``tests/test_oracle_pins.py``):
   * closed forms of tests/energy_test.py:284-342,479-520,533-562 (LJ, soft
     sphere, Morse, the cutoff);
   * periodic_general identities of tests/space_test.py:302-350,456-600;
+  * per-particle parameters, neighbour list = all pairs
+    (tests/smap_test.py:1308-1340);
   * capacity / overflow shapes of tests/partition_test.py:363-401,489-546.
 """
 from __future__ import annotations
@@ -436,9 +438,17 @@ class PairSpec:
     per_pair_cutoff: bool = False    # r_on/r_c scaled by sigma_ij instead of max sigma
     species: Optional[np.ndarray] = None
 
-    def params(self, si, sj):
+    def params(self, si, sj, ai=None, aj=None):
+        """Per-pair parameters: scalars as they are, [S,S] matrices by the
+        species of the two atoms, and per-particle [N] arrays combined as
+        0.5 (p_i + p_j) from the atom indices ai, aj (the default combinator,
+        smap.py:833-838 with smap.py:704-713)."""
         def look(p):
             p = np.asarray(p, np.float64)
+            if p.ndim == 1:
+                if ai is None:
+                    raise ValueError('per-particle parameters need the atom indices')
+                return 0.5 * (p[ai] + p[aj])
             if p.ndim == 0 or self.species is None:
                 return p
             return p[si, sj]
@@ -448,9 +458,10 @@ class PairSpec:
         return float(np.max(np.asarray(self.sigma)))
 
 
-def pair_terms(spec: PairSpec, r, si=None, sj=None):
-    """U, U', U'' per pair (f64)."""
-    sig, eps, alp = spec.params(si, sj)
+def pair_terms(spec: PairSpec, r, si=None, sj=None, ai=None, aj=None):
+    """U, U', U'' per pair (f64); si / sj species, ai / aj atom indices of the
+    pairs (for per-particle parameters)."""
+    sig, eps, alp = spec.params(si, sj, ai, aj)
     if spec.kind == 'soft_sphere':
         return soft_sphere(r, sig, eps, alp)
     if spec.kind == 'morse':
@@ -489,7 +500,7 @@ def pair_force_abs_sum(spec: PairSpec, R, nbrs_idx, fmt, box=None):
     r = np.sqrt((dR * dR).sum(-1))
     si = spec.species[i] if spec.species is not None else None
     sj = spec.species[j] if spec.species is not None else None
-    _, dU, _ = pair_terms(spec, r, si, sj)
+    _, dU, _ = pair_terms(spec, r, si, sj, i, j)
     out = np.zeros(N)
     np.add.at(out, i, np.abs(dU))
     np.add.at(out, j, np.abs(dU))
@@ -519,7 +530,7 @@ def pair_energy_forces(spec: PairSpec, R, nbrs_idx, fmt, box=None,
     r = np.sqrt((dR * dR).sum(-1))
     si = species[i] if species is not None else None
     sj = species[j] if species is not None else None
-    U, dU, _ = pair_terms(spec, r, si, sj)
+    U, dU, _ = pair_terms(spec, r, si, sj, i, j)
     with np.errstate(invalid='ignore', divide='ignore'):
         g = np.where(r > 0, dU / r, 0.0)              # U'(r)/r
     # E = sum U / norm ; dE/dR_j = U'/r * dR / norm ; dE/dR_i = -U'/r dR / norm
@@ -567,7 +578,7 @@ def pair_force_vjp(spec: PairSpec, R, nbrs_idx, fmt, lam, box=None):
     u = dR / r[:, None]
     si = spec.species[i] if spec.species is not None else None
     sj = spec.species[j] if spec.species is not None else None
-    U, dU, d2U = pair_terms(spec, r, si, sj)
+    U, dU, d2U = pair_terms(spec, r, si, sj, i, j)
     dl = lam[j] - lam[i]                                   # (lam_j - lam_i)
     ul = (u * dl).sum(-1)
     # F_i += U' u ; F_j -= U' u  (per entry /norm). d(U' u)/dR_j = H_p, /dR_i = -H_p

@@ -327,3 +327,42 @@ def test_periodic_general_triclinic_parameterisations_agree():
     np.testing.assert_allclose(F_f, F_r, rtol=1e-9, atol=1e-9)
     E_0 = O.all_pairs_energy_forces(spec, R_f, O.PeriodicGeneral(np.diag(np.diag(T))))[0]
     assert abs(E_f - E_0) > 1e-6 * abs(E_0)
+
+
+@pytest.mark.parametrize('fmt', [O.DENSE, O.SPARSE, O.ORDERED_SPARSE])
+@pytest.mark.parametrize('dim', [2, 3])
+def test_per_particle_params_neighbor_list_matches_all_pairs(dim, fmt):
+    """tests/smap_test.py:1308-1340: per-particle sigma_i ~ U[0.5, 1.5]
+    combined as 0.5 (sigma_i + sigma_j); a list with cutoff max sigma gives
+    the all-pairs energy, in every format."""
+    rng = np.random.default_rng(31 + dim)
+    n = 120
+    L = 2.0 * n ** (1.0 / dim)
+    box = np.full(dim, L)
+    R = rng.uniform(0.0, L, (n, dim))
+    sig = rng.uniform(0.5, 1.5, n)
+    spec = O.PairSpec(kind='soft_sphere', sigma=sig)
+    E0, F0, _ = O.all_pairs_energy_forces(spec, R, box)
+    nl = O.NeighborListOracle(box, float(sig.max()), 0.0, fmt=fmt)
+    E, F, _ = O.pair_energy_forces(spec, R, nl.allocate(R).idx, fmt, box)
+    assert E0 > 0 and abs(E - E0) <= 1e-12 * E0
+    np.testing.assert_allclose(F, F0, atol=1e-12)
+
+
+def test_per_particle_params_combinator_and_uniform_arrays():
+    """The pair parameter is the mean of the two atoms' values; uniform
+    per-particle arrays reproduce the scalar parameters (LJ, radii from
+    max sigma)."""
+    R = np.array([[0.0, 0.0, 0.0], [1.1, 0.0, 0.0]])
+    spec = O.PairSpec(kind='lj', sigma=np.array([0.9, 1.3]), epsilon=np.array([1.0, 2.0]))
+    E = O.all_pairs_energy_forces(spec, R)[0]
+    U, _, _ = O.pair_terms(O.PairSpec(kind='lj', sigma=1.1, epsilon=1.5, r_onset=2.0 * 1.3 / 1.1,
+                                      r_cutoff=2.5 * 1.3 / 1.1), np.array([1.1]))
+    assert abs(E - U[0]) < 1e-12
+    box = np.full(3, 7.0)
+    Rb = random_box(80, 3, box.astype(np.float32), seed=2)
+    a = O.all_pairs_energy_forces(O.PairSpec(kind='lj', sigma=np.full(80, 1.05),
+                                             epsilon=np.full(80, 0.8)), Rb, box)
+    b = O.all_pairs_energy_forces(O.PairSpec(kind='lj', sigma=1.05, epsilon=0.8), Rb, box)
+    assert abs(a[0] - b[0]) <= 1e-12 * abs(b[0])
+    np.testing.assert_allclose(a[1], b[1], atol=1e-10)
