@@ -21,6 +21,9 @@ Parity pins for this oracle (see ``tests/test_oracle_pins.py``):
   * periodic_general identities of tests/space_test.py:302-350,456-600;
   * per-particle parameters, neighbour list = all pairs
     (tests/smap_test.py:1308-1340);
+  * Langevin (BAOAB): the damped oscillator's mean position and momentum
+    autocorrelation and the equilibrium temperature
+    (tests/simulate_test.py:827-915, statistical);
   * capacity / overflow shapes of tests/partition_test.py:363-401,489-546.
 """
 from __future__ import annotations
@@ -603,6 +606,32 @@ def velocity_verlet(force_fn, R, P, F, mass, dt, box):
         R = np.mod(R, box)
     F = force_fn(R)
     P = P + 0.5 * dt * F
+    return R, P, F
+
+
+def nvt_langevin_step(force_fn, R, P, F, mass, dt, kT, gamma, box, xi):
+    """jax_md/simulate.py:1161-1171 (BAOAB, Davidchack, Ouldridge and
+    Tretyakov 2015): half kick, half drift, the O step
+    p <- c1 p + sqrt(kT (1 - c1^2) m) xi with c1 = exp(-gamma dt)
+    (stochastic_step, simulate.py:1102-1110), half drift, force, half kick.
+    xi is the standard-normal draw of the O step, passed in so that a device
+    run can be replayed exactly from the noise it drew."""
+    m = np.asarray(mass, np.float64)
+    if m.ndim == 1:
+        m = m[:, None]
+    h = 0.5 * dt
+    P = P + h * F
+    R = R + h * P / m
+    if box is not None:
+        R = np.mod(R, box)
+    c1 = math.exp(-gamma * dt)
+    c2 = math.sqrt(kT * (1.0 - c1 * c1))
+    P = c1 * P + c2 * np.sqrt(m) * xi
+    R = R + h * P / m
+    if box is not None:
+        R = np.mod(R, box)
+    F = force_fn(R)
+    P = P + h * F
     return R, P, F
 
 

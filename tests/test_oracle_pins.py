@@ -366,3 +366,59 @@ def test_per_particle_params_combinator_and_uniform_arrays():
     b = O.all_pairs_energy_forces(O.PairSpec(kind='lj', sigma=1.05, epsilon=0.8), Rb, box)
     assert abs(a[0] - b[0]) <= 1e-12 * abs(b[0])
     np.testing.assert_allclose(a[1], b[1], atol=1e-10)
+
+
+def test_langevin_harmonic_matches_theory():
+    """tests/simulate_test.py:872-915: 200,000 independent 1-D oscillators
+    (alpha 1, mass 3, gamma 3, kT 0.25, dt 1e-4) from x = 1 and thermal
+    momenta; after 1000 BAOAB steps the mean position and the momentum
+    autocorrelation follow the overdamped-oscillator solution.  The
+    reference's 1e-3 holds for its own random stream; with another stream the
+    bound is four standard errors of the sample mean (SE ~ 2.4e-3 for the
+    autocorrelation) plus 1e-3 relative."""
+    alpha, mass, gamma, kT, dt, steps, n = 1.0, 3.0, 3.0, 0.25, 1e-4, 1000, 200000
+    rng = np.random.default_rng(41)
+    X = np.ones((n, 1))
+    P = rng.standard_normal((n, 1)) * math.sqrt(kT * mass)
+    P0 = P.copy()
+    force = lambda x: -alpha * x
+    F = force(X)
+    for _ in range(steps):
+        X, P, F = O.nvt_langevin_step(force, X, P, F, mass, dt, kT, gamma, None,
+                                      rng.standard_normal((n, 1)))
+    d = math.sqrt(gamma ** 2 / 4 - alpha / mass)
+    b1, b2 = gamma / 2 + d, gamma / 2 - d
+    A, B = -b2 / (b1 - b2), b1 / (b1 - b2)
+    Z = kT / (2 * d * mass)
+    t = steps * dt
+    pos = A * math.exp(-b1 * t) + B * math.exp(-b2 * t)
+    mom = Z * (-b2 * math.exp(-b2 * t) + b1 * math.exp(-b1 * t)) * mass ** 2
+    se_x = X.std() / math.sqrt(n)
+    pp = P * P0
+    se_p = pp.std() / math.sqrt(n)
+    assert abs(X.mean() - pos) <= 4 * se_x + 1e-3 * abs(pos), (X.mean(), pos, se_x)
+    assert abs(pp.mean() - mom) <= 4 * se_p + 1e-3 * abs(mom), (pp.mean(), mom, se_p)
+    # and the bound is not met trivially: the start is more than 4 SE from the theory
+    assert abs(1.0 - pos) > 4 * se_x and abs(kT * mass - mom) > 4 * se_p
+
+
+def test_langevin_equilibrium_temperature():
+    """tests/simulate_test.py:827-870: particles in harmonic wells with masses
+    U[0.1, 10] thermalise to the bath: the mean kinetic temperature of the
+    later half of the run is within 0.1 of kT."""
+    rng = np.random.default_rng(43)
+    n, dim, dt, gamma = 2000, 3, 1e-2, 0.3
+    R0 = rng.standard_normal((n, dim))
+    R = rng.standard_normal((n, dim))
+    mass = rng.uniform(0.1, 10.0, n)
+    kT = float(rng.uniform(0.3, 1.4))
+    force = lambda x: -2.0 * (x - R0)
+    P = rng.standard_normal((n, dim)) * np.sqrt(mass)[:, None]
+    F = force(R)
+    Ts = []
+    for step in range(6000):
+        R, P, F = O.nvt_langevin_step(force, R, P, F, mass, dt, kT, gamma, None,
+                                      rng.standard_normal((n, dim)))
+        if step > 3000 and step % 100 == 0:
+            Ts.append(float((P * P / mass[:, None]).sum() / (n * dim)))
+    assert abs(np.mean(Ts) - kT) < 0.1, (np.mean(Ts), kT)
