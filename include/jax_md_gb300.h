@@ -51,6 +51,9 @@ extern "C" {
 #define JMD_LJ 0            /* energy.lennard_jones x multiplicative_isotropic_cutoff (energy.py:246-272,534-580) */
 #define JMD_LJ_TRUNCATED 1  /* energy.lennard_jones, hard truncation at r_cutoff */
 #define JMD_SOFT_SPHERE 2   /* energy.soft_sphere (energy.py:125-173) */
+#define JMD_MORSE 3         /* energy.morse (energy.py:346-371), times the multiplicative cutoff
+                               between r_onset and r_cutoff when r_onset < r_cutoff
+                               (energy.py:374-440); sigma = position of the minimum */
 
 #define JMD_MAX_SPECIES 8
 
@@ -79,15 +82,15 @@ typedef struct {
 /* Pair potential parameters.  n_species == 0 means scalar parameters stored
  * at [0][0]; otherwise species matrices [S][S] (smap.py:778-823). */
 typedef struct {
-  int32_t kind;            /* JMD_LJ / JMD_LJ_TRUNCATED / JMD_SOFT_SPHERE */
+  int32_t kind;            /* JMD_LJ / JMD_LJ_TRUNCATED / JMD_SOFT_SPHERE / JMD_MORSE */
   int32_t n_species;
   int32_t per_pair_cutoff; /* 1: r_onset/r_cutoff scale with sigma_ij instead of max sigma */
   int32_t pad_;
-  float r_onset;           /* absolute onset radius (LJ), energy.py:319 */
-  float r_cutoff;          /* absolute cutoff radius (LJ), energy.py:320 */
+  float r_onset;           /* absolute onset radius (LJ, Morse), energy.py:319 */
+  float r_cutoff;          /* absolute cutoff radius (LJ, Morse), energy.py:320 */
   float sigma[JMD_MAX_SPECIES][JMD_MAX_SPECIES];
   float epsilon[JMD_MAX_SPECIES][JMD_MAX_SPECIES];
-  float alpha[JMD_MAX_SPECIES][JMD_MAX_SPECIES];
+  float alpha[JMD_MAX_SPECIES][JMD_MAX_SPECIES];  /* soft-sphere exponent / Morse range */
 } jmd_pair;
 
 const char* jmd_last_error(void);
@@ -312,7 +315,8 @@ int jmd_scale_momentum(float* momentum, int64_t p_stride, int64_t n,
 
 /* ------------------------------------------------------- fused kernels -- */
 
-/* Threads per atom of the float4 Dense pair kernels (4, 8 or 16; default 8). */
+/* Threads per atom of the float4 Dense pair kernels (4, 8 or 16; default 8;
+ * JMD_MORSE always runs at 8). */
 int jmd_set_dense_threads_per_atom(int tpa);
 /* Threads per atom of the generic-stride Dense pair kernel (4, 8, 16, 32). */
 int jmd_set_pair_threads_per_atom(int tpa);

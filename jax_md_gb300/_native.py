@@ -17,7 +17,7 @@ LIB_PATH = PKG / 'libjaxmd_gb300.so'
 
 MAX_SPECIES = 8
 DENSE, SPARSE, ORDERED_SPARSE = 0, 1, 2
-LJ, LJ_TRUNCATED, SOFT_SPHERE = 0, 1, 2
+LJ, LJ_TRUNCATED, SOFT_SPHERE, MORSE = 0, 1, 2, 3
 
 NEIGHBOR_LIST_OVERFLOW = 1
 CELL_LIST_OVERFLOW = 2

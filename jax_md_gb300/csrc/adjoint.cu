@@ -446,10 +446,12 @@ int adjoint_vjp_step(const jmd_nve_system& s, float* xbar, const float* rec, flo
   if (s.space.dim == 3) {
     if (s.pair.kind == JMD_LJ) step_launch<3, JMD_LJ>(tpa, sp, pr, a, t, sg, st);
     else if (s.pair.kind == JMD_LJ_TRUNCATED) step_launch<3, JMD_LJ_TRUNCATED>(tpa, sp, pr, a, t, sg, st);
+    else if (s.pair.kind == JMD_MORSE) step_launch<3, JMD_MORSE>(tpa, sp, pr, a, t, sg, st);
     else step_launch<3, JMD_SOFT_SPHERE>(tpa, sp, pr, a, t, sg, st);
   } else {
     if (s.pair.kind == JMD_LJ) step_launch<2, JMD_LJ>(tpa, sp, pr, a, t, sg, st);
     else if (s.pair.kind == JMD_LJ_TRUNCATED) step_launch<2, JMD_LJ_TRUNCATED>(tpa, sp, pr, a, t, sg, st);
+    else if (s.pair.kind == JMD_MORSE) step_launch<2, JMD_MORSE>(tpa, sp, pr, a, t, sg, st);
     else step_launch<2, JMD_SOFT_SPHERE>(tpa, sp, pr, a, t, sg, st);
   }
   JMD_CUDA(cudaGetLastError());
@@ -501,10 +503,12 @@ int jmd_pair_force_vjp(const jmd_pair* pp, const jmd_space* space, const float* 
   if (space->dim == 3) {
     if (pp->kind == JMD_LJ) vjp_launch<3, JMD_LJ>(sp, eg, a, t, sg, st);
     else if (pp->kind == JMD_LJ_TRUNCATED) vjp_launch<3, JMD_LJ_TRUNCATED>(sp, eg, a, t, sg, st);
+    else if (pp->kind == JMD_MORSE) vjp_launch<3, JMD_MORSE>(sp, eg, a, t, sg, st);
     else vjp_launch<3, JMD_SOFT_SPHERE>(sp, eg, a, t, sg, st);
   } else {
     if (pp->kind == JMD_LJ) vjp_launch<2, JMD_LJ>(sp, eg, a, t, sg, st);
     else if (pp->kind == JMD_LJ_TRUNCATED) vjp_launch<2, JMD_LJ_TRUNCATED>(sp, eg, a, t, sg, st);
+    else if (pp->kind == JMD_MORSE) vjp_launch<2, JMD_MORSE>(sp, eg, a, t, sg, st);
     else vjp_launch<2, JMD_SOFT_SPHERE>(sp, eg, a, t, sg, st);
   }
   return check_launch("jmd_pair_force_vjp");
@@ -550,10 +554,12 @@ int jmd_pair_force_vjp_sparse(const jmd_pair* pp, const jmd_space* space, int32_
   if (space->dim == 3) {
     if (pp->kind == JMD_LJ) svjp_launch<3, JMD_LJ>(sp, eg, a, t, sg, st);
     else if (pp->kind == JMD_LJ_TRUNCATED) svjp_launch<3, JMD_LJ_TRUNCATED>(sp, eg, a, t, sg, st);
+    else if (pp->kind == JMD_MORSE) svjp_launch<3, JMD_MORSE>(sp, eg, a, t, sg, st);
     else svjp_launch<3, JMD_SOFT_SPHERE>(sp, eg, a, t, sg, st);
   } else {
     if (pp->kind == JMD_LJ) svjp_launch<2, JMD_LJ>(sp, eg, a, t, sg, st);
     else if (pp->kind == JMD_LJ_TRUNCATED) svjp_launch<2, JMD_LJ_TRUNCATED>(sp, eg, a, t, sg, st);
+    else if (pp->kind == JMD_MORSE) svjp_launch<2, JMD_MORSE>(sp, eg, a, t, sg, st);
     else svjp_launch<2, JMD_SOFT_SPHERE>(sp, eg, a, t, sg, st);
   }
   return check_launch("jmd_pair_force_vjp_sparse");

@@ -2,9 +2,10 @@
 // kernels (adjoint.cu, batched.cu).
 //
 // Reference: the derivatives jax.grad takes through energy.lennard_jones x
-// multiplicative_isotropic_cutoff and energy.soft_sphere (energy.py:125-173,
-// 246-272, 534-580), with the LJ cutoff radii following max(sigma)
-// (energy.py:319-320).
+// multiplicative_isotropic_cutoff, energy.soft_sphere and energy.morse x
+// multiplicative_isotropic_cutoff (energy.py:125-173, 246-272, 346-440,
+// 534-580), with the LJ cutoff radii following max(sigma) (energy.py:319-320);
+// the Morse radii are absolute.
 #pragma once
 
 #include <algorithm>
@@ -30,6 +31,19 @@ struct PairD {
 template <int KIND>
 __device__ __forceinline__ PairD pair_derivs(float r2, const PairCoef& c, float sigma, float kappa) {
   PairD o;
+  if (KIND == JMD_MORSE) {
+    const MorseTerms m = morse_terms(r2, sigma, c.eps, c.alpha, c.ro2, c.rc2, c.inv_den);
+    o.U = m.U;
+    o.g = m.g;
+    o.hh = m.hh;
+    o.dU_e = m.dU_e;
+    o.dg_e = m.dg_e;
+    o.dU_s = m.dU_s;
+    o.dg_s = m.dg_s;
+    o.dU_k = 0.f;
+    o.dg_k = 0.f;
+    return o;
+  }
   if (KIND == JMD_SOFT_SPHERE) {
     const float r = sqrtf(r2);
     const float is = c.inv_sig;

@@ -812,13 +812,16 @@ int badj_launch(int mode, const jmd_pair& pp, const jmd_batch& bt, const jmd_bat
   using KL = std::integral_constant<int, JMD_LJ>;
   using KT = std::integral_constant<int, JMD_LJ_TRUNCATED>;
   using KS = std::integral_constant<int, JMD_SOFT_SPHERE>;
+  using KM = std::integral_constant<int, JMD_MORSE>;
   if (bt.dim == 3) {
     if (pp.kind == JMD_LJ) go(I3{}, KL{});
     else if (pp.kind == JMD_LJ_TRUNCATED) go(I3{}, KT{});
+    else if (pp.kind == JMD_MORSE) go(I3{}, KM{});
     else go(I3{}, KS{});
   } else {
     if (pp.kind == JMD_LJ) go(I2{}, KL{});
     else if (pp.kind == JMD_LJ_TRUNCATED) go(I2{}, KT{});
+    else if (pp.kind == JMD_MORSE) go(I2{}, KM{});
     else go(I2{}, KS{});
   }
   JMD_CUDA(cudaGetLastError());
@@ -926,10 +929,12 @@ int force_impl(const jmd_pair& pp, const jmd_batch& b, const jmd_batch_nlist& nl
   if (b.dim == 3) {
     if (pp.kind == JMD_LJ) force_launch2<3, JMD_LJ>(mode, sp, v, a, t, gr, energy, ns, st);
     else if (pp.kind == JMD_LJ_TRUNCATED) force_launch2<3, JMD_LJ_TRUNCATED>(mode, sp, v, a, t, gr, energy, ns, st);
+    else if (pp.kind == JMD_MORSE) force_launch2<3, JMD_MORSE>(mode, sp, v, a, t, gr, energy, ns, st);
     else force_launch2<3, JMD_SOFT_SPHERE>(mode, sp, v, a, t, gr, energy, ns, st);
   } else {
     if (pp.kind == JMD_LJ) force_launch2<2, JMD_LJ>(mode, sp, v, a, t, gr, energy, ns, st);
     else if (pp.kind == JMD_LJ_TRUNCATED) force_launch2<2, JMD_LJ_TRUNCATED>(mode, sp, v, a, t, gr, energy, ns, st);
+    else if (pp.kind == JMD_MORSE) force_launch2<2, JMD_MORSE>(mode, sp, v, a, t, gr, energy, ns, st);
     else force_launch2<2, JMD_SOFT_SPHERE>(mode, sp, v, a, t, gr, energy, ns, st);
   }
   JMD_CUDA(cudaGetLastError());

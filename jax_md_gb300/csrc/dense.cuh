@@ -36,7 +36,7 @@ __device__ __forceinline__ float2 rsqrt2(float2 x) {
 
 // Coefficients of two pairs, packed.
 struct Coef2 {
-  float2 sig2, eps, alpha, ro2, rc2, inv_den, inv_sig;
+  float2 sig2, eps, alpha, ro2, rc2, inv_den, inv_sig, sig;
 };
 
 __device__ __forceinline__ Coef2 coef2(const PairCoef& a, const PairCoef& b) {
@@ -48,6 +48,7 @@ __device__ __forceinline__ Coef2 coef2(const PairCoef& a, const PairCoef& b) {
   c.rc2 = f2(a.rc2, b.rc2);
   c.inv_den = f2(a.inv_den, b.inv_den);
   c.inv_sig = f2(a.inv_sig, b.inv_sig);
+  c.sig = f2(a.pad, b.pad);
   return c;
 }
 
@@ -57,6 +58,16 @@ __device__ __forceinline__ Coef2 coef2(const PairCoef& a) { return coef2(a, a); 
 // pairs beyond the cutoff afterwards).
 template <int KIND, bool NEED_U>
 __device__ __forceinline__ void pair_eval2(float2 r2, const Coef2& c, float2& U, float2& g) {
+  if (KIND == JMD_MORSE) {
+    // two scalar evaluations: the exponential has no packed form
+    const MorseTerms a = morse_terms(r2.x, c.sig.x, c.eps.x, c.alpha.x, c.ro2.x, c.rc2.x,
+                                     c.inv_den.x);
+    const MorseTerms b = morse_terms(r2.y, c.sig.y, c.eps.y, c.alpha.y, c.ro2.y, c.rc2.y,
+                                     c.inv_den.y);
+    g = f2(a.g, b.g);
+    if (NEED_U) U = f2(a.U, b.U);
+    return;
+  }
   if (KIND == JMD_SOFT_SPHERE) {
     float2 rs = rsqrt2(r2);            // 1/r
     float2 r = mul2(r2, rs);           // r

@@ -289,12 +289,17 @@ template <int DIM, int TPA, int MODE>
 void launch_kind(int kind, bool sp, bool cnt, const D2Args& a, const PairTable& t, cudaStream_t st) {
   if (kind == JMD_LJ) launch_sp<DIM, TPA, JMD_LJ, MODE>(sp, cnt, a, t, st);
   else if (kind == JMD_LJ_TRUNCATED) launch_sp<DIM, TPA, JMD_LJ_TRUNCATED, MODE>(sp, cnt, a, t, st);
-  else launch_sp<DIM, TPA, JMD_SOFT_SPHERE, MODE>(sp, cnt, a, t, st);
+  else if (kind == JMD_MORSE) {
+    if constexpr (TPA == 8) launch_sp<DIM, 8, JMD_MORSE, MODE>(sp, cnt, a, t, st);
+  } else launch_sp<DIM, TPA, JMD_SOFT_SPHERE, MODE>(sp, cnt, a, t, st);
 }
 
 template <int DIM, int MODE>
 void launch_tpa(int tpa, int kind, bool sp, bool cnt, const D2Args& a, const PairTable& t,
                 cudaStream_t st) {
+  // Morse runs at 8 lanes per atom only: its two exponentials per pair make
+  // the lane width matter little, and one width keeps the build small
+  if (kind == JMD_MORSE) tpa = 8;
   switch (tpa) {
     case 4: launch_kind<DIM, 4, MODE>(kind, sp, cnt, a, t, st); break;
     case 16: launch_kind<DIM, 16, MODE>(kind, sp, cnt, a, t, st); break;

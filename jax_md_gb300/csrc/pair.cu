@@ -37,6 +37,7 @@ PairTable make_pair_table(const jmd_pair& pp) {
       c.eps = pp.epsilon[a][b];
       c.alpha = pp.alpha[a][b];
       c.inv_sig = 1.0f / sig;
+      c.pad = sig;
       if (pp.kind == JMD_SOFT_SPHERE) {
         c.rc2 = sig * sig;
         c.ro2 = c.rc2;
@@ -322,6 +323,7 @@ void dispatch_kind(int kind, bool species, bool ev, const DenseArgs& a, const Pa
                    cudaStream_t st) {
   if (kind == JMD_LJ) dispatch_sp<DIM, TPA, JMD_LJ, VEC4>(species, ev, a, t, st);
   else if (kind == JMD_LJ_TRUNCATED) dispatch_sp<DIM, TPA, JMD_LJ_TRUNCATED, VEC4>(species, ev, a, t, st);
+  else if (kind == JMD_MORSE) dispatch_sp<DIM, TPA, JMD_MORSE, VEC4>(species, ev, a, t, st);
   else dispatch_sp<DIM, TPA, JMD_SOFT_SPHERE, VEC4>(species, ev, a, t, st);
 }
 
@@ -362,6 +364,7 @@ void sparse_kind(int kind, bool species, bool ev, bool v4, bool fv4, const Spars
                  const PairTable& t, cudaStream_t st) {
   if (kind == JMD_LJ) sparse_sp<DIM, JMD_LJ>(species, ev, v4, fv4, a, t, st);
   else if (kind == JMD_LJ_TRUNCATED) sparse_sp<DIM, JMD_LJ_TRUNCATED>(species, ev, v4, fv4, a, t, st);
+  else if (kind == JMD_MORSE) sparse_sp<DIM, JMD_MORSE>(species, ev, v4, fv4, a, t, st);
   else sparse_sp<DIM, JMD_SOFT_SPHERE>(species, ev, v4, fv4, a, t, st);
 }
 
@@ -372,13 +375,15 @@ bool g_force_generic = false;
 
 int validate_pair(const jmd_pair* pp) {
   JMD_REQUIRE(pp != nullptr, "pair parameters are null");
-  JMD_REQUIRE(pp->kind >= 0 && pp->kind <= 2, "unknown pair potential");
+  JMD_REQUIRE(pp->kind >= 0 && pp->kind <= 3, "unknown pair potential");
   JMD_REQUIRE(pp->n_species >= 0 && pp->n_species <= JMD_MAX_SPECIES, "n_species out of range");
   int S = pp->n_species > 0 ? pp->n_species : 1;
   for (int a = 0; a < S; ++a)
     for (int b = 0; b < S; ++b) JMD_REQUIRE(pp->sigma[a][b] > 0.f, "sigma must be positive");
   if (pp->kind != JMD_SOFT_SPHERE)
     JMD_REQUIRE(pp->r_cutoff > 0.f && pp->r_onset <= pp->r_cutoff, "need 0 < r_onset <= r_cutoff");
+  JMD_REQUIRE(pp->kind != JMD_MORSE || !pp->per_pair_cutoff,
+              "Morse radii are absolute (per_pair_cutoff must be 0)");
   return JMD_OK;
 }
 
@@ -451,11 +456,13 @@ int jmd_pair_forces(const jmd_pair* pp, const jmd_space* space, int32_t format,
     a.counter = w.counter;
     a.totals = w.totals;
     a.geo = geo;
-    const int tpa = g_default_tpa;
-    if (ev && ceil_div(n * tpa, 256) > kMaxPairBlocks)
-      return fail(JMD_ERR_UNSUPPORTED, "system too large for the energy reduction");
     const bool fast = !g_force_generic &&
                       dense2_applicable(position, pos_stride, idx, idx_ld, force, force_stride);
+    // lanes per atom of the kernel that will run (the packed path uses its
+    // own width, 8 for Morse): one partial per block must fit the workspace
+    const int tpa = !fast ? g_default_tpa : (pp->kind == JMD_MORSE ? 8 : dense_tpa());
+    if (ev && ceil_div(n * tpa, 256) > kMaxPairBlocks)
+      return fail(JMD_ERR_UNSUPPORTED, "system too large for the energy reduction");
     if (fast) {
       int rc = dense2_forces(pp, space, position, species, n, idx, idx_ld, idx_width, nbr_count,
                              force, energy, per_atom_energy, virial, w.partials, w.counter,

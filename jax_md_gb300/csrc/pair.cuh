@@ -5,6 +5,7 @@
 //   lennard_jones                     :246-272  4 eps ((s/r)^12 - (s/r)^6)
 //   multiplicative_isotropic_cutoff   :534-580  S(r) between r_onset, r_cutoff
 //   soft_sphere                       :125-173  eps/alpha (1 - r/sigma)^alpha
+//   morse                             :346-371  eps (1 - exp(-alpha (r - sigma)))^2 - eps
 #pragma once
 
 #include <functional>
@@ -23,7 +24,7 @@ struct PairCoef {
   float rc2;      // interaction cutoff^2 (LJ r_cutoff, soft sphere sigma^2)
   float inv_den;  // 1 / (rc2 - ro2)^3
   float inv_sig;  // 1 / sigma
-  float pad;
+  float pad;      // sigma (the Morse minimum; unused by the other kinds)
 };
 
 struct PairTable {
@@ -54,12 +55,60 @@ __device__ __forceinline__ float rcp_nr(float x) {
   return fmaf(y, e, y);
 }
 
+// Morse pair under the multiplicative cutoff with absolute radii: U0 =
+// eps ((1 - e)^2 - 1), e = exp(-alpha (r - sigma)); U = U0 S(r^2) with S of
+// multiplicative_isotropic_cutoff for ro2 < r^2 (S = 1 below).  Gives U,
+// g = U'(r)/r, hh = U''(r) and the derivatives of U and g with respect to
+// sigma (U0 depends on r - sigma only, the radii not at all) and epsilon (U
+// is linear in it).  Host and device code: the host copy is unit-tested
+// against the FP64 oracle.
+struct MorseTerms {
+  float U, g, hh, dU_s, dg_s, dU_e, dg_e;
+};
+
+__host__ __device__ inline MorseTerms morse_terms(float r2, float sigma, float eps, float alpha,
+                                                  float ro2, float rc2, float inv_den) {
+  MorseTerms o;
+  const float r = sqrtf(r2);
+  const float ir = 1.0f / r;
+  const float e = expf(-alpha * (r - sigma));
+  const float om = 1.0f - e;
+  const float U0 = eps * om * om - eps;
+  const float U0p = 2.0f * eps * alpha * e * om;                          // U0'
+  const float U0pp = 2.0f * eps * alpha * alpha * e * (2.0f * e - 1.0f);  // U0''
+  float S = 1.f, Su = 0.f, Suu = 0.f;  // S and its derivatives in u = r^2
+  if (r2 > ro2) {
+    const float A = rc2 - r2;
+    const float B = rc2 + 2.0f * r2 - 3.0f * ro2;
+    S = A * A * B * inv_den;
+    Su = 6.0f * A * (ro2 - r2) * inv_den;
+    Suu = 6.0f * (2.0f * r2 - rc2 - ro2) * inv_den;
+  }
+  // U' = U0' S + U0 S' with S' = 2 r Su;  U'' = U0'' S + 2 U0' S' + U0 (4 r^2 Suu + 2 Su)
+  o.U = U0 * S;
+  o.g = U0p * ir * S + 2.0f * U0 * Su;
+  o.hh = U0pp * S + 4.0f * r * U0p * Su + U0 * (4.0f * r2 * Suu + 2.0f * Su);
+  o.dU_s = -U0p * S;
+  o.dg_s = -U0pp * ir * S - 2.0f * U0p * Su;
+  const float U0e = om * om - 1.0f, U0pe = 2.0f * alpha * e * om;  // d/d eps of U0, U0'
+  o.dU_e = U0e * S;
+  o.dg_e = U0pe * ir * S + 2.0f * U0e * Su;
+  return o;
+}
+
 // Evaluates one pair at squared distance r2 (0 < r2 < c.rc2 is the caller's
 // job).  Returns U and g = U'(r)/r; d2 = U''(r) (second derivative) when
 // SECOND, for the adjoint.
 template <int KIND, bool SECOND>
 __device__ __forceinline__ void pair_eval(float r2, const PairCoef& c, float& U, float& g,
                                           float& h) {
+  if (KIND == JMD_MORSE) {
+    const MorseTerms m = morse_terms(r2, c.pad, c.eps, c.alpha, c.ro2, c.rc2, c.inv_den);
+    U = m.U;
+    g = m.g;
+    if (SECOND) h = m.hh;
+    return;
+  }
   if (KIND == JMD_SOFT_SPHERE) {
     float r = sqrtf(r2);
     float x = r * c.inv_sig;

@@ -172,10 +172,12 @@ void tl_launch(int dim, int kind, bool sp, const TArgs& a, const PairTable& t, c
   if (dim == 3) {
     if (kind == JMD_LJ) tl_sp<3, JMD_LJ, MODE>(sp, a, t, st);
     else if (kind == JMD_LJ_TRUNCATED) tl_sp<3, JMD_LJ_TRUNCATED, MODE>(sp, a, t, st);
+    else if (kind == JMD_MORSE) tl_sp<3, JMD_MORSE, MODE>(sp, a, t, st);
     else tl_sp<3, JMD_SOFT_SPHERE, MODE>(sp, a, t, st);
   } else {
     if (kind == JMD_LJ) tl_sp<2, JMD_LJ, MODE>(sp, a, t, st);
     else if (kind == JMD_LJ_TRUNCATED) tl_sp<2, JMD_LJ_TRUNCATED, MODE>(sp, a, t, st);
+    else if (kind == JMD_MORSE) tl_sp<2, JMD_MORSE, MODE>(sp, a, t, st);
     else tl_sp<2, JMD_SOFT_SPHERE, MODE>(sp, a, t, st);
   }
 }

@@ -59,7 +59,10 @@ def make_pair_struct(fn, params: dict, n_species: int) -> N.Pair:
     p.r_cutoff = float(np.float32(rc)) if np.isfinite(rc) else 3.0e38
     ro = fn.r_onset
     p.r_onset = float(np.float32(ro)) if np.isfinite(ro) else p.r_cutoff
-    for key, default in (('sigma', 1.0), ('epsilon', 1.0), ('alpha', 2.0)):
+    # the elementwise functions' own defaults (energy.py:125-131, 246-250, 346-352)
+    defaults = {'sigma': 1.0, 'epsilon': 5.0, 'alpha': 5.0} if fn.kind == N.MORSE else \
+        {'sigma': 1.0, 'epsilon': 1.0, 'alpha': 2.0}
+    for key, default in defaults.items():
         m = _param_matrix(params.get(key, default), n_species, key)
         arr = getattr(p, key)
         for a in range(N.MAX_SPECIES):
@@ -154,8 +157,8 @@ class PairNeighborListEnergy:
                  params):
         if not hasattr(fn, 'kind'):
             raise NotImplementedError('pair_neighbor_list needs a potential from '
-                                      'jax_md_gb300.energy (lennard_jones, soft_sphere or their '
-                                      'multiplicative_isotropic_cutoff); there is no kernel for '
+                                      'jax_md_gb300.energy (lennard_jones, soft_sphere, morse or '
+                                      'their multiplicative_isotropic_cutoff); there is no kernel for '
                                       f'{fn!r}')
         self.fn = fn
         self.geometry = _space.geometry_of(displacement_or_metric)
