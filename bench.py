@@ -154,6 +154,42 @@ def nvt_section(dev, efn, nfn, shift, R, P, steps, warmup):
             'temperature': T, 'overflow': bool(nb.did_buffer_overflow)}
 
 
+def morse_section(dev, R, P, L, steps, warmup):
+    """Morse pairs (energy.morse x the multiplicative cutoff: eps 5, alpha 5,
+    radii 2.0 / 2.5) on the same N = 864,000 FCC positions, sigma at the
+    lattice's nearest-neighbour distance (the crystal sits at the minimum),
+    momenta at half the LJ run's: NVE, K steps as one graph launch.  The
+    list (cutoff 2.5 + skin 0.3) matches the LJ run's, so the rates compare
+    directly; a Morse pair costs two exponentials."""
+    import torch
+    from jax_md_gb300 import energy, partition, quantity, simulate, space
+    sigma = float(np.float32((4 / DENSITY) ** (1 / 3) / np.sqrt(2)))
+    disp, shift = space.periodic(float(L))
+    nfn, efn = energy.morse_neighbor_list(disp, float(L), sigma=sigma, dr_threshold=SKIN,
+                                          format=partition.Dense)
+    Rt = torch.tensor(R, device=dev)
+    nb = nfn.allocate(Rt)
+    init, apply = simulate.nve(efn, shift, DT)
+    st = init(0, Rt, momenta=torch.tensor(P, device=dev) * 0.5, neighbor=nb)
+    st, nb = simulate.run(apply, st, nb, max(3, warmup), neighbor_fn=nfn)
+    st, nb = simulate.run(apply, st, nb, steps, neighbor_fn=nfn)   # records the graph
+    E0 = float(efn.energy_f64(st.position, nb) + quantity._ke_f64(st.momentum))
+    cur = torch.cuda.current_stream(dev)
+    e0, e1 = _events(dev)
+    torch.cuda.synchronize()
+    e0.record(cur)
+    simulate.run(apply, st, nb, steps)
+    e1.record(cur)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    n = len(R)
+    E1 = float(efn.energy_f64(st.position, nb) + quantity._ke_f64(st.momentum))
+    return {'workload': f'Morse NVE (eps 5, alpha 5, sigma {sigma:.4f}, radii 2.0/2.5), same '
+                        f'N={n} FCC positions, momenta x0.5',
+            'steps': steps, 'atom_steps_per_s': n * steps / (ms / 1e3), 'ms_per_step': ms / steps,
+            'energy_drift_per_atom': (E1 - E0) / n, 'overflow': bool(nb.did_buffer_overflow)}
+
+
 def batched_section(dev, n_sys=512, fire_steps=200, nve_steps=200, seed=0, use_graph=True,
                     with_plain=True):
     """512 uneven 2D bidisperse soft-sphere systems (N ~ U[64, 4096], phi
@@ -697,6 +733,13 @@ def main():
         line['batched_adjoint'] = batched_adjoint_section(dev)
     if rank == 0 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline(R, P, L)
+    if rank == 0 and not args.no_extras:
+        # last, and guarded: the newest kernels, so that nothing they do can
+        # cost the line above
+        try:
+            line['morse'] = morse_section(dev, R, P, L, args.steps, args.warmup)
+        except (RuntimeError, MemoryError) as ex:
+            line['morse'] = {'error': str(ex)[:300]}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
