@@ -106,7 +106,7 @@ def _box_list(box, dim):
         if b.ndim == 2:
             if not np.allclose(b, np.diag(np.diag(b))):
                 raise NotImplementedError('general (triclinic) boxes need periodic_general, '
-                                          'which this build does not provide')
+                                          'which the kernels do not implement yet')
             b = np.diag(b)
         return [float(v) for v in b.reshape(-1)[:dim]]
     return [float(box)] * dim
@@ -363,8 +363,8 @@ def neighbor_list(displacement_or_metric, box, r_cutoff, dr_threshold=0.0,
         raise NotImplementedError('custom_mask_function is not supported by the GB300 neighbour '
                                   'list kernels')
     if fractional_coordinates:
-        raise NotImplementedError('fractional_coordinates (periodic_general) is not supported by '
-                                  'this build')
+        raise NotImplementedError('fractional_coordinates (periodic_general) is not implemented '
+                                  'by the kernels yet')
     r_cutoff = float(torch.as_tensor(r_cutoff).max()) if isinstance(r_cutoff, torch.Tensor) else r_cutoff
     dr_threshold = float(dr_threshold)
     always_rebuild = dr_threshold == 0
