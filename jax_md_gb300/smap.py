@@ -50,6 +50,44 @@ def _param_matrix(v, n_species: int, name: str):
                      f'Found ndim={a.ndim}.')
 
 
+def _host(v):
+    return v.detach().cpu().numpy() if isinstance(v, torch.Tensor) else np.asarray(v)
+
+
+def _per_particle_table(params: dict):
+    """Per-particle [N] parameter arrays as a species table.
+
+    The reference combines a per-particle array as 0.5 (p_i + p_j)
+    (smap.py:833-838 with :704-713).  Atoms whose per-particle values are all
+    equal share a species, and the species matrices hold the pairwise means
+    (in float32, as the reference computes them), so the species kernels give
+    exactly the reference's pair parameters.  Returns (params with the
+    matrices, species [N] int32, number of species), or None when no
+    parameter is per-particle.  At most 8 distinct value combinations."""
+    keys = [k for k in ('sigma', 'epsilon', 'alpha')
+            if params.get(k) is not None and np.ndim(_host(params[k])) == 1]
+    if not keys:
+        return None
+    if any(params.get(k) is not None and np.ndim(_host(params[k])) == 2
+           for k in ('sigma', 'epsilon', 'alpha')):
+        raise NotImplementedError('per-particle parameter arrays together with species matrices '
+                                  'are not supported by the pair kernels')
+    cols = [_host(params[k]).astype(np.float32) for k in keys]
+    n = cols[0].shape[0]
+    if any(c.shape[0] != n for c in cols):
+        raise ValueError('per-particle parameter arrays must have one entry per atom')
+    uniq, inv = np.unique(np.stack(cols, 1), axis=0, return_inverse=True)
+    if len(uniq) > N.MAX_SPECIES:
+        raise NotImplementedError(f'per-particle parameters with more than {N.MAX_SPECIES} distinct '
+                                  'values are not supported by the pair kernels (they are mapped '
+                                  'onto species)')
+    out = dict(params)
+    for c, k in enumerate(keys):
+        v = uniq[:, c]
+        out[k] = (np.float32(0.5) * (v[:, None] + v[None, :])).astype(np.float64)
+    return out, np.asarray(inv).reshape(-1).astype(np.int32), len(uniq)
+
+
 def make_pair_struct(fn, params: dict, n_species: int) -> N.Pair:
     p = N.Pair()
     p.kind = fn.kind
@@ -72,6 +110,9 @@ def make_pair_struct(fn, params: dict, n_species: int) -> N.Pair:
 
 
 def _param_tensor(v):
+    if isinstance(v, torch.Tensor) and v.requires_grad and v.dim() == 1:
+        raise NotImplementedError('gradients with respect to per-particle parameter arrays are not '
+                                  'available (the kernels accumulate them per species pair)')
     return v if isinstance(v, torch.Tensor) and v.requires_grad else None
 
 
@@ -166,6 +207,10 @@ class PairNeighborListEnergy:
         self.reduce_axis = reduce_axis
         self.ignore_unused_parameters = ignore_unused_parameters
         self.params = dict(params)
+        # per-particle arrays given here are read once, as the reference's
+        # closure captures them
+        self._pp_static = _per_particle_table(self.params)
+        self._pp_species = {}
         if reduce_axis is not None and tuple(reduce_axis) not in ((1,), (0, 1)):
             raise NotImplementedError('reduce_axis must be None, (1,) or (0, 1) for the pair kernels')
 
@@ -173,9 +218,25 @@ class PairNeighborListEnergy:
     def _resolve(self, R, dynamic):
         species = dynamic.get('species', self.species)
         params = dict(self.params)
+        overridden = False
         for k in ('sigma', 'epsilon', 'alpha'):
             if k in dynamic:
                 params[k] = dynamic[k]
+                overridden = True
+        pp = _per_particle_table(params) if overridden else self._pp_static
+        if pp is not None:
+            if species is not None and not isinstance(species, int):
+                raise NotImplementedError('per-particle parameter arrays together with a species '
+                                          'array are not supported by the pair kernels')
+            params, sp_host, S = pp
+            if len(sp_host) != R.shape[0]:
+                raise ValueError('per-particle parameter arrays must have one entry per atom')
+            species = self._pp_species.get(R.device) if not overridden else None
+            if species is None:
+                species = torch.as_tensor(sp_host).to(device=R.device, dtype=torch.int32)
+                if not overridden:
+                    self._pp_species = {R.device: species}
+            return species, make_pair_struct(self.fn, params, S)
         S = 0
         for k in ('sigma', 'epsilon', 'alpha'):
             v = params.get(k)
