@@ -313,6 +313,18 @@ int jmd_fire_update(float* momentum, const float* force, int64_t n, int32_t dim,
 int jmd_scale_momentum(float* momentum, int64_t p_stride, int64_t n,
                        int32_t dim, const double* scale, void* stream);
 
+/* The O step of simulate.nvt_langevin's BAOAB step (stochastic_step,
+ * simulate.py:1102-1110): p <- c1 p + c2 sqrt(m) xi with c1 = exp(-gamma dt),
+ * c2 = sqrt(kT (1 - c1^2)).  xi is standard normal, drawn per atom from
+ * Philox4x32-10 (Salmon et al., SC'11) on counter (atom, 0, step) and key
+ * seed, then Box-Muller: the same (seed, step) gives the same draws.  The
+ * reference draws from jax.random instead, so runs agree in distribution,
+ * not draw for draw.  noise_out (float4 rows, may be NULL) receives the four
+ * normals of each atom (the first dim are used). */
+int jmd_langevin_o_step(float* momentum, int64_t p_stride, int64_t n, int32_t dim,
+                        const float* mass, float mass_scalar, float c1, float c2, uint64_t seed,
+                        uint64_t step, float* noise_out, void* stream);
+
 /* ------------------------------------------------------- fused kernels -- */
 
 /* Threads per atom of the float4 Dense pair kernels (4, 8 or 16; default 8;

@@ -161,6 +161,8 @@ SIGNATURES = {
     'jmd_pair_force_vjp_sparse': (C.c_int, [C.POINTER(Pair), C.POINTER(Space), I32, P, I64, P, I64,
                                             P, I64, I64, P, I64, F32, P, I64, P, P, P]),
     'jmd_nhc_half_step_vjp': (C.c_int, [C.POINTER(Nhc), P, P, I32, P, P, P, P, P]),
+    'jmd_langevin_o_step': (C.c_int, [P, I64, I64, I32, P, F32, F32, F32, C.c_uint64, C.c_uint64,
+                                      P, P]),
     'jmd_nvt_run': (C.c_int, [C.POINTER(NveSystem), C.POINTER(Nvt), I64, I32, P]),
     'jmd_nvt_run_sorted': (C.c_int, [C.POINTER(NveSystem), C.POINTER(SortedState), C.POINTER(Nvt),
                                      I64, I32, P]),

@@ -9,6 +9,7 @@
 
 #include "common.cuh"
 #include "nhc.cuh"
+#include "rng.cuh"
 
 namespace jmd {
 namespace {
@@ -138,6 +139,24 @@ __global__ void k_scale(float* p, int64_t ps, int n, const double* scale) {
   r[0] *= s;
   r[1] *= s;
   if (DIM == 3) r[2] *= s;
+}
+
+// Langevin O step (simulate.py:1102-1110): p <- c1 p + c2 sqrt(m) xi, xi
+// drawn from (seed, step, atom) (rng.cuh); the draws are optionally written
+// out (float4 rows) so a run can be replayed.
+template <int DIM>
+__global__ void k_langevin_o(float* p, int64_t ps, int n, const float* mass, float m0, float c1,
+                             float c2, uint64_t seed, uint64_t step, float4* noise) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float z[4];
+  langevin_normals(seed, step, (uint32_t)i, z);
+  const float s = c2 * sqrtf(mass ? mass[i] : m0);
+  float* r = p + i * ps;
+  r[0] = fmaf(c1, r[0], s * z[0]);
+  r[1] = fmaf(c1, r[1], s * z[1]);
+  if (DIM == 3) r[2] = fmaf(c1, r[2], s * z[2]);
+  if (noise) noise[i] = make_float4(z[0], z[1], z[2], z[3]);
 }
 
 // ------------------------------------------------------- Nose-Hoover -------
@@ -390,6 +409,28 @@ int jmd_scale_momentum(float* momentum, int64_t p_stride, int64_t n, int32_t dim
   if (dim == 3) k_scale<3><<<gr, 256, 0, as_stream(stream)>>>(momentum, p_stride, (int)n, scale);
   else k_scale<2><<<gr, 256, 0, as_stream(stream)>>>(momentum, p_stride, (int)n, scale);
   return check_launch("jmd_scale_momentum");
+}
+
+int jmd_langevin_o_step(float* momentum, int64_t p_stride, int64_t n, int32_t dim,
+                        const float* mass, float mass_scalar, float c1, float c2, uint64_t seed,
+                        uint64_t step, float* noise_out, void* stream) {
+  JMD_REQUIRE(dim == 2 || dim == 3, "dim must be 2 or 3");
+  JMD_REQUIRE(n >= 0 && n < INT32_MAX, "atom count out of range");
+  JMD_REQUIRE(momentum != nullptr || n == 0, "momentum is null");
+  JMD_REQUIRE(p_stride >= dim, "momentum rows are narrower than dim");
+  JMD_REQUIRE(c1 >= 0.f && c1 <= 1.f && c2 >= 0.f, "need 0 <= c1 <= 1 and c2 >= 0");
+  JMD_REQUIRE(noise_out == nullptr || (reinterpret_cast<uintptr_t>(noise_out) % 16) == 0,
+              "noise rows must be 16-byte aligned");
+  if (n == 0) return JMD_OK;
+  const unsigned gr = (unsigned)ceil_div(n, 256);
+  float4* z = reinterpret_cast<float4*>(noise_out);
+  if (dim == 3)
+    k_langevin_o<3><<<gr, 256, 0, as_stream(stream)>>>(momentum, p_stride, (int)n, mass,
+                                                       mass_scalar, c1, c2, seed, step, z);
+  else
+    k_langevin_o<2><<<gr, 256, 0, as_stream(stream)>>>(momentum, p_stride, (int)n, mass,
+                                                       mass_scalar, c1, c2, seed, step, z);
+  return check_launch("jmd_langevin_o_step");
 }
 
 int jmd_fire_kick_drift(float* position, float* momentum, const float* force, const float* mass,

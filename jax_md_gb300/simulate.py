@@ -372,6 +372,67 @@ def _nvt_struct(chain_fns: '_Chain', state: 'NVTNoseHooverState') -> N.Nvt:
     return v
 
 
+@dataclasses.dataclass
+class NVTLangevinState(_StateMixin):
+    """simulate.py:1075-1099.  The reference's PRNG key becomes the
+    counter-based generator's (seed, step): step k of a run draws from
+    (seed, k, atom), so a run is reproducible from its seed."""
+    position: torch.Tensor
+    momentum: torch.Tensor
+    force: torch.Tensor
+    mass: object
+    seed: int
+    step: int
+
+    @property
+    def velocity(self):
+        return self.momentum / _mass_col(self.mass)
+
+
+def nvt_langevin(energy_or_force_fn, shift_fn, dt, kT, gamma=0.1, center_velocity=True,
+                 **sim_kwargs):
+    """simulate.nvt_langevin (simulate.py:1113-1171): BAOAB (Davidchack,
+    Ouldridge and Tretyakov 2015) -- half kick, half drift, the O step
+    p <- c1 p + sqrt(kT (1 - c1^2) m) xi with c1 = exp(-gamma dt), half drift,
+    force, half kick.  The O step is one kernel drawing xi from a counter-based
+    generator (jmd_langevin_o_step); `key` seeds it (and the initial momenta).
+    The reference's draws come from jax.random, so trajectories agree with it
+    in distribution, not draw for draw."""
+    st = _Stepper(energy_or_force_fn, shift_fn, dt)
+
+    def init_fn(key, R, mass=1.0, momenta=None, **kwargs):
+        _kT = kwargs.pop('kT', kT)
+        R4, F4 = st.new_state_tensors(R, **kwargs)
+        m = canonicalize_mass(mass, R.shape[0], R.device)
+        seed = int(key) if key is not None and not isinstance(key, torch.Generator) else 0
+        P = initialize_momenta(R4, m, key, _kT) if momenta is None else momenta
+        return NVTLangevinState(R4, _rows4(P), F4, m, seed & 0xFFFFFFFFFFFFFFFF, 0)
+
+    def apply_fn(state, **kwargs):
+        _dt = float(np.float32(kwargs.pop('dt', st.dt)))
+        _kT = float(kwargs.pop('kT', kT))
+        h = float(np.float32(_dt / 2))
+        momentum_step(state, h)
+        position_step(state, shift_fn, h)
+        c1 = math.exp(-gamma * _dt)
+        c2 = math.sqrt(_kT * (1.0 - c1 * c1))
+        P = state.momentum
+        mptr, m0 = _mass_ptr(state.mass)
+        N.check(N.lib().jmd_langevin_o_step(P.data_ptr(), P.stride(0), P.shape[0], P.shape[1],
+                                            mptr, m0, float(np.float32(c1)),
+                                            float(np.float32(c2)), state.seed, state.step, None,
+                                            N.stream_ptr()), 'langevin_o_step')
+        state.step += 1
+        position_step(state, shift_fn, h)
+        st.forces_into(state.position, state.force, **kwargs)
+        momentum_step(state, h)
+        return state
+
+    init_fn.stepper = st
+    apply_fn.stepper = st
+    return init_fn, apply_fn
+
+
 def nvt_nose_hoover_invariant(energy_fn, state: NVTNoseHooverState, kT, **kwargs):
     """simulate.py:672-701 (f64)."""
     if quantity._kernel_energy(energy_fn):

@@ -609,6 +609,45 @@ def velocity_verlet(force_fn, R, P, F, mass, dt, box):
     return R, P, F
 
 
+def philox4x32_10(c0, c1, c2, c3, k0, k1):
+    """Philox4x32-10 (Salmon, Moraes, Dror and Shaw, SC'11) on uint32 arrays:
+    ten rounds of two 32x32 -> 64-bit products, word swaps and XORs with
+    the key, the key bumped by the Weyl constants after each round."""
+    m0, m1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
+    w0, w1 = np.uint64(0x9E3779B9), np.uint64(0xBB67AE85)
+    mask = np.uint64(0xFFFFFFFF)
+    c = [np.asarray(x, np.uint64) & mask for x in (c0, c1, c2, c3)]
+    k0 = np.asarray(k0, np.uint64) & mask
+    k1 = np.asarray(k1, np.uint64) & mask
+    for _ in range(10):
+        p0, p1 = m0 * c[0], m1 * c[2]
+        hi0, lo0 = p0 >> np.uint64(32), p0 & mask
+        hi1, lo1 = p1 >> np.uint64(32), p1 & mask
+        c = [hi1 ^ c[1] ^ k0, lo1, hi0 ^ c[3] ^ k1, lo0]
+        k0 = (k0 + w0) & mask
+        k1 = (k1 + w1) & mask
+    return [x.astype(np.uint32) for x in c]
+
+
+def langevin_normals(seed, step, n):
+    """The device's Langevin draws restated: atom i at `step` under `seed`
+    takes Philox4x32-10 on counter (i, 0, step lo, step hi) and key
+    (seed lo, seed hi); each word pair (u0, u1) -> sqrt(-2 ln u0)
+    (cos, sin)(2 pi u1) with u = (top 24 bits + 1/2) / 2^24.  Returns the
+    words [n, 4] (uint32) and the normals [n, 4] (f64)."""
+    i = np.arange(n, dtype=np.uint64)
+    lo, hi = np.uint64(step & 0xFFFFFFFF), np.uint64(step >> 32)
+    w = philox4x32_10(i, np.zeros_like(i), np.full_like(i, lo), np.full_like(i, hi),
+                      np.uint64(seed & 0xFFFFFFFF), np.uint64(seed >> 32))
+    u = [((x >> np.uint32(8)).astype(np.float64) + 0.5) / 16777216.0 for x in w]
+    z = np.empty((n, 4))
+    for h in range(2):
+        rad = np.sqrt(-2.0 * np.log(u[2 * h]))
+        z[:, 2 * h] = rad * np.cos(2 * np.pi * u[2 * h + 1])
+        z[:, 2 * h + 1] = rad * np.sin(2 * np.pi * u[2 * h + 1])
+    return np.stack(w, 1), z
+
+
 def nvt_langevin_step(force_fn, R, P, F, mass, dt, kT, gamma, box, xi):
     """jax_md/simulate.py:1161-1171 (BAOAB, Davidchack, Ouldridge and
     Tretyakov 2015): half kick, half drift, the O step
