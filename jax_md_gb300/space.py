@@ -1,7 +1,8 @@
 """Spaces: periodic and free boundary conditions (jax_md/space.py).
 
-``periodic(side)`` and ``free()`` return ``(displacement_fn, shift_fn)`` with
-the reference's call signatures (space.py:258-329).  The returned callables
+``periodic(side)``, ``free()`` and ``periodic_general(box)`` return
+``(displacement_fn, shift_fn)`` with the reference's call signatures
+(space.py:258-468).  The returned callables
 also carry the geometry (``box``, ``periodic``, ``dim``) so the neighbour-list
 and pair kernels can be configured from them; applied to tensors they compute
 the reference's formulas on the tensor's device.
@@ -107,6 +108,108 @@ class Shift:
         return R + dR
 
 
+def inverse(box):
+    """space.py:109-119: 1 / box for a scalar or sides, the matrix inverse
+    for a cell matrix."""
+    b = box if isinstance(box, torch.Tensor) else torch.as_tensor(box, dtype=torch.float64)
+    return torch.linalg.inv(b) if b.dim() == 2 else 1.0 / b
+
+
+class _Transform(torch.autograd.Function):
+    """x = T u row by row, with the reference's derivative (space.py:155-185):
+    the position tangent passes through unchanged, so gradients taken with
+    respect to fractional positions are real-space gradients."""
+
+    @staticmethod
+    def forward(ctx, box, R):
+        ctx.save_for_backward(box, R)
+        return R * box if box.dim() <= 1 else torch.einsum('ij,...j->...i', box, R)
+
+    @staticmethod
+    def backward(ctx, g):
+        box, R = ctx.saved_tensors
+        gb = None
+        if ctx.needs_input_grad[0]:
+            if box.dim() == 0:
+                gb = (g * R).sum()
+            elif box.dim() == 1:
+                gb = (g * R).reshape(-1, R.shape[-1]).sum(0)
+            else:
+                gb = torch.einsum('...i,...j->ij', g, R)
+        return gb, g
+
+
+def transform(box, R: torch.Tensor) -> torch.Tensor:
+    """space.py:125-185: R * box for a scalar or per-axis sides, R @ box^T
+    for a cell matrix (x = T u), with the reference's pass-through
+    derivative in R."""
+    b = torch.as_tensor(box, dtype=R.dtype, device=R.device)
+    return _Transform.apply(b, R)
+
+
+class GeneralDisplacement:
+    """Displacement of space.periodic_general (space.py:413-434)."""
+
+    def __init__(self, box, fractional_coordinates: bool):
+        self.box = box
+        self.inv_box = inverse(box)
+        self.fractional_coordinates = fractional_coordinates
+
+    def __call__(self, Ra, Rb, perturbation=None, **kwargs):
+        box, inv = self.box, self.inv_box
+        if 'box' in kwargs:
+            box = kwargs['box']
+            if not self.fractional_coordinates:
+                inv = inverse(box)
+        if 'new_box' in kwargs:
+            box = kwargs['new_box']
+        if not self.fractional_coordinates:
+            Ra, Rb = transform(inv, Ra), transform(inv, Rb)
+        dR = transform(box, periodic_displacement(1.0, Ra - Rb))
+        if perturbation is not None:
+            p = torch.as_tensor(perturbation, dtype=dR.dtype, device=dR.device)
+            dR = dR * p if p.dim() <= 1 else torch.einsum('ij,...j->...i', p, dR)
+        return dR
+
+
+class GeneralShift:
+    """Shift of space.periodic_general (space.py:436-466): dR lives in the
+    cell; R in the unit cube (fractional) or in the cell."""
+
+    def __init__(self, box, fractional_coordinates: bool, wrapped: bool):
+        self.box = box
+        self.inv_box = inverse(box)
+        self.fractional_coordinates = fractional_coordinates
+        self.wrapped = wrapped
+
+    def __call__(self, R, dR, **kwargs):
+        if not self.fractional_coordinates and not self.wrapped:
+            return R + dR
+        box, inv = self.box, self.inv_box
+        if 'box' in kwargs:
+            box = kwargs['box']
+            inv = inverse(box)
+        if 'new_box' in kwargs:
+            box = kwargs['new_box']
+        dR = transform(inv, dR)
+        if not self.fractional_coordinates:
+            R = transform(inv, R)
+        R = periodic_shift(1.0, R, dR) if self.wrapped else R + dR
+        if not self.fractional_coordinates:
+            R = transform(box, R)
+        return R
+
+
+def periodic_general(box, fractional_coordinates: bool = True, wrapped: bool = True):
+    """space.periodic_general (space.py:332-468): periodic boundary conditions
+    on the cell T [0, 1]^d (T a scalar, per-axis sides or a cell matrix),
+    positions in the unit cube (fractional_coordinates) or in the cell.  These
+    are tensor functions; the pair and neighbour-list kernels take
+    space.periodic / space.free geometries."""
+    return (GeneralDisplacement(box, fractional_coordinates),
+            GeneralShift(box, fractional_coordinates, wrapped))
+
+
 def periodic(side, wrapped: bool = True):
     """space.periodic (space.py:275-329)."""
     box = _as_box(side)
@@ -139,6 +242,10 @@ def geometry_of(displacement_or_metric):
     inner = getattr(d, 'displacement', None)
     if isinstance(inner, Displacement):
         return inner
+    if isinstance(d, GeneralDisplacement) or isinstance(inner, GeneralDisplacement):
+        raise NotImplementedError('the pair and neighbour-list kernels take space.periodic or '
+                                  'space.free geometries; periodic_general cells are not '
+                                  'implemented by the kernels yet')
     raise TypeError('jax_md_gb300 kernels need a displacement from jax_md_gb300.space.periodic '
                     'or space.free; got ' + repr(d))
 

@@ -1,0 +1,105 @@
+"""space.periodic_general, transform and inverse (space.py:109-185, 332-468)
+on CPU tensors against the oracle's pinned PeriodicGeneral, the reference's
+gradient semantics for fractional coordinates, and the kernels' refusal of
+general cells."""
+import numpy as np
+import pytest
+import torch
+
+from jax_md_gb300 import energy, partition, space
+from oracle import md_oracle as O
+
+
+def _cell(dim, seed):
+    rng = np.random.default_rng(seed)
+    T = np.triu(rng.uniform(-0.6, 0.6, (dim, dim))) + np.diag(rng.uniform(4.0, 6.0, dim))
+    return T, rng
+
+
+@pytest.mark.parametrize('fractional', [True, False])
+@pytest.mark.parametrize('dim', [2, 3])
+def test_periodic_general_matches_oracle(dim, fractional):
+    T, rng = _cell(dim, 10 + dim)
+    U = rng.uniform(0.0, 1.0, (40, dim))
+    R = U if fractional else U @ T.T
+    dR = rng.standard_normal((40, dim))
+    disp, shift = space.periodic_general(torch.tensor(T), fractional_coordinates=fractional)
+    ref = O.PeriodicGeneral(T, fractional_coordinates=fractional)
+    Rt = torch.tensor(R)
+    got = disp(Rt[:, None], Rt[None]).numpy()
+    np.testing.assert_allclose(got, ref.displacement(R[:, None], R[None]), atol=1e-12)
+    np.testing.assert_allclose(shift(Rt, torch.tensor(dR)).numpy(), ref.shift(R, dR), atol=1e-12)
+    T2 = T * 0.9
+    for kw in ({'box': T2}, {'new_box': T2}):
+        got = disp(Rt[:, None], Rt[None], **{k: torch.tensor(v) for k, v in kw.items()}).numpy()
+        np.testing.assert_allclose(got, ref.displacement(R[:, None], R[None], **kw), atol=1e-12)
+        got = shift(Rt, torch.tensor(dR), **{k: torch.tensor(v) for k, v in kw.items()}).numpy()
+        np.testing.assert_allclose(got, ref.shift(R, dR, **kw), atol=1e-12)
+
+
+def test_periodic_general_unwrapped_and_perturbation():
+    T, rng = _cell(3, 4)
+    U = rng.uniform(0.0, 1.0, (20, 3))
+    dR = 3.0 * rng.standard_normal((20, 3))
+    _, sh = space.periodic_general(T, wrapped=False)
+    np.testing.assert_allclose(sh(torch.tensor(U), torch.tensor(dR)).numpy(),
+                               O.PeriodicGeneral(T, wrapped=False).shift(U, dR), atol=1e-12)
+    disp, _ = space.periodic_general(T)
+    eps = np.eye(3) + 0.01 * rng.standard_normal((3, 3))
+    Ut = torch.tensor(U)
+    got = disp(Ut[:, None], Ut[None], perturbation=torch.tensor(eps)).numpy()
+    want = np.einsum('ij,...j->...i', eps, O.PeriodicGeneral(T).displacement(U[:, None], U[None]))
+    np.testing.assert_allclose(got, want, atol=1e-12)
+
+
+def test_transform_inverse_roundtrip_and_pass_through_derivative():
+    """space_test.py:88-170: transform(inverse(T), transform(T, R)) = R, and
+    the derivative in R passes through unchanged (space.py:155-185)."""
+    T, rng = _cell(3, 6)
+    R = torch.tensor(rng.standard_normal((7, 3)), requires_grad=True)
+    X = space.transform(torch.tensor(T), R)
+    np.testing.assert_allclose(space.transform(space.inverse(torch.tensor(T)), X).detach().numpy(),
+                               R.detach().numpy(), atol=1e-12)
+    g = torch.tensor(rng.standard_normal((7, 3)))
+    (X * g).sum().backward()
+    np.testing.assert_array_equal(R.grad.numpy(), g.numpy())
+    for box in (2.5, np.array([2.0, 3.0, 4.0])):
+        np.testing.assert_allclose(space.transform(box, R.detach()).numpy(),
+                                   O.transform(box, R.detach().numpy()), atol=1e-14)
+
+
+@pytest.mark.parametrize('dim', [2, 3])
+def test_fractional_gradients_are_real_space(dim):
+    """space_test.py:351-400, 530-549: the gradient of an energy of
+    fractional positions equals the real-space gradient of the same energy
+    in real coordinates (diagonal and triclinic cells)."""
+    T, rng = _cell(dim, 20 + dim)
+    U = rng.uniform(0.0, 1.0, (30, dim))
+
+    def energy_of(disp, R):
+        d = disp(R[:, None], R[None])
+        r2 = (d * d).sum(-1) + torch.eye(len(R), dtype=R.dtype)
+        return (1.0 / r2).sum()
+    for cell in (np.diag(np.diag(T)), T):
+        df, _ = space.periodic_general(torch.tensor(cell))
+        dr, _ = space.periodic_general(torch.tensor(cell), fractional_coordinates=False)
+        Uf = torch.tensor(U, requires_grad=True)
+        Rr = torch.tensor(U @ cell.T, requires_grad=True)
+        energy_of(df, Uf).backward()
+        energy_of(dr, Rr).backward()
+        np.testing.assert_allclose(Uf.grad.numpy(), Rr.grad.numpy(), rtol=1e-9, atol=1e-9)
+    # the diagonal cell in real coordinates is space.periodic
+    side = np.diag(T)
+    dp, _ = space.periodic(side.tolist())
+    Rp = torch.tensor(U * side, requires_grad=True)
+    energy_of(dp, Rp).backward()
+    dr, _ = space.periodic_general(torch.tensor(np.diag(side)), fractional_coordinates=False)
+    Rr = torch.tensor(U * side, requires_grad=True)
+    energy_of(dr, Rr).backward()
+    np.testing.assert_allclose(Rp.grad.numpy(), Rr.grad.numpy(), rtol=1e-9, atol=1e-9)
+
+
+def test_kernels_refuse_general_cells():
+    disp, _ = space.periodic_general(np.eye(3) * 8.0)
+    with pytest.raises(NotImplementedError, match='periodic_general'):
+        energy.lennard_jones_neighbor_list(disp, 8.0, format=partition.Dense)
