@@ -250,6 +250,14 @@ def geometry_of(displacement_or_metric):
                     'or space.free; got ' + repr(d))
 
 
+def map_product(fn):
+    """space.py:480-484: fn over all pairs, out[b, a] = fn(Ra[a], Rb[b]) (the
+    reference's nested vmaps put Rb on the first axis)."""
+    def wrapped(Ra, Rb, **kwargs):
+        return fn(Ra[None, :, :], Rb[:, None, :], **kwargs)
+    return wrapped
+
+
 def map_bond(fn):
     """space.py:487-491 (tensors broadcast already)."""
     return fn

@@ -103,3 +103,25 @@ def test_kernels_refuse_general_cells():
     disp, _ = space.periodic_general(np.eye(3) * 8.0)
     with pytest.raises(NotImplementedError, match='periodic_general'):
         energy.lennard_jones_neighbor_list(disp, 8.0, format=partition.Dense)
+
+
+def test_map_product_layout():
+    """space.py:480-484: out[b, a] = displacement(Ra[a], Rb[b]), for periodic
+    and periodic_general displacements and for metrics."""
+    rng = np.random.default_rng(3)
+    Ra, Rb = rng.uniform(0, 5, (6, 3)), rng.uniform(0, 5, (4, 3))
+    d, _ = space.periodic(5.0)
+    got = space.map_product(d)(torch.tensor(Ra), torch.tensor(Rb)).numpy()
+    assert got.shape == (4, 6, 3)
+    for b in range(4):
+        for a in range(6):
+            np.testing.assert_allclose(got[b, a], O.displacement(Ra[a], Rb[b], np.full(3, 5.0)),
+                                       atol=1e-12)
+    T = np.array([[5.0, 0.4, 0.0], [0.0, 5.0, 0.3], [0.0, 0.0, 5.0]])
+    dg, _ = space.periodic_general(T)
+    Ua, Ub = Ra / 5.0, Rb / 5.0
+    got = space.map_product(dg)(torch.tensor(Ua), torch.tensor(Ub)).numpy()
+    np.testing.assert_allclose(got[2, 5], O.PeriodicGeneral(T).displacement(Ua[5], Ub[2]), atol=1e-12)
+    m = space.map_product(space.metric(d))(torch.tensor(Ra), torch.tensor(Rb)).numpy()
+    np.testing.assert_allclose(m[1, 3], np.linalg.norm(O.displacement(Ra[3], Rb[1], np.full(3, 5.0))),
+                               atol=1e-12)
