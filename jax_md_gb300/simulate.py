@@ -141,6 +141,9 @@ def _shift_space(shift_fn, dim) -> N.Space:
     s = N.Space()
     s.dim = dim
     periodic = isinstance(shift_fn, _space.Shift) and shift_fn.periodic and shift_fn.wrapped
+    if isinstance(shift_fn, _space.GeneralShift):
+        raise NotImplementedError('the integrator kernels take space.periodic / space.free shifts; '
+                                  'periodic_general cells are not implemented by them yet')
     if not isinstance(shift_fn, _space.Shift):
         raise NotImplementedError('the GB300 integrators need a shift_fn from jax_md_gb300.space')
     s.periodic = 1 if periodic else 0

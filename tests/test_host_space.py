@@ -125,3 +125,10 @@ def test_map_product_layout():
     m = space.map_product(space.metric(d))(torch.tensor(Ra), torch.tensor(Rb)).numpy()
     np.testing.assert_allclose(m[1, 3], np.linalg.norm(O.displacement(Ra[3], Rb[1], np.full(3, 5.0))),
                                atol=1e-12)
+
+
+def test_integrators_refuse_general_shifts():
+    from jax_md_gb300 import simulate
+    _, shift = space.periodic_general(np.eye(3) * 8.0)
+    with pytest.raises(NotImplementedError, match='periodic_general'):
+        simulate._shift_space(shift, 3)
