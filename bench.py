@@ -509,6 +509,31 @@ def adjoint_section(dev, steps=2000, checkpoint_every=100, seed=0):
     return out
 
 
+def cpu_nvt_baseline(R, P, L, budget_s=8.0):
+    """The float32 OpenMP port's Nose-Hoover run (chain 5, tau = 100 dt, chain
+    in f64) on a bounded number of steps of the same system."""
+    from oracle import build as ob
+    lib = ctypes.CDLL(str(ob.build()))
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib.md_cpu_run_nvt.argtypes = [fp, fp, ctypes.c_int] + [ctypes.c_float] * 5 + \
+        [ctypes.c_int] * 3 + [ctypes.c_double] * 2 + [ctypes.c_int] * 3 + [ctypes.c_void_p]
+
+    def run(steps):
+        x = np.ascontiguousarray(R, np.float32).copy()
+        p = np.ascontiguousarray(P, np.float32).copy()
+        t0 = time.perf_counter()
+        rb = lib.md_cpu_run_nvt(x.ctypes.data_as(fp), p.ctypes.data_as(fp), len(x), float(L), 2.0,
+                                2.5, SKIN, DT, 128, steps, 0, KT, 100 * DT, 5, 2, 3, None)
+        return time.perf_counter() - t0, rb
+    dt1, _ = run(2)
+    steps = min(200, max(2, int(budget_s / max(dt1 / 2, 1e-3))))
+    dt, rb = run(steps)
+    threads = ctypes.CDLL(str(ob.build())).md_cpu_max_threads()
+    return {'value': len(R) * steps / dt, 'unit': 'atom-steps/s', 'cores': threads, 'kind': 'port',
+            'sample': f'{steps} Nose-Hoover steps of the N={len(R)} LJ system ({rb} rebuilds), '
+                      f'float32 OpenMP restatement, {threads} threads'}
+
+
 def cpu_baseline(R, P, L, budget_s=15.0):
     """Times the float32 OpenMP port on a bounded number of steps of the same system."""
     dt1, _, threads = cpu_port_run(R, P, L, 2)
@@ -733,6 +758,8 @@ def main():
         line['batched_adjoint'] = batched_adjoint_section(dev)
     if rank == 0 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline(R, P, L)
+        if 'nvt' in line:
+            line['nvt']['cpu_baseline'] = cpu_nvt_baseline(R, P, L)
     if rank == 0 and not args.no_extras:
         # last, and guarded: the newest kernels, so that nothing they do can
         # cost the line above
