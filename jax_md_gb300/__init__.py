@@ -5,6 +5,6 @@ Submodules mirror jax_md: ``space``, ``partition``, ``smap``, ``energy``,
 CUDA library ``libjaxmd_gb300.so`` (C ABI in include/jax_md_gb300.h);
 PyTorch provides device memory and streams.
 """
-from . import space, partition, smap, energy, quantity, simulate, minimize, adjoint, batch  # noqa: F401
+from . import space, partition, smap, energy, quantity, simulate, minimize, adjoint, batch, util  # noqa: F401
 
 __all__ = ["space", "partition", "smap", "energy", "quantity", "simulate", "minimize", "adjoint", "batch"]

@@ -154,6 +154,14 @@ def _shift_space(shift_fn, dim) -> N.Space:
     return s
 
 
+def canonicalize_momenta(state, momenta):
+    """simulate.py:162-165: the state with the given momenta (as float4
+    rows), or unchanged without them."""
+    if momenta is None:
+        return state
+    return state.set(momentum=_rows4(momenta))
+
+
 def initialize_momenta(R, mass, key, kT):
     """simulate.py:141-159 with torch's generator (the JAX PRNG is not reproducible here)."""
     g = key if isinstance(key, torch.Generator) else None

@@ -1,0 +1,37 @@
+"""jax_md.util's numerical helpers and simulate.canonicalize_momenta on CPU
+tensors (util.py:85-112, simulate.py:162-165)."""
+import numpy as np
+import torch
+
+from jax_md_gb300 import simulate, util
+
+
+def test_high_precision_sum_accumulates_in_f64():
+    x = torch.full((1 << 22,), 0.1, dtype=torch.float32)
+    s = util.high_precision_sum(x)
+    assert s.dtype == torch.float32
+    assert float(s) == float(np.float32(np.float64(np.float32(0.1)) * (1 << 22)))
+    m = torch.arange(12, dtype=torch.float32).reshape(3, 4)
+    torch.testing.assert_close(util.high_precision_sum(m, axis=1), m.sum(1))
+    assert util.high_precision_sum(m, axis=(0, 1), keepdims=True).shape == (1, 1)
+    assert util.high_precision_sum(m, keepdims=True).shape == (1, 1)
+    i = torch.tensor([2 ** 30, 2 ** 30], dtype=torch.int32)
+    assert util.high_precision_sum(i).dtype == torch.int32
+
+
+def test_safe_mask_and_downcast():
+    r2 = torch.tensor([0.0, 4.0, 9.0], requires_grad=True)
+    d = util.safe_mask(r2 > 0, torch.sqrt, r2, placeholder=-1.0)
+    assert d.tolist() == [-1.0, 2.0, 3.0]
+    assert util.maybe_downcast(1.5).dtype == torch.float32
+    t = torch.ones(2, dtype=torch.float64)
+    assert util.maybe_downcast(t) is t
+    assert util.maybe_downcast(np.ones(2)).dtype == torch.float32
+
+
+def test_canonicalize_momenta():
+    st = simulate.NVEState(torch.zeros((3, 2)), torch.zeros((3, 2)), torch.zeros((3, 2)), 1.0)
+    assert simulate.canonicalize_momenta(st, None) is st
+    p = torch.arange(6, dtype=torch.float32).reshape(3, 2)
+    new = simulate.canonicalize_momenta(st, p)
+    assert torch.equal(new.momentum, p) and new.momentum.stride(0) == 4
