@@ -230,6 +230,32 @@ class _Stepper:
         return R4, F4
 
 
+class dispatch_by_state:
+    """simulate.py:100-116: wraps a step function and dispatches on the type
+    of ``state.position``; ``fn.register(T)(impl)`` installs ``impl`` for
+    positions of type T (the reference's plug-in point for custom position
+    types, e.g. rigid bodies)."""
+
+    def __init__(self, fn):
+        self._fn = fn
+        self._registry = {}
+        self.__doc__ = fn.__doc__
+        self.__name__ = getattr(fn, '__name__', 'step')
+
+    def __call__(self, state, *args, **kwargs):
+        impl = self._registry.get(type(state.position))
+        if impl is not None:
+            return impl(state, *args, **kwargs)
+        return self._fn(state, *args, **kwargs)
+
+    def register(self, oftype):
+        def register_fn(fn):
+            self._registry[oftype] = fn
+            return fn
+        return register_fn
+
+
+@dispatch_by_state
 def momentum_step(state, dt):
     """simulate.py:168-173 (in place)."""
     P, F = state.momentum, state.force
@@ -239,6 +265,7 @@ def momentum_step(state, dt):
     return state
 
 
+@dispatch_by_state
 def position_step(state, shift_fn, dt, **kwargs):
     """simulate.py:176-188 (in place)."""
     R, P = state.position, state.momentum
@@ -400,6 +427,23 @@ class NVTLangevinState(_StateMixin):
         return self.momentum / _mass_col(self.mass)
 
 
+@dispatch_by_state
+def stochastic_step(state, dt, kT, gamma):
+    """simulate.py:1102-1110, the O step (in place): p <- c1 p +
+    sqrt(kT (1 - c1^2) m) xi with c1 = exp(-gamma dt), xi drawn on the device
+    from (state.seed, state.step, atom); advances state.step."""
+    c1 = math.exp(-gamma * dt)
+    c2 = math.sqrt(kT * (1.0 - c1 * c1))
+    P = state.momentum
+    mptr, m0 = _mass_ptr(state.mass)
+    N.check(N.lib().jmd_langevin_o_step(P.data_ptr(), P.stride(0), P.shape[0], P.shape[1], mptr,
+                                        m0, float(np.float32(c1)), float(np.float32(c2)),
+                                        state.seed, state.step, None, N.stream_ptr()),
+            'langevin_o_step')
+    state.step += 1
+    return state
+
+
 def nvt_langevin(energy_or_force_fn, shift_fn, dt, kT, gamma=0.1, center_velocity=True,
                  **sim_kwargs):
     """simulate.nvt_langevin (simulate.py:1113-1171): BAOAB (Davidchack,
@@ -425,15 +469,7 @@ def nvt_langevin(energy_or_force_fn, shift_fn, dt, kT, gamma=0.1, center_velocit
         h = float(np.float32(_dt / 2))
         momentum_step(state, h)
         position_step(state, shift_fn, h)
-        c1 = math.exp(-gamma * _dt)
-        c2 = math.sqrt(_kT * (1.0 - c1 * c1))
-        P = state.momentum
-        mptr, m0 = _mass_ptr(state.mass)
-        N.check(N.lib().jmd_langevin_o_step(P.data_ptr(), P.stride(0), P.shape[0], P.shape[1],
-                                            mptr, m0, float(np.float32(c1)),
-                                            float(np.float32(c2)), state.seed, state.step, None,
-                                            N.stream_ptr()), 'langevin_o_step')
-        state.step += 1
+        stochastic_step(state, _dt, _kT, gamma)
         position_step(state, shift_fn, h)
         st.forces_into(state.position, state.force, **kwargs)
         momentum_step(state, h)

@@ -35,3 +35,25 @@ def test_canonicalize_momenta():
     p = torch.arange(6, dtype=torch.float32).reshape(3, 2)
     new = simulate.canonicalize_momenta(st, p)
     assert torch.equal(new.momentum, p) and new.momentum.stride(0) == 4
+
+
+def test_dispatch_by_state_registry():
+    """simulate.py:100-116: step functions dispatch on the type of
+    state.position; registered implementations replace the default one for
+    their type only."""
+    class Rigid:
+        pass
+
+    class State:
+        def __init__(self, pos):
+            self.position = pos
+    seen = []
+    for step in (simulate.momentum_step, simulate.position_step, simulate.stochastic_step):
+        step.register(Rigid)(lambda state, *a, _n=step.__name__, **k: seen.append(_n) or state)
+    st = State(Rigid())
+    simulate.momentum_step(st, 0.1)
+    simulate.position_step(st, None, 0.1)
+    simulate.stochastic_step(st, 0.1, 1.0, 0.5)
+    assert seen == ['momentum_step', 'position_step', 'stochastic_step']
+    for step in (simulate.momentum_step, simulate.position_step, simulate.stochastic_step):
+        step._registry.pop(Rigid)
