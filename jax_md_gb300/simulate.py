@@ -266,6 +266,18 @@ def momentum_step(state, dt):
 
 
 @dispatch_by_state
+def kinetic_energy(state):
+    """simulate.py:192-195: quantity.kinetic_energy of a state."""
+    return quantity.kinetic_energy(momentum=state.momentum, mass=state.mass)
+
+
+@dispatch_by_state
+def temperature(state):
+    """simulate.py:198-201: quantity.temperature of a state."""
+    return quantity.temperature(momentum=state.momentum, mass=state.mass)
+
+
+@dispatch_by_state
 def position_step(state, shift_fn, dt, **kwargs):
     """simulate.py:176-188 (in place)."""
     R, P = state.position, state.momentum

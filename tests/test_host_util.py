@@ -57,3 +57,8 @@ def test_dispatch_by_state_registry():
     assert seen == ['momentum_step', 'position_step', 'stochastic_step']
     for step in (simulate.momentum_step, simulate.position_step, simulate.stochastic_step):
         step._registry.pop(Rigid)
+    simulate.kinetic_energy.register(Rigid)(lambda state: 1.25)
+    simulate.temperature.register(Rigid)(lambda state: 0.5)
+    assert simulate.kinetic_energy(st) == 1.25 and simulate.temperature(st) == 0.5
+    simulate.kinetic_energy._registry.pop(Rigid)
+    simulate.temperature._registry.pop(Rigid)
