@@ -17,6 +17,7 @@ import numpy as np
 import torch
 
 from . import _native as N
+from . import quantity
 from . import simulate as _sim
 
 
@@ -40,6 +41,20 @@ class FireDescentState(_sim._StateMixin):
     @property
     def n_pos(self):
         return self.scalars[2].to(torch.int32)
+
+
+def gradient_descent(energy_or_force, shift_fn, step_size: float):
+    """minimize.gradient_descent (minimize.py:65-94): R <- shift(R,
+    step_size F(R)); the state is the positions themselves."""
+    force = quantity.canonicalize_force(energy_or_force)
+
+    def init_fn(R, **unused_kwargs):
+        return R
+
+    def apply_fn(R, **kwargs):
+        return shift_fn(R, step_size * force(R, **kwargs), **kwargs)
+
+    return init_fn, apply_fn
 
 
 def fire_descent(energy_or_force, shift_fn, dt_start=0.1, dt_max=0.4, n_min=5, f_inc=1.1,

@@ -62,3 +62,18 @@ def test_dispatch_by_state_registry():
     assert simulate.kinetic_energy(st) == 1.25 and simulate.temperature(st) == 0.5
     simulate.kinetic_energy._registry.pop(Rigid)
     simulate.temperature._registry.pop(Rigid)
+
+
+def test_gradient_descent_on_a_harmonic_well():
+    """minimize.py:65-94 with a Python energy: each step moves R by
+    step_size F(R), so a harmonic well contracts by (1 - step_size k)."""
+    from jax_md_gb300 import minimize, space
+    _, shift = space.free()
+    k, step = 2.0, 0.1
+    init, apply = minimize.gradient_descent(lambda R, **kw: 0.5 * k * (R * R).sum(), shift, step)
+    R = init(torch.tensor([[1.0, -2.0], [0.5, 0.25]], dtype=torch.float64))
+    for _ in range(5):
+        R = apply(R)
+    np.testing.assert_allclose(R.detach().numpy(),
+                               np.array([[1.0, -2.0], [0.5, 0.25]]) * (1 - step * k) ** 5,
+                               rtol=1e-12)
