@@ -486,6 +486,17 @@ def neighbor_list(displacement_or_metric, box, r_cutoff, dr_threshold=0.0,
     return NeighborListFns(allocate_fn, update_fn)
 
 
+def is_box_valid(box) -> bool:
+    """partition.py:676-681: scalars and side vectors are valid; a cell
+    matrix must be upper triangular."""
+    b = np.asarray(box.detach().cpu() if isinstance(box, torch.Tensor) else box)
+    if b.ndim <= 1:
+        return True
+    if b.ndim == 2:
+        return bool(np.all(np.triu(b) == b))
+    return False
+
+
 def neighbor_list_mask(neighbor: NeighborList, mask_self: bool = False) -> torch.Tensor:
     """partition.py:1167-1182."""
     if is_sparse(neighbor.format):

@@ -9,6 +9,7 @@ instead of differentiating through a box perturbation (quantity.py:202-282).
 from __future__ import annotations
 
 import ctypes
+import math
 from typing import Optional
 
 import numpy as np
@@ -163,3 +164,51 @@ def stress(energy_fn, position, box, mass=1.0, velocity=None, **kwargs):
         m = mass.double().reshape(-1, 1) if isinstance(mass, torch.Tensor) else float(mass)
         VxV = torch.einsum('na,nb->ab', m * v, v)
     return ((VxV - W) / V).to(position.dtype)
+
+
+def clipped_force(energy_fn, max_force: float):
+    """quantity.py:63-73: the force with each atom's vector clipped to norm
+    max_force."""
+    force_fn = force(energy_fn)
+
+    def wrapped(R, *args, **kwargs):
+        f = force_fn(R, *args, **kwargs)
+        n = torch.linalg.norm(f, dim=-1, keepdim=True)
+        return torch.where(n > max_force, f / n * max_force, f)
+    return wrapped
+
+
+def nball_unit_volume(spatial_dimension: int) -> float:
+    """quantity.py:592-596: volume of the unit ball in d dimensions."""
+    return math.pi ** (spatial_dimension / 2) / math.gamma(spatial_dimension / 2 + 1)
+
+
+def particle_volume(radii, spatial_dimension: int, particle_count=1, species=None):
+    """quantity.py:599-624: total volume of balls of the given radii (per
+    particle, per species with `species`, or with counts)."""
+    r = np.asarray(radii.detach().cpu() if isinstance(radii, torch.Tensor) else radii, np.float64)
+    v = nball_unit_volume(spatial_dimension) * r ** spatial_dimension
+    if species is not None:
+        sp = np.asarray(species.detach().cpu() if isinstance(species, torch.Tensor) else species)
+        particle_count = np.bincount(sp.reshape(-1))
+    return float(np.sum(np.asarray(particle_count) * v))
+
+
+def volume_fraction(box, radii, spatial_dimension: int, particle_count=1, species=None) -> float:
+    """quantity.py:627-639."""
+    return particle_volume(radii, spatial_dimension, particle_count, species) / \
+        volume(spatial_dimension, box)
+
+
+def box_size_at_volume_fraction(volume_fraction: float, radii, spatial_dimension: int,
+                                particle_count=1, species=None) -> float:
+    """quantity.py:642-654."""
+    v = particle_volume(radii, spatial_dimension, particle_count, species)
+    return (v / volume_fraction) ** (1.0 / spatial_dimension)
+
+
+def box_size_at_number_density(particle_count: int, number_density: float,
+                               spatial_dimension: int) -> float:
+    """quantity.py:657-660."""
+    return (particle_count / number_density) ** (1.0 / spatial_dimension)
+

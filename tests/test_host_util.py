@@ -77,3 +77,27 @@ def test_gradient_descent_on_a_harmonic_well():
     np.testing.assert_allclose(R.detach().numpy(),
                                np.array([[1.0, -2.0], [0.5, 0.25]]) * (1 - step * k) ** 5,
                                rtol=1e-12)
+
+
+def test_setup_quantities_and_clipped_force():
+    """quantity.py:592-660 (unit-ball volume, particle volume, volume
+    fraction, box sizes), quantity.py:63-73 (clipped force) and
+    partition.py:676-681 (box validity)."""
+    import math
+    from jax_md_gb300 import partition, quantity
+    assert math.isclose(quantity.nball_unit_volume(2), math.pi)
+    assert math.isclose(quantity.nball_unit_volume(3), 4 * math.pi / 3)
+    # the 2D bidisperse packing of the batched workload: phi = 0.84
+    radii = np.array([0.5, 0.7])
+    species = np.array([0, 1, 1, 0, 1, 0])
+    L = quantity.box_size_at_volume_fraction(0.84, radii, 2, species=species)
+    assert math.isclose(quantity.volume_fraction(L, radii, 2, species=species), 0.84)
+    assert math.isclose(L, math.sqrt(3 * math.pi * (0.25 + 0.49) / 0.84))
+    assert math.isclose(quantity.box_size_at_number_density(864000, 0.8442, 3),
+                        (864000 / 0.8442) ** (1 / 3))
+    f = quantity.clipped_force(lambda R: 0.5 * 100.0 * (R * R).sum(), 1.0)
+    F = f(torch.tensor([[0.001, 0.0], [3.0, 4.0]], dtype=torch.float64))
+    np.testing.assert_allclose(F.numpy(), [[-0.1, 0.0], [-0.6, -0.8]], rtol=1e-12)
+    assert partition.is_box_valid(5.0) and partition.is_box_valid(np.ones(3))
+    assert partition.is_box_valid(np.triu(np.ones((3, 3))))
+    assert not partition.is_box_valid(np.ones((3, 3)))
