@@ -1,0 +1,54 @@
+"""Host-side logic of partition (no GPU): the float32 cell grid
+(partition.py:146-188) against the oracle's, the sticky PartitionError bits
+and messages (partition.py:494-561), format predicates, Dense row strides and
+box parsing."""
+import numpy as np
+import pytest
+import torch
+
+from jax_md_gb300 import partition
+from oracle import md_oracle as O
+
+
+@pytest.mark.parametrize('box,cut,dim', [(10.0, 2.8, 3), ([9.0, 4.0, 7.25], 0.615, 3),
+                                         ([8.65, 8.0], 1.0, 2), (100.776, 2.8, 3),
+                                         (16.796, 2.8, 3)])
+def test_cell_dimensions_match_oracle(box, cut, dim):
+    cps, cs, count = partition.cell_dimensions(dim, box, cut)
+    ref = O.cell_dimensions(np.broadcast_to(np.asarray(box, np.float64), (dim,)), cut, dim)
+    ref_cps, ref_cs = np.asarray(ref[0]).reshape(-1)[:dim], np.asarray(ref[1]).reshape(-1)[:dim]
+    assert cps.tolist() == [int(v) for v in ref_cps]
+    np.testing.assert_array_equal(cs, ref_cs.astype(np.float32))
+    assert count == int(np.prod(cps))
+
+
+def test_benchmark_grid():
+    """The LJ benchmark's grid: 35 cells of 2.879 per side at N = 864,000."""
+    cps, cs, count = partition.cell_dimensions(3, 100.776, np.float32(2.5) + np.float32(0.3))
+    assert cps.tolist() == [35, 35, 35] and count == 42875
+    assert abs(float(cs[0]) - 2.879) < 1e-3
+
+
+def test_partition_error_bits_are_sticky():
+    e = partition.PartitionError(torch.zeros((), dtype=torch.uint8))
+    assert str(e) == ''
+    e = e.update(partition.PEC.CELL_SIZE_TOO_SMALL, True)
+    e = e.update(partition.PEC.NEIGHBOR_LIST_OVERFLOW, False)
+    assert int(e.code) == 4 and 'Cell size too small' in str(e)
+    e = e.update(partition.PEC.NEIGHBOR_LIST_OVERFLOW, True)
+    assert int(e.code) == 5 and 'Neighbor list buffer overflow' in str(e)
+    e = e.update(partition.PEC.NEIGHBOR_LIST_OVERFLOW, False)
+    assert int(e.code) == 5
+    assert [int(b) for b in partition.PEC] == [0, 1, 2, 4, 8]
+
+
+def test_formats_row_stride_and_boxes():
+    assert partition.is_sparse(partition.Sparse) and partition.is_sparse(partition.OrderedSparse)
+    assert not partition.is_sparse(partition.Dense)
+    for w, ld in ((1, 8), (8, 8), (9, 16), (98, 104)):
+        assert partition._row_ld(w) == ld
+    assert partition._box_list(5.0, 3) == [5.0] * 3
+    assert partition._box_list(np.diag([3.0, 4.0]), 2) == [3.0, 4.0]
+    assert partition._box_list(torch.tensor([2.0, 3.0, 4.0]), 3) == [2.0, 3.0, 4.0]
+    with pytest.raises(NotImplementedError, match='periodic_general'):
+        partition._box_list(np.array([[3.0, 0.5], [0.0, 4.0]]), 2)
