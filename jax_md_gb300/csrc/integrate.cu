@@ -127,8 +127,12 @@ __global__ void k_ke(const float* p, int64_t ps, const float* mass, float m0, in
   grid_reduce<1>(v, partials, counter, out, false);
 }
 
-// Blocks of a grid-stride reduction over n atoms: 8 atoms per thread at most.
-inline unsigned ke_blocks(int64_t n) { return (unsigned)std::max<int64_t>(1, ceil_div(n, 256 * 8)); }
+// Blocks of a grid-stride reduction over n atoms: 256 threads, 8 atoms per
+// thread at most, so 2048 atoms per block.
+constexpr int64_t kKeAtomsPerBlock = 256 * 8;
+inline unsigned ke_blocks(int64_t n) {
+  return (unsigned)std::max<int64_t>(1, ceil_div(n, kKeAtomsPerBlock));
+}
 
 template <int DIM>
 __global__ void k_scale(float* p, int64_t ps, int n, const double* scale) {
@@ -498,10 +502,14 @@ size_t jmd_fire_workspace_bytes(int64_t n) {
 namespace jmd {
 namespace {
 
-constexpr int64_t kStaticReduceBlocks = 16384;  // 256 atoms per block: 4,194,304 atoms
-constexpr int64_t kStaticMaxAtoms = kStaticReduceBlocks * 256;
+// The documented limit, and the blocks ke_blocks launches for it (2048 atoms
+// per block: 2048 blocks).  The array holds one f64 partial per block.
+constexpr int64_t kStaticMaxAtoms = 4194304;
+constexpr int64_t kStaticReduceBlocks = (kStaticMaxAtoms + kKeAtomsPerBlock - 1) / kKeAtomsPerBlock;
+static_assert(kStaticReduceBlocks * kKeAtomsPerBlock >= kStaticMaxAtoms,
+              "the static partials must cover every block ke_blocks launches at the limit");
 constexpr size_t kStaticCounterOffset = sizeof(double) * kStaticReduceBlocks;
-// 128 KiB of partials + one counter (256 bytes keep the counter aligned).
+// 16 KiB of partials + one counter (256 bytes keep the counter aligned).
 static __device__ __align__(256) unsigned char g_reduce_scratch[kStaticCounterOffset + 256];
 
 constexpr int kMaxDevices = 64;
@@ -554,6 +562,7 @@ int jmd_kinetic_energy_static_scratch(const float* momentum, int64_t p_stride, c
   // the completion counter must start at zero; the partials are overwritten
   JMD_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), st));
   const unsigned gr = ke_blocks(n);
+  JMD_REQUIRE(gr <= kStaticReduceBlocks, "static scratch smaller than the reduction's block count");
   if (dim == 3)
     k_ke<3><<<gr, 256, 0, st>>>(momentum, p_stride, mass, mass_scalar, (int)n, partials, counter, out);
   else

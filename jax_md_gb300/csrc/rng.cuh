@@ -40,19 +40,16 @@ __host__ __device__ inline Words4 philox4x32_10(uint32_t c0, uint32_t c1, uint32
   return o;
 }
 
-// A word as a uniform in (0, 1): the top 24 bits, centred in their interval
-// (never 0, so the logarithm is finite).
+// A word as a uniform in (0, 1): the top 23 bits k give (2k + 1) / 2^24, the
+// centre of the k-th interval of width 2^-23.  2k + 1 < 2^24 fits a float32
+// significand, so the value is exact (no rounding, never 0 or 1, and the
+// logarithm is finite); the oracle forms the same number.
 __host__ __device__ inline float word_to_unit(uint32_t w) {
-  return ((float)(w >> 8) + 0.5f) * (1.0f / 16777216.0f);
+  return (float)(w >> 9) * (1.0f / 8388608.0f) + (1.0f / 16777216.0f);
 }
 
-// Four standard normals of atom `atom` at step `step` under `seed`: Philox on
-// counter (atom, 0, step lo, step hi) and key (seed lo, seed hi), then
-// Box-Muller on word pairs (0, 1) and (2, 3).
-__host__ __device__ inline void langevin_normals(uint64_t seed, uint64_t step, uint32_t atom,
-                                                 float z[4]) {
-  const Words4 r = philox4x32_10(atom, 0u, (uint32_t)step, (uint32_t)(step >> 32), (uint32_t)seed,
-                                 (uint32_t)(seed >> 32));
+// Box-Muller on word pairs (0, 1) and (2, 3): sqrt(-2 ln u0) (cos, sin)(2 pi u1).
+__host__ __device__ inline void normals_from_words(const Words4& r, float z[4]) {
   const float two_pi = 6.283185307179586f;
   for (int h = 0; h < 2; ++h) {
     const float u0 = word_to_unit(r.w[2 * h]), u1 = word_to_unit(r.w[2 * h + 1]);
@@ -60,6 +57,16 @@ __host__ __device__ inline void langevin_normals(uint64_t seed, uint64_t step, u
     z[2 * h] = rad * cosf(two_pi * u1);
     z[2 * h + 1] = rad * sinf(two_pi * u1);
   }
+}
+
+// Four standard normals of atom `atom` at step `step` under `seed`: Philox on
+// counter (atom, 0, step lo, step hi) and key (seed lo, seed hi), then
+// Box-Muller on the four words.
+__host__ __device__ inline void langevin_normals(uint64_t seed, uint64_t step, uint32_t atom,
+                                                 float z[4]) {
+  const Words4 r = philox4x32_10(atom, 0u, (uint32_t)step, (uint32_t)(step >> 32), (uint32_t)seed,
+                                 (uint32_t)(seed >> 32));
+  normals_from_words(r, z);
 }
 
 }  // namespace jmd

@@ -456,13 +456,35 @@ def stochastic_step(state, dt, kT, gamma):
     return state
 
 
+def _mix64(x: int) -> int:
+    """SplitMix64's finaliser (Steele, Lea and Flood 2014): a bijective 64-bit
+    hash, used to derive independent seeds from one key."""
+    x &= 0xFFFFFFFFFFFFFFFF
+    x = ((x ^ (x >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    x = ((x ^ (x >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+    return x ^ (x >> 31)
+
+
+def split_key(key, stream: int) -> int:
+    """The seed of `stream` under `key`: the role random.split plays in the
+    reference (simulate.py:1157), so the initial momenta and the O-step noise
+    of one key are independent.  `key` is an int, a torch.Generator (its
+    initial seed) or None (0)."""
+    if isinstance(key, torch.Generator):
+        base = key.initial_seed()
+    else:
+        base = 0 if key is None else int(key)
+    return _mix64(_mix64(base) ^ (0x9E3779B97F4A7C15 * (stream + 1)))
+
+
 def nvt_langevin(energy_or_force_fn, shift_fn, dt, kT, gamma=0.1, center_velocity=True,
                  **sim_kwargs):
     """simulate.nvt_langevin (simulate.py:1113-1171): BAOAB (Davidchack,
     Ouldridge and Tretyakov 2015) -- half kick, half drift, the O step
     p <- c1 p + sqrt(kT (1 - c1^2) m) xi with c1 = exp(-gamma dt), half drift,
     force, half kick.  The O step is one kernel drawing xi from a counter-based
-    generator (jmd_langevin_o_step); `key` seeds it (and the initial momenta).
+    generator (jmd_langevin_o_step); `key` seeds it and the initial momenta
+    through two independent streams (split_key).
     The reference's draws come from jax.random, so trajectories agree with it
     in distribution, not draw for draw."""
     st = _Stepper(energy_or_force_fn, shift_fn, dt)
@@ -471,9 +493,16 @@ def nvt_langevin(energy_or_force_fn, shift_fn, dt, kT, gamma=0.1, center_velocit
         _kT = kwargs.pop('kT', kT)
         R4, F4 = st.new_state_tensors(R, **kwargs)
         m = canonicalize_mass(mass, R.shape[0], R.device)
-        seed = int(key) if key is not None and not isinstance(key, torch.Generator) else 0
-        P = initialize_momenta(R4, m, key, _kT) if momenta is None else momenta
-        return NVTLangevinState(R4, _rows4(P), F4, m, seed & 0xFFFFFFFFFFFFFFFF, 0)
+        # two streams of one key, as the reference splits its key: the O-step
+        # noise (stream 0) and the initial momenta (stream 1, or the caller's
+        # Generator itself)
+        seed = split_key(key, 0)
+        if momenta is None:
+            mkey = key if isinstance(key, torch.Generator) else split_key(key, 1)
+            P = initialize_momenta(R4, m, mkey, _kT)
+        else:
+            P = momenta
+        return NVTLangevinState(R4, _rows4(P), F4, m, seed, 0)
 
     def apply_fn(state, **kwargs):
         _dt = float(np.float32(kwargs.pop('dt', st.dt)))

@@ -629,23 +629,38 @@ def philox4x32_10(c0, c1, c2, c3, k0, k1):
     return [x.astype(np.uint32) for x in c]
 
 
+def word_to_unit(w):
+    """A 32-bit word as the uniform the device forms: the top 23 bits k give
+    (2k + 1) / 2^24, exact in float32 (so f64 here is the same number)."""
+    w = np.asarray(w, np.uint64)
+    return (2.0 * (w >> np.uint64(9)).astype(np.float64) + 1.0) / 16777216.0
+
+
+def normals_from_words(w):
+    """Box-Muller on word pairs (0, 1) and (2, 3) of w [n, 4]:
+    sqrt(-2 ln u0) (cos, sin)(2 pi u1), in f64."""
+    w = np.asarray(w, np.uint64).reshape(-1, 4)
+    u = [word_to_unit(w[:, k]) for k in range(4)]
+    z = np.empty((len(w), 4))
+    for h in range(2):
+        rad = np.sqrt(-2.0 * np.log(u[2 * h]))
+        z[:, 2 * h] = rad * np.cos(2 * np.pi * u[2 * h + 1])
+        z[:, 2 * h + 1] = rad * np.sin(2 * np.pi * u[2 * h + 1])
+    return z
+
+
 def langevin_normals(seed, step, n):
     """The device's Langevin draws restated: atom i at `step` under `seed`
     takes Philox4x32-10 on counter (i, 0, step lo, step hi) and key
     (seed lo, seed hi); each word pair (u0, u1) -> sqrt(-2 ln u0)
-    (cos, sin)(2 pi u1) with u = (top 24 bits + 1/2) / 2^24.  Returns the
+    (cos, sin)(2 pi u1) with u = (2 (w >> 9) + 1) / 2^24.  Returns the
     words [n, 4] (uint32) and the normals [n, 4] (f64)."""
     i = np.arange(n, dtype=np.uint64)
     lo, hi = np.uint64(step & 0xFFFFFFFF), np.uint64(step >> 32)
     w = philox4x32_10(i, np.zeros_like(i), np.full_like(i, lo), np.full_like(i, hi),
                       np.uint64(seed & 0xFFFFFFFF), np.uint64(seed >> 32))
-    u = [((x >> np.uint32(8)).astype(np.float64) + 0.5) / 16777216.0 for x in w]
-    z = np.empty((n, 4))
-    for h in range(2):
-        rad = np.sqrt(-2.0 * np.log(u[2 * h]))
-        z[:, 2 * h] = rad * np.cos(2 * np.pi * u[2 * h + 1])
-        z[:, 2 * h + 1] = rad * np.sin(2 * np.pi * u[2 * h + 1])
-    return np.stack(w, 1), z
+    w = np.stack(w, 1)
+    return w, normals_from_words(w)
 
 
 def nvt_langevin_step(force_fn, R, P, F, mass, dt, kT, gamma, box, xi):

@@ -51,7 +51,9 @@ def jammed(ref: Path):
 
 
 if __name__ == '__main__':
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    if len(sys.argv) != 2:
+        sys.exit('usage: python tests/golden/make_golden.py /path/to/jax-md')
+    ref = Path(sys.argv[1])
     lammps(ref)
     jammed(ref)
     print('wrote', sorted(p.name for p in HERE.glob('*.npz')))

@@ -38,6 +38,28 @@ def test_device_generator_matches_restatement(driver, seed, step):
     np.testing.assert_allclose(got[:, 4:].astype(np.float64), z, rtol=2e-6, atol=2e-6)
 
 
+def test_uniforms_are_exact_at_the_ends_of_the_word_range(driver):
+    """Words near 0 and 0xFFFFFFFF: the device's float32 uniform equals the
+    oracle's (2 (w >> 9) + 1) / 2^24 exactly and lies strictly inside (0, 1),
+    so u0 near 1 (small Box-Muller radius) replays to float32 rounding of the
+    normals rather than to the rounding of u."""
+    edge = [0, 1, 511, 512, 0xFFFFFFFF, 0xFFFFFFFE, 0xFFFFFE00, 0xFFFFFDFF, 0xFFFFFC00,
+            0x80000000, 0x7FFFFFFF, 0xFFFF0000]
+    rng = np.random.default_rng(7)
+    words = np.array([[a, b, c, d] for a in edge for b, c, d in rng.integers(0, 2 ** 32, (4, 3))],
+                     dtype=np.uint64)
+    words = np.concatenate([words, rng.integers(0xFFFFF000, 2 ** 32, (200, 4), dtype=np.uint64)])
+    text = ''.join('W ' + ' '.join(str(int(x)) for x in w) + '\n' for w in words)
+    out = subprocess.run([str(driver)], input=text, capture_output=True, text=True, check=True)
+    got = np.array([l.split() for l in out.stdout.strip().split('\n')], dtype=np.float64)
+    u = np.stack([O.word_to_unit(words[:, k]) for k in range(4)], 1)
+    np.testing.assert_array_equal(got[:, :4], u)
+    assert np.all(u > 0) and np.all(u < 1)
+    z = O.normals_from_words(words)
+    # the float32 Box-Muller: a few ulp of the radius and of the angle's sin/cos
+    np.testing.assert_allclose(got[:, 4:], z, rtol=2e-6, atol=2e-6)
+
+
 def test_draws_are_standard_normal_and_independent():
     """Moments over 400,000 draws (and across steps and seeds): mean 0,
     variance 1, no correlation between components, steps or seeds, within
