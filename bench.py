@@ -37,9 +37,16 @@ sys.path.insert(0, str(ROOT))
 METRIC = 'atom-steps/s LJ N=864k NVE fp32'
 N_CELLS = 60
 DENSITY, KT, DT, SKIN = 0.8442, 0.722, 0.005, 0.3
-# DRAM bytes of one fused-step launch per atom, from one ncu capture at
-# N=864,000 (dram__bytes_read.sum + dram__bytes_write.sum = 326.9 MB)
-TILED_DRAM_BYTES_PER_ATOM = 378.35
+# DRAM bytes per atom of one segment fused-step launch, from one ncu capture
+# at N=864,000 (dram__bytes_read.sum + dram__bytes_write.sum); None until
+# captured
+SEG_DRAM_BYTES_PER_ATOM = None
+
+
+def workload(cells: int, n: int) -> str:
+    """The workload string both arms print (same physics, same inputs)."""
+    return (f'LJ fluid FCC {cells}^3x4 N={n} rho=0.8442 rc=2.5 r_onset=2.0 skin=0.3 '
+            'dt=0.005 NVE Dense')
 
 
 def peaks():
@@ -568,8 +575,7 @@ def run_reference(args):
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': per * 1e3,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
             'data': 'synthetic', 'impl': 'reference',
-            'config': {'workload': 'LJ fluid FCC 60^3x4 N=864000 rho=0.8442 rc=2.5 skin=0.3 '
-                                   'dt=0.005 NVE Dense', 'inputs': 'host memory (CPU run)'},
+            'config': {'workload': workload(N_CELLS, len(R)), 'inputs': 'host memory (CPU run)'},
             'cpu_baseline': {'value': v, 'unit': 'atom-steps/s', 'cores': threads, 'kind': 'port',
                              'sample': f'{sample_steps} NVE steps per timed step incl. cell list, '
                                        'neighbour list and forces (float32 OpenMP restatement; '
@@ -634,9 +640,10 @@ def main():
     init, apply = simulate.nve(efn, shift, DT)
     st = init(0, Rt, momenta=torch.tensor(P, device=dev), neighbor=nb)
 
-    # launch shape: project autotuner (threads per atom of the fused step)
+    # launch shape: project autotuner (cells per segment, threads per CTA of
+    # the engine's segment-local list), timed on copies of this state
     from jax_md_gb300 import tune
-    tpa, tpa_ms = tune.autotune_dense(efn, st, nb, shift, DT, use_cache=False)
+    seg_choice, seg_ms = tune.autotune_segment(apply, st, nb, steps=20, use_cache=False)
     # warm-up: the engine run (also builds and caches its CUDA graph)
     graphed = not args.direct
     simulate.run(apply, st, nb, max(3, args.warmup), use_graph=graphed)
@@ -667,25 +674,36 @@ def main():
     E1 = float(efn.energy_f64(st.position, nb) + quantity._ke_f64(st.momentum))
     overflow = bool(nb.did_buffer_overflow)
 
-    # dominant kernel alone: the tiled fused step kernel on the engine's
+    # dominant kernel alone: the segment fused step on the engine's
     # cell-ordered state (force + both half kicks + drift + skin test)
     import ctypes as _C
-    nbar = float(nb.nbr_count.float().mean())
+    sb = st._sorted
+    nbar = float(sb.cnt.float().mean())
+    # list bytes as read: 16-byte chunks of 8 two-byte entries per atom
+    chunk_bytes = float((16 * ((sb.cnt.clamp(max=nb.max_occupancy) + 7) // 8)).double().mean())
     species, pair = efn._resolve(st.position, {})
     sp = simulate._shift_space(shift, 3)
-    sb = st._sorted
     xo = torch.empty((n, 4), dtype=torch.float32, device=dev)
     pm = sb.p.clone()
     flag = torch.zeros((), dtype=torch.int32, device=dev)
     L_ = NAT.lib()
+    seg_on = sb.seg is not None
 
     def fused():
-        NAT.check(L_.jmd_nve_fused_step_tiled(_C.byref(pair), _C.byref(sp), sb.xa.data_ptr(),
-                                              xo.data_ptr(), pm.data_ptr(), 1.0, None, n,
-                                              sb.idx.data_ptr(), sb.ld, nb.max_occupancy,
-                                              sb.cnt.data_ptr(), DT, sb.ref.data_ptr(),
-                                              nb.plan.threshold_sq, flag.data_ptr(),
-                                              NAT.stream_ptr()), 'fused step')
+        if seg_on:
+            NAT.check(L_.jmd_nve_fused_step_segment(
+                _C.byref(pair), _C.byref(sp), _C.byref(nb.plan.nl), sb.seg_cells, sb.seg_threads,
+                sb.xa.data_ptr(), xo.data_ptr(), pm.data_ptr(), 1.0, n, 0, sb.seg.data_ptr(),
+                sb.seg_nch, sb.cnt.data_ptr(), DT, sb.ref.data_ptr(), nb.plan.threshold_sq,
+                flag.data_ptr(), sb.ws.data_ptr(), sb.ws.numel(), sb.seg_status.data_ptr(),
+                NAT.stream_ptr()), 'segment fused step')
+        else:
+            NAT.check(L_.jmd_nve_fused_step_tiled(_C.byref(pair), _C.byref(sp), sb.xa.data_ptr(),
+                                                  xo.data_ptr(), pm.data_ptr(), 1.0, None, n,
+                                                  sb.idx.data_ptr(), sb.ld, nb.max_occupancy,
+                                                  sb.cnt.data_ptr(), DT, sb.ref.data_ptr(),
+                                                  nb.plan.threshold_sq, flag.data_ptr(),
+                                                  NAT.stream_ptr()), 'fused step')
     for _ in range(3):
         fused()
     torch.cuda.synchronize()
@@ -697,26 +715,32 @@ def main():
     e1.record(cur)
     torch.cuda.synchronize()
     kern_ms = e0.elapsed_time(e1) / reps
-    # algorithmic bytes of one fused-step launch: Dense index rows (4 B x mean
-    # neighbours), position read + write, momentum read + write, reference read
-    kern_bytes = n * (4 * nbar + 80)
+    assert int(sb.seg_status) == 0, 'segment staging reported a problem'
+    # algorithmic bytes of one fused-step launch: the list as read (16-byte
+    # chunks of 8 two-byte staged slots; int32 entries on the tiled list),
+    # the count, position read + write, momentum read + write, reference read
+    list_bytes = chunk_bytes if seg_on else 4 * nbar
+    kern_bytes = n * (list_bytes + 4 + 80)
     hbm, src = peaks()
     achieved = kern_bytes / (kern_ms / 1e3) / 1e9
-    step_bytes = n * (4 * nbar + 96)
+    # per step: + force row written by the closing kick and read by the next
+    # opening kick is fused away; the skin flag and rebuilds are extra
+    step_bytes = n * (list_bytes + 4 + 80)
 
-    # e2e: host pinned buffers through the public API, every step
+    # e2e: host pinned buffers through the public API (simulate.run, default
+    # path), every step: positions and momenta copied in, one step, copied out
     xh = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
     ph = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
     xh.copy_(st.position)
     ph.copy_(st.momentum)
     e2e_steps = max(5, min(args.steps, 50))
-    simulate.run(apply, st, nb, 1, sort=False)
+    simulate.run(apply, st, nb, 1)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         st.position.copy_(xh, non_blocking=True)
         st.momentum.copy_(ph, non_blocking=True)
-        simulate.run(apply, st, nb, 1, sort=False)
+        simulate.run(apply, st, nb, 1)
         xh.copy_(st.position, non_blocking=True)
         ph.copy_(st.momentum, non_blocking=True)
     torch.cuda.synchronize()
@@ -731,20 +755,28 @@ def main():
         'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_per_step,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
         'data': 'synthetic',
-        'config': {'workload': f'LJ fluid FCC {args.cells}^3x4 N={n} rho=0.8442 rc=2.5 '
-                               'r_onset=2.0 skin=0.3 dt=0.005 NVE Dense, replicas only',
-                   'l2': 'inputs larger than L2 (neighbour rows ~%d MB)' % int(n * 4 * nbar / 1e6),
+        'config': {'workload': workload(args.cells, n),
+                   'multi_gpu': 'replicas only (one independent system per GPU)',
+                   'l2': 'inputs larger than L2 (neighbour list ~%d MB)' % int(n * list_bytes / 1e6),
                    'mean_neighbors': nbar, 'max_occupancy': nb.max_occupancy,
                    'launch': 'cuda graph' if graphed else 'direct',
-                   'threads_per_atom': tpa, 'tpa_ms': {str(k): v for k, v in tpa_ms.items()},
+                   'private_list': 'segment-local (16-bit staged slots)' if seg_on else 'tiled int32',
+                   'segment': {'cells': seg_choice[0] if seg_choice else None,
+                               'threads': seg_choice[1] if seg_choice else None,
+                               'autotune_ms_per_step': {f'{k[0]}x{k[1]}': v
+                                                        for k, v in seg_ms.items()}},
                    'energy_drift_per_atom': (E1 - E0) / n, 'overflow': overflow},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
-                     'frac': achieved / hbm, 'traffic': TILED_DRAM_BYTES_PER_ATOM * n,
+                     'frac': achieved / hbm,
+                     'traffic': (SEG_DRAM_BYTES_PER_ATOM * n
+                                 if (seg_on and SEG_DRAM_BYTES_PER_ATOM) else None),
                      'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one '
-                                       'k_tiled launch at N=864000 (378.35 B/atom), scaled by N',
+                                       'k_seg_step launch at N=864000, scaled by N',
                      'peak_source': src,
-                     'kernel': 'k_tiled fused NVE step (LJ, Dense tiled, FP32x2)', 'kernel_ms': kern_ms,
-                     'bytes_per_atom': 4 * nbar + 80,
+                     'kernel': ('k_seg_step fused NVE step (LJ, segment-local list, FP32x2)'
+                                if seg_on else 'k_tiled fused NVE step (LJ, Dense tiled, FP32x2)'),
+                     'kernel_ms': kern_ms,
+                     'bytes_per_atom': list_bytes + 84,
                      'step_algorithmic_GBps': step_bytes * args.steps / (ms / 1e3) / 1e9},
         'e2e': {'value': e2e_value, 'unit': 'atom-steps/s', 'h2d_bytes_per_step': 2 * n * 12,
                 'd2h_bytes_per_step': 2 * n * 12},

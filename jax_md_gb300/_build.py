@@ -18,8 +18,8 @@ CSRC = PKG / 'csrc'
 BUILD = PKG / '_build'
 LIB = PKG / 'libjaxmd_gb300.so'
 
-SOURCES = ['api.cu', 'nlist.cu', 'pair.cu', 'integrate.cu', 'fused.cu', 'tiled.cu', 'adjoint.cu',
-           'batched.cu', 'engine.cu']
+SOURCES = ['api.cu', 'nlist.cu', 'pair.cu', 'integrate.cu', 'fused.cu', 'tiled.cu', 'segment.cu',
+           'adjoint.cu', 'batched.cu', 'engine.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', '--expt-relaxed-constexpr',
               '-Xptxas', '-warn-spills']

@@ -255,14 +255,21 @@ int enqueue_adjoint(const jmd_nve_system& s, const float* traj, int64_t steps, b
 }
 
 // ---------------------------------------------------------- sorted run ----
+// Copies the caller's state into the private buffers.  With species_in_w the
+// species id rides in the fourth float of the private position rows (the
+// segment kernels read it from the staged positions).
 __global__ void k_load_user(int n, const float4* x, const float4* p, const float4* f,
                             const int32_t* species, float4* xs, float4* ps, float4* fs,
-                            int32_t* ss, int32_t* perm, uint8_t* err) {
+                            int32_t* ss, int32_t* perm, uint8_t* err, int32_t* seg_status,
+                            bool species_in_w) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) *err = 0;
+  if (i == 0) {
+    *err = 0;
+    if (seg_status) *seg_status = 0;
+  }
   if (i >= n) return;
   float4 r = x[i];
-  r.w = 0.f;
+  r.w = (species_in_w && species) ? __int_as_float(species[i]) : 0.f;
   xs[i] = r;
   ps[i] = p[i];
   fs[i] = f[i];
@@ -286,15 +293,38 @@ __global__ void k_store_user(int n, const int32_t* perm, const float4* xs, const
 
 __global__ void k_or_error(uint8_t* dst, const uint8_t* src) { *dst = (uint8_t)(*dst | *src); }
 
+// Segment grid of a run, from the cell grid and the caller's K; false when
+// the segment layout does not apply (the host planned it with jmd_segment_plan).
+bool run_seg_grid(const jmd_nve_system& s, const jmd_sorted_state& z, SegGrid* g) {
+  if (!z.seg_list) return false;
+  if (!make_seg_grid(s.nlist, z.seg_cells, 1, g)) return false;
+  const int rows = s.space.dim == 3 ? 9 : 3;
+  g->cap = rows * (g->K + 2) * s.nlist.cell_capacity;
+  g->threads = z.seg_threads;
+  return true;
+}
+
 int validate_sorted(const jmd_nve_system& s, const jmd_sorted_state& z) {
   JMD_REQUIRE(s.mass == nullptr, "the sorted run needs a scalar mass");
   JMD_REQUIRE(s.nlist.use_cell_list, "the sorted run needs a cell grid");
   JMD_REQUIRE(z.position_a && z.position_b && z.momentum && z.force && z.reference_position &&
                   z.scratch4a && z.scratch4b && z.perm && z.scratch_i_a && z.scratch_i_b &&
-                  z.idx && z.nbr_count && z.error_code && z.occupancy && z.rebuild_flag,
+                  (z.idx || z.seg_list) && z.nbr_count && z.error_code && z.occupancy &&
+                  z.rebuild_flag,
               "null buffer in jmd_sorted_state");
   JMD_REQUIRE(!s.species || z.species, "sorted species buffer required");
-  JMD_REQUIRE(z.idx_ld >= s.nlist.max_occupancy, "tile depth (idx_ld) < max_occupancy");
+  if (z.seg_list) {
+    SegGrid g;
+    JMD_REQUIRE(run_seg_grid(s, z, &g), "the segment layout does not apply to this cell grid");
+    JMD_REQUIRE(g.cap <= kSegMaxStaged, "segment staging capacity beyond 16-bit slots");
+    JMD_REQUIRE(z.seg_nch * 8 >= s.nlist.max_occupancy, "seg_nch * 8 < max_occupancy");
+    JMD_REQUIRE(z.seg_status != nullptr, "seg_status is required with seg_list");
+    JMD_REQUIRE(z.seg_threads >= 32 && z.seg_threads <= kSegMaxThreads && z.seg_threads % 32 == 0,
+                "seg_threads must be a multiple of 32 in [32, 256]");
+    JMD_REQUIRE((reinterpret_cast<uintptr_t>(z.seg_list) % 16) == 0, "seg_list must be 16-byte aligned");
+  } else {
+    JMD_REQUIRE(z.idx_ld >= s.nlist.max_occupancy, "tile depth (idx_ld) < max_occupancy");
+  }
   for (const void* p : {(const void*)z.position_a, (const void*)z.position_b,
                         (const void*)z.momentum, (const void*)z.force,
                         (const void*)z.reference_position, (const void*)z.scratch4a,
@@ -309,6 +339,10 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
   const bool always = s.threshold_sq < 0.f;
   const int n = (int)s.n;
   const unsigned gr = (unsigned)ceil_div(n, 256);
+  SegGrid sg{};
+  const bool seg = run_seg_grid(s, z, &sg);
+  const int32_t* starts = seg ? sort_cell_starts(&s.nlist, s.n, z.workspace, z.workspace_bytes) : nullptr;
+  if (seg && !starts) return fail(JMD_ERR_WORKSPACE, "sorted-run workspace too small");
   // sort + build on the private copy; gated by the flag unless `force_now`
   auto rebuild_at = [&](float* x, bool gated, bool with_force, cudaStream_t q) -> int {
     int32_t* flag = gated ? z.rebuild_flag : nullptr;
@@ -316,9 +350,22 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
                               z.perm, s.n, z.scratch4a, z.scratch4b, z.scratch_i_a, z.scratch_i_b,
                               flag, z.workspace, z.workspace_bytes, q);
     if (rc) return rc;
+    if (seg)
+      return build_segment_after_sort(&s.nlist, sg, x, s.n, z.seg_list, z.seg_nch, z.nbr_count,
+                                      z.occupancy, z.error_code, z.reference_position, z.seg_status,
+                                      flag, z.workspace, z.workspace_bytes, q);
     return build_tiled_after_sort(&s.nlist, x, s.n, z.idx, z.idx_ld, z.nbr_count, z.occupancy,
                                   z.error_code, z.reference_position, flag, z.workspace,
                                   z.workspace_bytes, q);
+  };
+  const bool sp = s.species != nullptr;
+  auto force_kick_at = [&](const float* x, cudaStream_t q) -> int {
+    if (seg)
+      return seg_step(3, s.pair, s.space, sg, x, starts, z.seg_list, z.seg_nch,
+                      s.nlist.max_occupancy, z.nbr_count, z.force, z.momentum, nullptr,
+                      s.mass_scalar, s.dt, nullptr, 0.f, nullptr, z.seg_status, sp, q);
+    return jmd_force_kick_tiled(&s.pair, &s.space, x, z.force, z.momentum, z.species, s.n, z.idx,
+                                z.idx_ld, s.nlist.max_occupancy, z.nbr_count, s.dt, q);
   };
   auto gate = [&](float* x) -> int {
     if (always) return rebuild_at(x, false, false, st);
@@ -334,17 +381,14 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
                                   reinterpret_cast<float4*>(z.position_a),
                                   reinterpret_cast<float4*>(z.momentum),
                                   reinterpret_cast<float4*>(z.force), z.species, z.perm,
-                                  z.error_code);
+                                  z.error_code, seg ? z.seg_status : nullptr, seg);
   JMD_CUDA(cudaGetLastError());
   if ((rc = rebuild_at(z.position_a, false, true, st))) return rc;
   float* cur = z.position_a;
   float* nxt = z.position_b;
   const int64_t width = s.nlist.max_occupancy;
   if (nvt) {
-    auto force_kick = [&](const float* x) -> int {
-      return jmd_force_kick_tiled(&s.pair, &s.space, x, z.force, z.momentum, z.species, s.n,
-                                  z.idx, z.idx_ld, width, z.nbr_count, s.dt, st);
-    };
+    auto force_kick = [&](const float* x) -> int { return force_kick_at(x, st); };
     for (int64_t k = 0; k < steps; ++k) {
       rc = nvt_step(s, *nvt, cur, z.momentum, z.force, nullptr, z.reference_position,
                     z.rebuild_flag, always, gate, force_kick, st);
@@ -358,17 +402,21 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
     if (rc) return rc;
     for (int64_t k = 1; k < steps; ++k) {
       if ((rc = gate(cur))) return rc;
-      rc = jmd_nve_fused_step_tiled(&s.pair, &s.space, cur, nxt, z.momentum, s.mass_scalar,
-                                    z.species, s.n, z.idx, z.idx_ld, width, z.nbr_count, s.dt,
-                                    always ? nullptr : z.reference_position, s.threshold_sq,
-                                    always ? nullptr : z.rebuild_flag, st);
+      if (seg)
+        rc = seg_step(2, s.pair, s.space, sg, cur, starts, z.seg_list, z.seg_nch, width,
+                      z.nbr_count, nullptr, z.momentum, nxt, s.mass_scalar, s.dt,
+                      always ? nullptr : z.reference_position, s.threshold_sq,
+                      always ? nullptr : z.rebuild_flag, z.seg_status, sp, st);
+      else
+        rc = jmd_nve_fused_step_tiled(&s.pair, &s.space, cur, nxt, z.momentum, s.mass_scalar,
+                                      z.species, s.n, z.idx, z.idx_ld, width, z.nbr_count, s.dt,
+                                      always ? nullptr : z.reference_position, s.threshold_sq,
+                                      always ? nullptr : z.rebuild_flag, st);
       if (rc) return rc;
       std::swap(cur, nxt);
     }
     if ((rc = gate(cur))) return rc;
-    rc = jmd_force_kick_tiled(&s.pair, &s.space, cur, z.force, z.momentum, z.species, s.n, z.idx,
-                              z.idx_ld, width, z.nbr_count, s.dt, st);
-    if (rc) return rc;
+    if ((rc = force_kick_at(cur, st))) return rc;
   }
   k_store_user<<<gr, 256, 0, st>>>(n, z.perm, reinterpret_cast<const float4*>(cur),
                                    reinterpret_cast<const float4*>(z.momentum),
@@ -379,11 +427,14 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
                                    reinterpret_cast<float4*>(s.force),
                                    reinterpret_cast<float4*>(s.reference_position));
   JMD_CUDA(cudaGetLastError());
-  // the caller's list, in the reference's order, at the last rebuild's positions
-  rc = jmd_neighbor_list_build(&s.nlist, s.reference_position, 4, s.n, s.idx, s.idx_ld,
-                               s.nbr_count, s.occupancy, s.error_code, s.reference_position, 4,
-                               nullptr, s.nl_workspace, s.nl_workspace_bytes, st);
-  if (rc) return rc;
+  // the caller's list, in the reference's order, at the last rebuild's
+  // positions (unless the caller builds it when it is read)
+  if (!(z.flags & JMD_RUN_SKIP_EXIT_LIST)) {
+    rc = jmd_neighbor_list_build(&s.nlist, s.reference_position, 4, s.n, s.idx, s.idx_ld,
+                                 s.nbr_count, s.occupancy, s.error_code, s.reference_position, 4,
+                                 nullptr, s.nl_workspace, s.nl_workspace_bytes, st);
+    if (rc) return rc;
+  }
   k_or_error<<<1, 1, 0, st>>>(s.error_code, z.error_code);
   JMD_CUDA(cudaGetLastError());
   return JMD_OK;
@@ -628,6 +679,62 @@ int jmd_nvt_run_sorted(const jmd_nve_system* sys, const jmd_sorted_state* sorted
   return launch_graphed(key, [&](cudaStream_t cs, cudaStream_t bs) {
     return enqueue_run_sorted(*sys, *sorted, n_steps, true, cs, bs, nvt);
   }, st);
+}
+
+int jmd_segment_plan(const jmd_nlist* nl, int32_t cells, int32_t* n_segments,
+                     int32_t* capacity_atoms, int64_t* smem_bytes, int32_t* cells_used) {
+  JMD_REQUIRE(nl != nullptr, "nlist descriptor is null");
+  SegGrid g;
+  if (!make_seg_grid(*nl, cells, 1, &g))
+    return fail(JMD_ERR_INVALID_ARGUMENT,
+                "the segment layout needs a cell grid with >= 3 cells per side and 1 <= K <= 14");
+  const int rows = nl->space.dim == 3 ? 9 : 3;
+  const int64_t cap = (int64_t)rows * (g.K + 2) * std::max(1, nl->cell_capacity);
+  // the shared memory a CTA may opt into (227 KB on this part); without a
+  // device (host-only use) assume that figure
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+    cudaGetLastError();
+    optin = 227 * 1024;
+  }
+  const int64_t smem = cap * (int64_t)sizeof(float4);
+  const int64_t static_smem = (int64_t)sizeof(SegShared) + 64 * (int64_t)sizeof(PairCoef) + 64;
+  if (cap > kSegMaxStaged || smem + static_smem > optin)
+    return fail(JMD_ERR_INVALID_ARGUMENT, "segment staging exceeds a CTA's shared memory");
+  if (n_segments) *n_segments = g.nseg;
+  if (capacity_atoms) *capacity_atoms = (int32_t)cap;
+  if (smem_bytes) *smem_bytes = smem;
+  if (cells_used) *cells_used = g.K;
+  return JMD_OK;
+}
+
+int jmd_nve_fused_step_segment(const jmd_pair* pair, const jmd_space* space, const jmd_nlist* nl,
+                               int32_t cells, int32_t threads, const float* position,
+                               float* position_next, float* momentum, float mass_scalar, int64_t n,
+                               int32_t species_in_w, const uint16_t* seg_list, int64_t seg_nch,
+                               const int32_t* nbr_count, float dt, const float* reference_position,
+                               float threshold_sq, int32_t* rebuild_flag, void* workspace,
+                               size_t workspace_bytes, int32_t* seg_status, void* stream) {
+  JMD_REQUIRE(pair && space && nl, "null descriptor");
+  JMD_REQUIRE(n > 0 && n < INT32_MAX, "atom count out of range");
+  JMD_REQUIRE(position && position_next && momentum && seg_list && nbr_count && seg_status,
+              "null buffer");
+  JMD_REQUIRE(position != position_next, "position and position_next must differ");
+  JMD_REQUIRE(reference_position == nullptr || rebuild_flag != nullptr, "skin test needs a flag");
+  JMD_REQUIRE(threads >= 32 && threads <= kSegMaxThreads && threads % 32 == 0,
+              "threads must be a multiple of 32 in [32, 256]");
+  JMD_REQUIRE(seg_nch * 8 >= nl->max_occupancy, "seg_nch * 8 < max_occupancy");
+  SegGrid g;
+  JMD_REQUIRE(make_seg_grid(*nl, cells, 1, &g), "the segment layout does not apply to this cell grid");
+  g.cap = (nl->space.dim == 3 ? 9 : 3) * (g.K + 2) * nl->cell_capacity;
+  g.threads = threads;
+  JMD_REQUIRE(g.cap <= kSegMaxStaged, "segment staging capacity beyond 16-bit slots");
+  const int32_t* starts = sort_cell_starts(nl, n, workspace, workspace_bytes);
+  if (!starts) return fail(JMD_ERR_WORKSPACE, "workspace too small for the cell starts");
+  return seg_step(2, *pair, *space, g, position, starts, seg_list, seg_nch, nl->max_occupancy,
+                  nbr_count, nullptr, momentum, position_next, mass_scalar, dt, reference_position,
+                  threshold_sq, rebuild_flag, seg_status, species_in_w != 0, as_stream(stream));
 }
 
 int jmd_engine_clear_cache(void) {

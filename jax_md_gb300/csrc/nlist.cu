@@ -18,7 +18,8 @@
 // (including the slot rotation that the reference's `rank mod cap` slot rule
 // implies), and compacts hits with a warp ballot straight into the atom's
 // row, so the Dense list is bit-identical to the reference's, order included.
-#include "common.cuh"
+#include "dense.cuh"
+#include "segment.cuh"
 
 namespace jmd {
 namespace {
@@ -903,6 +904,162 @@ int build_impl(const jmd_nlist* nl, const float* x, int64_t stride, int64_t n64,
 }
 
 }  // namespace
+
+namespace {
+// ------------------------------------------------ segment-local search ----
+// The engine's private list on the segment layout (segment.cuh): one CTA per
+// segment stages the neighbourhood with bulk copies, then each thread takes
+// one own atom and tests the 3^(d-1) staged runs of cells x-1 .. x+1 around
+// it (about 27 cells x occupancy candidates, read from shared memory; the
+// threads of one cell read the same candidate at the same time, so the reads
+// broadcast).  Hits are kept as 16-bit staged slots, 8 per 16-byte store.
+// Entry order inside a row is the staged order (not the reference's); the
+// forces do not depend on it.  Pairs are compared in float32 as
+// d^2 < cutoff^2 with the minimum image taken only for atoms within the list
+// cutoff of a face, so a pair within an ulp of the list cutoff may be kept
+// where the reference drops it (or the reverse): such pairs lie beyond the
+// interaction cutoff and change no force.
+template <int DIM>
+__global__ void __launch_bounds__(kSegMaxThreads)
+k_seg_search(SegGrid sg, const float4* __restrict__ x, Bins b, Geo geo, float cut2, float margin,
+             int mask_self, uint16_t* __restrict__ list, int64_t nch, int width,
+             int32_t* __restrict__ count, float4* __restrict__ ref, int32_t* status,
+             const int32_t* flag) {
+  if (skip(flag)) return;
+  extern __shared__ float4 spos[];
+  __shared__ SegShared sh;
+  __shared__ unsigned cta_max;
+  if (threadIdx.x == 0) cta_max = 0u;
+  seg_stage<DIM>(sg, x, b.start, spos, sh, status);
+  if (!sh.ok) {
+    if (threadIdx.x == 0) atomicOr(&b.sc->flags, (unsigned)JMD_CELL_LIST_OVERFLOW);
+    return;
+  }
+  const int W = sh.W;
+  const int rows = sh.rows;
+  unsigned my_max = 0u;
+  for (int a = threadIdx.x; a < sh.own_cnt; a += blockDim.x) {
+    const int is = sh.own_sm + a, s = sh.own_beg + a;
+    const float4 xi = spos[is];
+    const int u = seg_own_cell<DIM>(sh, is);
+    const bool inner = interior<DIM>(xi, geo, margin);
+    uint16_t* base = list + seg_list_base(s, nch);
+    int cnt = 0;
+    uint32_t w0 = 0u, w1 = 0u, w2 = 0u, w3 = 0u;
+    auto push = [&](int j) {
+      const int p = cnt & 7;
+      const uint32_t v = (uint32_t)j << ((p & 1) * 16);
+      const int q = p >> 1;
+      w0 |= q == 0 ? v : 0u;
+      w1 |= q == 1 ? v : 0u;
+      w2 |= q == 2 ? v : 0u;
+      w3 |= q == 3 ? v : 0u;
+      if (p == 7) {
+        if ((cnt >> 3) < nch)
+          *reinterpret_cast<uint4*>(base + (int64_t)(cnt >> 3) * 256) = make_uint4(w0, w1, w2, w3);
+        w0 = w1 = w2 = w3 = 0u;
+      }
+      ++cnt;
+    };
+    const float2 xx = f2s(xi.x), xy = f2s(xi.y), xz = f2s(xi.z);
+    for (int r = 0; r < rows; ++r) {
+      const int j0 = sh.coff[r * W + u - 1], j1 = sh.coff[r * W + u + 2];
+      for (int j = j0; j < j1; j += 2) {
+        const bool two = j + 1 < j1;
+        const float4 b0 = spos[j];
+        const float4 b1 = spos[two ? j + 1 : j];
+        float2 dx = sub2(xx, f2(b0.x, b1.x));
+        float2 dy = sub2(xy, f2(b0.y, b1.y));
+        float2 dz = DIM == 3 ? sub2(xz, f2(b0.z, b1.z)) : f2s(0.f);
+        if (!inner) {
+          dx.x = min_image(xi.x, b0.x, geo.L[0], geo.halfL[0]);
+          dx.y = min_image(xi.x, b1.x, geo.L[0], geo.halfL[0]);
+          dy.x = min_image(xi.y, b0.y, geo.L[1], geo.halfL[1]);
+          dy.y = min_image(xi.y, b1.y, geo.L[1], geo.halfL[1]);
+          if (DIM == 3) {
+            dz.x = min_image(xi.z, b0.z, geo.L[2], geo.halfL[2]);
+            dz.y = min_image(xi.z, b1.z, geo.L[2], geo.halfL[2]);
+          }
+        }
+        float2 r2 = mul2(dx, dx);
+        r2 = fma2(dy, dy, r2);
+        if (DIM == 3) r2 = fma2(dz, dz, r2);
+        if (r2.x < cut2 && (j != is || !mask_self)) push(j);
+        if (two && r2.y < cut2 && (j + 1 != is || !mask_self)) push(j + 1);
+      }
+    }
+    if ((cnt & 7) != 0 && (cnt >> 3) < nch)
+      *reinterpret_cast<uint4*>(base + (int64_t)(cnt >> 3) * 256) = make_uint4(w0, w1, w2, w3);
+    count[s] = cnt;
+    float4 rr = xi;
+    rr.w = 0.f;
+    ref[s] = rr;
+    my_max = max(my_max, (unsigned)cnt);
+  }
+  my_max = __reduce_max_sync(0xffffffffu, my_max);
+  if ((threadIdx.x & 31) == 0) atomicMax(&cta_max, my_max);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicMax(&b.sc->occupancy, (unsigned long long)cta_max);
+    if ((int)cta_max > width) atomicOr(&b.sc->flags, (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
+  }
+}
+
+}  // namespace
+
+// Dynamic shared memory above the default 48 KB needs an opt-in per kernel.
+template <typename K>
+int seg_smem_optin(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return JMD_OK;
+  JMD_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return JMD_OK;
+}
+
+const int32_t* sort_cell_starts(const jmd_nlist* nl, int64_t n, void* workspace,
+                                size_t workspace_bytes) {
+  bool ok;
+  Bins b = carve_bins(workspace, workspace_bytes, n, make_grid(*nl).count, &ok);
+  return ok ? b.start : nullptr;
+}
+
+int build_segment_after_sort(const jmd_nlist* nl, const SegGrid& sg, const float* position,
+                             int64_t n, uint16_t* list, int64_t nch, int32_t* nbr_count,
+                             int64_t* occupancy, uint8_t* error_code, float* reference_position,
+                             int32_t* seg_status, int32_t* rebuild_flag, void* workspace,
+                             size_t workspace_bytes, cudaStream_t st) {
+  int e = validate(nl, n);
+  if (e) return e;
+  JMD_REQUIRE(nl->format == JMD_DENSE && nl->use_cell_list, "segment lists are Dense with a cell grid");
+  JMD_REQUIRE(list && nbr_count && nch * 8 >= nl->max_occupancy, "segment list needs 8 * nch >= max_occupancy");
+  JMD_REQUIRE(is_vec4(position, 4) && is_vec4(reference_position, 4), "float4 rows must be 16-byte aligned");
+  JMD_REQUIRE(nl->max_occupancy < INT32_MAX, "max_occupancy out of range");
+  Grid g = make_grid(*nl);
+  bool ok;
+  Bins b = carve_bins(workspace, workspace_bytes, n, g.count, &ok);
+  if (!ok) return fail(JMD_ERR_WORKSPACE, "neighbour-list workspace too small");
+  const Geo geo = make_geo(nl->space);
+  const float margin = sqrtf(nl->cutoff_sq);
+  const size_t smem = (size_t)sg.cap * sizeof(float4);
+  const float4* x = reinterpret_cast<const float4*>(position);
+  float4* ref = reinterpret_cast<float4*>(reference_position);
+  const int width = (int)nl->max_occupancy;
+  if (n > 0) {
+    if (nl->space.dim == 3) {
+      if ((e = seg_smem_optin(k_seg_search<3>, smem))) return e;
+      k_seg_search<3><<<(unsigned)sg.nseg, (unsigned)sg.threads, smem, st>>>(sg, x, b, geo, nl->cutoff_sq, margin,
+                                                            nl->mask_self, list, nch, width,
+                                                            nbr_count, ref, seg_status, rebuild_flag);
+    } else {
+      if ((e = seg_smem_optin(k_seg_search<2>, smem))) return e;
+      k_seg_search<2><<<(unsigned)sg.nseg, (unsigned)sg.threads, smem, st>>>(sg, x, b, geo, nl->cutoff_sq, margin,
+                                                            nl->mask_self, list, nch, width,
+                                                            nbr_count, ref, seg_status, rebuild_flag);
+    }
+  }
+  FinalizeArgs f{JMD_DENSE, nl->max_occupancy, 1, nl->cell_capacity, (int)n};
+  k_finalize<<<1, 1, 0, st>>>(b, f, occupancy, error_code, rebuild_flag);
+  return check_launch("jmd segment list build");
+}
 
 // The tiled build right after jmd_sort_by_cell on the same positions and
 // workspace: the sort's bins already describe the reordered atoms (its

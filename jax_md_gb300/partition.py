@@ -299,7 +299,12 @@ class _Plan:
 
 @dataclasses.dataclass
 class NeighborList:
-    """partition.py:684-737."""
+    """partition.py:684-737.
+
+    ``idx`` may be built lazily: a device run that keeps its own private list
+    (simulate.run) leaves the caller's list unbuilt and records here how to
+    build it at ``reference_position``; reading ``idx`` (or updating the list)
+    builds it first, so a caller that never reads it never pays for it."""
     idx: torch.Tensor
     reference_position: torch.Tensor
     error: PartitionError
@@ -310,6 +315,28 @@ class NeighborList:
     cell_list_fn: Optional[object]
     update_fn: Callable
     plan: Optional[_Plan] = None
+
+    def __getattribute__(self, name):
+        if name == 'idx':
+            d = object.__getattribute__(self, '__dict__')
+            pending = d.get('_pending')
+            if pending is not None:
+                d['_pending'] = None
+                pending()
+        return object.__getattribute__(self, name)
+
+    def set_pending_build(self, build: Optional[Callable]) -> None:
+        """Records (or clears) a deferred build of ``idx``."""
+        object.__setattr__(self, '_pending', build)
+
+    @property
+    def has_pending_build(self) -> bool:
+        return object.__getattribute__(self, '__dict__').get('_pending') is not None
+
+    def idx_buffer(self) -> torch.Tensor:
+        """``idx`` without running a pending build (for kernels that only
+        write it)."""
+        return object.__getattribute__(self, 'idx')
 
     def update(self, position, **kwargs) -> 'NeighborList':
         return self.update_fn(position, self, **kwargs)
@@ -352,6 +379,28 @@ def _row_ld(width: int) -> int:
     return max(8, (width + 7) // 8 * 8)
 
 
+def _run_build(plan: '_Plan', R, rs, idx, ld, error, ref, use_flag):
+    """One jmd_neighbor_list_build of `plan` at positions R (row stride rs)."""
+    L = N.lib()
+    cnt = plan.count
+    N.check(L.jmd_neighbor_list_build(
+        C_ref(plan.nl), R.data_ptr(), rs, plan.n, N.ptr(idx), ld, N.ptr(cnt),
+        plan.occupancy.data_ptr(), N.ptr(error), N.ptr(ref),
+        ref.stride(0) if ref is not None else 0,
+        plan.flag.data_ptr() if use_flag else None,
+        plan.workspace.data_ptr(), plan.workspace.numel(), N.stream_ptr()), 'neighbor_list')
+
+
+def build_at_reference(neighbors: 'NeighborList') -> None:
+    """Builds a Dense list in place at its own reference positions (the list
+    the reference would hold after its last rebuild), in the reference's
+    entry order."""
+    plan = neighbors.plan
+    ref = neighbors.reference_position
+    _run_build(plan, ref, ref.stride(0), neighbors.idx_buffer(), plan.ld, neighbors.error.code,
+               ref, False)
+
+
 def neighbor_list(displacement_or_metric, box, r_cutoff, dr_threshold=0.0,
                   capacity_multiplier: float = 1.25, disable_cell_list: bool = False,
                   mask_self: bool = True, custom_mask_function: Optional[Callable] = None,
@@ -390,15 +439,7 @@ def neighbor_list(displacement_or_metric, box, r_cutoff, dr_threshold=0.0,
         nl.max_occupancy = int(max_occ)
         return nl
 
-    def run_build(plan: _Plan, R, rs, idx, ld, error, ref, use_flag):
-        L = N.lib()
-        cnt = plan.count
-        N.check(L.jmd_neighbor_list_build(
-            C_ref(plan.nl), R.data_ptr(), rs, plan.n, N.ptr(idx), ld, N.ptr(cnt),
-            plan.occupancy.data_ptr(), N.ptr(error), N.ptr(ref),
-            ref.stride(0) if ref is not None else 0,
-            plan.flag.data_ptr() if use_flag else None,
-            plan.workspace.data_ptr(), plan.workspace.numel(), N.stream_ptr()), 'neighbor_list')
+    run_build = _run_build
 
     def allocate_fn(position, extra_capacity: int = 0, **kwargs):
         if 'box' in kwargs:

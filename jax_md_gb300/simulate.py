@@ -43,8 +43,12 @@ class _StateMixin:
 
     def copy(self):
         def c(v):
-            return v.clone() if isinstance(v, torch.Tensor) else (
-                v.copy() if hasattr(v, 'copy') else v)
+            if isinstance(v, torch.Tensor):
+                # float4-row views stay float4 rows (the kernels' layout)
+                if v.dim() == 2 and v.shape[1] < 4 and v.stride() == (4, 1):
+                    return partition.padded_rows(v)
+                return v.clone()
+            return v.copy() if hasattr(v, 'copy') else v
         return dataclasses.replace(self, **{f.name: c(getattr(self, f.name))
                                             for f in dataclasses.fields(self)})
 
@@ -568,7 +572,7 @@ def _nve_system(st: '_Stepper', state: NVEState, nbrs, alt: torch.Tensor) -> N.N
     s.species = N.ptr(species)
     s.pair = pair
     s.nlist = plan.nl
-    s.idx = nbrs.idx.data_ptr()
+    s.idx = nbrs.idx_buffer().data_ptr()
     s.idx_ld = plan.ld
     s.nbr_count = plan.count.data_ptr()
     s.reference_position = nbrs.reference_position.data_ptr()
@@ -582,17 +586,63 @@ def _nve_system(st: '_Stepper', state: NVEState, nbrs, alt: torch.Tensor) -> N.N
     return s, species
 
 
-class _SortedBuffers:
-    """Engine-private, cell-ordered copy of a system (see jmd_nve_run_sorted)."""
+# Cells per segment of the segment-local engine list (jmd_segment_plan): the
+# default, and the (cells, threads) choices the autotuner
+# (tune.autotune_segment) records per cell grid.
+SEGMENT_CELLS_DEFAULT = 5
+_segment_choice = {}
 
-    def __init__(self, n, ld, species: bool, workspace_bytes: int, device):
+
+def _grid_key(nl: N.NList):
+    d = nl.space.dim
+    return (d, tuple(nl.cells_per_side[:d]), nl.cell_capacity)
+
+
+def segment_threads_default(cells: int, cell_capacity: int) -> int:
+    """Threads per segment CTA: about the own atoms of a segment (cells x
+    0.8 x cell capacity, the capacity being 1.25 x the fullest cell at
+    allocation), in whole warps, 64 to 256."""
+    t = int(math.ceil(cells * cell_capacity * 0.8 / 32.0)) * 32
+    return max(64, min(256, t))
+
+
+def segment_plan(nl: N.NList, cells: int):
+    """(n_segments, capacity_atoms, smem_bytes, cells_used) of the segment
+    layout for a cell grid, or None when it does not apply."""
+    ns, cap, cu = N.I32(), N.I32(), N.I32()
+    sm = N.I64()
+    rc = N.lib().jmd_segment_plan(ctypes.byref(nl), int(cells), ctypes.byref(ns), ctypes.byref(cap),
+                                  ctypes.byref(sm), ctypes.byref(cu))
+    if rc != 0:
+        return None
+    return ns.value, cap.value, sm.value, cu.value
+
+
+class _SortedBuffers:
+    """Engine-private, cell-ordered copy of a system (see jmd_nve_run_sorted).
+    With `seg_cells` the private list is the segment-local one (16-bit staged
+    slots, 8-entry chunks); otherwise the tiled int32 list."""
+
+    def __init__(self, n, ld, species: bool, workspace_bytes: int, device, seg_cells=None,
+                 seg_threads=128):
         f4 = lambda: torch.empty((n, 4), dtype=torch.float32, device=device)
         i4 = lambda: torch.empty(n, dtype=torch.int32, device=device)
         self.n, self.ld = n, ld
         self.xa, self.xb, self.p, self.f, self.ref, self.t4a, self.t4b = (f4() for _ in range(7))
         self.perm, self.tia, self.tib = i4(), i4(), i4()
         self.species = i4() if species else None
-        self.idx = torch.empty(((n + 31) // 32) * 32 * ld, dtype=torch.int32, device=device)
+        self.seg_cells = seg_cells
+        self.seg_threads = seg_threads
+        self.seg_nch = (ld + 7) // 8
+        if seg_cells is None:
+            self.idx = torch.empty(((n + 31) // 32) * 32 * ld, dtype=torch.int32, device=device)
+            self.seg = None
+        else:
+            self.idx = None
+            self.seg = torch.empty(((n + 31) // 32) * 32 * self.seg_nch * 8, dtype=torch.int16,
+                                   device=device)
+        self.seg_status = torch.zeros((), dtype=torch.int32, device=device)
+        self.flags = 0
         self.cnt = i4()
         self.err = torch.zeros((), dtype=torch.uint8, device=device)
         self.occ = torch.zeros((), dtype=torch.int64, device=device)
@@ -607,27 +657,66 @@ class _SortedBuffers:
         z.scratch4a, z.scratch4b = self.t4a.data_ptr(), self.t4b.data_ptr()
         z.species = N.ptr(self.species)
         z.perm, z.scratch_i_a, z.scratch_i_b = self.perm.data_ptr(), self.tia.data_ptr(), self.tib.data_ptr()
-        z.idx, z.idx_ld, z.nbr_count = self.idx.data_ptr(), self.ld, self.cnt.data_ptr()
+        z.idx, z.idx_ld, z.nbr_count = N.ptr(self.idx), self.ld, self.cnt.data_ptr()
         z.error_code, z.occupancy = self.err.data_ptr(), self.occ.data_ptr()
         z.rebuild_flag = self.flag.data_ptr()
         z.workspace, z.workspace_bytes = self.ws.data_ptr(), self.ws.numel()
+        if self.seg is not None:
+            z.seg_list, z.seg_nch, z.seg_cells = self.seg.data_ptr(), self.seg_nch, self.seg_cells
+            z.seg_threads = self.seg_threads
+        z.seg_status = self.seg_status.data_ptr()
+        z.flags = self.flags
         return z
 
 
-def _sorted_buffers(state, nbrs, species):
+def _segment_shape(nbrs, layout):
+    """(cells per segment, threads per CTA) for a run, or None for the tiled
+    list.  `layout`: None / 'segment' (autotuned choice or default), an int
+    (cells), a (cells, threads) pair, or 'tiled'."""
+    if layout == 'tiled':
+        return None
+    nl = nbrs.plan.nl
+    threads = None
+    if layout is None or layout == 'segment':
+        cells, threads = _segment_choice.get(_grid_key(nl), (SEGMENT_CELLS_DEFAULT, None))
+    elif isinstance(layout, (tuple, list)):
+        cells, threads = int(layout[0]), int(layout[1])
+    else:
+        cells = int(layout)
+    plan = segment_plan(nl, cells)
+    if plan is None:
+        if layout not in (None, 'segment'):
+            raise ValueError('the segment layout does not apply to this cell grid')
+        return None
+    cells = plan[3]
+    if threads is None:
+        threads = segment_threads_default(cells, nl.cell_capacity)
+    return cells, threads
+
+
+def _sorted_buffers(state, nbrs, species, seg=None):
     plan = nbrs.plan
-    key = (plan.ld, species is not None, plan.workspace.numel())
+    key = (plan.ld, species is not None, plan.workspace.numel(), seg)
     b = getattr(state, '_sorted', None)
     if b is None or b.n != state.position.shape[0] or getattr(b, 'key', None) != key:
         b = _SortedBuffers(state.position.shape[0], plan.ld, species is not None,
-                           plan.workspace.numel(), state.position.device)
+                           plan.workspace.numel(), state.position.device,
+                           None if seg is None else seg[0], 128 if seg is None else seg[1])
         b.key = key
         object.__setattr__(state, '_sorted', b)
     return b
 
 
+def last_run_status(state) -> int:
+    """Status word of the last sorted run on `state`: 0, or bit 1 (a segment
+    neighbourhood exceeded its staging capacity; the run's list also carries
+    the cell-list overflow bit) / bit 2 (a staging copy timed out)."""
+    b = getattr(state, '_sorted', None)
+    return 0 if b is None else int(b.seg_status)
+
+
 def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bool = True,
-        max_reallocations: int = 4, sort=None):
+        max_reallocations: int = 4, sort=None, layout=None, lazy_list: bool = True):
     """Runs the reference loop body ``n_steps`` times on the device:
 
         nbrs = nbrs.update(state.position); state = apply_fn(state, neighbor=nbrs)
@@ -641,7 +730,11 @@ def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bo
     the atoms in cell order inside the run so neighbour gathers are
     coalesced; on return the state is back in the caller's order and the
     caller's list is rebuilt, in the reference's entry order, at the
-    positions of the last rebuild.  Returns (state, neighbor)."""
+    positions of the last rebuild -- when it is first read (``lazy_list``) or
+    before returning.  ``layout`` picks the private list of a sorted run:
+    None / 'segment' (the segment-local list wherever it applies, with the
+    autotuned or default cells per segment), an int (that many cells per
+    segment), or 'tiled' (the tiled int32 list).  Returns (state, neighbor)."""
     st = apply_fn.stepper
     nvt = isinstance(state, NVTNoseHooverState)
     if not (isinstance(state, NVEState) or nvt):
@@ -662,8 +755,11 @@ def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bo
             use_sort = (not isinstance(state.mass, torch.Tensor)) and bool(sysd.nlist.use_cell_list)
         v = _nvt_struct(apply_fn.chain_fns, state) if nvt else None
         if use_sort:
-            sb = _sorted_buffers(state, neighbor, species)
+            seg = _segment_shape(neighbor, layout)
+            sb = _sorted_buffers(state, neighbor, species, seg)
+            sb.flags = N.RUN_SKIP_EXIT_LIST if lazy_list else 0
             z = sb.struct()
+            neighbor.set_pending_build(None)
             if nvt:
                 N.check(N.lib().jmd_nvt_run_sorted(ctypes.byref(sysd), ctypes.byref(z),
                                                    ctypes.byref(v), int(n_steps),
@@ -673,13 +769,22 @@ def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bo
                 N.check(N.lib().jmd_nve_run_sorted(ctypes.byref(sysd), ctypes.byref(z),
                                                    int(n_steps), 1 if use_graph else 0,
                                                    N.stream_ptr()), 'nve_run_sorted')
+            if lazy_list:
+                nb = neighbor
+                neighbor.set_pending_build(lambda: partition.build_at_reference(nb))
         elif nvt:
+            neighbor.idx  # a deferred build of the caller's list must land first
             N.check(N.lib().jmd_nvt_run(ctypes.byref(sysd), ctypes.byref(v), int(n_steps),
                                         1 if use_graph else 0, N.stream_ptr()), 'nvt_run')
         else:
+            neighbor.idx
             N.check(N.lib().jmd_nve_run(ctypes.byref(sysd), int(n_steps), 1 if use_graph else 0,
                                         N.stream_ptr()), 'nve_run')
-        if neighbor_fn is None or not bool(neighbor.did_buffer_overflow):
+        if neighbor_fn is None:
+            return state, neighbor
+        if use_sort and last_run_status(state) & 2:
+            raise N.NativeError('a segment staging copy did not complete within its wait limit')
+        if not bool(neighbor.did_buffer_overflow):
             return state, neighbor
         # overflow: restore the starting state, re-allocate there (with growing
         # headroom, so a block whose occupancy peaks above the start's fits), repeat

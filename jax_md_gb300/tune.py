@@ -1,10 +1,14 @@
-"""Launch-shape autotuner for the Dense pair kernels.
+"""Launch-shape autotuners.
 
-Times the fused NVE step kernel for each threads-per-atom choice (4, 8, 16) on
-the caller's own system, keeps the fastest, and caches the choice on disk keyed
-by (device name, atom-count bucket, row width, dimension, potential, species).
-The kernels read the choice from a library-wide setting
-(jmd_set_dense_threads_per_atom).
+autotune_segment: the device engine's segment-local list (simulate.run with a
+cell-sorted state): cells per segment K and threads per segment CTA, timed as
+whole engine runs (rebuilds included) on a copy of the caller's own state;
+the choice is recorded for the cell grid (simulate.run picks it up) and cached
+on disk keyed by (device name, grid, cell capacity, potential, species).
+
+autotune_dense: threads per atom (4, 8, 16) of the row-major Dense fused
+step kernel (the caller's-list path, jmd_nve_fused_step), read by the kernels
+from a library-wide setting (jmd_set_dense_threads_per_atom).
 """
 from __future__ import annotations
 
@@ -92,3 +96,70 @@ def autotune_dense(energy_fn, state, neighbor, shift_fn, dt, reps: int = 20, use
         cache[key] = {'tpa': best, 'ms': timings}
         _save(cache)
     return best, timings
+
+
+def _seg_key(nl, pair) -> str:
+    dev = torch.cuda.get_device_name()
+    d = nl.space.dim
+    cps = 'x'.join(str(c) for c in nl.cells_per_side[:d])
+    return f'seg|{dev}|c{cps}|cap{nl.cell_capacity}|k{pair.kind}|s{pair.n_species}'
+
+
+def segment_candidates(nl):
+    """(cells, threads) pairs to try: K in 2..8 (those the grid admits) with
+    the default thread count and the neighbouring multiples of 32."""
+    from . import simulate
+    out = []
+    for K in (2, 3, 4, 5, 6, 8):
+        plan = simulate.segment_plan(nl, K)
+        if plan is None or plan[3] != K:
+            continue
+        t0 = simulate.segment_threads_default(K, nl.cell_capacity)
+        for t in sorted({t0 - 32, t0, t0 + 32}):
+            if 64 <= t <= 256:
+                out.append((K, t))
+    return out
+
+
+def autotune_segment(apply_fn, state, neighbor, steps: int = 20, reps: int = 2,
+                     use_cache: bool = True, candidates=None):
+    """Picks (cells per segment, threads per CTA) for simulate.run on this
+    system by timing `steps`-step engine runs (CUDA graph, rebuilds included)
+    from copies of `state`; records the choice for the cell grid and returns
+    ((cells, threads), {choice: ms per step}).  Returns (None, {}) when the
+    segment layout does not apply."""
+    from . import simulate
+    nl = neighbor.plan.nl
+    species, pair = apply_fn.stepper.energy_fn._resolve(state.position, {})
+    key = _seg_key(nl, pair)
+    gk = simulate._grid_key(nl)
+    cache = _load() if use_cache else {}
+    if key in cache:
+        choice = tuple(cache[key]['choice'])
+        simulate._segment_choice[gk] = choice
+        return choice, {tuple(json.loads(k)): v for k, v in cache[key]['ms'].items()}
+    cands = list(candidates) if candidates is not None else segment_candidates(nl)
+    if not cands:
+        return None, {}
+    timings = {}
+    for c in cands:
+        st = state.copy()
+        simulate.run(apply_fn, st, neighbor, steps, layout=c)   # captures the graph
+        best = float('inf')
+        for _ in range(reps):
+            st = state.copy()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            simulate.run(apply_fn, st, neighbor, steps, layout=c)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1) / steps)
+        timings[c] = best
+        del st
+    choice = min(timings, key=timings.get)
+    simulate._segment_choice[gk] = choice
+    if use_cache:
+        cache[key] = {'choice': list(choice), 'ms': {json.dumps(list(k)): v for k, v in timings.items()}}
+        _save(cache)
+    return choice, timings

@@ -331,6 +331,32 @@ class NeighborListOracle:
         return NeighborListO(out, R.copy(), err, cl_capacity, max_occupancy,
                              self.fmt, use_cell_list, occupancy)
 
+    def dense_rows(self, R, atoms, cl_capacity):
+        """Dense rows of `atoms` only, in the reference's entry order
+        (partition.py:911-977 restricted to those rows): the cell list of all
+        atoms, then the candidates, masks and compaction of the chosen rows.
+        For systems too large for build()'s [N, 3^d cap] candidate array.
+        Returns (rows [len(atoms), 3^d cap] with sentinel N, counts)."""
+        R = np.asarray(R)
+        N, dim = R.shape
+        atoms = np.asarray(atoms, np.int64)
+        cl = cell_list(R, self.box, self.cutoff, cl_capacity, self.bdt)
+        shifts = neighboring_cells(dim)
+        cps = cl.cells_per_side
+        shifted = np.mod(cl.particle_cell_id[atoms][:, None, :] + shifts[None], cps)
+        mult = np.cumprod(np.concatenate([[1], cps[:-1]]))
+        cand = cl.id_buffer[(shifted * mult).sum(-1)].reshape(len(atoms), -1)
+        valid = cand < N
+        d2 = self._d2(R[atoms][:, None, :], R[np.where(valid, cand, 0)])
+        mask = valid & (d2 < self.cutoff_sq)
+        if self.mask_self:
+            mask &= cand != atoms[:, None]
+        out = np.full(cand.shape, N, np.int64)
+        for k in range(len(atoms)):
+            sel = cand[k][mask[k]]
+            out[k, :len(sel)] = sel
+        return out, mask.sum(1)
+
     def allocate(self, R, extra_capacity=0):
         return self.build(R, extra_capacity=extra_capacity)
 

@@ -5,7 +5,9 @@ into the force kernel and gates each step's rebuild with a device-side
 conditional graph node.  Graph and direct launches must agree bit for bit;
 against the per-step API (which checks the skin one step earlier, as the
 reference loop does) and the FP64 oracle, trajectories agree to fp32 accuracy
-over short runs.
+over short runs.  The sorted run is tested with both of its private lists:
+the segment-local list (16-bit slots of a shared-memory staged neighbourhood)
+and the tiled int32 list.
 """
 import numpy as np
 import pytest
@@ -29,14 +31,20 @@ def _setup(cuda, n_cells=6, skin=0.3):
     return R, P, L, nfn, efn, init, apply, st, nb
 
 
-@pytest.mark.parametrize('sort', [False, True])
+# (sort, layout) of a run: unsorted, sorted with the segment-local list,
+# sorted with the tiled list
+RUNS = [(False, None), (True, 'segment'), (True, 'tiled')]
+RUN_IDS = ['unsorted', 'segment', 'tiled']
+
+
+@pytest.mark.parametrize('sort,layout', RUNS, ids=RUN_IDS)
 @pytest.mark.parametrize('steps', [1, 2, 7, 40])
-def test_graph_equals_direct(cuda, steps, sort):
+def test_graph_equals_direct(cuda, steps, sort, layout):
     from jax_md_gb300 import simulate
     _, _, _, nfn, efn, init, apply, st_a, nb_a = _setup(cuda)
     _, _, _, nfn2, _, _, apply2, st_b, nb_b = _setup(cuda)
-    simulate.run(apply, st_a, nb_a, steps, use_graph=True, sort=sort)
-    simulate.run(apply2, st_b, nb_b, steps, use_graph=False, sort=sort)
+    simulate.run(apply, st_a, nb_a, steps, use_graph=True, sort=sort, layout=layout)
+    simulate.run(apply2, st_b, nb_b, steps, use_graph=False, sort=sort, layout=layout)
     torch.cuda.synchronize()
     assert torch.equal(st_a.position, st_b.position)
     assert torch.equal(st_a.momentum, st_b.momentum)
@@ -58,13 +66,14 @@ def test_graph_replay_repeats(cuda):
     assert torch.equal(st_a.position, st_b.position)
 
 
-@pytest.mark.parametrize('sort', [False, True])
-def test_runner_matches_per_step_api_and_oracle(cuda, sort):
+@pytest.mark.parametrize('n_cells', [6, 10])
+@pytest.mark.parametrize('sort,layout', RUNS, ids=RUN_IDS)
+def test_runner_matches_per_step_api_and_oracle(cuda, sort, layout, n_cells):
     from jax_md_gb300 import simulate
-    R, P, L, nfn, efn, init, apply, st, nb = _setup(cuda)
-    _, _, _, nfn2, efn2, init2, apply2, st2, nb2 = _setup(cuda)
+    R, P, L, nfn, efn, init, apply, st, nb = _setup(cuda, n_cells=n_cells)
+    _, _, _, nfn2, efn2, init2, apply2, st2, nb2 = _setup(cuda, n_cells=n_cells)
     steps = 40
-    simulate.run(apply, st, nb, steps, sort=sort)
+    simulate.run(apply, st, nb, steps, sort=sort, layout=layout)
     for _ in range(steps):
         nb2 = nb2.update(st2.position)
         st2 = apply2(st2, neighbor=nb2)
@@ -197,8 +206,8 @@ def _nvt_setup(cuda, n_cells=6, kT=0.722):
     return efn, init, apply, st, nb
 
 
-@pytest.mark.parametrize('sort', [False, True])
-def test_nvt_runner_matches_apply_loop(cuda, sort):
+@pytest.mark.parametrize('sort,layout', RUNS, ids=RUN_IDS)
+def test_nvt_runner_matches_apply_loop(cuda, sort, layout):
     """simulate.run on a Nose-Hoover state (jmd_nvt_run / jmd_nvt_run_sorted)
     against the per-step apply_fn loop: same chain, same trajectory to fp32
     accuracy over 60 steps."""
@@ -206,7 +215,7 @@ def test_nvt_runner_matches_apply_loop(cuda, sort):
     efn, init, apply, st_a, nb_a = _nvt_setup(cuda)
     _, _, apply_b, st_b, nb_b = _nvt_setup(cuda)
     steps = 60
-    simulate.run(apply, st_a, nb_a, steps, sort=sort)
+    simulate.run(apply, st_a, nb_a, steps, sort=sort, layout=layout)
     for _ in range(steps):
         nb_b = nb_b.update(st_b.position)
         st_b = apply_b(st_b, neighbor=nb_b)
@@ -232,3 +241,93 @@ def test_nvt_runner_conserves_invariant(cuda):
     assert abs(H1 - H0) / n < 1e-3, (H0, H1)
     T = float((st.momentum.double() ** 2).sum() / (3 * n))
     assert 0.5 < T < 1.0
+
+
+@pytest.mark.parametrize('n_cells', [6, 10])
+def test_segment_and_tiled_layouts_agree(cuda, n_cells):
+    """The two private lists hold the same pairs: one step from the same state
+    gives the same forces (to fp32 summation order) and positions."""
+    from jax_md_gb300 import simulate
+    _, _, _, _, _, _, apply_a, st_a, nb_a = _setup(cuda, n_cells=n_cells)
+    _, _, _, _, _, _, apply_b, st_b, nb_b = _setup(cuda, n_cells=n_cells)
+    simulate.run(apply_a, st_a, nb_a, 3, layout='segment')
+    simulate.run(apply_b, st_b, nb_b, 3, layout='tiled')
+    torch.cuda.synchronize()
+    assert (st_a.force - st_b.force).abs().max().item() < 2e-5
+    assert (st_a.position - st_b.position).abs().max().item() < 1e-5
+    assert simulate.last_run_status(st_a) == 0
+    assert torch.equal(nb_a.idx, nb_b.idx)
+
+
+@pytest.mark.parametrize('cells', [1, 2, 3, 5, 8])
+def test_segment_widths_agree(cuda, cells):
+    """Every segment width K gives the same run to fp32 summation order (the
+    staged neighbourhoods differ, the pairs do not); 12 cells per side, so
+    K = 5 and 8 leave a shorter last segment in each row."""
+    from jax_md_gb300 import simulate
+    _, _, _, _, _, _, apply_a, st_a, nb_a = _setup(cuda, n_cells=20)
+    _, _, _, _, _, _, apply_b, st_b, nb_b = _setup(cuda, n_cells=20)
+    simulate.run(apply_a, st_a, nb_a, 5, layout=cells)
+    simulate.run(apply_b, st_b, nb_b, 5, layout='tiled')
+    torch.cuda.synchronize()
+    assert (st_a.force - st_b.force).abs().max().item() < 2e-5
+    assert (st_a.position - st_b.position).abs().max().item() < 1e-5
+
+
+def test_lazy_caller_list_is_built_when_read(cuda):
+    """A sorted run leaves the caller's list for its first read; that read (or
+    an update) gives the list an eager run returns."""
+    from jax_md_gb300 import simulate
+    _, _, _, _, _, _, apply_a, st_a, nb_a = _setup(cuda, n_cells=8)
+    _, _, _, _, _, _, apply_b, st_b, nb_b = _setup(cuda, n_cells=8)
+    simulate.run(apply_a, st_a, nb_a, 30, lazy_list=True)
+    simulate.run(apply_b, st_b, nb_b, 30, lazy_list=False)
+    assert nb_a.has_pending_build and not nb_b.has_pending_build
+    assert torch.equal(nb_a.idx, nb_b.idx)
+    assert not nb_a.has_pending_build
+    # an update resolves the deferred build first, then tests the skin
+    simulate.run(apply_a, st_a, nb_a, 30, lazy_list=True)
+    simulate.run(apply_b, st_b, nb_b, 30, lazy_list=False)
+    nb_a = nb_a.update(st_a.position)
+    nb_b = nb_b.update(st_b.position)
+    torch.cuda.synchronize()
+    assert torch.equal(nb_a.idx, nb_b.idx)
+    assert torch.equal(st_a.position, st_b.position)
+
+
+@pytest.mark.parametrize('layout', ['segment', 'tiled'])
+def test_sorted_engine_species_matches_per_step_api(cuda, layout):
+    """A Kob-Andersen mixture (species matrices) through the sorted engine:
+    the segment kernels read species from the private position rows."""
+    from jax_md_gb300 import energy, partition, simulate, space
+    rng = np.random.default_rng(3)
+    n_side = 16
+    L = float((n_side ** 3 / 1.2) ** (1 / 3))
+    g = (np.arange(n_side) + 0.5) * (L / n_side)
+    R = np.stack(np.meshgrid(g, g, g, indexing='ij'), -1).reshape(-1, 3)
+    R = (R + rng.uniform(-0.05, 0.05, R.shape)).astype(np.float32) % np.float32(L)
+    n = len(R)
+    species = (rng.permutation(n) < int(0.2 * n)).astype(np.int32)
+    sigma = torch.tensor([[1.0, 0.8], [0.8, 0.88]])
+    eps = torch.tensor([[1.0, 1.5], [1.5, 0.5]])
+    disp, shift = space.periodic(L)
+
+    def make():
+        nfn, efn = energy.lennard_jones_neighbor_list(
+            disp, L, species=torch.tensor(species, device=cuda), sigma=sigma, epsilon=eps,
+            dr_threshold=0.3, format=partition.Dense)
+        Rt = torch.tensor(R, device=cuda)
+        nb = nfn.allocate(Rt)
+        init, apply = simulate.nve(efn, shift, 0.002)
+        P = torch.tensor(O.maxwell_boltzmann(n, 3, 0.8, 4), device=cuda)
+        return apply, init(0, Rt, momenta=P, neighbor=nb), nb
+    apply_a, st_a, nb_a = make()
+    apply_b, st_b, nb_b = make()
+    simulate.run(apply_a, st_a, nb_a, 20, layout=layout)
+    for _ in range(20):
+        nb_b = nb_b.update(st_b.position)
+        st_b = apply_b(st_b, neighbor=nb_b)
+    torch.cuda.synchronize()
+    d = O.displacement(st_a.position.cpu().numpy(), st_b.position.cpu().numpy(), np.full(3, L))
+    assert np.abs(d).max() < 1e-4
+    assert (st_a.momentum - st_b.momentum).abs().max().item() < 1e-3

@@ -52,3 +52,50 @@ def test_formats_row_stride_and_boxes():
     assert partition._box_list(torch.tensor([2.0, 3.0, 4.0]), 3) == [2.0, 3.0, 4.0]
     with pytest.raises(NotImplementedError, match='periodic_general'):
         partition._box_list(np.array([[3.0, 0.5], [0.0, 4.0]]), 2)
+
+
+def _nl(cps, cap, dim=3):
+    from jax_md_gb300 import _native as N
+    nl = N.NList()
+    nl.space.dim = dim
+    nl.use_cell_list = 1
+    for d in range(dim):
+        nl.cells_per_side[d] = cps
+        nl.cell_size[d] = 2.9
+    nl.cell_capacity = cap
+    nl.format = N.DENSE
+    return nl
+
+
+@pytest.mark.parametrize('cps,cap,K,dim,want', [
+    (35, 40, 5, 3, (8575, 2520, 5)),     # the LJ benchmark grid: 7 segments per row
+    (12, 40, 5, 3, (432, 2520, 5)),      # 5 + 5 + 2 cells per row
+    (5, 52, 5, 3, (50, 2340, 3)),        # K clipped to cells - 2
+    (3, 46, 5, 3, (27, 1242, 1)),
+    (12, 10, 8, 2, (24, 300, 8)),        # 2D: 3 staged rows
+])
+def test_segment_plan(cps, cap, K, dim, want):
+    """jmd_segment_plan (host arithmetic, no device needed): segments =
+    ceil(cells_x / K) x cells_y (x cells_z), capacity 3^(d-1) (K + 2) x cell
+    capacity atoms of 16 bytes, K at most cells_x - 2."""
+    from jax_md_gb300 import simulate
+    plan = simulate.segment_plan(_nl(cps, cap, dim), K)
+    assert plan is not None
+    nseg, capa, smem, used = plan
+    assert (nseg, capa, used) == want
+    assert smem == capa * 16
+
+
+@pytest.mark.parametrize('cps,cap,K', [(2, 40, 5), (35, 40, 0), (35, 40, 15), (35, 800, 5)])
+def test_segment_plan_rejects(cps, cap, K):
+    """Fewer than 3 cells per side, K outside 1..14, or a staging block beyond
+    a CTA's shared memory: the segment layout does not apply."""
+    from jax_md_gb300 import simulate
+    assert simulate.segment_plan(_nl(cps, cap), K) is None
+
+
+def test_segment_threads_default():
+    from jax_md_gb300 import simulate
+    assert simulate.segment_threads_default(5, 40) == 160
+    assert simulate.segment_threads_default(1, 46) == 64
+    assert simulate.segment_threads_default(14, 60) == 256

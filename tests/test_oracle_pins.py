@@ -422,3 +422,19 @@ def test_langevin_equilibrium_temperature():
         if step > 3000 and step % 100 == 0:
             Ts.append(float((P * P / mass[:, None]).sum() / (n * dim)))
     assert abs(np.mean(Ts) - kT) < 0.1, (np.mean(Ts), kT)
+
+
+@pytest.mark.parametrize('dim', [2, 3])
+def test_oracle_dense_rows_of_a_subset_match_build(dim):
+    """NeighborListOracle.dense_rows (the rows of chosen atoms, for systems too
+    large for build's candidate array) equals build's rows, order included."""
+    box = np.array([9.0, 7.5] if dim == 2 else [9.0, 6.0, 7.25], np.float32)
+    R = random_box(700, dim, box, seed=5)
+    onl = O.NeighborListOracle(box, np.float32(1.0), np.float32(0.2))
+    full = onl.allocate(R)
+    atoms = np.arange(0, 700, 13)
+    rows, counts = onl.dense_rows(R, atoms, full.cell_list_capacity)
+    w = full.idx.shape[1]
+    assert np.array_equal(rows[:, :w], full.idx[atoms])
+    assert np.all(rows[:, w:] == 700)
+    assert np.array_equal(counts, (full.idx[atoms] < 700).sum(1))
