@@ -597,6 +597,8 @@ def main():
     ap.add_argument('--cells', type=int, default=N_CELLS)
     ap.add_argument('--workload', default='lj864k', choices=['lj864k', 'batched'],
                     help='batched: only the batched soft-sphere workload (FIRE + NVE)')
+    ap.add_argument('--no-tune', action='store_true',
+                    help='skip the segment autotuner (default cells per segment and threads)')
     ap.add_argument('--direct', action='store_true',
                     help='launch the engine kernels directly instead of replaying its CUDA '
                          'graph (profilers list every kernel of the timed region this way)')
@@ -643,7 +645,10 @@ def main():
     # launch shape: project autotuner (cells per segment, threads per CTA of
     # the engine's segment-local list), timed on copies of this state
     from jax_md_gb300 import tune
-    seg_choice, seg_ms = tune.autotune_segment(apply, st, nb, steps=20, use_cache=False)
+    if args.no_tune:
+        seg_choice, seg_ms = None, {}
+    else:
+        seg_choice, seg_ms = tune.autotune_segment(apply, st, nb, steps=20, use_cache=False)
     # warm-up: the engine run (also builds and caches its CUDA graph)
     graphed = not args.direct
     simulate.run(apply, st, nb, max(3, args.warmup), use_graph=graphed)
@@ -679,8 +684,8 @@ def main():
     import ctypes as _C
     sb = st._sorted
     nbar = float(sb.cnt.float().mean())
-    # list bytes as read: 16-byte chunks of 8 two-byte entries per atom
-    chunk_bytes = float((16 * ((sb.cnt.clamp(max=nb.max_occupancy) + 7) // 8)).double().mean())
+    # list bytes per atom a perfect kernel reads: two-byte entries + count
+    chunk_bytes = 2.0 * float(sb.cnt.clamp(max=nb.max_occupancy).double().mean()) + 2.0
     species, pair = efn._resolve(st.position, {})
     sp = simulate._shift_space(shift, 3)
     xo = torch.empty((n, 4), dtype=torch.float32, device=dev)
@@ -693,8 +698,8 @@ def main():
         if seg_on:
             NAT.check(L_.jmd_nve_fused_step_segment(
                 _C.byref(pair), _C.byref(sp), _C.byref(nb.plan.nl), sb.seg_cells, sb.seg_threads,
-                sb.xa.data_ptr(), xo.data_ptr(), pm.data_ptr(), 1.0, n, 0, sb.seg.data_ptr(),
-                sb.seg_nch, sb.cnt.data_ptr(), DT, sb.ref.data_ptr(), nb.plan.threshold_sq,
+                sb.seg_list_smem, sb.xa.data_ptr(), xo.data_ptr(), pm.data_ptr(), 1.0, n, 0,
+                sb.seg.data_ptr(), sb.seg.numel(), DT, sb.ref.data_ptr(), nb.plan.threshold_sq,
                 flag.data_ptr(), sb.ws.data_ptr(), sb.ws.numel(), sb.seg_status.data_ptr(),
                 NAT.stream_ptr()), 'segment fused step')
         else:
@@ -719,13 +724,13 @@ def main():
     # algorithmic bytes of one fused-step launch: the list as read (16-byte
     # chunks of 8 two-byte staged slots; int32 entries on the tiled list),
     # the count, position read + write, momentum read + write, reference read
-    list_bytes = chunk_bytes if seg_on else 4 * nbar
-    kern_bytes = n * (list_bytes + 4 + 80)
+    list_bytes = chunk_bytes if seg_on else 4 * nbar + 4
+    kern_bytes = n * (list_bytes + 80)
     hbm, src = peaks()
     achieved = kern_bytes / (kern_ms / 1e3) / 1e9
     # per step: + force row written by the closing kick and read by the next
     # opening kick is fused away; the skin flag and rebuilds are extra
-    step_bytes = n * (list_bytes + 4 + 80)
+    step_bytes = n * (list_bytes + 80)
 
     # e2e: host pinned buffers through the public API (simulate.run, default
     # path), every step: positions and momenta copied in, one step, copied out
@@ -761,10 +766,11 @@ def main():
                    'mean_neighbors': nbar, 'max_occupancy': nb.max_occupancy,
                    'launch': 'cuda graph' if graphed else 'direct',
                    'private_list': 'segment-local (16-bit staged slots)' if seg_on else 'tiled int32',
-                   'segment': {'cells': seg_choice[0] if seg_choice else None,
-                               'threads': seg_choice[1] if seg_choice else None,
-                               'autotune_ms_per_step': {f'{k[0]}x{k[1]}': v
-                                                        for k, v in seg_ms.items()}},
+                   'segment': {'cells': sb.seg_cells, 'threads': sb.seg_threads,
+                               'list_smem_bytes': sb.seg_list_smem,
+                               'autotuned': seg_choice is not None,
+                               'autotune_ms_per_step': {'x'.join(str(int(v)) for v in k): t
+                                                        for k, t in seg_ms.items()}},
                    'energy_drift_per_atom': (E1 - E0) / n, 'overflow': overflow},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
                      'frac': achieved / hbm,
@@ -776,7 +782,7 @@ def main():
                      'kernel': ('k_seg_step fused NVE step (LJ, segment-local list, FP32x2)'
                                 if seg_on else 'k_tiled fused NVE step (LJ, Dense tiled, FP32x2)'),
                      'kernel_ms': kern_ms,
-                     'bytes_per_atom': list_bytes + 84,
+                     'bytes_per_atom': list_bytes + 80,
                      'step_algorithmic_GBps': step_bytes * args.steps / (ms / 1e3) / 1e9},
         'e2e': {'value': e2e_value, 'unit': 'atom-steps/s', 'h2d_bytes_per_step': 2 * n * 12,
                 'd2h_bytes_per_step': 2 * n * 12},

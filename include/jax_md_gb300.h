@@ -473,10 +473,12 @@ typedef struct {
   size_t workspace_bytes;
   /* Segment-local list (see jmd_segment_plan); seg_list == NULL runs the
    * tiled int32 list above instead.  With seg_list set, idx may be NULL. */
-  uint16_t* seg_list;         /* ceil(n/32)*32 * seg_nch * 8 entries */
-  int64_t seg_nch;            /* 8-entry chunks per atom, 8 * seg_nch >= max_occupancy */
+  uint8_t* seg_list;          /* segment blocks, 16-byte aligned */
+  int64_t seg_list_bytes;     /* >= the list_bytes jmd_segment_plan reports */
   int32_t seg_cells;          /* cells per segment along x (K) */
   int32_t seg_threads;        /* threads per segment CTA: a multiple of 32 in [32, 256] */
+  int32_t seg_list_smem;      /* shared-memory bytes for staging a segment's list block
+                                 with its positions (0: lists are read from global) */
   int32_t flags;              /* JMD_RUN_* bits */
   int32_t* seg_status;        /* device int32: staging overflow (1) / copy timeout (2) */
 } jmd_sorted_state;
@@ -496,24 +498,26 @@ typedef struct {
  * per side, a capacity within 16-bit slots and the shared memory of a CTA),
  * JMD_ERR_INVALID_ARGUMENT otherwise. */
 int jmd_segment_plan(const jmd_nlist* nl, int32_t cells, int32_t* n_segments,
-                     int32_t* capacity_atoms, int64_t* smem_bytes, int32_t* cells_used);
+                     int32_t* capacity_atoms, int64_t* smem_bytes, int32_t* cells_used,
+                     int64_t* list_bytes);
 
 /* One fused NVE step (jmd_nve_fused_step's arithmetic: force, both half
  * kicks, drift, skin test) on the segment-local list of the last sorted
  * rebuild: positions in cell order as float4 rows, `workspace` the sort's
- * workspace (its cell starts place the segments), seg_list / nbr_count as
- * the engine's build wrote them, species ids (when species_in_w) in the
- * fourth float of the position rows.  The engine's per-step kernel, exposed
+ * workspace (its cell starts place the segments), seg_list as the engine's
+ * build wrote it, species ids (when species_in_w) in the fourth float of the
+ * position rows; list_smem as jmd_sorted_state.seg_list_smem.  The engine's per-step kernel, exposed
  * so it can be timed and tested alone; no reference counterpart (it replaces
  * the force evaluation inside simulate.py:227-243 for the engine's private
  * layout). */
 int jmd_nve_fused_step_segment(const jmd_pair* pair, const jmd_space* space, const jmd_nlist* nl,
-                               int32_t cells, int32_t threads, const float* position,
-                               float* position_next, float* momentum, float mass_scalar, int64_t n,
-                               int32_t species_in_w, const uint16_t* seg_list, int64_t seg_nch,
-                               const int32_t* nbr_count, float dt, const float* reference_position,
-                               float threshold_sq, int32_t* rebuild_flag, void* workspace,
-                               size_t workspace_bytes, int32_t* seg_status, void* stream);
+                               int32_t cells, int32_t threads, int32_t list_smem,
+                               const float* position, float* position_next, float* momentum,
+                               float mass_scalar, int64_t n, int32_t species_in_w,
+                               const uint8_t* seg_list, int64_t seg_list_bytes, float dt,
+                               const float* reference_position, float threshold_sq,
+                               int32_t* rebuild_flag, void* workspace, size_t workspace_bytes,
+                               int32_t* seg_status, void* stream);
 
 /* jmd_nve_run with the atoms kept in cell order inside the run: on entry the
  * caller's state is copied in and sorted, the steps run on the sorted copy

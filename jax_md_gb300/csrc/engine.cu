@@ -301,7 +301,23 @@ bool run_seg_grid(const jmd_nve_system& s, const jmd_sorted_state& z, SegGrid* g
   const int rows = s.space.dim == 3 ? 9 : 3;
   g->cap = rows * (g->K + 2) * s.nlist.cell_capacity;
   g->threads = z.seg_threads;
+  g->lcap = std::max(0, z.seg_list_smem) / 16 * 16;
   return true;
+}
+
+// Shared memory of a segment step CTA: staged positions + far slot + the
+// list block capacity; checked against what a CTA may opt into.
+int seg_check_smem(const SegGrid& g) {
+  int dev = 0, optin = 227 * 1024;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+    cudaGetLastError();
+    optin = 227 * 1024;
+  }
+  const int64_t need = (int64_t)(g.cap + 1) * 16 + g.lcap + (int64_t)sizeof(SegShared) +
+                       64 * (int64_t)sizeof(PairCoef) + 64;
+  JMD_REQUIRE(need <= optin, "segment staging (positions + list block) exceeds a CTA's shared memory");
+  return JMD_OK;
 }
 
 int validate_sorted(const jmd_nve_system& s, const jmd_sorted_state& z) {
@@ -316,8 +332,11 @@ int validate_sorted(const jmd_nve_system& s, const jmd_sorted_state& z) {
   if (z.seg_list) {
     SegGrid g;
     JMD_REQUIRE(run_seg_grid(s, z, &g), "the segment layout does not apply to this cell grid");
-    JMD_REQUIRE(g.cap <= kSegMaxStaged, "segment staging capacity beyond 16-bit slots");
-    JMD_REQUIRE(z.seg_nch * 8 >= s.nlist.max_occupancy, "seg_nch * 8 < max_occupancy");
+    JMD_REQUIRE(g.cap < kSegMaxStaged, "segment staging capacity beyond 16-bit slots");
+    JMD_REQUIRE(s.nlist.max_occupancy < 65536, "the segment list stores counts in 16 bits");
+    JMD_REQUIRE(z.seg_list_bytes >= seg_list_bytes(g), "seg_list smaller than the plan's list_bytes");
+    int e = seg_check_smem(g);
+    if (e) return e;
     JMD_REQUIRE(z.seg_status != nullptr, "seg_status is required with seg_list");
     JMD_REQUIRE(z.seg_threads >= 32 && z.seg_threads <= kSegMaxThreads && z.seg_threads % 32 == 0,
                 "seg_threads must be a multiple of 32 in [32, 256]");
@@ -351,9 +370,9 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
                               flag, z.workspace, z.workspace_bytes, q);
     if (rc) return rc;
     if (seg)
-      return build_segment_after_sort(&s.nlist, sg, x, s.n, z.seg_list, z.seg_nch, z.nbr_count,
-                                      z.occupancy, z.error_code, z.reference_position, z.seg_status,
-                                      flag, z.workspace, z.workspace_bytes, q);
+      return build_segment_after_sort(&s.nlist, sg, x, s.n, z.seg_list, z.nbr_count, z.occupancy,
+                                      z.error_code, z.reference_position, z.seg_status, flag,
+                                      z.workspace, z.workspace_bytes, q);
     return build_tiled_after_sort(&s.nlist, x, s.n, z.idx, z.idx_ld, z.nbr_count, z.occupancy,
                                   z.error_code, z.reference_position, flag, z.workspace,
                                   z.workspace_bytes, q);
@@ -361,8 +380,7 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
   const bool sp = s.species != nullptr;
   auto force_kick_at = [&](const float* x, cudaStream_t q) -> int {
     if (seg)
-      return seg_step(3, s.pair, s.space, sg, x, starts, z.seg_list, z.seg_nch,
-                      s.nlist.max_occupancy, z.nbr_count, z.force, z.momentum, nullptr,
+      return seg_step(3, s.pair, s.space, sg, x, starts, z.seg_list, z.force, z.momentum, nullptr,
                       s.mass_scalar, s.dt, nullptr, 0.f, nullptr, z.seg_status, sp, q);
     return jmd_force_kick_tiled(&s.pair, &s.space, x, z.force, z.momentum, z.species, s.n, z.idx,
                                 z.idx_ld, s.nlist.max_occupancy, z.nbr_count, s.dt, q);
@@ -403,10 +421,9 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
     for (int64_t k = 1; k < steps; ++k) {
       if ((rc = gate(cur))) return rc;
       if (seg)
-        rc = seg_step(2, s.pair, s.space, sg, cur, starts, z.seg_list, z.seg_nch, width,
-                      z.nbr_count, nullptr, z.momentum, nxt, s.mass_scalar, s.dt,
-                      always ? nullptr : z.reference_position, s.threshold_sq,
-                      always ? nullptr : z.rebuild_flag, z.seg_status, sp, st);
+        rc = seg_step(2, s.pair, s.space, sg, cur, starts, z.seg_list, nullptr, z.momentum, nxt,
+                      s.mass_scalar, s.dt, always ? nullptr : z.reference_position,
+                      s.threshold_sq, always ? nullptr : z.rebuild_flag, z.seg_status, sp, st);
       else
         rc = jmd_nve_fused_step_tiled(&s.pair, &s.space, cur, nxt, z.momentum, s.mass_scalar,
                                       z.species, s.n, z.idx, z.idx_ld, width, z.nbr_count, s.dt,
@@ -682,7 +699,8 @@ int jmd_nvt_run_sorted(const jmd_nve_system* sys, const jmd_sorted_state* sorted
 }
 
 int jmd_segment_plan(const jmd_nlist* nl, int32_t cells, int32_t* n_segments,
-                     int32_t* capacity_atoms, int64_t* smem_bytes, int32_t* cells_used) {
+                     int32_t* capacity_atoms, int64_t* smem_bytes, int32_t* cells_used,
+                     int64_t* list_bytes) {
   JMD_REQUIRE(nl != nullptr, "nlist descriptor is null");
   SegGrid g;
   if (!make_seg_grid(*nl, cells, 1, &g))
@@ -698,43 +716,47 @@ int jmd_segment_plan(const jmd_nlist* nl, int32_t cells, int32_t* n_segments,
     cudaGetLastError();
     optin = 227 * 1024;
   }
-  const int64_t smem = cap * (int64_t)sizeof(float4);
+  const int64_t smem = (cap + 1) * (int64_t)sizeof(float4);  // + the far slot
   const int64_t static_smem = (int64_t)sizeof(SegShared) + 64 * (int64_t)sizeof(PairCoef) + 64;
-  if (cap > kSegMaxStaged || smem + static_smem > optin)
+  if (cap >= kSegMaxStaged || smem + static_smem > optin || nl->max_occupancy >= 65536)
     return fail(JMD_ERR_INVALID_ARGUMENT, "segment staging exceeds a CTA's shared memory");
   if (n_segments) *n_segments = g.nseg;
   if (capacity_atoms) *capacity_atoms = (int32_t)cap;
   if (smem_bytes) *smem_bytes = smem;
   if (cells_used) *cells_used = g.K;
+  if (list_bytes) *list_bytes = seg_list_bytes(g);
   return JMD_OK;
 }
 
 int jmd_nve_fused_step_segment(const jmd_pair* pair, const jmd_space* space, const jmd_nlist* nl,
-                               int32_t cells, int32_t threads, const float* position,
-                               float* position_next, float* momentum, float mass_scalar, int64_t n,
-                               int32_t species_in_w, const uint16_t* seg_list, int64_t seg_nch,
-                               const int32_t* nbr_count, float dt, const float* reference_position,
-                               float threshold_sq, int32_t* rebuild_flag, void* workspace,
-                               size_t workspace_bytes, int32_t* seg_status, void* stream) {
+                               int32_t cells, int32_t threads, int32_t list_smem,
+                               const float* position, float* position_next, float* momentum,
+                               float mass_scalar, int64_t n, int32_t species_in_w,
+                               const uint8_t* seg_list, int64_t seg_list_bytes_, float dt,
+                               const float* reference_position, float threshold_sq,
+                               int32_t* rebuild_flag, void* workspace, size_t workspace_bytes,
+                               int32_t* seg_status, void* stream) {
   JMD_REQUIRE(pair && space && nl, "null descriptor");
   JMD_REQUIRE(n > 0 && n < INT32_MAX, "atom count out of range");
-  JMD_REQUIRE(position && position_next && momentum && seg_list && nbr_count && seg_status,
-              "null buffer");
+  JMD_REQUIRE(position && position_next && momentum && seg_list && seg_status, "null buffer");
   JMD_REQUIRE(position != position_next, "position and position_next must differ");
   JMD_REQUIRE(reference_position == nullptr || rebuild_flag != nullptr, "skin test needs a flag");
   JMD_REQUIRE(threads >= 32 && threads <= kSegMaxThreads && threads % 32 == 0,
               "threads must be a multiple of 32 in [32, 256]");
-  JMD_REQUIRE(seg_nch * 8 >= nl->max_occupancy, "seg_nch * 8 < max_occupancy");
   SegGrid g;
   JMD_REQUIRE(make_seg_grid(*nl, cells, 1, &g), "the segment layout does not apply to this cell grid");
   g.cap = (nl->space.dim == 3 ? 9 : 3) * (g.K + 2) * nl->cell_capacity;
   g.threads = threads;
-  JMD_REQUIRE(g.cap <= kSegMaxStaged, "segment staging capacity beyond 16-bit slots");
+  g.lcap = std::max(0, list_smem) / 16 * 16;
+  JMD_REQUIRE(g.cap < kSegMaxStaged, "segment staging capacity beyond 16-bit slots");
+  JMD_REQUIRE(seg_list_bytes_ >= seg_list_bytes(g), "seg_list smaller than the plan's list_bytes");
+  int e = seg_check_smem(g);
+  if (e) return e;
   const int32_t* starts = sort_cell_starts(nl, n, workspace, workspace_bytes);
   if (!starts) return fail(JMD_ERR_WORKSPACE, "workspace too small for the cell starts");
-  return seg_step(2, *pair, *space, g, position, starts, seg_list, seg_nch, nl->max_occupancy,
-                  nbr_count, nullptr, momentum, position_next, mass_scalar, dt, reference_position,
-                  threshold_sq, rebuild_flag, seg_status, species_in_w != 0, as_stream(stream));
+  return seg_step(2, *pair, *space, g, position, starts, seg_list, nullptr, momentum,
+                  position_next, mass_scalar, dt, reference_position, threshold_sq, rebuild_flag,
+                  seg_status, species_in_w != 0, as_stream(stream));
 }
 
 int jmd_engine_clear_cache(void) {

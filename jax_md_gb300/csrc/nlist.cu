@@ -251,9 +251,9 @@ __global__ void k_cell_rank(const float* __restrict__ x, int64_t stride, int64_t
     }
     if (a < k) {
       b.sorted_id[beg + rank] = mine;
-      float4 r = load_row<DIM, VEC4>(x, stride, mine);
-      r.w = 0.f;
-      b.sorted_pos[beg + rank] = r;
+      // the fourth float travels with the atom (the engine keeps species ids
+      // there; plain rows have w = 0 and strided rows load it as 0)
+      b.sorted_pos[beg + rank] = load_row<DIM, VEC4>(x, stride, mine);
     }
   }
 }
@@ -919,89 +919,160 @@ namespace {
 // cutoff of a face, so a pair within an ulp of the list cutoff may be kept
 // where the reference drops it (or the reverse): such pairs lie beyond the
 // interaction cutoff and change no force.
-template <int DIM>
+template <int DIM, bool FRAME>
 __global__ void __launch_bounds__(kSegMaxThreads)
 k_seg_search(SegGrid sg, const float4* __restrict__ x, Bins b, Geo geo, float cut2, float margin,
-             int mask_self, uint16_t* __restrict__ list, int64_t nch, int width,
-             int32_t* __restrict__ count, float4* __restrict__ ref, int32_t* status,
-             const int32_t* flag) {
+             int mask_self, uint8_t* __restrict__ blocks, int32_t* __restrict__ nck_table,
+             SegRecord* __restrict__ recs, int width, int32_t* __restrict__ count,
+             float4* __restrict__ ref, int32_t* status, const int32_t* flag) {
   if (skip(flag)) return;
   extern __shared__ float4 spos[];
   __shared__ SegShared sh;
   __shared__ unsigned cta_max;
-  if (threadIdx.x == 0) cta_max = 0u;
-  seg_stage<DIM>(sg, x, b.start, spos, sh, status);
-  if (!sh.ok) {
-    if (threadIdx.x == 0) atomicOr(&b.sc->flags, (unsigned)JMD_CELL_LIST_OVERFLOW);
+  __shared__ int cta_nck;
+  if (threadIdx.x == 0) {
+    cta_max = 0u;
+    cta_nck = 0;
+  }
+  SegRecord* rec = recs + blockIdx.x;
+  if (!seg_stage<DIM>(sg, x, b.start, spos, sh, status, rec)) {
+    if (threadIdx.x == 0) {
+      atomicOr(&b.sc->flags, (unsigned)JMD_CELL_LIST_OVERFLOW);
+      nck_table[blockIdx.x] = 0;
+      rec->nck = 0;
+      rec->total = -1;
+    }
     return;
   }
+  const int fmask = FRAME ? seg_frame<DIM>(sg, sh, spos, geo.L) : 0;
   const int W = sh.W;
   const int rows = sh.rows;
+  const uint64_t far = (uint64_t)sg.cap;  // the far slot: pads chunks and rows past width
+  const int nch = sg.nch;
+  const int P = seg_pad(sh.own_cnt);
+  uint8_t* blk = blocks + (int64_t)blockIdx.x * sg.stride;
+  // a segment with more own atoms than a block holds only occurs with a cell
+  // over capacity (flagged by the binning); its list is not written
+  const bool fits = P <= sg.pmax;
+  if (!fits && threadIdx.x == 0) atomicOr(&b.sc->flags, (unsigned)JMD_CELL_LIST_OVERFLOW);
   unsigned my_max = 0u;
-  for (int a = threadIdx.x; a < sh.own_cnt; a += blockDim.x) {
-    const int is = sh.own_sm + a, s = sh.own_beg + a;
-    const float4 xi = spos[is];
-    const int u = seg_own_cell<DIM>(sh, is);
-    const bool inner = interior<DIM>(xi, geo, margin);
-    uint16_t* base = list + seg_list_base(s, nch);
+  int my_nck = 0;
+  // one warp per own cell (u = 1..nx of the centre row): the cell's atoms are
+  // the lanes (32 at a time), and every lane walks the same candidate runs
+  // (cells u-1..u+1 of each staged row), so trip counts are uniform and
+  // each candidate read is a shared-memory broadcast
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int cr = seg_centre_row<DIM>() * W;
+  for (int task = warp; ; task += nwarps) {
+    // task -> (own cell u, group of 32 of its atoms)
+    int u = 1, t = task;
+    while (u <= sh.nx) {
+      const int groups = (sh.coff[cr + u + 1] - sh.coff[cr + u] + 31) >> 5;
+      if (t < groups) break;
+      t -= groups;
+      ++u;
+    }
+    if (u > sh.nx) break;
+    const int cb = sh.coff[cr + u], ce = sh.coff[cr + u + 1];
+    const int is = cb + 32 * t + lane;
+    const bool active = is < ce;
+    const int ia = is - sh.own_sm;  // own index of the lane's atom
+    const int s = sh.own_beg + ia;
+    const float4 xi = spos[active ? is : cb];
+    const bool inner = FRAME || interior<DIM>(xi, geo, margin);
     int cnt = 0;
-    uint32_t w0 = 0u, w1 = 0u, w2 = 0u, w3 = 0u;
-    auto push = [&](int j) {
-      const int p = cnt & 7;
-      const uint32_t v = (uint32_t)j << ((p & 1) * 16);
-      const int q = p >> 1;
-      w0 |= q == 0 ? v : 0u;
-      w1 |= q == 1 ? v : 0u;
-      w2 |= q == 2 ? v : 0u;
-      w3 |= q == 3 ? v : 0u;
-      if (p == 7) {
-        if ((cnt >> 3) < nch)
-          *reinterpret_cast<uint4*>(base + (int64_t)(cnt >> 3) * 256) = make_uint4(w0, w1, w2, w3);
-        w0 = w1 = w2 = w3 = 0u;
+    // the chunk being filled: entries 0-3 in `lo`, 4-7 in `acc` (16 bits each)
+    uint64_t lo = 0, acc = 0;
+    auto put = [&](uint64_t j, int p) {  // entry j at position p of the chunk
+      acc |= j << (16 * (p & 3));
+      if ((p & 3) == 3) {
+        if (p == 3) {
+          lo = acc;
+        } else if ((cnt >> 3) < nch && fits) {
+          *reinterpret_cast<uint4*>(blk + seg_chunk_off(P, cnt >> 3, ia)) =
+              make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)acc, (uint32_t)(acc >> 32));
+        }
+        acc = 0;
       }
-      ++cnt;
     };
     const float2 xx = f2s(xi.x), xy = f2s(xi.y), xz = f2s(xi.z);
     for (int r = 0; r < rows; ++r) {
       const int j0 = sh.coff[r * W + u - 1], j1 = sh.coff[r * W + u + 2];
-      for (int j = j0; j < j1; j += 2) {
-        const bool two = j + 1 < j1;
-        const float4 b0 = spos[j];
-        const float4 b1 = spos[two ? j + 1 : j];
-        float2 dx = sub2(xx, f2(b0.x, b1.x));
-        float2 dy = sub2(xy, f2(b0.y, b1.y));
-        float2 dz = DIM == 3 ? sub2(xz, f2(b0.z, b1.z)) : f2s(0.f);
-        if (!inner) {
-          dx.x = min_image(xi.x, b0.x, geo.L[0], geo.halfL[0]);
-          dx.y = min_image(xi.x, b1.x, geo.L[0], geo.halfL[0]);
-          dy.x = min_image(xi.y, b0.y, geo.L[1], geo.halfL[1]);
-          dy.y = min_image(xi.y, b1.y, geo.L[1], geo.halfL[1]);
-          if (DIM == 3) {
-            dz.x = min_image(xi.z, b0.z, geo.L[2], geo.halfL[2]);
-            dz.y = min_image(xi.z, b1.z, geo.L[2], geo.halfL[2]);
+      for (int jb = j0; jb < j1; jb += 32) {
+        // distance tests of up to 32 candidates into a hit mask; j + 1 may
+        // read one slot past the run (still inside the staged block or the
+        // far slot) and its bit is masked below
+        const int nb = min(32, j1 - jb);
+        uint32_t hits = 0u;
+        for (int k = 0; k < nb; k += 2) {
+          const int j = jb + k;
+          const float4 b0 = spos[j];
+          const float4 b1 = spos[j + 1];
+          float2 dx = sub2(xx, f2(b0.x, b1.x));
+          float2 dy = sub2(xy, f2(b0.y, b1.y));
+          float2 dz = DIM == 3 ? sub2(xz, f2(b0.z, b1.z)) : f2s(0.f);
+          if (!inner) {
+            dx.x = min_image(xi.x, b0.x, geo.L[0], geo.halfL[0]);
+            dx.y = min_image(xi.x, b1.x, geo.L[0], geo.halfL[0]);
+            dy.x = min_image(xi.y, b0.y, geo.L[1], geo.halfL[1]);
+            dy.y = min_image(xi.y, b1.y, geo.L[1], geo.halfL[1]);
+            if (DIM == 3) {
+              dz.x = min_image(xi.z, b0.z, geo.L[2], geo.halfL[2]);
+              dz.y = min_image(xi.z, b1.z, geo.L[2], geo.halfL[2]);
+            }
           }
+          float2 r2 = mul2(dx, dx);
+          r2 = fma2(dy, dy, r2);
+          if (DIM == 3) r2 = fma2(dz, dz, r2);
+          hits |= ((r2.x < cut2 ? 1u : 0u) | (r2.y < cut2 ? 2u : 0u)) << k;
         }
-        float2 r2 = mul2(dx, dx);
-        r2 = fma2(dy, dy, r2);
-        if (DIM == 3) r2 = fma2(dz, dz, r2);
-        if (r2.x < cut2 && (j != is || !mask_self)) push(j);
-        if (two && r2.y < cut2 && (j + 1 != is || !mask_self)) push(j + 1);
+        if (nb < 32) hits &= (1u << nb) - 1u;
+        if (mask_self && is >= jb && is < jb + nb) hits &= ~(1u << (is - jb));
+        if (!active) hits = 0u;
+        // append the hits in candidate order; rows past `width` keep the far
+        // slot so the chunk stays valid
+        while (hits) {
+          const int bit = __ffs(hits) - 1;
+          hits &= hits - 1;
+          put(cnt < width ? (uint64_t)(jb + bit) : far, cnt & 7);
+          ++cnt;
+        }
       }
     }
-    if ((cnt & 7) != 0 && (cnt >> 3) < nch)
-      *reinterpret_cast<uint4*>(base + (int64_t)(cnt >> 3) * 256) = make_uint4(w0, w1, w2, w3);
-    count[s] = cnt;
-    float4 rr = xi;
-    rr.w = 0.f;
-    ref[s] = rr;
-    my_max = max(my_max, (unsigned)cnt);
+    if (active) {
+      // pad the last chunk with the far slot
+      if (cnt & 7)
+        for (int p = cnt & 7; p < 8; ++p) put(far, p);
+      count[s] = cnt;
+      const int kept = min(cnt, width);
+      if (fits) reinterpret_cast<uint16_t*>(blk + 16)[ia] = (uint16_t)kept;
+      my_nck = max(my_nck, (kept + 7) >> 3);
+      float4 rr = xi;
+      if (FRAME && fmask) {
+        if ((fmask & 1) && rr.x < 0.f) rr.x += geo.L[0];
+        if ((fmask & 2) && rr.y < 0.f) rr.y += geo.L[1];
+        if (DIM == 3 && (fmask & 4) && rr.z < 0.f) rr.z += geo.L[2];
+      }
+      rr.w = 0.f;
+      ref[s] = rr;
+      my_max = max(my_max, (unsigned)cnt);
+    }
   }
   my_max = __reduce_max_sync(0xffffffffu, my_max);
-  if ((threadIdx.x & 31) == 0) atomicMax(&cta_max, my_max);
+  my_nck = __reduce_max_sync(0xffffffffu, (unsigned)my_nck);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&cta_max, my_max);
+    atomicMax(&cta_nck, my_nck);
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     atomicMax(&b.sc->occupancy, (unsigned long long)cta_max);
     if ((int)cta_max > width) atomicOr(&b.sc->flags, (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
+    const int nck = fits ? min(cta_nck, nch) : 0;
+    reinterpret_cast<int32_t*>(blk)[0] = nck;
+    reinterpret_cast<int32_t*>(blk)[1] = sh.own_cnt;
+    nck_table[blockIdx.x] = nck;
+    rec->nck = nck;
   }
 }
 
@@ -1023,14 +1094,16 @@ const int32_t* sort_cell_starts(const jmd_nlist* nl, int64_t n, void* workspace,
 }
 
 int build_segment_after_sort(const jmd_nlist* nl, const SegGrid& sg, const float* position,
-                             int64_t n, uint16_t* list, int64_t nch, int32_t* nbr_count,
-                             int64_t* occupancy, uint8_t* error_code, float* reference_position,
-                             int32_t* seg_status, int32_t* rebuild_flag, void* workspace,
-                             size_t workspace_bytes, cudaStream_t st) {
+                             int64_t n, uint8_t* list, int32_t* nbr_count, int64_t* occupancy,
+                             uint8_t* error_code, float* reference_position, int32_t* seg_status,
+                             int32_t* rebuild_flag, void* workspace, size_t workspace_bytes,
+                             cudaStream_t st) {
   int e = validate(nl, n);
   if (e) return e;
   JMD_REQUIRE(nl->format == JMD_DENSE && nl->use_cell_list, "segment lists are Dense with a cell grid");
-  JMD_REQUIRE(list && nbr_count && nch * 8 >= nl->max_occupancy, "segment list needs 8 * nch >= max_occupancy");
+  JMD_REQUIRE(list && nbr_count && (int64_t)sg.nch * 8 >= nl->max_occupancy,
+              "segment list needs 8 * nch >= max_occupancy");
+  JMD_REQUIRE((reinterpret_cast<uintptr_t>(list) % 16) == 0, "segment list must be 16-byte aligned");
   JMD_REQUIRE(is_vec4(position, 4) && is_vec4(reference_position, 4), "float4 rows must be 16-byte aligned");
   JMD_REQUIRE(nl->max_occupancy < INT32_MAX, "max_occupancy out of range");
   Grid g = make_grid(*nl);
@@ -1039,22 +1112,29 @@ int build_segment_after_sort(const jmd_nlist* nl, const SegGrid& sg, const float
   if (!ok) return fail(JMD_ERR_WORKSPACE, "neighbour-list workspace too small");
   const Geo geo = make_geo(nl->space);
   const float margin = sqrtf(nl->cutoff_sq);
-  const size_t smem = (size_t)sg.cap * sizeof(float4);
+  const size_t smem = (size_t)(sg.cap + 1) * sizeof(float4);
   const float4* x = reinterpret_cast<const float4*>(position);
   float4* ref = reinterpret_cast<float4*>(reference_position);
   const int width = (int)nl->max_occupancy;
+  auto go = [&](auto kernel) -> int {
+    int rc = seg_smem_optin(kernel, smem);
+    if (rc) return rc;
+    // one warp per own cell of a segment (at most 8 warps)
+    const unsigned threads = (unsigned)(32 * std::min(sg.K, kSegMaxThreads / 32));
+    int32_t* table = reinterpret_cast<int32_t*>(list);
+    SegRecord* recs = reinterpret_cast<SegRecord*>(list + seg_table_bytes(sg.nseg));
+    uint8_t* blocks = list + seg_table_bytes(sg.nseg) + seg_records_bytes(sg.nseg);
+    kernel<<<(unsigned)sg.nseg, threads, smem, st>>>(
+        sg, x, b, geo, nl->cutoff_sq, margin, nl->mask_self, blocks, table, recs, width, nbr_count,
+        ref, seg_status, rebuild_flag);
+    return JMD_OK;
+  };
   if (n > 0) {
-    if (nl->space.dim == 3) {
-      if ((e = seg_smem_optin(k_seg_search<3>, smem))) return e;
-      k_seg_search<3><<<(unsigned)sg.nseg, (unsigned)sg.threads, smem, st>>>(sg, x, b, geo, nl->cutoff_sq, margin,
-                                                            nl->mask_self, list, nch, width,
-                                                            nbr_count, ref, seg_status, rebuild_flag);
-    } else {
-      if ((e = seg_smem_optin(k_seg_search<2>, smem))) return e;
-      k_seg_search<2><<<(unsigned)sg.nseg, (unsigned)sg.threads, smem, st>>>(sg, x, b, geo, nl->cutoff_sq, margin,
-                                                            nl->mask_self, list, nch, width,
-                                                            nbr_count, ref, seg_status, rebuild_flag);
-    }
+    if (nl->space.dim == 3)
+      e = sg.frame ? go(k_seg_search<3, true>) : go(k_seg_search<3, false>);
+    else
+      e = sg.frame ? go(k_seg_search<2, true>) : go(k_seg_search<2, false>);
+    if (e) return e;
   }
   FinalizeArgs f{JMD_DENSE, nl->max_occupancy, 1, nl->cell_capacity, (int)n};
   k_finalize<<<1, 1, 0, st>>>(b, f, occupancy, error_code, rebuild_flag);

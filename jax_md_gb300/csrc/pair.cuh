@@ -222,13 +222,12 @@ namespace jmd {
 const int32_t* sort_cell_starts(const jmd_nlist* nl, int64_t n, void* workspace,
                                 size_t workspace_bytes);
 int build_segment_after_sort(const jmd_nlist* nl, const SegGrid& sg, const float* position,
-                             int64_t n, uint16_t* list, int64_t nch, int32_t* nbr_count,
-                             int64_t* occupancy, uint8_t* error_code, float* reference_position,
-                             int32_t* seg_status, int32_t* rebuild_flag, void* workspace,
-                             size_t workspace_bytes, cudaStream_t st);
+                             int64_t n, uint8_t* list, int32_t* nbr_count, int64_t* occupancy,
+                             uint8_t* error_code, float* reference_position, int32_t* seg_status,
+                             int32_t* rebuild_flag, void* workspace, size_t workspace_bytes,
+                             cudaStream_t st);
 int seg_step(int mode, const jmd_pair& pp, const jmd_space& space, const SegGrid& g,
-             const float* x, const int32_t* start, const uint16_t* list, int64_t nch, int64_t width,
-             const int32_t* cnt, float* f, float* p, float* x_next, float m0, float dt,
-             const float* ref, float thr2, int32_t* flag, int32_t* status, bool species,
-             cudaStream_t st);
+             const float* x, const int32_t* start, const uint8_t* list, float* f, float* p,
+             float* x_next, float m0, float dt, const float* ref, float thr2, int32_t* flag,
+             int32_t* status, bool species, cudaStream_t st);
 }  // namespace jmd

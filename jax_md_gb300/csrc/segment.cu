@@ -23,11 +23,8 @@ enum { S_FORCE = 0, S_STEP = 2, S_KICK = 3 };
 
 struct SegStepArgs {
   const float4* x;
-  const int32_t* start;
-  const uint16_t* list;
-  int64_t nch;
-  int width;
-  const int32_t* cnt;
+  const SegRecord* recs;     // per-segment staging records of the last rebuild
+  const uint8_t* blocks;     // segment blocks (segment.cuh)
   float4* f;
   Geo geo;
   float margin;
@@ -43,24 +40,74 @@ struct SegStepArgs {
 
 __device__ __forceinline__ int sclamp(int s, int nsp) { return s < 0 ? 0 : (s >= nsp ? nsp - 1 : s); }
 
-template <int DIM, int KIND, bool SPECIES, int MODE>
-__global__ void __launch_bounds__(kSegMaxThreads)
+// FRAME: the staged block is in the CTA's periodic frame (seg_frame), pair
+// displacements are plain differences; otherwise atoms within the cutoff of
+// a face take the minimum image per pair.
+template <int DIM, int KIND, bool SPECIES, int MODE, bool FRAME>
+__global__ void __maxnreg__(72)
 k_seg_step(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
   extern __shared__ float4 spos[];
   __shared__ SegShared sh;
   __shared__ PairCoef sc[SPECIES ? JMD_MAX_SPECIES * JMD_MAX_SPECIES : 1];
   if (SPECIES)
     for (int k = threadIdx.x; k < JMD_MAX_SPECIES * JMD_MAX_SPECIES; k += blockDim.x) sc[k] = tab.c[k];
-  seg_stage<DIM>(sg, a.x, a.start, spos, sh, a.status);
-  if (!sh.ok) return;
+  // staging from the segment's record: the positions (and the list block
+  // when it fits in shared memory) arrive on one mbarrier; each thread's
+  // first list chunks are requested meanwhile when the block stays in global
+  // memory
+  uint8_t* slist = reinterpret_cast<uint8_t*>(spos + sg.cap + 1);
+  const uint8_t* gblk = a.blocks + (int64_t)blockIdx.x * sg.stride;
+  const SegHead hd = seg_stage_record<DIM>(sg, a.x, a.recs + blockIdx.x, spos, sh, a.status, gblk,
+                                           sg.lcap > 0 ? slist : nullptr);
+  if (hd.total < 0) return;  // neighbourhood over capacity (flagged at the rebuild)
+  const int P = seg_pad(hd.own_cnt);
+  // more own atoms than a block holds (a cell over capacity, flagged at the
+  // rebuild): the block was not written and is not read
+  const bool blk_ok = P <= sg.pmax;
+  const int nck_seg = blk_ok ? hd.nck : 0;
+  const uint8_t* blk = hd.list_sm ? slist : gblk;
+  const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
+  const int o0 = threadIdx.x;
+  int c_pre = 0;
+  uint4 n1_pre = z4, n2_pre = z4;
+  if (!hd.list_sm && blk_ok && o0 < hd.own_cnt) {
+    const uint4* lp = reinterpret_cast<const uint4*>(gblk + seg_chunk_off(P, 0, o0));
+    c_pre = min((int)reinterpret_cast<const uint16_t*>(gblk + 16)[o0], 8 * nck_seg);
+    if (nck_seg > 0) n1_pre = lp[0];
+    if (nck_seg > 1) n2_pre = lp[P];
+  }
+  bool ok = seg_wait_one(sh, a.status);
+  int fmask = 0;
+  if (FRAME) {
+    const SegPos sp = seg_pos<DIM>(sg);
+    if (sp.x0 == 0 || sp.x0 + sp.nx >= sg.cps[0]) fmask |= 1;
+    if (sp.cy == 0 || sp.cy == sg.cps[1] - 1) fmask |= 2;
+    if (DIM == 3 && (sp.cz == 0 || sp.cz == sg.cps[2] - 1)) fmask |= 4;
+    if (fmask) {
+      // face segments: all threads agree on the staged block, then shift it
+      if (!__syncthreads_and(ok)) return;
+      const float h0 = 0.5f * a.geo.L[0], h1 = 0.5f * a.geo.L[1], h2 = 0.5f * a.geo.L[2];
+      for (int t = threadIdx.x; t < hd.total; t += blockDim.x) {
+        float4 v = spos[t];
+        if ((fmask & 1) && v.x >= h0) v.x -= a.geo.L[0];
+        if ((fmask & 2) && v.y >= h1) v.y -= a.geo.L[1];
+        if (DIM == 3 && (fmask & 4) && v.z >= h2) v.z -= a.geo.L[2];
+        spos[t] = v;
+      }
+      __syncthreads();
+    }
+  }
+  if (!ok) return;
   const float rc2m = tab.rc2_max;
   const Coef2 c0 = coef2(tab.c[0]);
-  for (int o = threadIdx.x; o < sh.own_cnt; o += blockDim.x) {
-    const int is = sh.own_sm + o, s = sh.own_beg + o;
-    const float4 xi = spos[is];
-    const int c = min(__ldg(a.cnt + s), a.width);
-    const uint4* lp = reinterpret_cast<const uint4*>(a.list + seg_list_base(s, a.nch));
-    const bool inner = interior<DIM>(xi, a.geo, a.margin);
+  for (int o = threadIdx.x; o < hd.own_cnt; o += blockDim.x) {
+    const int is = hd.own_sm + o, s = hd.own_beg + o;
+    float4 xi = spos[is];
+    const bool first = o == o0 && !hd.list_sm;
+    // a block written for fewer chunks is read no further than it was written
+    const int c = !blk_ok ? 0 : (first ? c_pre : min((int)reinterpret_cast<const uint16_t*>(blk + 16)[o], 8 * nck_seg));
+    const uint4* lp = reinterpret_cast<const uint4*>(blk + seg_chunk_off(P, 0, o));
+    const bool inner = FRAME || interior<DIM>(xi, a.geo, a.margin);
     const int si = SPECIES ? sclamp(__float_as_int(xi.w), tab.nsp) : 0;
     const float2 xx = f2s(xi.x), xy = f2s(xi.y), xz = f2s(xi.z);
     float2 ax = f2s(0.f), ay = f2s(0.f), az = f2s(0.f);
@@ -100,22 +147,29 @@ k_seg_step(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
       if (DIM == 3) az = fma2(g, dz, az);
     };
 
-    // entries past the count point at the atom itself (distance 0: masked)
+    // entries past the count (to the end of the last chunk) point at the
+    // far slot, beyond every cutoff
+    // chunk k of this atom at lp + k P; two chunks in flight ahead (the
+    // block is in shared memory, or in global memory when it did not fit)
     const int nck = (c + 7) >> 3;
-    uint4 nxt = nck > 0 ? __ldcs(lp) : make_uint4(0u, 0u, 0u, 0u);
+    uint4 n1 = first ? n1_pre : (nck > 0 ? lp[0] : z4);
+    uint4 n2 = first ? n2_pre : (nck > 1 ? lp[P] : z4);
     for (int kc = 0; kc < nck; ++kc) {
-      const uint4 cur = nxt;
-      if (kc + 1 < nck) nxt = __ldcs(lp + (int64_t)(kc + 1) * 32);
-      const int k0 = kc * 8;
-      const uint32_t wv[4] = {cur.x, cur.y, cur.z, cur.w};
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        const int j0 = (k0 + 2 * m < c) ? (int)(wv[m] & 0xFFFFu) : is;
-        const int j1 = (k0 + 2 * m + 1 < c) ? (int)(wv[m] >> 16) : is;
-        pair2(j0, j1);
-      }
+      const uint4 cur = n1;
+      n1 = n2;
+      if (kc + 2 < nck) n2 = lp[(int64_t)(kc + 2) * P];
+      pair2((int)(cur.x & 0xFFFFu), (int)(cur.x >> 16));
+      pair2((int)(cur.y & 0xFFFFu), (int)(cur.y >> 16));
+      pair2((int)(cur.z & 0xFFFFu), (int)(cur.z >> 16));
+      pair2((int)(cur.w & 0xFFFFu), (int)(cur.w >> 16));
     }
     const float fx = -(ax.x + ax.y), fy = -(ay.x + ay.y), fz = DIM == 3 ? -(az.x + az.y) : 0.f;
+    if (FRAME && fmask) {
+      // back to the box's coordinates, exactly (the frame subtracted L)
+      if ((fmask & 1) && xi.x < 0.f) xi.x += a.geo.L[0];
+      if ((fmask & 2) && xi.y < 0.f) xi.y += a.geo.L[1];
+      if (DIM == 3 && (fmask & 4) && xi.z < 0.f) xi.z += a.geo.L[2];
+    }
     float4 q = make_float4(0.f, 0.f, 0.f, 0.f), rf = q;
     if (MODE == S_STEP || MODE == S_KICK) q = a.p[s];
     if (MODE == S_STEP && a.ref) rf = __ldg(a.ref + s);
@@ -157,21 +211,23 @@ k_seg_step(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
   }
 }
 
+template <int DIM, int KIND, bool SP, int MODE, bool FRAME>
+int seg_go(const SegGrid& g, const SegStepArgs& a, const PairTable& t, cudaStream_t st) {
+  const size_t smem = (size_t)(g.cap + 1) * sizeof(float4) + (size_t)g.lcap;
+  auto k = k_seg_step<DIM, KIND, SP, MODE, FRAME>;
+  if (smem > 48 * 1024)
+    JMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k<<<(unsigned)g.nseg, (unsigned)g.threads, smem, st>>>(g, a, t);
+  return JMD_OK;
+}
+
 template <int DIM, int KIND, int MODE>
 int seg_sp(bool sp, const SegGrid& g, const SegStepArgs& a, const PairTable& t, cudaStream_t st) {
-  const size_t smem = (size_t)g.cap * sizeof(float4);
-  if (sp) {
-    auto k = k_seg_step<DIM, KIND, true, MODE>;
-    if (smem > 48 * 1024)
-      JMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<(unsigned)g.nseg, (unsigned)g.threads, smem, st>>>(g, a, t);
-  } else {
-    auto k = k_seg_step<DIM, KIND, false, MODE>;
-    if (smem > 48 * 1024)
-      JMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<(unsigned)g.nseg, (unsigned)g.threads, smem, st>>>(g, a, t);
-  }
-  return JMD_OK;
+  if (g.frame)
+    return sp ? seg_go<DIM, KIND, true, MODE, true>(g, a, t, st)
+              : seg_go<DIM, KIND, false, MODE, true>(g, a, t, st);
+  return sp ? seg_go<DIM, KIND, true, MODE, false>(g, a, t, st)
+            : seg_go<DIM, KIND, false, MODE, false>(g, a, t, st);
 }
 
 template <int MODE>
@@ -194,20 +250,17 @@ int seg_launch(int dim, int kind, bool sp, const SegGrid& g, const SegStepArgs& 
 // Engine entry (declared in pair.cuh): mode 0 forces, 2 fused NVE step, 3
 // force + closing half kick.
 int seg_step(int mode, const jmd_pair& pp, const jmd_space& space, const SegGrid& g,
-             const float* x, const int32_t* start, const uint16_t* list, int64_t nch, int64_t width,
-             const int32_t* cnt, float* f, float* p, float* x_next, float m0, float dt,
-             const float* ref, float thr2, int32_t* flag, int32_t* status, bool species,
-             cudaStream_t st) {
+             const float* x, const int32_t* start, const uint8_t* list, float* f, float* p,
+             float* x_next, float m0, float dt, const float* ref, float thr2, int32_t* flag,
+             int32_t* status, bool species, cudaStream_t st) {
   int e = validate_pair(&pp);
   if (e) return e;
   PairTable t = make_pair_table(pp);
   SegStepArgs a{};
   a.x = reinterpret_cast<const float4*>(x);
-  a.start = start;
-  a.list = list;
-  a.nch = nch;
-  a.width = (int)std::min<int64_t>(width, nch * 8);
-  a.cnt = cnt;
+  a.recs = reinterpret_cast<const SegRecord*>(list + seg_table_bytes(g.nseg));
+  a.blocks = list + seg_table_bytes(g.nseg) + seg_records_bytes(g.nseg);
+  (void)start;
   a.f = reinterpret_cast<float4*>(f);
   a.geo = make_geo(space);
   a.margin = sqrtf(t.rc2_max);

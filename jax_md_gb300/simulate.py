@@ -607,15 +607,30 @@ def segment_threads_default(cells: int, cell_capacity: int) -> int:
 
 
 def segment_plan(nl: N.NList, cells: int):
-    """(n_segments, capacity_atoms, smem_bytes, cells_used) of the segment
-    layout for a cell grid, or None when it does not apply."""
+    """(n_segments, capacity_atoms, smem_bytes, cells_used, list_bytes) of the
+    segment layout for a cell grid, or None when it does not apply."""
     ns, cap, cu = N.I32(), N.I32(), N.I32()
-    sm = N.I64()
+    sm, lb = N.I64(), N.I64()
     rc = N.lib().jmd_segment_plan(ctypes.byref(nl), int(cells), ctypes.byref(ns), ctypes.byref(cap),
-                                  ctypes.byref(sm), ctypes.byref(cu))
+                                  ctypes.byref(sm), ctypes.byref(cu), ctypes.byref(lb))
     if rc != 0:
         return None
-    return ns.value, cap.value, sm.value, cu.value
+    return ns.value, cap.value, sm.value, cu.value, lb.value
+
+
+def segment_list_smem(nl: N.NList, cells: int, n_atoms: int) -> int:
+    """Shared-memory bytes for staging a segment's list block with its
+    positions: a block of 1.2 x the mean own atoms of a segment (rounded to
+    8) at the list's full chunk depth; segments with larger blocks read
+    theirs from global memory."""
+    d = nl.space.dim
+    ncell = 1
+    for k in range(d):
+        ncell *= int(nl.cells_per_side[k])
+    own = 1.2 * cells * n_atoms / max(1, ncell)
+    P = (int(math.ceil(own)) + 7) // 8 * 8
+    nch = max(1, (int(nl.max_occupancy) + 7) // 8)
+    return 16 + 2 * P + nch * P * 16
 
 
 class _SortedBuffers:
@@ -624,7 +639,7 @@ class _SortedBuffers:
     slots, 8-entry chunks); otherwise the tiled int32 list."""
 
     def __init__(self, n, ld, species: bool, workspace_bytes: int, device, seg_cells=None,
-                 seg_threads=128):
+                 seg_threads=128, seg_list_bytes=0, seg_list_smem=0):
         f4 = lambda: torch.empty((n, 4), dtype=torch.float32, device=device)
         i4 = lambda: torch.empty(n, dtype=torch.int32, device=device)
         self.n, self.ld = n, ld
@@ -633,14 +648,13 @@ class _SortedBuffers:
         self.species = i4() if species else None
         self.seg_cells = seg_cells
         self.seg_threads = seg_threads
-        self.seg_nch = (ld + 7) // 8
+        self.seg_list_smem = seg_list_smem
         if seg_cells is None:
             self.idx = torch.empty(((n + 31) // 32) * 32 * ld, dtype=torch.int32, device=device)
             self.seg = None
         else:
             self.idx = None
-            self.seg = torch.empty(((n + 31) // 32) * 32 * self.seg_nch * 8, dtype=torch.int16,
-                                   device=device)
+            self.seg = torch.empty(max(16, seg_list_bytes), dtype=torch.uint8, device=device)
         self.seg_status = torch.zeros((), dtype=torch.int32, device=device)
         self.flags = 0
         self.cnt = i4()
@@ -662,25 +676,29 @@ class _SortedBuffers:
         z.rebuild_flag = self.flag.data_ptr()
         z.workspace, z.workspace_bytes = self.ws.data_ptr(), self.ws.numel()
         if self.seg is not None:
-            z.seg_list, z.seg_nch, z.seg_cells = self.seg.data_ptr(), self.seg_nch, self.seg_cells
-            z.seg_threads = self.seg_threads
+            z.seg_list, z.seg_list_bytes = self.seg.data_ptr(), self.seg.numel()
+            z.seg_cells, z.seg_threads = self.seg_cells, self.seg_threads
+            z.seg_list_smem = self.seg_list_smem
         z.seg_status = self.seg_status.data_ptr()
         z.flags = self.flags
         return z
 
 
 def _segment_shape(nbrs, layout):
-    """(cells per segment, threads per CTA) for a run, or None for the tiled
-    list.  `layout`: None / 'segment' (autotuned choice or default), an int
-    (cells), a (cells, threads) pair, or 'tiled'."""
+    """(cells per segment, threads per CTA, list bytes, list staging bytes)
+    for a run, or None for the tiled list.  `layout`: None / 'segment'
+    (autotuned choice or default), an int (cells), a (cells, threads) or
+    (cells, threads, stage_lists) tuple, or 'tiled'."""
     if layout == 'tiled':
         return None
     nl = nbrs.plan.nl
-    threads = None
+    threads, stage = None, True
     if layout is None or layout == 'segment':
-        cells, threads = _segment_choice.get(_grid_key(nl), (SEGMENT_CELLS_DEFAULT, None))
+        choice = _segment_choice.get(_grid_key(nl), (SEGMENT_CELLS_DEFAULT, None, True))
+        cells, threads, stage = (tuple(choice) + (True,))[:3]
     elif isinstance(layout, (tuple, list)):
         cells, threads = int(layout[0]), int(layout[1])
+        stage = bool(layout[2]) if len(layout) > 2 else True
     else:
         cells = int(layout)
     plan = segment_plan(nl, cells)
@@ -691,7 +709,10 @@ def _segment_shape(nbrs, layout):
     cells = plan[3]
     if threads is None:
         threads = segment_threads_default(cells, nl.cell_capacity)
-    return cells, threads
+    smem = segment_list_smem(nl, cells, nbrs.plan.n) if stage else 0
+    if stage and plan[2] + smem + 4096 > 227 * 1024:
+        smem = 0   # positions and list block do not fit one CTA together
+    return cells, threads, plan[4], smem
 
 
 def _sorted_buffers(state, nbrs, species, seg=None):
@@ -701,7 +722,7 @@ def _sorted_buffers(state, nbrs, species, seg=None):
     if b is None or b.n != state.position.shape[0] or getattr(b, 'key', None) != key:
         b = _SortedBuffers(state.position.shape[0], plan.ld, species is not None,
                            plan.workspace.numel(), state.position.device,
-                           None if seg is None else seg[0], 128 if seg is None else seg[1])
+                           *(() if seg is None else seg))
         b.key = key
         object.__setattr__(state, '_sorted', b)
     return b

@@ -106,8 +106,10 @@ def _seg_key(nl, pair) -> str:
 
 
 def segment_candidates(nl):
-    """(cells, threads) pairs to try: K in 2..8 (those the grid admits) with
-    the default thread count and the neighbouring multiples of 32."""
+    """(cells, threads, stage_lists) to try: K in 2..8 (those the grid
+    admits) with the default thread count and the neighbouring multiples of
+    32, each with the list block staged in shared memory or read from global
+    memory."""
     from . import simulate
     out = []
     for K in (2, 3, 4, 5, 6, 8):
@@ -117,7 +119,8 @@ def segment_candidates(nl):
         t0 = simulate.segment_threads_default(K, nl.cell_capacity)
         for t in sorted({t0 - 32, t0, t0 + 32}):
             if 64 <= t <= 256:
-                out.append((K, t))
+                out.append((K, t, 1))
+                out.append((K, t, 0))
     return out
 
 

@@ -245,33 +245,39 @@ def test_nvt_runner_conserves_invariant(cuda):
 
 @pytest.mark.parametrize('n_cells', [6, 10])
 def test_segment_and_tiled_layouts_agree(cuda, n_cells):
-    """The two private lists hold the same pairs: one step from the same state
-    gives the same forces (to fp32 summation order) and positions."""
+    """The two private lists hold the same pairs: three steps from the same
+    state give the same forces and positions to fp32 summation order (forces
+    within the 1e-4 force tolerance: single pair forces reach ~50 on the
+    jittered lattice)."""
     from jax_md_gb300 import simulate
     _, _, _, _, _, _, apply_a, st_a, nb_a = _setup(cuda, n_cells=n_cells)
     _, _, _, _, _, _, apply_b, st_b, nb_b = _setup(cuda, n_cells=n_cells)
     simulate.run(apply_a, st_a, nb_a, 3, layout='segment')
     simulate.run(apply_b, st_b, nb_b, 3, layout='tiled')
     torch.cuda.synchronize()
-    assert (st_a.force - st_b.force).abs().max().item() < 2e-5
+    assert (st_a.force - st_b.force).abs().max().item() < 1e-4
     assert (st_a.position - st_b.position).abs().max().item() < 1e-5
     assert simulate.last_run_status(st_a) == 0
     assert torch.equal(nb_a.idx, nb_b.idx)
 
 
-@pytest.mark.parametrize('cells', [1, 2, 3, 5, 8])
-def test_segment_widths_agree(cuda, cells):
-    """Every segment width K gives the same run to fp32 summation order (the
-    staged neighbourhoods differ, the pairs do not); 12 cells per side, so
-    K = 5 and 8 leave a shorter last segment in each row."""
+@pytest.mark.parametrize('cells', [1, 2, 3, 4, 5, 8])
+def test_segment_widths_match_oracle(cuda, cells):
+    """Every segment width K gives forces within 1e-4 of the FP64 oracle at
+    the run's own final positions (11 cells per side: K = 5 and 8 leave a
+    shorter last segment in each row; K <= 3 stage in the CTA's periodic
+    frame, wider segments take the minimum image per pair)."""
     from jax_md_gb300 import simulate
-    _, _, _, _, _, _, apply_a, st_a, nb_a = _setup(cuda, n_cells=20)
-    _, _, _, _, _, _, apply_b, st_b, nb_b = _setup(cuda, n_cells=20)
+    spatial = pytest.importorskip('scipy.spatial')
+    _, _, L, _, _, _, apply_a, st_a, nb_a = _setup(cuda, n_cells=20)
     simulate.run(apply_a, st_a, nb_a, 5, layout=cells)
-    simulate.run(apply_b, st_b, nb_b, 5, layout='tiled')
     torch.cuda.synchronize()
-    assert (st_a.force - st_b.force).abs().max().item() < 2e-5
-    assert (st_a.position - st_b.position).abs().max().item() < 1e-5
+    assert simulate.last_run_status(st_a) == 0
+    X = st_a.position.double().cpu().numpy()
+    pairs = spatial.cKDTree(np.mod(X, L), boxsize=L).query_pairs(2.5, output_type='ndarray')
+    idx = np.stack([pairs.min(1), pairs.max(1)])
+    _, Fo, _ = O.pair_energy_forces(lj_spec(), X, idx, O.ORDERED_SPARSE, np.full(3, L))
+    assert np.abs(st_a.force.cpu().numpy() - Fo).max() < 1e-4
 
 
 def test_lazy_caller_list_is_built_when_read(cuda):

@@ -64,6 +64,7 @@ def _nl(cps, cap, dim=3):
         nl.cell_size[d] = 2.9
     nl.cell_capacity = cap
     nl.format = N.DENSE
+    nl.max_occupancy = 100
     return nl
 
 
@@ -81,9 +82,16 @@ def test_segment_plan(cps, cap, K, dim, want):
     from jax_md_gb300 import simulate
     plan = simulate.segment_plan(_nl(cps, cap, dim), K)
     assert plan is not None
-    nseg, capa, smem, used = plan
+    nseg, capa, smem, used, list_bytes = plan
     assert (nseg, capa, used) == want
-    assert smem == capa * 16
+    assert smem == (capa + 1) * 16   # + the far slot
+    # list buffer: the chunk-count table, a 256-byte staging record per
+    # segment, one block per segment (header, 16-bit counts, chunks of 8
+    # slots for K x cell capacity own atoms)
+    P = (used * cap + 7) // 8 * 8
+    nch = 13
+    assert list_bytes == ((4 * nseg + 15) // 16 * 16 + nseg * 256
+                          + nseg * (16 + 2 * P + nch * P * 16))
 
 
 @pytest.mark.parametrize('cps,cap,K', [(2, 40, 5), (35, 40, 0), (35, 40, 15), (35, 800, 5)])
