@@ -684,8 +684,10 @@ def main():
     import ctypes as _C
     sb = st._sorted
     nbar = float(sb.cnt.float().mean())
-    # list bytes per atom a perfect kernel reads: two-byte entries + count
-    chunk_bytes = 2.0 * float(sb.cnt.clamp(max=nb.max_occupancy).double().mean()) + 2.0
+    # list bytes per atom a perfect kernel reads: two-byte entries (half of
+    # them with half lists) + count
+    chunk_bytes = (2.0 * float(sb.cnt.clamp(max=nb.max_occupancy).double().mean())
+                   / (2.0 if getattr(sb, 'seg_half', 0) else 1.0) + 2.0)
     species, pair = efn._resolve(st.position, {})
     sp = simulate._shift_space(shift, 3)
     xo = torch.empty((n, 4), dtype=torch.float32, device=dev)
@@ -693,15 +695,16 @@ def main():
     flag = torch.zeros((), dtype=torch.int32, device=dev)
     L_ = NAT.lib()
     seg_on = sb.seg is not None
+    facc = torch.zeros((n, 4), dtype=torch.float32, device=dev)  # half lists' force accumulator
 
     def fused():
         if seg_on:
             NAT.check(L_.jmd_nve_fused_step_segment(
                 _C.byref(pair), _C.byref(sp), _C.byref(nb.plan.nl), sb.seg_cells, sb.seg_threads,
-                sb.seg_list_smem, sb.xa.data_ptr(), xo.data_ptr(), pm.data_ptr(), 1.0, n, 0,
-                sb.seg.data_ptr(), sb.seg.numel(), DT, sb.ref.data_ptr(), nb.plan.threshold_sq,
-                flag.data_ptr(), sb.ws.data_ptr(), sb.ws.numel(), sb.seg_status.data_ptr(),
-                NAT.stream_ptr()), 'segment fused step')
+                sb.seg_list_smem, sb.seg_half, sb.xa.data_ptr(), xo.data_ptr(), pm.data_ptr(),
+                facc.data_ptr(), 1.0, n, 0, sb.seg.data_ptr(), sb.seg.numel(), DT,
+                sb.ref.data_ptr(), nb.plan.threshold_sq, flag.data_ptr(), sb.ws.data_ptr(),
+                sb.ws.numel(), sb.seg_status.data_ptr(), NAT.stream_ptr()), 'segment fused step')
         else:
             NAT.check(L_.jmd_nve_fused_step_tiled(_C.byref(pair), _C.byref(sp), sb.xa.data_ptr(),
                                                   xo.data_ptr(), pm.data_ptr(), 1.0, None, n,
@@ -725,12 +728,14 @@ def main():
     # chunks of 8 two-byte staged slots; int32 entries on the tiled list),
     # the count, position read + write, momentum read + write, reference read
     list_bytes = chunk_bytes if seg_on else 4 * nbar + 4
-    kern_bytes = n * (list_bytes + 80)
+    half = bool(getattr(sb, 'seg_half', 0)) and seg_on
+    # half lists: + the force accumulator, reduced into, read and cleared
+    kern_bytes = n * (list_bytes + 80 + (48 if half else 0))
     hbm, src = peaks()
     achieved = kern_bytes / (kern_ms / 1e3) / 1e9
     # per step: + force row written by the closing kick and read by the next
     # opening kick is fused away; the skin flag and rebuilds are extra
-    step_bytes = n * (list_bytes + 80)
+    step_bytes = kern_bytes
 
     # e2e: host pinned buffers through the public API (simulate.run, default
     # path), every step: positions and momenta copied in, one step, copied out
@@ -768,6 +773,7 @@ def main():
                    'private_list': 'segment-local (16-bit staged slots)' if seg_on else 'tiled int32',
                    'segment': {'cells': sb.seg_cells, 'threads': sb.seg_threads,
                                'list_smem_bytes': sb.seg_list_smem,
+                               'half_lists': bool(getattr(sb, 'seg_half', 0)),
                                'autotuned': seg_choice is not None,
                                'autotune_ms_per_step': {'x'.join(str(int(v)) for v in k): t
                                                         for k, t in seg_ms.items()}},
@@ -779,10 +785,12 @@ def main():
                      'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one '
                                        'k_seg_step launch at N=864000, scaled by N',
                      'peak_source': src,
-                     'kernel': ('k_seg_step fused NVE step (LJ, segment-local list, FP32x2)'
-                                if seg_on else 'k_tiled fused NVE step (LJ, Dense tiled, FP32x2)'),
+                     'kernel': (('k_seg_half + k_seg_integrate (LJ, segment-local half lists, '
+                                 'Newton\'s third law, FP32x2)') if half else
+                                ('k_seg_step fused NVE step (LJ, segment-local list, FP32x2)'
+                                 if seg_on else 'k_tiled fused NVE step (LJ, Dense tiled, FP32x2)')),
                      'kernel_ms': kern_ms,
-                     'bytes_per_atom': list_bytes + 80,
+                     'bytes_per_atom': kern_bytes / n,
                      'step_algorithmic_GBps': step_bytes * args.steps / (ms / 1e3) / 1e9},
         'e2e': {'value': e2e_value, 'unit': 'atom-steps/s', 'h2d_bytes_per_step': 2 * n * 12,
                 'd2h_bytes_per_step': 2 * n * 12},

@@ -479,6 +479,8 @@ typedef struct {
   int32_t seg_threads;        /* threads per segment CTA: a multiple of 32 in [32, 256] */
   int32_t seg_list_smem;      /* shared-memory bytes for staging a segment's list block
                                  with its positions (0: lists are read from global) */
+  int32_t seg_half;           /* 1: half lists (Newton's third law, forward stencil);
+                                 forces are accumulated, then integrated */
   int32_t flags;              /* JMD_RUN_* bits */
   int32_t* seg_status;        /* device int32: staging overflow (1) / copy timeout (2) */
 } jmd_sorted_state;
@@ -506,14 +508,17 @@ int jmd_segment_plan(const jmd_nlist* nl, int32_t cells, int32_t* n_segments,
  * rebuild: positions in cell order as float4 rows, `workspace` the sort's
  * workspace (its cell starts place the segments), seg_list as the engine's
  * build wrote it, species ids (when species_in_w) in the fourth float of the
- * position rows; list_smem as jmd_sorted_state.seg_list_smem.  The engine's per-step kernel, exposed
+ * position rows; list_smem and half as jmd_sorted_state.seg_list_smem and
+ * seg_half.  With half lists the step is two kernels (forces accumulated
+ * into `force`, which must be zero on entry, then the integration, which
+ * clears it again); otherwise `force` is not used.  The engine's per-step kernel, exposed
  * so it can be timed and tested alone; no reference counterpart (it replaces
  * the force evaluation inside simulate.py:227-243 for the engine's private
  * layout). */
 int jmd_nve_fused_step_segment(const jmd_pair* pair, const jmd_space* space, const jmd_nlist* nl,
-                               int32_t cells, int32_t threads, int32_t list_smem,
+                               int32_t cells, int32_t threads, int32_t list_smem, int32_t half,
                                const float* position, float* position_next, float* momentum,
-                               float mass_scalar, int64_t n, int32_t species_in_w,
+                               float* force, float mass_scalar, int64_t n, int32_t species_in_w,
                                const uint8_t* seg_list, int64_t seg_list_bytes, float dt,
                                const float* reference_position, float threshold_sq,
                                int32_t* rebuild_flag, void* workspace, size_t workspace_bytes,

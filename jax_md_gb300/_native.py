@@ -71,7 +71,7 @@ class SortedState(C.Structure):
                 ('rebuild_flag', C.c_void_p), ('workspace', C.c_void_p),
                 ('workspace_bytes', C.c_size_t), ('seg_list', C.c_void_p),
                 ('seg_list_bytes', C.c_int64), ('seg_cells', C.c_int32), ('seg_threads', C.c_int32),
-                ('seg_list_smem', C.c_int32), ('flags', C.c_int32),
+                ('seg_list_smem', C.c_int32), ('seg_half', C.c_int32), ('flags', C.c_int32),
                 ('seg_status', C.c_void_p)]
 
 
@@ -159,8 +159,8 @@ SIGNATURES = {
     'jmd_segment_plan': (C.c_int, [C.POINTER(NList), I32, C.POINTER(I32), C.POINTER(I32),
                                    C.POINTER(I64), C.POINTER(I32), C.POINTER(I64)]),
     'jmd_nve_fused_step_segment': (C.c_int, [C.POINTER(Pair), C.POINTER(Space), C.POINTER(NList),
-                                             I32, I32, I32, P, P, P, F32, I64, I32, P, I64, F32,
-                                             P, F32, P, P, C.c_size_t, P, P]),
+                                             I32, I32, I32, I32, P, P, P, P, F32, I64, I32, P,
+                                             I64, F32, P, F32, P, P, C.c_size_t, P, P]),
     'jmd_neighbor_list_build_tiled': (C.c_int, [C.POINTER(NList), P, I64, P, I64, P, P, P, P, P, P,
                                                 SZ, P]),
     'jmd_pair_forces_tiled': (C.c_int, [C.POINTER(Pair), C.POINTER(Space), P, P, I64, P, I64, I64,

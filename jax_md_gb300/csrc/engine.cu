@@ -301,7 +301,11 @@ bool run_seg_grid(const jmd_nve_system& s, const jmd_sorted_state& z, SegGrid* g
   const int rows = s.space.dim == 3 ? 9 : 3;
   g->cap = rows * (g->K + 2) * s.nlist.cell_capacity;
   g->threads = z.seg_threads;
-  g->lcap = std::max(0, z.seg_list_smem) / 16 * 16;
+  g->half = z.seg_half ? 1 : 0;
+  // half lists read their blocks from global memory (shared memory holds
+  // the reaction accumulators instead)
+  g->lcap = g->half ? 0 : std::max(0, z.seg_list_smem) / 16 * 16;
+  if (g->half) g->cap = seg_rows(s.space.dim, 1) * (g->K + 2) * s.nlist.cell_capacity;
   return true;
 }
 
@@ -314,7 +318,8 @@ int seg_check_smem(const SegGrid& g) {
     cudaGetLastError();
     optin = 227 * 1024;
   }
-  const int64_t need = (int64_t)(g.cap + 1) * 16 + g.lcap + (int64_t)sizeof(SegShared) +
+  const int64_t per_slot = 16 + (g.half ? 12 : 0);  // + reaction accumulators
+  const int64_t need = (int64_t)(g.cap + 1) * per_slot + g.lcap + (int64_t)sizeof(SegShared) +
                        64 * (int64_t)sizeof(PairCoef) + 64;
   JMD_REQUIRE(need <= optin, "segment staging (positions + list block) exceeds a CTA's shared memory");
   return JMD_OK;
@@ -378,7 +383,14 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
                                   z.workspace_bytes, q);
   };
   const bool sp = s.species != nullptr;
+  const size_t frows = sizeof(float4) * (size_t)s.n;
   auto force_kick_at = [&](const float* x, cudaStream_t q) -> int {
+    if (seg && sg.half) {
+      // the half-list forces accumulate into a cleared force buffer
+      JMD_CUDA(cudaMemsetAsync(z.force, 0, frows, q));
+      return seg_step(3, s.pair, s.space, sg, x, starts, z.seg_list, z.force, z.momentum, nullptr,
+                      s.mass_scalar, s.dt, nullptr, 0.f, nullptr, z.seg_status, sp, q, s.n);
+    }
     if (seg)
       return seg_step(3, s.pair, s.space, sg, x, starts, z.seg_list, z.force, z.momentum, nullptr,
                       s.mass_scalar, s.dt, nullptr, 0.f, nullptr, z.seg_status, sp, q);
@@ -418,9 +430,16 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
                                always ? nullptr : z.reference_position, 4, s.threshold_sq,
                                always ? nullptr : z.rebuild_flag, st);
     if (rc) return rc;
+    // half lists: the force buffer is an accumulator, zero between steps
+    // (the integration clears it after use)
+    if (seg && sg.half && steps > 1) JMD_CUDA(cudaMemsetAsync(z.force, 0, frows, st));
     for (int64_t k = 1; k < steps; ++k) {
       if ((rc = gate(cur))) return rc;
-      if (seg)
+      if (seg && sg.half)
+        rc = seg_step(2, s.pair, s.space, sg, cur, starts, z.seg_list, z.force, z.momentum, nxt,
+                      s.mass_scalar, s.dt, always ? nullptr : z.reference_position,
+                      s.threshold_sq, always ? nullptr : z.rebuild_flag, z.seg_status, sp, st, s.n);
+      else if (seg)
         rc = seg_step(2, s.pair, s.space, sg, cur, starts, z.seg_list, nullptr, z.momentum, nxt,
                       s.mass_scalar, s.dt, always ? nullptr : z.reference_position,
                       s.threshold_sq, always ? nullptr : z.rebuild_flag, z.seg_status, sp, st);
@@ -729,9 +748,9 @@ int jmd_segment_plan(const jmd_nlist* nl, int32_t cells, int32_t* n_segments,
 }
 
 int jmd_nve_fused_step_segment(const jmd_pair* pair, const jmd_space* space, const jmd_nlist* nl,
-                               int32_t cells, int32_t threads, int32_t list_smem,
+                               int32_t cells, int32_t threads, int32_t list_smem, int32_t half,
                                const float* position, float* position_next, float* momentum,
-                               float mass_scalar, int64_t n, int32_t species_in_w,
+                               float* force, float mass_scalar, int64_t n, int32_t species_in_w,
                                const uint8_t* seg_list, int64_t seg_list_bytes_, float dt,
                                const float* reference_position, float threshold_sq,
                                int32_t* rebuild_flag, void* workspace, size_t workspace_bytes,
@@ -745,18 +764,20 @@ int jmd_nve_fused_step_segment(const jmd_pair* pair, const jmd_space* space, con
               "threads must be a multiple of 32 in [32, 256]");
   SegGrid g;
   JMD_REQUIRE(make_seg_grid(*nl, cells, 1, &g), "the segment layout does not apply to this cell grid");
-  g.cap = (nl->space.dim == 3 ? 9 : 3) * (g.K + 2) * nl->cell_capacity;
+  g.half = half ? 1 : 0;
+  JMD_REQUIRE(!g.half || force != nullptr, "half lists accumulate forces: force is required");
+  g.cap = seg_rows(nl->space.dim, g.half) * (g.K + 2) * nl->cell_capacity;
   g.threads = threads;
-  g.lcap = std::max(0, list_smem) / 16 * 16;
+  g.lcap = g.half ? 0 : std::max(0, list_smem) / 16 * 16;
   JMD_REQUIRE(g.cap < kSegMaxStaged, "segment staging capacity beyond 16-bit slots");
   JMD_REQUIRE(seg_list_bytes_ >= seg_list_bytes(g), "seg_list smaller than the plan's list_bytes");
   int e = seg_check_smem(g);
   if (e) return e;
   const int32_t* starts = sort_cell_starts(nl, n, workspace, workspace_bytes);
   if (!starts) return fail(JMD_ERR_WORKSPACE, "workspace too small for the cell starts");
-  return seg_step(2, *pair, *space, g, position, starts, seg_list, nullptr, momentum,
-                  position_next, mass_scalar, dt, reference_position, threshold_sq, rebuild_flag,
-                  seg_status, species_in_w != 0, as_stream(stream));
+  return seg_step(2, *pair, *space, g, position, starts, seg_list, g.half ? force : nullptr,
+                  momentum, position_next, mass_scalar, dt, reference_position, threshold_sq,
+                  rebuild_flag, seg_status, species_in_w != 0, as_stream(stream), n);
 }
 
 int jmd_engine_clear_cache(void) {

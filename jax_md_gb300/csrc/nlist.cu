@@ -919,7 +919,13 @@ namespace {
 // cutoff of a face, so a pair within an ulp of the list cutoff may be kept
 // where the reference drops it (or the reverse): such pairs lie beyond the
 // interaction cutoff and change no force.
-template <int DIM, bool FRAME>
+// HALF: half lists (Newton's third law).  A warp walks the forward half of
+// the stencil (segment.cuh): in the centre row its own cell (atoms after
+// the lane's atom) and the next cell, then the forward rows.  Each pair is
+// listed once; every atom's full neighbour count (list length + the times
+// it is listed by others) is accumulated in `count` (zeroed by
+// k_seg_zero_counts) for the occupancy and overflow of the Dense contract.
+template <int DIM, bool FRAME, bool HALF>
 __global__ void __launch_bounds__(kSegMaxThreads)
 k_seg_search(SegGrid sg, const float4* __restrict__ x, Bins b, Geo geo, float cut2, float margin,
              int mask_self, uint8_t* __restrict__ blocks, int32_t* __restrict__ nck_table,
@@ -944,7 +950,13 @@ k_seg_search(SegGrid sg, const float4* __restrict__ x, Bins b, Geo geo, float cu
     }
     return;
   }
+  // half lists: full-count contributions of each staged atom
+  int* hcnt = reinterpret_cast<int*>(spos + sg.cap + 1);
+  if (HALF) {
+    for (int t = threadIdx.x; t < sh.total; t += blockDim.x) hcnt[t] = 0;
+  }
   const int fmask = FRAME ? seg_frame<DIM>(sg, sh, spos, geo.L) : 0;
+  if (HALF && !FRAME) __syncthreads();  // seg_frame ends with one
   const int W = sh.W;
   const int rows = sh.rows;
   const uint64_t far = (uint64_t)sg.cap;  // the far slot: pads chunks and rows past width
@@ -962,7 +974,7 @@ k_seg_search(SegGrid sg, const float4* __restrict__ x, Bins b, Geo geo, float cu
   // (cells u-1..u+1 of each staged row), so trip counts are uniform and
   // each candidate read is a shared-memory broadcast
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const int cr = seg_centre_row<DIM>() * W;
+  const int cr = seg_centre_row<DIM>(HALF ? 1 : 0) * W;
   for (int task = warp; ; task += nwarps) {
     // task -> (own cell u, group of 32 of its atoms)
     int u = 1, t = task;
@@ -997,7 +1009,8 @@ k_seg_search(SegGrid sg, const float4* __restrict__ x, Bins b, Geo geo, float cu
     };
     const float2 xx = f2s(xi.x), xy = f2s(xi.y), xz = f2s(xi.z);
     for (int r = 0; r < rows; ++r) {
-      const int j0 = sh.coff[r * W + u - 1], j1 = sh.coff[r * W + u + 2];
+      // half: the centre row from the own cell on (later atoms only)
+      const int j0 = sh.coff[r * W + u - ((HALF && r == 0) ? 0 : 1)], j1 = sh.coff[r * W + u + 2];
       for (int jb = j0; jb < j1; jb += 32) {
         // distance tests of up to 32 candidates into a hit mask; j + 1 may
         // read one slot past the run (still inside the staged block or the
@@ -1027,13 +1040,21 @@ k_seg_search(SegGrid sg, const float4* __restrict__ x, Bins b, Geo geo, float cu
           hits |= ((r2.x < cut2 ? 1u : 0u) | (r2.y < cut2 ? 2u : 0u)) << k;
         }
         if (nb < 32) hits &= (1u << nb) - 1u;
-        if (mask_self && is >= jb && is < jb + nb) hits &= ~(1u << (is - jb));
+        if (HALF && r == 0) {
+          // keep j > is: bits of candidates at or before the lane's atom go
+          const int cut_bits = is + 1 - jb;
+          if (cut_bits >= 32) hits = 0u;
+          else if (cut_bits > 0) hits &= ~((1u << cut_bits) - 1u);
+        } else if (mask_self && is >= jb && is < jb + nb) {
+          hits &= ~(1u << (is - jb));
+        }
         if (!active) hits = 0u;
         // append the hits in candidate order; rows past `width` keep the far
         // slot so the chunk stays valid
         while (hits) {
           const int bit = __ffs(hits) - 1;
           hits &= hits - 1;
+          if (HALF) atomicAdd(hcnt + jb + bit, 1);
           put(cnt < width ? (uint64_t)(jb + bit) : far, cnt & 7);
           ++cnt;
         }
@@ -1043,7 +1064,10 @@ k_seg_search(SegGrid sg, const float4* __restrict__ x, Bins b, Geo geo, float cu
       // pad the last chunk with the far slot
       if (cnt & 7)
         for (int p = cnt & 7; p < 8; ++p) put(far, p);
-      count[s] = cnt;
+      if (HALF)  // the atom's own entries (and itself without mask_self); others add theirs below
+        atomicAdd(count + s, cnt + (mask_self ? 0 : 1));
+      else
+        count[s] = cnt;
       const int kept = min(cnt, width);
       if (fits) reinterpret_cast<uint16_t*>(blk + 16)[ia] = (uint16_t)kept;
       my_nck = max(my_nck, (kept + 7) >> 3);
@@ -1058,6 +1082,15 @@ k_seg_search(SegGrid sg, const float4* __restrict__ x, Bins b, Geo geo, float cu
       my_max = max(my_max, (unsigned)cnt);
     }
   }
+  if (HALF) {
+    // the times each staged atom was listed here, to its full count
+    __syncthreads();
+    for (int c = warp; c < rows * W; c += nwarps) {
+      const int cb = sh.coff[c], ce = sh.coff[c + 1];
+      for (int t = cb + lane; t < ce; t += 32)
+        if (hcnt[t]) atomicAdd(count + sh.gbeg[c] + (t - cb), hcnt[t]);
+    }
+  }
   my_max = __reduce_max_sync(0xffffffffu, my_max);
   my_nck = __reduce_max_sync(0xffffffffu, (unsigned)my_nck);
   if ((threadIdx.x & 31) == 0) {
@@ -1066,13 +1099,39 @@ k_seg_search(SegGrid sg, const float4* __restrict__ x, Bins b, Geo geo, float cu
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    atomicMax(&b.sc->occupancy, (unsigned long long)cta_max);
-    if ((int)cta_max > width) atomicOr(&b.sc->flags, (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
+    if (!HALF) {
+      // half lists: occupancy and overflow come from the full counts
+      // (k_seg_occupancy)
+      atomicMax(&b.sc->occupancy, (unsigned long long)cta_max);
+      if ((int)cta_max > width) atomicOr(&b.sc->flags, (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
+    }
     const int nck = fits ? min(cta_nck, nch) : 0;
     reinterpret_cast<int32_t*>(blk)[0] = nck;
     reinterpret_cast<int32_t*>(blk)[1] = sh.own_cnt;
     nck_table[blockIdx.x] = nck;
     rec->nck = nck;
+  }
+}
+
+// Half lists: zero the full counts before the search (gated like the rest of
+// the rebuild chain).
+__global__ void k_seg_zero_counts(int32_t* count, int n, const int32_t* flag) {
+  if (skip(flag)) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    count[i] = 0;
+}
+
+// Half lists: occupancy (largest full count) and the overflow bit.
+__global__ void k_seg_occupancy(const int32_t* count, int n, int width, Bins b,
+                                const int32_t* flag) {
+  if (skip(flag)) return;
+  int m = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    m = max(m, count[i]);
+  m = __reduce_max_sync(0xffffffffu, (unsigned)m);
+  if ((threadIdx.x & 31) == 0 && m > 0) {
+    atomicMax(&b.sc->occupancy, (unsigned long long)m);
+    if (m > width) atomicOr(&b.sc->flags, (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
   }
 }
 
@@ -1112,10 +1171,13 @@ int build_segment_after_sort(const jmd_nlist* nl, const SegGrid& sg, const float
   if (!ok) return fail(JMD_ERR_WORKSPACE, "neighbour-list workspace too small");
   const Geo geo = make_geo(nl->space);
   const float margin = sqrtf(nl->cutoff_sq);
-  const size_t smem = (size_t)(sg.cap + 1) * sizeof(float4);
+  // staged positions + far slot (+ the half search's per-slot counts)
+  const size_t smem = (size_t)(sg.cap + 1) * (sizeof(float4) + (sg.half ? sizeof(int) : 0));
   const float4* x = reinterpret_cast<const float4*>(position);
   float4* ref = reinterpret_cast<float4*>(reference_position);
   const int width = (int)nl->max_occupancy;
+  const unsigned zgrid = (unsigned)std::min<int64_t>(std::max<int64_t>(1, ceil_div(n, 256)), 4096);
+  if (sg.half && n > 0) k_seg_zero_counts<<<zgrid, 256, 0, st>>>(nbr_count, (int)n, rebuild_flag);
   auto go = [&](auto kernel) -> int {
     int rc = seg_smem_optin(kernel, smem);
     if (rc) return rc;
@@ -1130,11 +1192,15 @@ int build_segment_after_sort(const jmd_nlist* nl, const SegGrid& sg, const float
     return JMD_OK;
   };
   if (n > 0) {
-    if (nl->space.dim == 3)
-      e = sg.frame ? go(k_seg_search<3, true>) : go(k_seg_search<3, false>);
-    else
-      e = sg.frame ? go(k_seg_search<2, true>) : go(k_seg_search<2, false>);
+    if (nl->space.dim == 3) {
+      if (sg.half) e = sg.frame ? go(k_seg_search<3, true, true>) : go(k_seg_search<3, false, true>);
+      else e = sg.frame ? go(k_seg_search<3, true, false>) : go(k_seg_search<3, false, false>);
+    } else {
+      if (sg.half) e = sg.frame ? go(k_seg_search<2, true, true>) : go(k_seg_search<2, false, true>);
+      else e = sg.frame ? go(k_seg_search<2, true, false>) : go(k_seg_search<2, false, false>);
+    }
     if (e) return e;
+    if (sg.half) k_seg_occupancy<<<zgrid, 256, 0, st>>>(nbr_count, (int)n, width, b, rebuild_flag);
   }
   FinalizeArgs f{JMD_DENSE, nl->max_occupancy, 1, nl->cell_capacity, (int)n};
   k_finalize<<<1, 1, 0, st>>>(b, f, occupancy, error_code, rebuild_flag);

@@ -229,5 +229,5 @@ int build_segment_after_sort(const jmd_nlist* nl, const SegGrid& sg, const float
 int seg_step(int mode, const jmd_pair& pp, const jmd_space& space, const SegGrid& g,
              const float* x, const int32_t* start, const uint8_t* list, float* f, float* p,
              float* x_next, float m0, float dt, const float* ref, float thr2, int32_t* flag,
-             int32_t* status, bool species, cudaStream_t st);
+             int32_t* status, bool species, cudaStream_t st, int64_t n_atoms = 0);
 }  // namespace jmd

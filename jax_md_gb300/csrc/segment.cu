@@ -211,6 +211,237 @@ k_seg_step(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
   }
 }
 
+// Shared-memory reduction without a returned value (red.shared.add.f32).
+__device__ __forceinline__ void red_shared(float* p, float v) {
+  asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(smem_u32(p)), "f"(v) : "memory");
+}
+
+// Half lists (Newton's third law): each pair once, from the atom whose
+// forward stencil holds the other.  The own atom keeps its force in
+// registers; the partner's reaction goes to a shared-memory accumulator per
+// staged atom; the CTA then adds every staged atom's accumulated force to
+// `f` in global memory with one vector reduction (f is zero before the
+// kernel; k_seg_integrate consumes and clears it).
+template <int DIM, int KIND, bool SPECIES, bool FRAME>
+__global__ void __maxnreg__(72)
+k_seg_half(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
+  extern __shared__ float4 spos[];
+  __shared__ SegShared sh;
+  __shared__ PairCoef sc[SPECIES ? JMD_MAX_SPECIES * JMD_MAX_SPECIES : 1];
+  if (SPECIES)
+    for (int k = threadIdx.x; k < JMD_MAX_SPECIES * JMD_MAX_SPECIES; k += blockDim.x) sc[k] = tab.c[k];
+  float* fx = reinterpret_cast<float*>(spos + sg.cap + 1);
+  float* fy = fx + (sg.cap + 1);
+  float* fz = fy + (sg.cap + 1);
+  const SegRecord* rec = a.recs + blockIdx.x;
+  const uint8_t* gblk = a.blocks + (int64_t)blockIdx.x * sg.stride;
+  const SegHead hd = seg_stage_record<DIM>(sg, a.x, rec, spos, sh, a.status, gblk, nullptr);
+  if (hd.total < 0) return;  // neighbourhood over capacity (flagged at the rebuild)
+  for (int t = threadIdx.x; t < hd.total; t += blockDim.x) {
+    fx[t] = 0.f;
+    fy[t] = 0.f;
+    if (DIM == 3) fz[t] = 0.f;
+  }
+  const int P = seg_pad(hd.own_cnt);
+  const bool blk_ok = P <= sg.pmax;
+  const int nck_seg = blk_ok ? hd.nck : 0;
+  bool ok = seg_wait_one(sh, a.status);
+  // every thread meets this barrier: the accumulators are zero and, for a
+  // face segment, the staged block is about to be shifted
+  if (!__syncthreads_and(ok)) return;
+  if (FRAME) {
+    const SegPos sp = seg_pos<DIM>(sg);
+    int fmask = 0;
+    if (sp.x0 == 0 || sp.x0 + sp.nx >= sg.cps[0]) fmask |= 1;
+    if (sp.cy == 0 || sp.cy == sg.cps[1] - 1) fmask |= 2;
+    if (DIM == 3 && (sp.cz == 0 || sp.cz == sg.cps[2] - 1)) fmask |= 4;
+    if (fmask) {
+      const float h0 = 0.5f * a.geo.L[0], h1 = 0.5f * a.geo.L[1], h2 = 0.5f * a.geo.L[2];
+      for (int t = threadIdx.x; t < hd.total; t += blockDim.x) {
+        float4 v = spos[t];
+        if ((fmask & 1) && v.x >= h0) v.x -= a.geo.L[0];
+        if ((fmask & 2) && v.y >= h1) v.y -= a.geo.L[1];
+        if (DIM == 3 && (fmask & 4) && v.z >= h2) v.z -= a.geo.L[2];
+        spos[t] = v;
+      }
+      __syncthreads();
+    }
+  }
+  const float rc2m = tab.rc2_max;
+  const Coef2 c0 = coef2(tab.c[0]);
+  for (int o = threadIdx.x; o < hd.own_cnt; o += blockDim.x) {
+    const int is = hd.own_sm + o;
+    const float4 xi = spos[is];
+    const int c = blk_ok ? min((int)reinterpret_cast<const uint16_t*>(gblk + 16)[o], 8 * nck_seg) : 0;
+    const uint4* lp = reinterpret_cast<const uint4*>(gblk + seg_chunk_off(P, 0, o));
+    const bool inner = FRAME || interior<DIM>(xi, a.geo, a.margin);
+    const int si = SPECIES ? sclamp(__float_as_int(xi.w), tab.nsp) : 0;
+    const float2 xx = f2s(xi.x), xy = f2s(xi.y), xz = f2s(xi.z);
+    float2 ax = f2s(0.f), ay = f2s(0.f), az = f2s(0.f);
+    auto pair2 = [&](int j0, int j1) {
+      const float4 b0 = spos[j0], b1 = spos[j1];
+      float2 dx = sub2(xx, f2(b0.x, b1.x));
+      float2 dy = sub2(xy, f2(b0.y, b1.y));
+      float2 dz = DIM == 3 ? sub2(xz, f2(b0.z, b1.z)) : f2s(0.f);
+      if (!inner) {
+        float ex, ey, ez;
+        displacement<DIM>(xi, b0, a.geo, ex, ey, ez);
+        dx.x = ex; dy.x = ey; dz.x = ez;
+        displacement<DIM>(xi, b1, a.geo, ex, ey, ez);
+        dx.y = ex; dy.y = ey; dz.y = ez;
+      }
+      float2 r2 = mul2(dx, dx);
+      r2 = fma2(dy, dy, r2);
+      if (DIM == 3) r2 = fma2(dz, dz, r2);
+      Coef2 cc;
+      if (SPECIES)
+        cc = coef2(sc[si * JMD_MAX_SPECIES + sclamp(__float_as_int(b0.w), tab.nsp)],
+                   sc[si * JMD_MAX_SPECIES + sclamp(__float_as_int(b1.w), tab.nsp)]);
+      else
+        cc = c0;
+      const float rc0 = SPECIES ? cc.rc2.x : rc2m, rc1 = SPECIES ? cc.rc2.y : rc2m;
+      const bool m0 = r2.x < rc0 && r2.x > 0.f;
+      const bool m1 = r2.y < rc1 && r2.y > 0.f;
+      float2 U, g;
+      pair_eval2<KIND, false>(r2, cc, U, g);
+      g.x = m0 ? g.x : 0.f;
+      g.y = m1 ? g.y : 0.f;
+      const float2 gx = mul2(g, dx), gy = mul2(g, dy);
+      ax = add2(ax, gx);
+      ay = add2(ay, gy);
+      float2 gz = f2s(0.f);
+      if (DIM == 3) {
+        gz = mul2(g, dz);
+        az = add2(az, gz);
+      }
+      // reactions (the far slot past a row's count takes zeros harmlessly:
+      // its g is 0, and it lies past the staged atoms the flush reads)
+      if (m0) {
+        red_shared(fx + j0, gx.x);
+        red_shared(fy + j0, gy.x);
+        if (DIM == 3) red_shared(fz + j0, gz.x);
+      }
+      if (m1) {
+        red_shared(fx + j1, gx.y);
+        red_shared(fy + j1, gy.y);
+        if (DIM == 3) red_shared(fz + j1, gz.y);
+      }
+    };
+    const int nck = (c + 7) >> 3;
+    const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
+    uint4 n1 = nck > 0 ? lp[0] : z4;
+    uint4 n2 = nck > 1 ? lp[P] : z4;
+    for (int kc = 0; kc < nck; ++kc) {
+      const uint4 cur = n1;
+      n1 = n2;
+      if (kc + 2 < nck) n2 = lp[(int64_t)(kc + 2) * P];
+      pair2((int)(cur.x & 0xFFFFu), (int)(cur.x >> 16));
+      pair2((int)(cur.y & 0xFFFFu), (int)(cur.y >> 16));
+      pair2((int)(cur.z & 0xFFFFu), (int)(cur.z >> 16));
+      pair2((int)(cur.w & 0xFFFFu), (int)(cur.w >> 16));
+    }
+    // the own atom's force: F_i = -sum g d (reactions were +g d)
+    red_shared(fx + is, -(ax.x + ax.y));
+    red_shared(fy + is, -(ay.x + ay.y));
+    if (DIM == 3) red_shared(fz + is, -(az.x + az.y));
+  }
+  __syncthreads();
+  // flush: every staged atom's accumulated force to its sorted slot
+  const int npieces = kSegMaxPieces;
+  for (int p = 0; p < npieces; ++p) {
+    const int n_at = __ldg(rec->pn + p);
+    if (n_at <= 0) continue;
+    const int ps = __ldg(rec->ps + p), pg = __ldg(rec->pg + p);
+    for (int t = threadIdx.x; t < n_at; t += blockDim.x) {
+      const float vx = fx[ps + t], vy = fy[ps + t], vz = DIM == 3 ? fz[ps + t] : 0.f;
+      if (vx != 0.f || vy != 0.f || vz != 0.f) {
+        float4* dst = a.f + pg + t;
+        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(vx), "f"(vy),
+                     "f"(vz), "f"(0.f)
+                     : "memory");
+      }
+    }
+  }
+}
+
+// Consumes the half-list forces: mode 2 (step) p += dt f, x' = x + dt p / m
+// (the closing half kick of step k, the opening one of k + 1, the drift),
+// skin test, f cleared; mode 3 (kick) p += dt/2 f, f kept.
+template <int DIM, int MODE>
+__global__ void k_seg_integrate(int n, float4* f, float4* p, const float4* x, float4* x_next,
+                                const float4* ref, float m0, float dt, float thr2, int32_t* flag,
+                                Geo geo) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  bool over = false;
+  if (s < n) {
+    const float4 fs = f[s];
+    float4 q = p[s];
+    const float h = 0.5f * dt;
+    q.x = fmaf(h, fs.x, q.x);
+    q.y = fmaf(h, fs.y, q.y);
+    if (DIM == 3) q.z = fmaf(h, fs.z, q.z);
+    if (MODE == S_STEP) {
+      q.x = fmaf(h, fs.x, q.x);
+      q.y = fmaf(h, fs.y, q.y);
+      if (DIM == 3) q.z = fmaf(h, fs.z, q.z);
+      float4 r = x[s];
+      const float ddx = dt * q.x / m0, ddy = dt * q.y / m0, ddz = dt * q.z / m0;
+      if (geo.periodic) {
+        r.x = wrap(r.x + ddx, geo.L[0]);
+        r.y = wrap(r.y + ddy, geo.L[1]);
+        if (DIM == 3) r.z = wrap(r.z + ddz, geo.L[2]);
+      } else {
+        r.x += ddx;
+        r.y += ddy;
+        if (DIM == 3) r.z += ddz;
+      }
+      x_next[s] = r;
+      f[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (ref) {
+        float ex, ey, ez;
+        displacement<DIM>(r, __ldg(ref + s), geo, ex, ey, ez);
+        over = ex * ex + ey * ey + ez * ez > thr2;
+      }
+    }
+    p[s] = q;
+  }
+  if (MODE == S_STEP && flag && __any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0)
+    atomicOr(flag, 1);
+}
+
+template <int DIM, int KIND, bool SP, bool FRAME>
+int seg_half_go(const SegGrid& g, const SegStepArgs& a, const PairTable& t, cudaStream_t st) {
+  const size_t smem = (size_t)(g.cap + 1) * (sizeof(float4) + (DIM == 3 ? 3 : 2) * sizeof(float));
+  auto k = k_seg_half<DIM, KIND, SP, FRAME>;
+  if (smem > 48 * 1024)
+    JMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k<<<(unsigned)g.nseg, (unsigned)g.threads, smem, st>>>(g, a, t);
+  return JMD_OK;
+}
+
+template <int DIM, int KIND>
+int seg_half_sp(bool sp, const SegGrid& g, const SegStepArgs& a, const PairTable& t, cudaStream_t st) {
+  if (g.frame)
+    return sp ? seg_half_go<DIM, KIND, true, true>(g, a, t, st)
+              : seg_half_go<DIM, KIND, false, true>(g, a, t, st);
+  return sp ? seg_half_go<DIM, KIND, true, false>(g, a, t, st)
+            : seg_half_go<DIM, KIND, false, false>(g, a, t, st);
+}
+
+int seg_half_launch(int dim, int kind, bool sp, const SegGrid& g, const SegStepArgs& a,
+                    const PairTable& t, cudaStream_t st) {
+  if (dim == 3) {
+    if (kind == JMD_LJ) return seg_half_sp<3, JMD_LJ>(sp, g, a, t, st);
+    if (kind == JMD_LJ_TRUNCATED) return seg_half_sp<3, JMD_LJ_TRUNCATED>(sp, g, a, t, st);
+    if (kind == JMD_MORSE) return seg_half_sp<3, JMD_MORSE>(sp, g, a, t, st);
+    return seg_half_sp<3, JMD_SOFT_SPHERE>(sp, g, a, t, st);
+  }
+  if (kind == JMD_LJ) return seg_half_sp<2, JMD_LJ>(sp, g, a, t, st);
+  if (kind == JMD_LJ_TRUNCATED) return seg_half_sp<2, JMD_LJ_TRUNCATED>(sp, g, a, t, st);
+  if (kind == JMD_MORSE) return seg_half_sp<2, JMD_MORSE>(sp, g, a, t, st);
+  return seg_half_sp<2, JMD_SOFT_SPHERE>(sp, g, a, t, st);
+}
+
 template <int DIM, int KIND, bool SP, int MODE, bool FRAME>
 int seg_go(const SegGrid& g, const SegStepArgs& a, const PairTable& t, cudaStream_t st) {
   const size_t smem = (size_t)(g.cap + 1) * sizeof(float4) + (size_t)g.lcap;
@@ -252,7 +483,7 @@ int seg_launch(int dim, int kind, bool sp, const SegGrid& g, const SegStepArgs& 
 int seg_step(int mode, const jmd_pair& pp, const jmd_space& space, const SegGrid& g,
              const float* x, const int32_t* start, const uint8_t* list, float* f, float* p,
              float* x_next, float m0, float dt, const float* ref, float thr2, int32_t* flag,
-             int32_t* status, bool species, cudaStream_t st) {
+             int32_t* status, bool species, cudaStream_t st, int64_t n_atoms) {
   int e = validate_pair(&pp);
   if (e) return e;
   PairTable t = make_pair_table(pp);
@@ -272,6 +503,31 @@ int seg_step(int mode, const jmd_pair& pp, const jmd_space& space, const SegGrid
   a.thr2 = thr2;
   a.flag = flag;
   a.status = status;
+  if (g.half) {
+    // forces into f (zero on entry), then the integration
+    a.f = reinterpret_cast<float4*>(f);
+    e = seg_half_launch(space.dim, pp.kind, species, g, a, t, st);
+    if (e) return e;
+    if (mode == S_FORCE) return check_launch("jmd segment half forces");
+    const unsigned gr = (unsigned)std::max<int64_t>(1, ceil_div(n_atoms, 256));
+    float4* f4 = reinterpret_cast<float4*>(f);
+    float4* p4 = reinterpret_cast<float4*>(p);
+    const float4* x4 = reinterpret_cast<const float4*>(x);
+    float4* xn4 = reinterpret_cast<float4*>(x_next);
+    const float4* r4 = reinterpret_cast<const float4*>(ref);
+    if (space.dim == 3) {
+      if (mode == S_STEP)
+        k_seg_integrate<3, S_STEP><<<gr, 256, 0, st>>>((int)n_atoms, f4, p4, x4, xn4, r4, m0, dt, thr2, flag, a.geo);
+      else
+        k_seg_integrate<3, S_KICK><<<gr, 256, 0, st>>>((int)n_atoms, f4, p4, x4, xn4, r4, m0, dt, thr2, flag, a.geo);
+    } else {
+      if (mode == S_STEP)
+        k_seg_integrate<2, S_STEP><<<gr, 256, 0, st>>>((int)n_atoms, f4, p4, x4, xn4, r4, m0, dt, thr2, flag, a.geo);
+      else
+        k_seg_integrate<2, S_KICK><<<gr, 256, 0, st>>>((int)n_atoms, f4, p4, x4, xn4, r4, m0, dt, thr2, flag, a.geo);
+    }
+    return check_launch("jmd segment half step");
+  }
   if (mode == S_STEP) e = seg_launch<S_STEP>(space.dim, pp.kind, species, g, a, t, st);
   else if (mode == S_KICK) e = seg_launch<S_KICK>(space.dim, pp.kind, species, g, a, t, st);
   else e = seg_launch<S_FORCE>(space.dim, pp.kind, species, g, a, t, st);

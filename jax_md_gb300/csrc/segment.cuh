@@ -43,6 +43,8 @@ struct SegGrid {
   int nch;      // 8-entry chunks per atom at most (8 nch >= max_occupancy)
   int64_t stride;  // bytes per segment block
   int lcap;     // shared-memory bytes for a staged segment block (0: never staged)
+  int half;     // 1: half lists (Newton's third law): only the forward half
+                //    of the neighbourhood is staged and searched
 };
 
 // Segment-block list layout.  The private list of segment g is one block of
@@ -99,6 +101,7 @@ inline bool make_seg_grid(const jmd_nlist& nl, int K, int cap, SegGrid* out) {
   if (g.nch < 1) g.nch = 1;
   g.stride = seg_block_used(g.pmax, g.nch);
   g.lcap = 0;
+  g.half = 0;
   *out = g;
   return true;
 }
@@ -204,11 +207,24 @@ struct SegRecord {
 static_assert(sizeof(SegRecord) == 256, "segment record is 256 bytes");
 inline int64_t seg_records_bytes(int64_t nseg) { return nseg * (int64_t)sizeof(SegRecord); }
 
-// Staged cells of a CTA: row r (dz = r / 3 - 1, dy = r % 3 - 1), column u
-// (x = x0 - 1 + u), at index r * W + u; the centre row is r = rows / 2.
+// Staged cells of a CTA: staged row r, column u (x = x0 - 1 + u), at index
+// r * W + u.  Full stencil: rows r = 0 .. 3^(d-1) - 1 with dy = r % 3 - 1,
+// dz = r / 3 - 1 (the centre row is r = 4 in 3-D, 1 in 2-D).  Half stencil
+// (g.half): the forward rows only -- full rows from the centre row on (the
+// centre row, then dy = +1, then the dz = +1 rows) -- and in the centre row
+// only the own cells and the one to their right (column 0 is left empty).
+// Every pair of atoms within a cutoff is then seen from exactly one side:
+// cells ahead of an atom's cell in (dz, dy, dx) order, and atoms after it in
+// its own cell.
+__host__ __device__ inline int seg_rows(int dim, int half) {
+  return half ? (dim == 3 ? 5 : 2) : (dim == 3 ? 9 : 3);
+}
+__host__ __device__ inline int seg_full_row(int dim, int half, int r) {
+  return half ? r + (dim == 3 ? 4 : 1) : r;
+}
 template <int DIM>
-__device__ __forceinline__ int seg_centre_row() {
-  return DIM == 3 ? 4 : 1;
+__device__ __forceinline__ int seg_centre_row(int half) {
+  return half ? 0 : (DIM == 3 ? 4 : 1);
 }
 
 // The segment of CTA blockIdx.x: its row, first cell and own cell count.
@@ -261,7 +277,7 @@ __device__ __forceinline__ void seg_stage_issue(const SegGrid& g, const float4* 
     const int lane = threadIdx.x;
     const SegPos sp = seg_pos<DIM>(g);
     const int W = sp.nx + 2;
-    const int rows = DIM == 3 ? 9 : 3;
+    const int rows = seg_rows(DIM, g.half);
     const int ncell = rows * W;
     if (lane == 0) {
       mbar_init(&sh.bar, 1);
@@ -279,14 +295,19 @@ __device__ __forceinline__ void seg_stage_issue(const SegGrid& g, const float4* 
       const int t = lo + k;
       if (t < hi) {
         const int r = t / W, u = t - r * W;
-        int y = sp.cy + (r % 3) - 1, z = DIM == 3 ? sp.cz + r / 3 - 1 : 0;
-        int xx = sp.x0 - 1 + u;
+        const int fr = seg_full_row(DIM, g.half, r);
+        int y = sp.cy + (fr % 3) - 1, z = DIM == 3 ? sp.cz + fr / 3 - 1 : 0;
+        // the half stencil's centre row starts at the own cells: column 0
+        // is empty, placed at the first own cell's start so the row stays
+        // one contiguous run
+        const bool skip0 = g.half && r == 0 && u == 0;
+        int xx = sp.x0 - 1 + (skip0 ? 1 : u);
         y = y < 0 ? y + g.cps[1] : (y >= g.cps[1] ? y - g.cps[1] : y);
         if (DIM == 3) z = z < 0 ? z + g.cps[2] : (z >= g.cps[2] ? z - g.cps[2] : z);
         xx = xx < 0 ? xx + g.cps[0] : (xx >= g.cps[0] ? xx - g.cps[0] : xx);
         const int h = xx + y * g.mult1 + z * g.mult2;
         beg[k] = __ldg(start + h);
-        cnt[k] = __ldg(start + h + 1) - beg[k];
+        cnt[k] = skip0 ? 0 : __ldg(start + h + 1) - beg[k];
       }
       sum += cnt[k];
     }
@@ -321,7 +342,7 @@ __device__ __forceinline__ void seg_stage_issue(const SegGrid& g, const float4* 
     __syncwarp();
     int64_t lbytes = 0;
     if (lane == 0) {
-      const int cr = seg_centre_row<DIM>() * W;
+      const int cr = seg_centre_row<DIM>(g.half) * W;
       sh.own_sm = sh.coff[cr + 1];
       sh.own_cnt = sh.coff[cr + sp.nx + 1] - sh.coff[cr + 1];
       sh.own_beg = sh.gbeg[cr + 1];
@@ -494,8 +515,8 @@ __device__ int seg_frame(const SegGrid& g, const SegShared& sh, float4* spos, co
 
 // Own cell (column u in 1..nx of the centre row) of the staged slot `is`.
 template <int DIM>
-__device__ __forceinline__ int seg_own_cell(const SegShared& sh, int is) {
-  const int cr = seg_centre_row<DIM>() * sh.W;
+__device__ __forceinline__ int seg_own_cell(const SegShared& sh, int is, int half) {
+  const int cr = seg_centre_row<DIM>(half) * sh.W;
   int u = 1;
   while (u < sh.nx && sh.coff[cr + u + 1] <= is) ++u;
   return u;

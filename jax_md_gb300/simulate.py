@@ -639,7 +639,7 @@ class _SortedBuffers:
     slots, 8-entry chunks); otherwise the tiled int32 list."""
 
     def __init__(self, n, ld, species: bool, workspace_bytes: int, device, seg_cells=None,
-                 seg_threads=128, seg_list_bytes=0, seg_list_smem=0):
+                 seg_threads=128, seg_list_bytes=0, seg_list_smem=0, seg_half=0):
         f4 = lambda: torch.empty((n, 4), dtype=torch.float32, device=device)
         i4 = lambda: torch.empty(n, dtype=torch.int32, device=device)
         self.n, self.ld = n, ld
@@ -649,6 +649,7 @@ class _SortedBuffers:
         self.seg_cells = seg_cells
         self.seg_threads = seg_threads
         self.seg_list_smem = seg_list_smem
+        self.seg_half = int(seg_half)
         if seg_cells is None:
             self.idx = torch.empty(((n + 31) // 32) * 32 * ld, dtype=torch.int32, device=device)
             self.seg = None
@@ -679,40 +680,45 @@ class _SortedBuffers:
             z.seg_list, z.seg_list_bytes = self.seg.data_ptr(), self.seg.numel()
             z.seg_cells, z.seg_threads = self.seg_cells, self.seg_threads
             z.seg_list_smem = self.seg_list_smem
+            z.seg_half = self.seg_half
         z.seg_status = self.seg_status.data_ptr()
         z.flags = self.flags
         return z
 
 
 def _segment_shape(nbrs, layout):
-    """(cells per segment, threads per CTA, list bytes, list staging bytes)
-    for a run, or None for the tiled list.  `layout`: None / 'segment'
-    (autotuned choice or default), an int (cells), a (cells, threads) or
-    (cells, threads, stage_lists) tuple, or 'tiled'."""
+    """(cells per segment, threads per CTA, list bytes, list staging bytes,
+    half lists) for a run, or None for the tiled list.  `layout`: None
+    (autotuned choice, else full segment lists with the default width),
+    'segment' / 'half' (full / half lists, default width), an int (cells), a
+    (cells, threads[, stage_lists[, half]]) tuple, or 'tiled'."""
     if layout == 'tiled':
         return None
     nl = nbrs.plan.nl
-    threads, stage = None, True
-    if layout is None or layout == 'segment':
-        choice = _segment_choice.get(_grid_key(nl), (SEGMENT_CELLS_DEFAULT, None, True))
-        cells, threads, stage = (tuple(choice) + (True,))[:3]
+    threads, stage, half = None, True, False
+    if layout is None:
+        choice = _segment_choice.get(_grid_key(nl), (SEGMENT_CELLS_DEFAULT, None, True, False))
+        cells, threads, stage, half = (tuple(choice) + (True, False))[:4]
+    elif layout in ('segment', 'half'):
+        cells, half = SEGMENT_CELLS_DEFAULT, layout == 'half'
     elif isinstance(layout, (tuple, list)):
         cells, threads = int(layout[0]), int(layout[1])
         stage = bool(layout[2]) if len(layout) > 2 else True
+        half = bool(layout[3]) if len(layout) > 3 else False
     else:
         cells = int(layout)
     plan = segment_plan(nl, cells)
     if plan is None:
-        if layout not in (None, 'segment'):
+        if layout not in (None, 'segment', 'half'):
             raise ValueError('the segment layout does not apply to this cell grid')
         return None
     cells = plan[3]
     if threads is None:
         threads = segment_threads_default(cells, nl.cell_capacity)
-    smem = segment_list_smem(nl, cells, nbrs.plan.n) if stage else 0
-    if stage and plan[2] + smem + 4096 > 227 * 1024:
+    smem = segment_list_smem(nl, cells, nbrs.plan.n) if (stage and not half) else 0
+    if smem and plan[2] + smem + 4096 > 227 * 1024:
         smem = 0   # positions and list block do not fit one CTA together
-    return cells, threads, plan[4], smem
+    return cells, threads, plan[4], smem, int(half)
 
 
 def _sorted_buffers(state, nbrs, species, seg=None):

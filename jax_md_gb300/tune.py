@@ -106,10 +106,10 @@ def _seg_key(nl, pair) -> str:
 
 
 def segment_candidates(nl):
-    """(cells, threads, stage_lists) to try: K in 2..8 (those the grid
-    admits) with the default thread count and the neighbouring multiples of
-    32, each with the list block staged in shared memory or read from global
-    memory."""
+    """(cells, threads, stage_lists, half) to try: K in 2..8 (those the
+    grid admits) with the default thread count and the neighbouring multiples
+    of 32, each with full lists (block staged in shared memory or read from
+    global memory) or half lists (Newton's third law)."""
     from . import simulate
     out = []
     for K in (2, 3, 4, 5, 6, 8):
@@ -119,8 +119,9 @@ def segment_candidates(nl):
         t0 = simulate.segment_threads_default(K, nl.cell_capacity)
         for t in sorted({t0 - 32, t0, t0 + 32}):
             if 64 <= t <= 256:
-                out.append((K, t, 1))
-                out.append((K, t, 0))
+                out.append((K, t, 1, 0))
+                out.append((K, t, 0, 0))
+                out.append((K, t, 0, 1))   # half lists (Newton's third law)
     return out
 
 

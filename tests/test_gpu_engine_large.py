@@ -32,7 +32,7 @@ def lj864k(cuda):
     disp, shift = space.periodic(L)
     nfn, efn = energy.lennard_jones_neighbor_list(disp, L, dr_threshold=0.3, format=partition.Dense)
     out = {}
-    for layout in ('segment', 'tiled'):
+    for layout in ('segment', 'half', 'tiled'):
         Rt = torch.tensor(R, device=cuda)
         nb = nfn.allocate(Rt)
         init, apply = simulate.nve(efn, shift, LJ_DT)
@@ -51,9 +51,10 @@ def _oracle_pairs(X, L, r):
     return tree, pairs
 
 
-def test_forces_and_energy_match_oracle(lj864k):
+@pytest.mark.parametrize('layout', ['segment', 'half'])
+def test_forces_and_energy_match_oracle(lj864k, layout):
     R, L, efn, out = lj864k
-    st, nb, _, status = out['segment']
+    st, nb, _, status = out[layout]
     assert status == 0
     X = st.position[:, :3].double().cpu().numpy()
     _, pairs = _oracle_pairs(X, L, 2.5)
@@ -99,12 +100,13 @@ def test_returned_list_matches_oracle_rows(lj864k):
     assert int(nb.error.code) == 0
 
 
-def test_layouts_agree_and_energy_is_conserved(lj864k):
-    """The segment and tiled runs agree to fp32 rounding over the run; the
-    segment run conserves energy."""
+@pytest.mark.parametrize('layout', ['segment', 'half'])
+def test_layouts_agree_and_energy_is_conserved(lj864k, layout):
+    """The segment (full or half lists) and tiled runs agree to fp32 rounding
+    over the run; the segment run conserves energy."""
     from jax_md_gb300 import simulate
     R, L, efn, out = lj864k
-    (sa, na, E0, _), (sb, nbb, _, _) = out['segment'], out['tiled']
+    (sa, na, E0, _), (sb, nbb, _, _) = out[layout], out['tiled']
     d = O.displacement(sa.position[:, :3].cpu().numpy(), sb.position[:, :3].cpu().numpy(),
                        np.full(3, L))
     assert np.abs(d).max() < 1e-4
