@@ -211,17 +211,34 @@ k_seg_step(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
   }
 }
 
-// Shared-memory reduction without a returned value (red.shared.add.f32).
-__device__ __forceinline__ void red_shared(float* p, float v) {
-  asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(smem_u32(p)), "f"(v) : "memory");
+// Reaction accumulators of the half-list kernel are fixed point: 32-bit
+// integer additions in shared memory are single native reductions on this
+// part, while float (and 64-bit) ones are compare-and-swap loops.  A reaction
+// component v with |v| < kFixMax is added as round(v 2^19) (resolution
+// 1.9e-6); an atom takes at most ~60 contributions within one CTA, so the
+// sum stays below 60 x 64 x 2^19 < 2^31.  Larger reactions (close contacts)
+// and the own atoms' forces go to global memory as float reductions.
+constexpr float kFixScale = 524288.0f;  // 2^19
+constexpr float kFixInv = 1.0f / 524288.0f;
+constexpr float kFixMax = 64.0f;
+
+// (two's complement: an unsigned 32-bit add is the signed one)
+__device__ __forceinline__ void red_shared_s32(int* p, int v) {
+  asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(smem_u32(p)), "r"((unsigned)v) : "memory");
+}
+
+__device__ __forceinline__ void red_global_v4(float4* dst, float x, float y, float z) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(x), "f"(y), "f"(z),
+               "f"(0.f)
+               : "memory");
 }
 
 // Half lists (Newton's third law): each pair once, from the atom whose
 // forward stencil holds the other.  The own atom keeps its force in
-// registers; the partner's reaction goes to a shared-memory accumulator per
-// staged atom; the CTA then adds every staged atom's accumulated force to
-// `f` in global memory with one vector reduction (f is zero before the
-// kernel; k_seg_integrate consumes and clears it).
+// registers and adds it to `f` once; the partner's reaction goes to a
+// fixed-point shared-memory accumulator per staged atom, which the CTA then
+// adds to `f` in global memory with one vector reduction per staged atom
+// (f is zero before the kernel; k_seg_integrate consumes and clears it).
 template <int DIM, int KIND, bool SPECIES, bool FRAME>
 __global__ void __maxnreg__(72)
 k_seg_half(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
@@ -230,17 +247,17 @@ k_seg_half(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
   __shared__ PairCoef sc[SPECIES ? JMD_MAX_SPECIES * JMD_MAX_SPECIES : 1];
   if (SPECIES)
     for (int k = threadIdx.x; k < JMD_MAX_SPECIES * JMD_MAX_SPECIES; k += blockDim.x) sc[k] = tab.c[k];
-  float* fx = reinterpret_cast<float*>(spos + sg.cap + 1);
-  float* fy = fx + (sg.cap + 1);
-  float* fz = fy + (sg.cap + 1);
+  int* fx = reinterpret_cast<int*>(spos + sg.cap + 1);
+  int* fy = fx + (sg.cap + 1);
+  int* fz = fy + (sg.cap + 1);
   const SegRecord* rec = a.recs + blockIdx.x;
   const uint8_t* gblk = a.blocks + (int64_t)blockIdx.x * sg.stride;
   const SegHead hd = seg_stage_record<DIM>(sg, a.x, rec, spos, sh, a.status, gblk, nullptr);
   if (hd.total < 0) return;  // neighbourhood over capacity (flagged at the rebuild)
   for (int t = threadIdx.x; t < hd.total; t += blockDim.x) {
-    fx[t] = 0.f;
-    fy[t] = 0.f;
-    if (DIM == 3) fz[t] = 0.f;
+    fx[t] = 0;
+    fy[t] = 0;
+    if (DIM == 3) fz[t] = 0;
   }
   const int P = seg_pad(hd.own_cnt);
   const bool blk_ok = P <= sg.pmax;
@@ -314,18 +331,27 @@ k_seg_half(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
         gz = mul2(g, dz);
         az = add2(az, gz);
       }
-      // reactions (the far slot past a row's count takes zeros harmlessly:
-      // its g is 0, and it lies past the staged atoms the flush reads)
-      if (m0) {
-        red_shared(fx + j0, gx.x);
-        red_shared(fy + j0, gy.x);
-        if (DIM == 3) red_shared(fz + j0, gz.x);
-      }
-      if (m1) {
-        red_shared(fx + j1, gx.y);
-        red_shared(fy + j1, gy.y);
-        if (DIM == 3) red_shared(fz + j1, gz.y);
-      }
+      // reactions (masked pairs, the far slot included, add nothing)
+      auto react = [&](int j, float vx, float vy, float vz) {
+        if (fabsf(vx) < kFixMax && fabsf(vy) < kFixMax && fabsf(vz) < kFixMax) {
+          red_shared_s32(fx + j, __float2int_rn(vx * kFixScale));
+          red_shared_s32(fy + j, __float2int_rn(vy * kFixScale));
+          if (DIM == 3) red_shared_s32(fz + j, __float2int_rn(vz * kFixScale));
+        } else {
+          // a close contact: straight to the partner's sorted slot (the
+          // pieces partition the staged slots; a slot outside them is
+          // skipped rather than written anywhere)
+          for (int q = 0; q < kSegMaxPieces; ++q) {
+            const int ps = __ldg(rec->ps + q), pn = __ldg(rec->pn + q);
+            if (pn > 0 && j >= ps && j < ps + pn) {
+              red_global_v4(a.f + __ldg(rec->pg + q) + (j - ps), vx, vy, vz);
+              break;
+            }
+          }
+        }
+      };
+      if (m0) react(j0, gx.x, gy.x, DIM == 3 ? gz.x : 0.f);
+      if (m1) react(j1, gx.y, gy.y, DIM == 3 ? gz.y : 0.f);
     };
     const int nck = (c + 7) >> 3;
     const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
@@ -340,10 +366,9 @@ k_seg_half(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
       pair2((int)(cur.z & 0xFFFFu), (int)(cur.z >> 16));
       pair2((int)(cur.w & 0xFFFFu), (int)(cur.w >> 16));
     }
-    // the own atom's force: F_i = -sum g d (reactions were +g d)
-    red_shared(fx + is, -(ax.x + ax.y));
-    red_shared(fy + is, -(ay.x + ay.y));
-    if (DIM == 3) red_shared(fz + is, -(az.x + az.y));
+    // the own atom's force, F_i = -sum g d (the reactions were +g d)
+    red_global_v4(a.f + hd.own_beg + o, -(ax.x + ax.y), -(ay.x + ay.y),
+                  DIM == 3 ? -(az.x + az.y) : 0.f);
   }
   __syncthreads();
   // flush: every staged atom's accumulated force to its sorted slot
@@ -353,13 +378,10 @@ k_seg_half(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
     if (n_at <= 0) continue;
     const int ps = __ldg(rec->ps + p), pg = __ldg(rec->pg + p);
     for (int t = threadIdx.x; t < n_at; t += blockDim.x) {
-      const float vx = fx[ps + t], vy = fy[ps + t], vz = DIM == 3 ? fz[ps + t] : 0.f;
-      if (vx != 0.f || vy != 0.f || vz != 0.f) {
-        float4* dst = a.f + pg + t;
-        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(vx), "f"(vy),
-                     "f"(vz), "f"(0.f)
-                     : "memory");
-      }
+      const int ix = fx[ps + t], iy = fy[ps + t], iz = DIM == 3 ? fz[ps + t] : 0;
+      if (ix | iy | iz)
+        red_global_v4(a.f + pg + t, (float)ix * kFixInv, (float)iy * kFixInv,
+                      (float)iz * kFixInv);
     }
   }
 }
