@@ -744,18 +744,26 @@ def main():
     xh.copy_(st.position)
     ph.copy_(st.momentum)
     e2e_steps = max(5, min(args.steps, 50))
-    simulate.run(apply, st, nb, 1)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        st.position.copy_(xh, non_blocking=True)
-        st.momentum.copy_(ph, non_blocking=True)
-        simulate.run(apply, st, nb, 1)
-        xh.copy_(st.position, non_blocking=True)
-        ph.copy_(st.momentum, non_blocking=True)
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    e2e_value = n * world * e2e_steps / e2e_s
+    # two public-API variants of a one-step call: the default (the atoms are
+    # sorted into cell order and the private list built on every call) and
+    # sort=False (the caller's Dense list, rebuilt only when the skin test
+    # fires); the faster is reported, with its name
+    e2e_variants = {}
+    for name, sort in (('simulate.run(apply, state, nbrs, 1)', None),
+                       ('simulate.run(apply, state, nbrs, 1, sort=False)', False)):
+        simulate.run(apply, st, nb, 1, sort=sort)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            st.position.copy_(xh, non_blocking=True)
+            st.momentum.copy_(ph, non_blocking=True)
+            simulate.run(apply, st, nb, 1, sort=sort)
+            xh.copy_(st.position, non_blocking=True)
+            ph.copy_(st.momentum, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_variants[name] = n * world * e2e_steps / (time.perf_counter() - t0)
+    e2e_call = max(e2e_variants, key=e2e_variants.get)
+    e2e_value = e2e_variants[e2e_call]
 
     # per step: the fused step kernel + the conditional-set kernel; the rebuild
     # chain (6 kernels) runs only on rebuild steps
@@ -793,7 +801,9 @@ def main():
                      'bytes_per_atom': kern_bytes / n,
                      'step_algorithmic_GBps': step_bytes * args.steps / (ms / 1e3) / 1e9},
         'e2e': {'value': e2e_value, 'unit': 'atom-steps/s', 'h2d_bytes_per_step': 2 * n * 12,
-                'd2h_bytes_per_step': 2 * n * 12},
+                'd2h_bytes_per_step': 2 * n * 12, 'call': e2e_call,
+                'variants': e2e_variants,
+                'per_step': 'pinned host positions and momenta copied in, one step, copied out'},
         'gpu_launches': launches_per_step * args.steps,
         'clocks': clk.summary(),
     }

@@ -91,6 +91,12 @@ typedef struct {
   float sigma[JMD_MAX_SPECIES][JMD_MAX_SPECIES];
   float epsilon[JMD_MAX_SPECIES][JMD_MAX_SPECIES];
   float alpha[JMD_MAX_SPECIES][JMD_MAX_SPECIES];  /* soft-sphere exponent / Morse range */
+  /* Per-particle parameters (smap.py:697-846 with the default combinator
+   * 0.5 (p_i + p_j), smap.py:704-713): device float arrays [n] or NULL.
+   * When set, sigma[0][0] holds max sigma (the cutoff scale) and n_species
+   * must be 0; only jmd_pair_forces (the generic kernels) accepts them. */
+  const float* particle_sigma;
+  const float* particle_epsilon;
 } jmd_pair;
 
 const char* jmd_last_error(void);
@@ -669,6 +675,30 @@ int jmd_batch_pair_forces(const jmd_pair* pair, const jmd_batch* batch,
 
 /* Per-system f64 kinetic energy ke[B] (quantity.kinetic_energy) and
  * largest atom force norm fmax[B] (either may be NULL). */
+/* Per-system dot products out[b] = sum over system b's atoms of a_i . c_i
+ * (dim components of rows of the given strides), f64 sums of fp32 products.
+ * The reductions of the batched Nose-Hoover adjoint (sum_i pbar_i . r_i):
+ * the derivative of the loss with respect to each system's momentum scale
+ * (simulate.py:639-669 differentiated).  No reference counterpart. */
+int jmd_batch_dot_per_system(const jmd_batch* batch, const float* a, int64_t a_stride,
+                             const float* c, int64_t c_stride, double* out, void* stream);
+
+/* One fused stage of the batched Nose-Hoover reverse step (the cotangent
+ * algebra around the force VJP and the chain VJPs; no reference
+ * counterpart, it is what jax.grad evaluates through simulate.py:639-669).
+ * Rows of [n, dim] floats unless noted; scale / kebar / sums are [B] f64.
+ *   stage 0: rbar = in_a s[sys] + kebar[sys] in_b / m -> out_a;
+ *            coef (rbar + pending) -> out_b ([n, 4] rows; pending may be NULL)
+ *   stage 1: qbar = in_a + coef pending ([n, 4] rows) -> out_a;
+ *            sums[b] = sum qbar . in_b
+ *   stage 2: out_a = in_a s[sys] + kebar[sys] in_b / m
+ * in_b rows have stride b_stride; inv_m = 1 / mass. */
+int jmd_batch_nvt_adjoint_update(const jmd_batch* batch, int32_t stage, const float* in_a,
+                                 const float* in_b, int64_t b_stride, const double* scale,
+                                 const double* kebar, float inv_m, float coef,
+                                 const float* pending, float* out_a, float* out_b,
+                                 double* sums, void* stream);
+
 int jmd_batch_kinetic_energy(const jmd_batch* batch, const float* momentum,
                              const float* force, const float* mass, float mass_scalar,
                              double* ke, float* fmax, void* stream);

@@ -41,7 +41,8 @@ class Pair(C.Structure):
                 ('pad_', C.c_int32), ('r_onset', C.c_float), ('r_cutoff', C.c_float),
                 ('sigma', (C.c_float * MAX_SPECIES) * MAX_SPECIES),
                 ('epsilon', (C.c_float * MAX_SPECIES) * MAX_SPECIES),
-                ('alpha', (C.c_float * MAX_SPECIES) * MAX_SPECIES)]
+                ('alpha', (C.c_float * MAX_SPECIES) * MAX_SPECIES),
+                ('particle_sigma', C.c_void_p), ('particle_epsilon', C.c_void_p)]
 
 
 class Nhc(C.Structure):
@@ -187,6 +188,9 @@ SIGNATURES = {
     'jmd_batch_pair_forces': (C.c_int, [C.POINTER(Pair), C.POINTER(Batch), C.POINTER(BatchNList),
                                         P, P, P, P, P]),
     'jmd_batch_kinetic_energy': (C.c_int, [C.POINTER(Batch), P, P, P, F32, P, P, P]),
+    'jmd_batch_dot_per_system': (C.c_int, [C.POINTER(Batch), P, I64, P, I64, P, P]),
+    'jmd_batch_nvt_adjoint_update': (C.c_int, [C.POINTER(Batch), I32, P, P, I64, P, P, F32, F32,
+                                               P, P, P, P, P]),
     'jmd_batch_fire_init': (C.c_int, [C.POINTER(BatchSystem), C.POINTER(FireParams), P]),
     'jmd_batch_nve_run': (C.c_int, [C.POINTER(BatchSystem), I64, I32, P]),
     'jmd_batch_fire_run': (C.c_int, [C.POINTER(BatchSystem), C.POINTER(FireParams), I64, I32, P]),

@@ -789,10 +789,14 @@ class _BatchNvtTrajectoryFn(torch.autograd.Function):
         lam4 = torch.zeros((n, 4), dtype=torch.float32, device=dev)
         rec = torch.zeros((2 * n, 4), dtype=torch.float32, device=dev)
         L = N.lib()
-
-        def per_system(v):
-            return torch.zeros(B, dtype=torch.float64, device=dev).index_add_(
-                0, sys_of, v.double().sum(1))
+        g = ctypes.byref(nb.grid.struct)
+        rbar = torch.empty((n, dim), dtype=torch.float32, device=dev)
+        qbar = torch.empty((n, dim), dtype=torch.float32, device=dev)
+        pend = torch.empty((n, dim), dtype=torch.float32, device=dev)
+        sbar1 = torch.empty(B, dtype=torch.float64, device=dev)
+        sbar2 = torch.empty(B, dtype=torch.float64, device=dev)
+        pbar = pbar.contiguous()
+        s_ptr = lambda t, k: t.data_ptr() + k * t.stride(0) * t.element_size()  # row k of [steps, B]
 
         def chain_vjp(chain_in, ke, update_mass, cot_p, cot_s, out_p):
             N.check(L.jmd_batch_nhc_half_step_vjp(
@@ -800,33 +804,44 @@ class _BatchNvtTrajectoryFn(torch.autograd.Function):
                 ke.data_ptr(), update_mass, cot_p.data_ptr(), cot_s.data_ptr(), out_p.data_ptr(),
                 kebar.data_ptr(), N.stream_ptr()), 'batch_nhc_half_step_vjp')
 
-        def vjp_at(x, lam):
+        def vjp_at(x):  # the cotangent is in lam4
             x4[:, :dim] = x
             tr.neighbor_fns.update(x4, nb)
-            lam4[:, :dim] = lam
             N.check(L.jmd_batch_pair_force_vjp(
                 ctypes.byref(pair), ctypes.byref(nb.grid.struct), ctypes.byref(nb.struct()),
                 x4.data_ptr(), lam4.data_ptr(), N.ptr(species), 1.0, xbar.data_ptr(),
                 bins.data_ptr() if want else None, rec.data_ptr(), N.stream_ptr()),
                 'batch_pair_force_vjp')
 
+        # one reverse step: fused per-system reductions and cotangent updates
+        # (jmd_batch_dot_per_system, jmd_batch_nvt_adjoint_update) around the
+        # chain VJPs and the force VJP
         pending = None
+        upd = L.jmd_batch_nvt_adjoint_update
         for k in range(len(tape) - 1, -1, -1):
             x_k, p_k, chain_a, r, chain_b = tape[k]
             x1 = tape[k + 1][0] if k + 1 < len(tape) else x_n
-            sbar2 = per_system(pbar * r)
-            rbar = pbar * s2[k][sys_of].float()[:, None]
+            N.check(L.jmd_batch_dot_per_system(g, pbar.data_ptr(), dim, r.data_ptr(), r.stride(0),
+                                               sbar2.data_ptr(), N.stream_ptr()), 'dot')
             chain_vjp(chain_b, ke2[k], 0, pxi, sbar2, pxi1)
-            rbar = rbar + (kebar[sys_of].float()[:, None] * r) * inv_m
-            lam = h * (rbar if pending is None else rbar + pending)
-            vjp_at(x1, lam)
-            qbar = rbar + (dt * inv_m) * xbar[:, :dim]
-            sbar1 = per_system(qbar * p_k)
-            pbar = qbar * s1[k][sys_of].float()[:, None]
+            # rbar = pbar s2 + kebar r / m ; lam4 = h (rbar + pending)
+            N.check(upd(g, 0, pbar.data_ptr(), r.data_ptr(), r.stride(0), s_ptr(s2, k),
+                        kebar.data_ptr(), inv_m, h, N.ptr(pending), rbar.data_ptr(),
+                        lam4.data_ptr(), None, N.stream_ptr()), 'nvt adjoint pre')
+            vjp_at(x1)
+            # qbar = rbar + (dt / m) xbar ; sbar1 = sum qbar . p_k
+            N.check(upd(g, 1, rbar.data_ptr(), p_k.data_ptr(), p_k.stride(0), None, None, inv_m,
+                        dt * inv_m, xbar.data_ptr(), qbar.data_ptr(), None, sbar1.data_ptr(),
+                        N.stream_ptr()), 'nvt adjoint post')
             chain_vjp(chain_a, chain_a[:, 64].contiguous(), 1, pxi1, sbar1, pxi)
-            pbar = pbar + (kebar[sys_of].float()[:, None] * p_k) * inv_m
-            pending = qbar
-        vjp_at(tape[0][0], h * pending)
+            # pbar = qbar s1 + kebar p_k / m
+            N.check(upd(g, 2, qbar.data_ptr(), p_k.data_ptr(), p_k.stride(0), s_ptr(s1, k),
+                        kebar.data_ptr(), inv_m, 0.0, None, pbar.data_ptr(), None, None,
+                        N.stream_ptr()), 'nvt adjoint pbar')
+            pend.copy_(qbar)
+            pending = pend
+        lam4[:, :dim] = h * pending
+        vjp_at(tape[0][0])
         gs, ge = _bins_to_grads(bins, None, sigma, epsilon) if want else (None, None)
         return xbar[:, :dim].clone(), pbar.contiguous(), gs, ge, None
 

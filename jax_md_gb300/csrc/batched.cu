@@ -435,6 +435,81 @@ __global__ void __launch_bounds__(256) k_bke(BatchView v, const float4* __restri
   }
 }
 
+// ------------------------------------------ Nose-Hoover adjoint helpers ----
+// The per-atom algebra of one reverse Nose-Hoover step of the batched
+// trajectory adjoint (batch.BatchNvtTrajectory), fused: per-system dot
+// products in f64 (CTA per system, no contended atomics) and the elementwise
+// cotangent updates.  Rows are [n, stride] float; `dim` components are used.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bdot(BatchView v, const float* __restrict__ a, int64_t as,
+                                              const float* __restrict__ c, int64_t cs,
+                                              double* out) {
+  const int b = blockIdx.x;
+  const int a0 = __ldg(v.sys_offset + b), a1 = __ldg(v.sys_offset + b + 1);
+  double acc = 0.0;
+  for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+    float d = a[i * as] * c[i * cs];
+    d = fmaf(a[i * as + 1], c[i * cs + 1], d);
+    if (DIM == 3) d = fmaf(a[i * as + 2], c[i * cs + 2], d);
+    acc += (double)d;
+  }
+  const double s = block_sum(acc);
+  if (threadIdx.x == 0) out[b] = s;
+}
+
+// rbar = pbar s2[sys] + kebar[sys] r / m ;  lam = h (rbar + pending)
+template <int DIM>
+__global__ void k_bnvt_pre(BatchView v, const float* pbar, const float* r, int64_t rs,
+                           const double* s2, const double* kebar, float inv_m, float h,
+                           const float* pending, float* rbar, float* lam4) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n) return;
+  const int b = __ldg(v.atom_sys + i);
+  const float sc = (float)s2[b], kb = (float)kebar[b];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    const float rb = fmaf(kb * r[i * rs + d], inv_m, pbar[i * DIM + d] * sc);
+    rbar[i * DIM + d] = rb;
+    lam4[i * 4 + d] = h * (pending ? rb + pending[i * DIM + d] : rb);
+  }
+}
+
+// qbar = rbar + (dt / m) xbar ;  sbar1[sys] = sum qbar . p_k
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bnvt_post(BatchView v, const float* rbar,
+                                                   const float* xbar4, float dt_inv_m,
+                                                   const float* pk, int64_t ps, float* qbar,
+                                                   double* sbar1) {
+  const int b = blockIdx.x;
+  const int a0 = __ldg(v.sys_offset + b), a1 = __ldg(v.sys_offset + b + 1);
+  double acc = 0.0;
+  for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+    float d = 0.f;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      const float q = fmaf(dt_inv_m, xbar4[i * 4 + k], rbar[i * DIM + k]);
+      qbar[i * DIM + k] = q;
+      d = fmaf(q, pk[i * ps + k], d);
+    }
+    acc += (double)d;
+  }
+  const double s = block_sum(acc);
+  if (threadIdx.x == 0) sbar1[b] = s;
+}
+
+// pbar = qbar s1[sys] + kebar[sys] p_k / m
+template <int DIM>
+__global__ void k_bnvt_pbar(BatchView v, const float* qbar, const double* s1, const double* kebar,
+                            const float* pk, int64_t ps, float inv_m, float* pbar) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n) return;
+  const int b = __ldg(v.atom_sys + i);
+  const float sc = (float)s1[b], kb = (float)kebar[b];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d)
+    pbar[i * DIM + d] = fmaf(kb * pk[i * ps + d], inv_m, qbar[i * DIM + d] * sc);
+}
+
 // --------------------------------------------------------- integration ----
 // Kick + drift with the skin test of the drifted positions.  FIRE: the time
 // step is the system's own (fire_state[8b]) and frozen systems are skipped.
@@ -1272,6 +1347,46 @@ int jmd_batch_pair_forces(const jmd_pair* pair, const jmd_batch* batch, const jm
   int rc = force_impl(*pair, *batch, *nl, position, species, force, nullptr, 0.f, nullptr, B_FORCE,
                       energy, as_stream(stream));
   return rc ? rc : check_launch("jmd_batch_pair_forces");
+}
+
+int jmd_batch_dot_per_system(const jmd_batch* batch, const float* a, int64_t a_stride,
+                             const float* c, int64_t c_stride, double* out, void* stream) {
+  int e = validate_batch(batch);
+  if (e) return e;
+  JMD_REQUIRE(a && c && out, "null buffer");
+  const BatchView v = view_of(*batch);
+  cudaStream_t st = as_stream(stream);
+  if (batch->dim == 3) k_bdot<3><<<batch->n_systems, 256, 0, st>>>(v, a, a_stride, c, c_stride, out);
+  else k_bdot<2><<<batch->n_systems, 256, 0, st>>>(v, a, a_stride, c, c_stride, out);
+  return check_launch("jmd_batch_dot_per_system");
+}
+
+int jmd_batch_nvt_adjoint_update(const jmd_batch* batch, int32_t stage, const float* in_a,
+                                 const float* in_b, int64_t b_stride, const double* scale,
+                                 const double* kebar, float inv_m, float coef,
+                                 const float* pending, float* out_a, float* out_b,
+                                 double* sums, void* stream) {
+  int e = validate_batch(batch);
+  if (e) return e;
+  JMD_REQUIRE(stage >= 0 && stage <= 2, "stage must be 0, 1 or 2");
+  const BatchView v = view_of(*batch);
+  cudaStream_t st = as_stream(stream);
+  const unsigned gr = (unsigned)std::max<int64_t>(1, ceil_div(v.n, 256));
+  const bool d3 = batch->dim == 3;
+  if (stage == 0) {  // rbar, lam4 from pbar (in_a), r (in_b)
+    JMD_REQUIRE(in_a && in_b && scale && kebar && out_a && out_b, "null buffer");
+    if (d3) k_bnvt_pre<3><<<gr, 256, 0, st>>>(v, in_a, in_b, b_stride, scale, kebar, inv_m, coef, pending, out_a, out_b);
+    else k_bnvt_pre<2><<<gr, 256, 0, st>>>(v, in_a, in_b, b_stride, scale, kebar, inv_m, coef, pending, out_a, out_b);
+  } else if (stage == 1) {  // qbar (out_a) and sums from rbar (in_a), xbar4 (pending), p_k (in_b)
+    JMD_REQUIRE(in_a && in_b && pending && out_a && sums, "null buffer");
+    if (d3) k_bnvt_post<3><<<batch->n_systems, 256, 0, st>>>(v, in_a, pending, coef, in_b, b_stride, out_a, sums);
+    else k_bnvt_post<2><<<batch->n_systems, 256, 0, st>>>(v, in_a, pending, coef, in_b, b_stride, out_a, sums);
+  } else {  // pbar (out_a) from qbar (in_a), p_k (in_b)
+    JMD_REQUIRE(in_a && in_b && scale && kebar && out_a, "null buffer");
+    if (d3) k_bnvt_pbar<3><<<gr, 256, 0, st>>>(v, in_a, scale, kebar, in_b, b_stride, inv_m, out_a);
+    else k_bnvt_pbar<2><<<gr, 256, 0, st>>>(v, in_a, scale, kebar, in_b, b_stride, inv_m, out_a);
+  }
+  return check_launch("jmd_batch_nvt_adjoint_update");
 }
 
 int jmd_batch_kinetic_energy(const jmd_batch* batch, const float* momentum, const float* force,

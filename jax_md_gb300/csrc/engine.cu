@@ -48,6 +48,9 @@ std::map<std::string, GraphPlan> g_cache;
 
 int validate_sys(const jmd_nve_system& s) {
   JMD_REQUIRE(s.n > 0 && s.n < INT32_MAX, "atom count out of range");
+  JMD_REQUIRE(s.pair.particle_sigma == nullptr && s.pair.particle_epsilon == nullptr,
+              "the engine's kernels take scalar or species parameters (per-particle parameters "
+              "run on jmd_pair_forces)");
   JMD_REQUIRE(s.space.dim == 2 || s.space.dim == 3, "dim must be 2 or 3");
   JMD_REQUIRE(s.nlist.format == JMD_DENSE, "the engine runs Dense neighbour lists");
   JMD_REQUIRE(s.position && s.position_alt && s.momentum && s.force && s.idx &&

@@ -57,6 +57,12 @@ PairTable make_pair_table(const jmd_pair& pp) {
       t.rc2_max = std::max(t.rc2_max, c.rc2);
     }
   }
+  t.psig = pp.particle_sigma;
+  t.peps = pp.particle_epsilon;
+  t.per_pair_cutoff = pp.per_pair_cutoff;
+  t.maxs = maxs;
+  t.r_onset = pp.r_onset;
+  t.r_cutoff = pp.r_cutoff;
   return t;
 }
 
@@ -125,9 +131,10 @@ __global__ void __launch_bounds__(256) k_pair_dense(DenseArgs a, const __grid_co
       r2 = fmaf(dy, dy, r2);
       if (DIM == 3) r2 = fmaf(dz, dz, r2);
       if (!(r2 < rc2m) || r2 == 0.f) continue;
-      const PairCoef& c =
-          SPECIES ? sc[si * JMD_MAX_SPECIES + sp_clamp(__ldg(a.species + j), tab.nsp)] : tab.c[0];
-      if (SPECIES && !(r2 < c.rc2)) continue;
+      const bool part = !SPECIES && (tab.psig != nullptr || tab.peps != nullptr);
+      const PairCoef c = SPECIES ? sc[si * JMD_MAX_SPECIES + sp_clamp(__ldg(a.species + j), tab.nsp)]
+                                 : (part ? particle_coef(tab, (int)atom, j) : tab.c[0]);
+      if ((SPECIES || part) && !(r2 < c.rc2)) continue;
       float U, g, h;
       pair_eval<KIND, false>(r2, c, U, g, h);
       // F_i = -U'(r)/r (R_i - R_j)
@@ -252,9 +259,10 @@ __global__ void __launch_bounds__(256) k_pair_sparse(SparseArgs a, const __grid_
       float r2 = dx * dx;
       r2 = fmaf(dy, dy, r2);
       if (DIM == 3) r2 = fmaf(dz, dz, r2);
-      const PairCoef& c = SPECIES ? sc[sp_clamp(__ldg(a.species + i), tab.nsp) * JMD_MAX_SPECIES +
-                                       sp_clamp(__ldg(a.species + j), tab.nsp)]
-                                  : tab.c[0];
+      const bool part = !SPECIES && (tab.psig != nullptr || tab.peps != nullptr);
+      const PairCoef c = SPECIES ? sc[sp_clamp(__ldg(a.species + i), tab.nsp) * JMD_MAX_SPECIES +
+                                      sp_clamp(__ldg(a.species + j), tab.nsp)]
+                                 : (part ? particle_coef(tab, i, j) : tab.c[0]);
       if (r2 < c.rc2 && r2 > 0.f) {
         float U, g, h;
         pair_eval<KIND, false>(r2, c, U, g, h);
@@ -373,8 +381,12 @@ bool g_force_generic = false;
 
 }  // namespace
 
-int validate_pair(const jmd_pair* pp) {
+int validate_pair(const jmd_pair* pp, bool allow_particle) {
   JMD_REQUIRE(pp != nullptr, "pair parameters are null");
+  const bool particle = pp->particle_sigma != nullptr || pp->particle_epsilon != nullptr;
+  JMD_REQUIRE(allow_particle || !particle,
+              "per-particle parameters run on jmd_pair_forces (the generic pair kernels) only");
+  JMD_REQUIRE(!particle || pp->n_species == 0, "per-particle parameters exclude species matrices");
   JMD_REQUIRE(pp->kind >= 0 && pp->kind <= 3, "unknown pair potential");
   JMD_REQUIRE(pp->n_species >= 0 && pp->n_species <= JMD_MAX_SPECIES, "n_species out of range");
   int S = pp->n_species > 0 ? pp->n_species : 1;
@@ -412,11 +424,12 @@ int jmd_pair_forces(const jmd_pair* pp, const jmd_space* space, int32_t format,
                     const int32_t* nbr_count, float* force, int64_t force_stride, double* energy,
                     float* per_atom_energy, double* virial, void* workspace,
                     size_t workspace_bytes, void* stream) {
-  int e = validate_pair(pp);
+  int e = validate_pair(pp, true);
   if (e) return e;
   JMD_REQUIRE(space && (space->dim == 2 || space->dim == 3), "bad space");
   JMD_REQUIRE(n >= 0 && n < INT32_MAX, "atom count out of range");
   JMD_REQUIRE(format >= 0 && format <= 2, "unknown format");
+  const bool particle = pp->particle_sigma != nullptr || pp->particle_epsilon != nullptr;
   JMD_REQUIRE(!(format == JMD_ORDERED_SPARSE && per_atom_energy),
               "per-particle energies are not defined for OrderedSparse lists");
   JMD_REQUIRE(idx_width >= 0 && idx_ld >= idx_width, "idx_ld must be >= idx_width");
@@ -456,7 +469,7 @@ int jmd_pair_forces(const jmd_pair* pp, const jmd_space* space, int32_t format,
     a.counter = w.counter;
     a.totals = w.totals;
     a.geo = geo;
-    const bool fast = !g_force_generic &&
+    const bool fast = !g_force_generic && !particle &&
                       dense2_applicable(position, pos_stride, idx, idx_ld, force, force_stride);
     // lanes per atom of the kernel that will run (the packed path uses its
     // own width, 8 for Morse): one partial per block must fit the workspace

@@ -34,10 +34,43 @@ struct PairTable {
   float rc2_max;   // largest rc2 in the table
   float pad;
   PairCoef c[JMD_MAX_SPECIES * JMD_MAX_SPECIES];
+  // per-particle parameters (generic kernels only): per-atom sigma / epsilon
+  // combined as 0.5 (p_i + p_j); maxs = max sigma, the cutoff scale
+  const float* psig;
+  const float* peps;
+  int per_pair_cutoff;
+  float maxs, r_onset, r_cutoff;
 };
 
 PairTable make_pair_table(const jmd_pair& pp);
-int validate_pair(const jmd_pair* pp);
+// allow_particle: the caller's kernels read per-particle parameters
+int validate_pair(const jmd_pair* pp, bool allow_particle = false);
+
+// Coefficients of pair (i, j) under per-particle parameters: the reference's
+// 0.5 (p_i + p_j) in float32 (smap.py:704-713), then the table's derived
+// values for that sigma / epsilon (make_pair_table).
+__device__ __forceinline__ PairCoef particle_coef(const PairTable& t, int i, int j) {
+  PairCoef c = t.c[0];
+  if (t.peps) c.eps = 0.5f * (__ldg(t.peps + i) + __ldg(t.peps + j));
+  if (t.psig) {
+    const float sig = 0.5f * (__ldg(t.psig + i) + __ldg(t.psig + j));
+    c.sig2 = sig * sig;
+    c.inv_sig = 1.0f / sig;
+    c.pad = sig;
+    if (t.kind == JMD_SOFT_SPHERE) {
+      c.rc2 = sig * sig;
+      c.ro2 = c.rc2;
+    } else if (t.per_pair_cutoff && t.maxs > 0.f) {
+      const float ro = t.r_onset * sig / t.maxs, rc = t.r_cutoff * sig / t.maxs;
+      c.ro2 = ro * ro;
+      c.rc2 = rc * rc;
+      const double den = (double)c.rc2 - (double)c.ro2;
+      c.inv_den = den > 0 ? (float)(1.0 / (den * den * den)) : 0.f;
+      if (t.kind == JMD_LJ_TRUNCATED) c.ro2 = c.rc2;
+    }
+  }
+  return c;
+}
 
 // Packed float4 Dense path (fused.cu).
 int dense_tpa();

@@ -742,6 +742,22 @@ def last_run_status(state) -> int:
     return 0 if b is None else int(b.seg_status)
 
 
+def _run_loop(apply_fn, state, neighbor, n_steps, neighbor_fn, max_reallocations):
+    """nbrs = nbrs.update(x); state = apply_fn(state, neighbor=nbrs), n_steps
+    times, repeated from the start with a re-allocated list on overflow."""
+    snapshot = state.copy() if neighbor_fn is not None else None
+    for attempt in range(max_reallocations + 1):
+        for _ in range(int(n_steps)):
+            neighbor = neighbor.update(state.position)
+            state = apply_fn(state, neighbor=neighbor)
+        if neighbor_fn is None or not bool(neighbor.did_buffer_overflow):
+            return state, neighbor
+        state = snapshot.copy()
+        extra = (attempt + 1) * max(1, neighbor.max_occupancy // 8)
+        neighbor = neighbor_fn.allocate(state.position, extra_capacity=extra)
+    raise RuntimeError('neighbour list kept overflowing after re-allocation')
+
+
 def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bool = True,
         max_reallocations: int = 4, sort=None, layout=None, lazy_list: bool = True):
     """Runs the reference loop body ``n_steps`` times on the device:
@@ -763,6 +779,11 @@ def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bo
     autotuned or default cells per segment), an int (that many cells per
     segment), or 'tiled' (the tiled int32 list).  Returns (state, neighbor)."""
     st = apply_fn.stepper
+    e = st.energy_fn
+    if isinstance(e, smap.PairNeighborListEnergy) and e.has_particle_arrays():
+        # per-particle parameter arrays: the generic pair kernels, step by
+        # step -- the reference's own loop (partition.py:841-854)
+        return _run_loop(apply_fn, state, neighbor, n_steps, neighbor_fn, max_reallocations)
     nvt = isinstance(state, NVTNoseHooverState)
     if not (isinstance(state, NVEState) or nvt):
         raise NotImplementedError('run() drives NVE and Nose-Hoover NVT states')

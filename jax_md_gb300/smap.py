@@ -78,14 +78,39 @@ def _per_particle_table(params: dict):
         raise ValueError('per-particle parameter arrays must have one entry per atom')
     uniq, inv = np.unique(np.stack(cols, 1), axis=0, return_inverse=True)
     if len(uniq) > N.MAX_SPECIES:
-        raise NotImplementedError(f'per-particle parameters with more than {N.MAX_SPECIES} distinct '
-                                  'values are not supported by the pair kernels (they are mapped '
-                                  'onto species)')
+        # continuous per-particle values: the generic pair kernels combine
+        # them per pair (jmd_pair.particle_sigma / particle_epsilon)
+        if 'alpha' in keys:
+            raise NotImplementedError('per-particle alpha arrays with more than '
+                                      f'{N.MAX_SPECIES} distinct values are not supported by the '
+                                      'pair kernels')
+        return _Continuous({k: c for k, c in zip(keys, cols)})
     out = dict(params)
     for c, k in enumerate(keys):
         v = uniq[:, c]
         out[k] = (np.float32(0.5) * (v[:, None] + v[None, :])).astype(np.float64)
     return out, np.asarray(inv).reshape(-1).astype(np.int32), len(uniq)
+
+
+class _Continuous:
+    """Per-particle sigma / epsilon arrays with more distinct values than the
+    species table holds: passed to the kernels as per-atom arrays."""
+
+    def __init__(self, host: dict):
+        self.host = host          # name -> float32 [N]
+        self.device = {}          # (name, device) -> tensor
+
+    @property
+    def n(self):
+        return next(iter(self.host.values())).shape[0]
+
+    def tensor(self, name, device):
+        key = (name, str(device))
+        t = self.device.get(key)
+        if t is None:
+            t = torch.as_tensor(self.host[name]).to(device=device, dtype=torch.float32).contiguous()
+            self.device[key] = t
+        return t
 
 
 def make_pair_struct(fn, params: dict, n_species: int) -> N.Pair:
@@ -215,6 +240,11 @@ class PairNeighborListEnergy:
             raise NotImplementedError('reduce_axis must be None, (1,) or (0, 1) for the pair kernels')
 
     # -- plumbing ---------------------------------------------------------
+    def has_particle_arrays(self) -> bool:
+        """Per-particle parameter arrays too varied for the species table:
+        only the generic pair kernels take them (not the device engine)."""
+        return isinstance(self._pp_static, _Continuous)
+
     def _resolve(self, R, dynamic):
         species = dynamic.get('species', self.species)
         params = dict(self.params)
@@ -224,6 +254,25 @@ class PairNeighborListEnergy:
                 params[k] = dynamic[k]
                 overridden = True
         pp = _per_particle_table(params) if overridden else self._pp_static
+        if isinstance(pp, _Continuous):
+            if species is not None and not isinstance(species, int):
+                raise NotImplementedError('per-particle parameter arrays together with a species '
+                                          'array are not supported by the pair kernels')
+            if pp.n != R.shape[0]:
+                raise ValueError('per-particle parameter arrays must have one entry per atom')
+            scal = dict(params)
+            for k, v in pp.host.items():
+                # the table's scalar entry: max sigma (the cutoff scale), or
+                # any epsilon (replaced per pair)
+                scal[k] = float(np.max(v)) if k == 'sigma' else 1.0
+            pair = make_pair_struct(self.fn, scal, 0)
+            if 'sigma' in pp.host:
+                pair.particle_sigma = pp.tensor('sigma', R.device).data_ptr()
+            if 'epsilon' in pp.host:
+                pair.particle_epsilon = pp.tensor('epsilon', R.device).data_ptr()
+            # keep the device arrays alive past the asynchronous launch
+            self._pp_live = pp
+            return None, pair
         if pp is not None:
             if species is not None and not isinstance(species, int):
                 raise NotImplementedError('per-particle parameter arrays together with a species '

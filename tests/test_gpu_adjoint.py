@@ -130,12 +130,18 @@ def _oracle_loss(R0, P0, L, species, sig, eps, steps, dt=0.005, msd_w=0.1):
     return E / len(R) + msd_w * float((d * d).sum(-1).mean())
 
 
-@pytest.mark.parametrize('k', [10, None], ids=['checkpointed', 'stored'])
-def test_trajectory_gradient_matches_fd(cuda, k):
+# Float32 trajectories of this Kob-Andersen liquid are chaotic: the adjoint
+# agrees with central differences of the float64 oracle to 5e-5 at 10 and 20
+# steps, to 1.2e-4 at 30, and drifts to ~5e-3 by 50 steps (the sigma_AB entry;
+# the others stay near 1e-4), which is the float32 floor rather than an
+# adjoint error. The 20-step case holds the 1e-4 bar; the 30-step cases hold
+# 1e-3.
+@pytest.mark.parametrize('k,steps,tol', [(10, 30, 1e-3), (None, 30, 1e-3), (10, 20, 1e-4)],
+                         ids=['checkpointed', 'stored', 'checkpointed-20-steps-1e-4'])
+def test_trajectory_gradient_matches_fd(cuda, k, steps, tol):
     from jax_md_gb300 import adjoint
     R, P, L, species = _ka(cuda)
     disp, shift, nfn, efn = _energy(cuda, L, species)
-    steps = 30
     Rt = torch.tensor(R, device=cuda)
     nb = nfn.allocate(Rt)
     traj = adjoint.nve_trajectory(efn, nfn, shift, 0.005, steps, checkpoint_every=k)
@@ -163,7 +169,7 @@ def test_trajectory_gradient_matches_fd(cuda, k):
                     (sig if mat == 'sigma' else eps)[a, b] += sgn * hh
                     lp.append(_oracle_loss(R, P, L, species, sig, eps, steps))
                 fd = (lp[0] - lp[1]) / (2 * hh)
-                assert abs(g[a, b] - fd) <= 1e-3 * max(abs(fd), 1e-2), (mat, a, b, g[a, b], fd)
+                assert abs(g[a, b] - fd) <= tol * max(abs(fd), 1e-2), (mat, a, b, g[a, b], fd)
     # initial positions: directional derivative along a random direction
     v = np.random.default_rng(5).standard_normal(R.shape)
     v /= np.linalg.norm(v)
@@ -172,7 +178,7 @@ def test_trajectory_gradient_matches_fd(cuda, k):
     lm = _oracle_loss((R - eps_r * v).astype(np.float64), P, L, species, SIG, EPS, steps)
     fd = (lp - lm) / (2 * eps_r)
     ad = float((R0.grad.cpu().numpy() * v).sum())
-    assert abs(ad - fd) <= 1e-3 * max(abs(fd), 1e-2), (ad, fd)
+    assert abs(ad - fd) <= tol * max(abs(fd), 1e-2), (ad, fd)
 
 
 @pytest.mark.parametrize('k', [10, None], ids=['checkpointed', 'stored'])

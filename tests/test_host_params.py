@@ -48,11 +48,31 @@ def test_resolve_maps_static_and_dynamic_arrays():
     assert species.tolist() == [0, 0, 1, 1] and abs(p.sigma[0][1] - 1.1) < 1e-6
 
 
+def test_continuous_per_particle_arrays_go_to_the_generic_kernels():
+    """More distinct per-particle values than the species table holds: the
+    pair struct carries per-atom arrays (sigma[0][0] = max sigma, the cutoff
+    scale), no species, and the energy reports it (the engine falls back to
+    the per-step loop)."""
+    disp, _ = space.periodic(10.0)
+    sig = np.linspace(1.0, 1.5, 12)
+    eps = np.linspace(0.5, 2.0, 12)
+    _, efn = energy.soft_sphere_neighbor_list(disp, 10.0, sigma=sig, epsilon=eps,
+                                              format=partition.Dense)
+    assert efn.has_particle_arrays()
+    species, pair = efn._resolve(torch.zeros((12, 2)), {})
+    assert species is None and pair.n_species == 0
+    assert pair.particle_sigma and pair.particle_epsilon
+    assert abs(pair.sigma[0][0] - 1.5) < 1e-6
+    # arrays the species table can hold stay on the species path
+    _, efn2 = energy.soft_sphere_neighbor_list(disp, 10.0, sigma=np.array([1.0, 1.4, 1.0]),
+                                               format=partition.Dense)
+    assert not efn2.has_particle_arrays()
+    with pytest.raises(NotImplementedError, match='alpha'):
+        smap._per_particle_table({'alpha': np.linspace(2.0, 3.0, 12)})
+
+
 def test_unsupported_per_particle_cases():
     disp, _ = space.periodic(10.0)
-    with pytest.raises(NotImplementedError, match='more than 8'):   # at construction
-        energy.soft_sphere_neighbor_list(disp, 10.0, sigma=np.linspace(1.0, 1.5, 12),
-                                         format=partition.Dense)
     _, efn = energy.soft_sphere_neighbor_list(disp, 10.0, sigma=np.array([1.0, 1.4, 1.0]),
                                               format=partition.Dense)
     with pytest.raises(ValueError, match='one entry per atom'):
