@@ -57,12 +57,20 @@ extern "C" {
 
 #define JMD_MAX_SPECIES 8
 
-/* Geometry: space.periodic (jax_md/space.py:275-329) or space.free (:258-272). */
+/* Geometry: space.periodic (jax_md/space.py:275-329), space.free (:258-272)
+ * or space.periodic_general with fractional coordinates (:332-468). */
 typedef struct {
   int32_t dim;       /* 2 or 3 */
-  int32_t periodic;  /* 1: minimum-image displacement and wrapped shift; 0: free */
-  float box[3];      /* side lengths; box[2] unused for dim 2 */
+  int32_t periodic;  /* 1: minimum-image displacement and wrapped shift; 0: free;
+                        JMD_GENERAL_CELL: positions u in the unit cube, displacement
+                        T d_U(u, v) and shift mod(u + T^-1 dR, 1) */
+  float box[3];      /* side lengths; box[2] unused for dim 2; 1 for a general cell */
+  float cell[9];     /* JMD_GENERAL_CELL: T, row-major 3x3 (upper triangular, the
+                        reference's is_box_valid, partition.py:676-681) */
+  float inv_cell[9]; /* JMD_GENERAL_CELL: T^-1, row-major */
 } jmd_space;
+
+#define JMD_GENERAL_CELL 2
 
 /* Static description of a neighbour list, the C mirror of the static fields
  * of jax_md's NeighborList (partition.py:684-737) plus the cell grid from

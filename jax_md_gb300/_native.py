@@ -25,8 +25,12 @@ CELL_SIZE_TOO_SMALL = 4
 MALFORMED_BOX = 8
 
 
+GENERAL_CELL = 2  # jmd_space.periodic of a general cell (JMD_GENERAL_CELL)
+
+
 class Space(C.Structure):
-    _fields_ = [('dim', C.c_int32), ('periodic', C.c_int32), ('box', C.c_float * 3)]
+    _fields_ = [('dim', C.c_int32), ('periodic', C.c_int32), ('box', C.c_float * 3),
+                ('cell', C.c_float * 9), ('inv_cell', C.c_float * 9)]
 
 
 class NList(C.Structure):

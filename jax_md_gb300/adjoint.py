@@ -241,38 +241,69 @@ def nve_trajectory(energy_fn, neighbor_fn, shift_fn, dt: float, n_steps: int,
 # and finally xbar += VJP(x_0, h qbar_0).
 
 
+def _nvt_steps(tf, st, nb, dyn, count, scale, tape=None):
+    """``count`` steps of the Nose-Hoover integrator on ``st`` in place (the
+    loop of NvtTrajectory's forward); with ``tape`` each step's
+    (x_k, p_k, chain_a, s1, r, chain_b, s2) is appended."""
+    init, apply = tf.integrator
+    stepper, chain_fns = apply.stepper, apply.chain_fns
+    P = st.momentum
+    dim = P.shape[1]
+    for _ in range(count):
+        nb = nb.update(st.position)
+        if tape is not None:
+            x_k, p_k = st.position.clone(), st.momentum.clone()
+            chain_a = st.chain.buffer.clone()
+        chain_fns.half_step(st.chain, scale, update_mass=True)
+        s1 = scale.clone() if tape is not None else None
+        stepper.velocity_verlet(st, p_scale=scale, neighbor=nb, **dyn)
+        r = st.momentum.clone() if tape is not None else None
+        quantity._ke_f64(st.momentum, st.mass, out=st.chain.buffer[64])
+        chain_b = st.chain.buffer.clone() if tape is not None else None
+        chain_fns.half_step(st.chain, scale, ke=None)
+        N.check(N.lib().jmd_scale_momentum(P.data_ptr(), P.stride(0), P.shape[0], dim,
+                                           scale.data_ptr(), N.stream_ptr()), 'scale_momentum')
+        if tape is not None:
+            tape.append((x_k, p_k, chain_a, s1, r, chain_b, scale.clone()))
+    return nb
+
+
+def _nvt_checkpoint(st):
+    return (st.position.clone(), st.momentum.clone(), st.force.clone(), st.chain.buffer.clone())
+
+
+def _nvt_restore(st, ck):
+    st.position.copy_(ck[0])
+    st.momentum.copy_(ck[1])
+    st.force.copy_(ck[2])
+    st.chain.buffer.copy_(ck[3])
+
+
 class _NvtTrajectoryFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, R0, P0, sigma, epsilon, cfg):
         tf, nbrs, dyn = cfg
         init, apply = tf.integrator
-        stepper, chain_fns = apply.stepper, apply.chain_fns
         R0d, P0d = R0.detach(), P0.detach()
-        dim = R0d.shape[1]
         nb = rebuild_now(tf.neighbor_fn, nbrs, simulate._rows4(R0d))
         st = init(0, R0d, mass=tf.mass, momenta=P0d.clone(), neighbor=nb, **dyn)
         scale = torch.empty((), dtype=torch.float64, device=R0d.device)
-        P = st.momentum
-        tape = []
-        for _ in range(tf.n_steps):
-            nb = nb.update(st.position)
-            x_k, p_k = st.position.clone(), st.momentum.clone()
-            chain_a = st.chain.buffer.clone()
-            chain_fns.half_step(st.chain, scale, update_mass=True)
-            s1 = scale.clone()
-            stepper.velocity_verlet(st, p_scale=scale, neighbor=nb, **dyn)
-            r = st.momentum.clone()
-            quantity._ke_f64(st.momentum, st.mass, out=st.chain.buffer[64])
-            chain_b = st.chain.buffer.clone()
-            chain_fns.half_step(st.chain, scale, ke=None)
-            s2 = scale.clone()
-            N.check(N.lib().jmd_scale_momentum(P.data_ptr(), P.stride(0), P.shape[0], dim,
-                                               scale.data_ptr(), N.stream_ptr()), 'scale_momentum')
-            tape.append((x_k, p_k, chain_a, s1, r, chain_b, s2))
+        seg = tf.segment_length()
+        tape, checkpoints = [], []
+        done = 0
+        while done < tf.n_steps:
+            count = min(seg, tf.n_steps - done)
+            if seg < tf.n_steps:
+                # a segment starts from a fresh list, so its replay in the
+                # reverse pass repeats these steps bit for bit
+                nb = rebuild_now(tf.neighbor_fn, nb, st.position)
+                checkpoints.append(_nvt_checkpoint(st))
+            nb = _nvt_steps(tf, st, nb, dyn, count, scale, tape if seg >= tf.n_steps else None)
+            done += count
         if bool(nb.did_buffer_overflow):
             raise RuntimeError('neighbour list overflowed during the trajectory; allocate it '
                                'with more capacity')
-        ctx.cfg = (tf, nb, dyn, tape, st.position.clone(), st.chain, st.mass)
+        ctx.cfg = (tf, nb, dyn, tape, checkpoints, seg, st, st.position.clone())
         ctx.has = (sigma is not None, epsilon is not None)
         ctx.save_for_backward(sigma if sigma is not None else torch.empty(0),
                               epsilon if epsilon is not None else torch.empty(0))
@@ -280,7 +311,8 @@ class _NvtTrajectoryFn(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, gx, gp):
-        tf, nb, dyn, tape, x_n, chain, mass = ctx.cfg
+        tf, nb, dyn, full_tape, checkpoints, seg, st, x_n = ctx.cfg
+        chain, mass = st.chain, st.mass
         sigma, epsilon = ctx.saved_tensors
         sigma = sigma if ctx.has[0] else None
         epsilon = epsilon if ctx.has[1] else None
@@ -303,6 +335,7 @@ class _NvtTrajectoryFn(torch.autograd.Function):
         pxibar = torch.zeros(16, dtype=torch.float64, device=dev)
         pxibar1 = torch.zeros(16, dtype=torch.float64, device=dev)
         kebar = torch.zeros((), dtype=torch.float64, device=dev)
+        scale = torch.empty((), dtype=torch.float64, device=dev)
         L = N.lib()
 
         def chain_vjp(chain_in, update_mass, cot_p, cot_s, out_p):
@@ -319,22 +352,38 @@ class _NvtTrajectoryFn(torch.autograd.Function):
                                    **dyn)
 
         pending = None
-        for k in range(len(tape) - 1, -1, -1):
-            x_k, p_k, chain_a, s1, r, chain_b, s2 = tape[k]
-            x1 = tape[k + 1][0] if k + 1 < len(tape) else x_n
-            sbar2 = (pbar.double() * r.double()).sum()
-            rbar = pbar * s2.float()
-            chain_vjp(chain_b, 0, pxibar, sbar2, pxibar1)
-            rbar = rbar + (kebar.float() * r) * inv_m
-            lam = h * (rbar if pending is None else rbar + pending)
-            vjp_at(x1, lam)
-            qbar = rbar + (dt * inv_m) * xbar
-            sbar1 = (qbar.double() * p_k.double()).sum()
-            pbar = qbar * s1.float()
-            chain_vjp(chain_a, 1, pxibar1, sbar1, pxibar)
-            pbar = pbar + (kebar.float() * p_k) * inv_m
-            pending = qbar
-        vjp_at(tape[0][0] if tape else x_n, h * pending if pending is not None else
+        # segments in reverse; a checkpointed segment is replayed from its
+        # checkpoint to rebuild its tape
+        starts = list(range(0, tf.n_steps, seg)) if checkpoints else [0]
+        x_end = x_n
+        x_first = x_n
+        for si in range(len(starts) - 1, -1, -1):
+            if checkpoints:
+                _nvt_restore(st, checkpoints[si])
+                nb = rebuild_now(tf.neighbor_fn, nb, st.position)
+                tape = []
+                nb = _nvt_steps(tf, st, nb, dyn, min(seg, tf.n_steps - starts[si]), scale, tape)
+            else:
+                tape = full_tape
+            for k in range(len(tape) - 1, -1, -1):
+                x_k, p_k, chain_a, s1, r, chain_b, s2 = tape[k]
+                x1 = tape[k + 1][0] if k + 1 < len(tape) else x_end
+                sbar2 = (pbar.double() * r.double()).sum()
+                rbar = pbar * s2.float()
+                chain_vjp(chain_b, 0, pxibar, sbar2, pxibar1)
+                rbar = rbar + (kebar.float() * r) * inv_m
+                lam = h * (rbar if pending is None else rbar + pending)
+                vjp_at(x1, lam)
+                qbar = rbar + (dt * inv_m) * xbar
+                sbar1 = (qbar.double() * p_k.double()).sum()
+                pbar = qbar * s1.float()
+                chain_vjp(chain_a, 1, pxibar1, sbar1, pxibar)
+                pbar = pbar + (kebar.float() * p_k) * inv_m
+                pending = qbar
+            if tape:
+                x_end = tape[0][0].clone()
+                x_first = x_end
+        vjp_at(x_first, h * pending if pending is not None else
                torch.zeros((n, dim), dtype=torch.float32, device=dev))
         gs, ge = _bins_to_grads(bins, None, sigma, epsilon)
         return xbar.contiguous(), pbar.contiguous(), gs, ge, None
@@ -346,10 +395,14 @@ class NvtTrajectory:
     with respect to R0, P0 and sigma / epsilon tensors that require grad,
     through the reverse pass of the chain (jmd_nhc_half_step_vjp) and of the
     Verlet step (jmd_pair_force_vjp).  Every step is recorded (positions,
-    momenta and the chain), so memory grows with n_steps."""
+    momenta and the chain) when ``checkpoint_every`` is None, so memory grows
+    with n_steps; with ``checkpoint_every=k`` only (position, momentum, force,
+    chain) at every k-th step is kept and each k-step segment is replayed
+    (from a forced list rebuild, as in the forward) before its reverse pass,
+    so memory is O(n_steps / k + k) states at the price of one extra forward."""
 
     def __init__(self, energy_fn, neighbor_fn, shift_fn, dt, kT, n_steps, chain_length=5,
-                 chain_steps=2, sy_steps=3, tau=None, mass=1.0):
+                 chain_steps=2, sy_steps=3, tau=None, mass=1.0, checkpoint_every=None):
         if not isinstance(energy_fn, smap.PairNeighborListEnergy):
             raise NotImplementedError('nvt_trajectory needs a neighbour-list energy from '
                                       'jax_md_gb300.energy')
@@ -363,8 +416,14 @@ class NvtTrajectory:
         self.chain_length, self.chain_steps, self.sy_steps = (int(chain_length), int(chain_steps),
                                                               int(sy_steps))
         self.mass = mass
+        self.checkpoint_every = checkpoint_every
         self.integrator = simulate.nvt_nose_hoover(energy_fn, shift_fn, dt, kT, chain_length,
                                                    chain_steps, sy_steps, tau)
+
+    def segment_length(self):
+        if self.checkpoint_every is None:
+            return self.n_steps
+        return max(1, min(int(self.checkpoint_every), self.n_steps))
 
     def __call__(self, R0, P0, nbrs, sigma=None, epsilon=None):
         if nbrs.format is not partition.Dense:
@@ -380,7 +439,7 @@ class NvtTrajectory:
 
 def nvt_trajectory(energy_fn, neighbor_fn, shift_fn, dt: float, kT: float, n_steps: int,
                    chain_length: int = 5, chain_steps: int = 2, sy_steps: int = 3, tau=None,
-                   mass=1.0) -> NvtTrajectory:
+                   mass=1.0, checkpoint_every: Optional[int] = None) -> NvtTrajectory:
     """Differentiable Nose-Hoover NVT run (see NvtTrajectory)."""
     return NvtTrajectory(energy_fn, neighbor_fn, shift_fn, dt, kT, n_steps, chain_length,
-                         chain_steps, sy_steps, tau, mass)
+                         chain_steps, sy_steps, tau, mass, checkpoint_every)

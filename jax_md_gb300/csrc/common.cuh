@@ -54,20 +54,43 @@ struct Carver {
 // ------------------------------------------------------------- geometry ----
 struct Geo {
   int dim;
-  int periodic;
+  int periodic;  // nonzero: minimum image over L (the unit cube for a general cell)
+  int general;   // space.periodic_general, fractional coordinates
   float L[3];
   float halfL[3];
+  float T[6];    // upper-triangular cell: xx xy xz yy yz zz
+  float Ti[6];   // its inverse, same layout
 };
 
 inline Geo make_geo(const jmd_space& s) {
   Geo g;
   g.dim = s.dim;
   g.periodic = s.periodic;
+  g.general = s.periodic == JMD_GENERAL_CELL;
   for (int d = 0; d < 3; ++d) {
-    g.L[d] = s.box[d];
-    g.halfL[d] = 0.5f * s.box[d];
+    g.L[d] = g.general ? 1.f : s.box[d];
+    g.halfL[d] = 0.5f * g.L[d];
+  }
+  const int up[6] = {0, 1, 2, 4, 5, 8};
+  for (int k = 0; k < 6; ++k) {
+    g.T[k] = g.general ? s.cell[up[k]] : 0.f;
+    g.Ti[k] = g.general ? s.inv_cell[up[k]] : 0.f;
   }
   return g;
+}
+
+// v <- M v for an upper-triangular M in the Geo layout (space.transform,
+// space.py:125-148, x = T u).  In 2D only xx, xy, yy enter.
+template <int DIM>
+__device__ __forceinline__ void cell_apply(const float* m, float& x, float& y, float& z) {
+  if (DIM == 3) {
+    x = fmaf(m[0], x, fmaf(m[1], y, m[2] * z));
+    y = fmaf(m[3], y, m[4] * z);
+    z = m[5] * z;
+  } else {
+    x = fmaf(m[0], x, m[1] * y);
+    y = m[3] * y;
+  }
 }
 
 // Minimum-image displacement a - b along one axis for coordinates inside the

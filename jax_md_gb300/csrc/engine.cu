@@ -52,6 +52,9 @@ int validate_sys(const jmd_nve_system& s) {
               "the engine's kernels take scalar or species parameters (per-particle parameters "
               "run on jmd_pair_forces)");
   JMD_REQUIRE(s.space.dim == 2 || s.space.dim == 3, "dim must be 2 or 3");
+  JMD_REQUIRE(s.space.periodic != JMD_GENERAL_CELL && s.nlist.space.periodic != JMD_GENERAL_CELL,
+              "the engine runs space.periodic / space.free systems (general cells run step by "
+              "step on jmd_pair_forces and the integrator kernels)");
   JMD_REQUIRE(s.nlist.format == JMD_DENSE, "the engine runs Dense neighbour lists");
   JMD_REQUIRE(s.position && s.position_alt && s.momentum && s.force && s.idx &&
                   s.reference_position && s.error_code && s.occupancy && s.rebuild_flag,
@@ -759,6 +762,7 @@ int jmd_nve_fused_step_segment(const jmd_pair* pair, const jmd_space* space, con
                                int32_t* rebuild_flag, void* workspace, size_t workspace_bytes,
                                int32_t* seg_status, void* stream) {
   JMD_REQUIRE(pair && space && nl, "null descriptor");
+  JMD_REQUIRE(space->periodic != JMD_GENERAL_CELL, "the segment kernels take orthorhombic boxes");
   JMD_REQUIRE(n > 0 && n < INT32_MAX, "atom count out of range");
   JMD_REQUIRE(position && position_next && momentum && seg_list && seg_status, "null buffer");
   JMD_REQUIRE(position != position_next, "position and position_next must differ");

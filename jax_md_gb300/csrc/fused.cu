@@ -377,6 +377,8 @@ int jmd_nve_fused_step(const jmd_pair* pp, const jmd_space* space, const float* 
   int e = validate_pair(pp);
   if (e) return e;
   JMD_REQUIRE(space && (space->dim == 2 || space->dim == 3), "bad space");
+  JMD_REQUIRE(space->periodic != JMD_GENERAL_CELL,
+              "the fused kernels take orthorhombic boxes (general cells: jmd_pair_forces)");
   JMD_REQUIRE(position != position_next, "position and position_next must differ");
   JMD_REQUIRE(dense2_applicable(position, 4, idx, idx_ld, position_next, 4) &&
                   is_vec4(momentum, 4) && (reference_position == nullptr || is_vec4(reference_position, 4)),
@@ -414,6 +416,8 @@ int jmd_force_kick(const jmd_pair* pp, const jmd_space* space, const float* posi
   int e = validate_pair(pp);
   if (e) return e;
   JMD_REQUIRE(space && (space->dim == 2 || space->dim == 3), "bad space");
+  JMD_REQUIRE(space->periodic != JMD_GENERAL_CELL,
+              "the fused kernels take orthorhombic boxes (general cells: jmd_pair_forces)");
   JMD_REQUIRE(dense2_applicable(position, 4, idx, idx_ld, force, 4) && is_vec4(momentum, 4),
               "force_kick needs 16-byte aligned float4 rows and an even, 8-byte aligned idx");
   if (n <= 0) return JMD_OK;

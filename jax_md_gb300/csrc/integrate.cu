@@ -36,6 +36,7 @@ __global__ void k_position(float* x, int64_t xs, const float* p, int64_t ps, con
   float m = mass ? mass[i] : m0;
   // shift_fn(R, dt * p / m)  (simulate.py:184)
   float dx = dt * q.x / m, dy = dt * q.y / m, dz = dt * q.z / m;
+  if (g.general) cell_apply<DIM>(g.Ti, dx, dy, dz);  // dR lives in the cell (space.py:456)
   if (g.periodic) {
     r.x = wrap(r.x + dx, g.L[0]);
     r.y = wrap(r.y + dy, g.L[1]);
@@ -87,6 +88,7 @@ __global__ void k_kick_drift(KickDriftArgs a) {
     q.z = fmaf(h, f.z, q.z);
     float m = a.mass ? a.mass[i] : a.m0;
     float dx = a.dt * q.x / m, dy = a.dt * q.y / m, dz = a.dt * q.z / m;
+    if (a.g.general) cell_apply<DIM>(a.g.Ti, dx, dy, dz);
     if (a.g.periodic) {
       r.x = wrap(r.x + dx, a.g.L[0]);
       r.y = wrap(r.y + dy, a.g.L[1]);
@@ -104,6 +106,7 @@ __global__ void k_kick_drift(KickDriftArgs a) {
       float ey = a.g.periodic ? min_image(r.y, c.y, a.g.L[1], a.g.halfL[1]) : r.y - c.y;
       float ez = 0.f;
       if (DIM == 3) ez = a.g.periodic ? min_image(r.z, c.z, a.g.L[2], a.g.halfL[2]) : r.z - c.z;
+      if (a.g.general) cell_apply<DIM>(a.g.T, ex, ey, ez);
       over = ex * ex + ey * ey + ez * ez > a.thr2;
     }
   }
@@ -200,7 +203,8 @@ __global__ void k_fire_kick_drift(float4* x, float4* p, const float4* f, const f
   q.y = fmaf(h, ff.y, q.y);
   q.z = fmaf(h, ff.z, q.z);
   const float m = mass ? mass[i] : m0;
-  const float dx = dt * q.x / m, dy = dt * q.y / m, dz = dt * q.z / m;
+  float dx = dt * q.x / m, dy = dt * q.y / m, dz = dt * q.z / m;
+  if (g.general) cell_apply<DIM>(g.Ti, dx, dy, dz);
   if (g.periodic) {
     r.x = wrap(r.x + dx, g.L[0]);
     r.y = wrap(r.y + dy, g.L[1]);

@@ -307,6 +307,7 @@ __device__ __forceinline__ float dist2(const float4& a, const float4& b, const G
     dx = min_image(a.x, b.x, g.L[0], g.halfL[0]);
     dy = min_image(a.y, b.y, g.L[1], g.halfL[1]);
     if (DIM == 3) dz = min_image(a.z, b.z, g.L[2], g.halfL[2]);
+    if (g.general) cell_apply<DIM>(g.T, dx, dy, dz);
   } else {
     dx = a.x - b.x;
     dy = a.y - b.y;
@@ -578,7 +579,9 @@ k_search_cells(const float* __restrict__ x, int64_t stride, Bins b, SearchArgs a
   cc[0] = c % a.grid.cps[0];
   cc[1] = (c / a.grid.cps[0]) % a.grid.cps[1];
   cc[2] = DIM == 3 ? c / (a.grid.cps[0] * a.grid.cps[1]) : 0;
-  bool frame = a.geo.periodic != 0;
+  // the shifted frame is a plain difference in box units; a general cell
+  // maps the unit-cube image through T, so it takes the exact path
+  bool frame = a.geo.periodic != 0 && !a.geo.general;
 #pragma unroll
   for (int d = 0; d < DIM; ++d) frame = frame && a.grid.cps[d] >= 4;
   const int geom = !a.geo.periodic ? S_PLAIN : (frame ? S_FRAME : S_EXACT);

@@ -469,7 +469,7 @@ int jmd_pair_forces(const jmd_pair* pp, const jmd_space* space, int32_t format,
     a.counter = w.counter;
     a.totals = w.totals;
     a.geo = geo;
-    const bool fast = !g_force_generic && !particle &&
+    const bool fast = !g_force_generic && !particle && !geo.general &&
                       dense2_applicable(position, pos_stride, idx, idx_ld, force, force_stride);
     // lanes per atom of the kernel that will run (the packed path uses its
     // own width, 8 for Morse): one partial per block must fit the workspace

@@ -212,6 +212,8 @@ __device__ __forceinline__ void displacement(const float4& a, const float4& b, c
       dy = min_image(a.y, b.y, g.L[1], g.halfL[1]);
       if (DIM == 3) dz = min_image(a.z, b.z, g.L[2], g.halfL[2]);
     }
+    // general cell: the unit-cube image mapped into the cell (space.py:430-431)
+    if (g.general) cell_apply<DIM>(g.T, dx, dy, dz);
   }
 }
 

@@ -187,6 +187,7 @@ int tl_validate(const jmd_pair* pp, const jmd_space* space, const float* x, cons
   int e = validate_pair(pp);
   if (e) return e;
   JMD_REQUIRE(space && (space->dim == 2 || space->dim == 3), "bad space");
+  JMD_REQUIRE(space->periodic != JMD_GENERAL_CELL, "the tiled kernels take orthorhombic boxes");
   JMD_REQUIRE(is_vec4(x, 4), "positions must be 16-byte aligned float4 rows");
   JMD_REQUIRE(tidx != nullptr && cnt != nullptr, "tiled list and counts are required");
   return JMD_OK;

@@ -12,8 +12,9 @@ Differences, by design:
     list it was called on, so an update costs no allocation and no host sync.
     The skin test of partition.py:1146-1154 runs on the device and gates the
     rebuild kernels through a device flag (the lax.cond).
-  * ``custom_mask_function`` and ``fractional_coordinates`` are not supported
-    (they raise NotImplementedError).
+  * ``custom_mask_function`` is not supported (it raises NotImplementedError);
+    ``fractional_coordinates`` bins the unit cube of a periodic_general cell
+    (upper-triangular cells, as the reference's is_box_valid requires).
 """
 from __future__ import annotations
 
@@ -140,8 +141,47 @@ def padded_rows(R: torch.Tensor) -> torch.Tensor:
     return buf[:, :d]
 
 
-def _space_struct(displacement, dim, box) -> N.Space:
+def fractional_cell_size(box, cutoff):
+    """partition.py:595-634 (_fractional_cell_size) in float32: the cell edge,
+    in units of the unit cube, whose perpendicular width in the cell T is at
+    least ``cutoff``."""
+    b = np.asarray(box.detach().cpu() if isinstance(box, torch.Tensor) else box, np.float32)
+    c = _f32(cutoff)
+    if b.ndim == 0 or b.size == 1 and b.ndim < 2:
+        return _f32(c / _f32(b.reshape(-1)[0]))
+    if b.ndim == 1:
+        return _f32(c / b.min())
+    if b.shape[0] == 1:
+        return _f32(_f32(1) / np.floor(b[0, 0] / c))
+    if b.shape[0] == 2:
+        xx, yy = b[0, 0], b[1, 1]
+        xy = _f32(b[0, 1] / yy)
+        nx = _f32(xx / np.sqrt(_f32(1) + xy * xy))
+        nmin = np.floor(min(nx, yy) / c)
+    elif b.shape[0] == 3:
+        xx, yy, zz = b[0, 0], b[1, 1], b[2, 2]
+        xy, xz, yz = _f32(b[0, 1] / yy), _f32(b[0, 2] / zz), _f32(b[1, 2] / zz)
+        nx = _f32(xx / np.sqrt(_f32(1) + xy * xy + (xy * yz - xz) ** 2))
+        ny = _f32(yy / np.sqrt(_f32(1) + yz * yz))
+        nmin = np.floor(min(nx, ny, zz) / c)
+    else:
+        raise ValueError(f'Expected box to be either 1-, 2-, or 3-dimensional found {b.shape[0]}')
+    nmin = _f32(1) if nmin == 0 else _f32(nmin)
+    return _f32(_f32(1) / nmin)
+
+
+def _cell_size(box, minimum_cell_size):
+    """partition.py:589-592: box / floor(box / minimum)."""
+    return _f32(_f32(box) / np.floor(_f32(box) / _f32(minimum_cell_size)))
+
+
+def _space_struct(displacement, dim, box, cell=None) -> N.Space:
+    """Kernel geometry of a list: ``box`` is the list's box argument; for a
+    periodic_general displacement ``cell`` (the ``box`` keyword of a call)
+    replaces the displacement's own cell."""
     geo = _space.geometry_of(displacement)
+    if isinstance(geo, _space.GeneralDisplacement):
+        return geo.space(dim, box=cell)
     s = N.Space()
     s.dim = dim
     s.periodic = 1 if geo.periodic else 0
@@ -295,6 +335,7 @@ class _Plan:
     flag: torch.Tensor         # int32 device rebuild flag (0 between calls)
     count: Optional[torch.Tensor]  # Dense per-atom counts (int32 [N])
     ld: int
+    space0: Optional[N.Space] = None  # the geometry without a box keyword
 
 
 @dataclasses.dataclass
@@ -411,9 +452,7 @@ def neighbor_list(displacement_or_metric, box, r_cutoff, dr_threshold=0.0,
     if custom_mask_function is not None:
         raise NotImplementedError('custom_mask_function is not supported by the GB300 neighbour '
                                   'list kernels')
-    if fractional_coordinates:
-        raise NotImplementedError('fractional_coordinates (periodic_general) is not implemented '
-                                  'by the kernels yet')
+    general = isinstance(_space.geometry_of(displacement_or_metric), _space.GeneralDisplacement)
     r_cutoff = float(torch.as_tensor(r_cutoff).max()) if isinstance(r_cutoff, torch.Tensor) else r_cutoff
     dr_threshold = float(dr_threshold)
     always_rebuild = dr_threshold == 0
@@ -423,13 +462,31 @@ def neighbor_list(displacement_or_metric, box, r_cutoff, dr_threshold=0.0,
     threshold_sq = _f32((_f32(dr_threshold) / _f32(2)) ** 2)
     fmt_code = {Dense: N.DENSE, Sparse: N.SPARSE, OrderedSparse: N.ORDERED_SPARSE}[format]
 
-    def make_nl(dim, use_cells, cell_cap, max_occ) -> N.NList:
+    def cell_grid(dim, cell_box):
+        """(use_cells, minimum cell size, binning box) as partition.py:1044-1054."""
+        if disable_cell_list:
+            return False, None, None
+        if fractional_coordinates:
+            fcs = fractional_cell_size(cell_box, cutoff)
+            return bool(fcs < _f32(1) / _f32(3)), fcs, 1.0
+        if general:
+            b = np.asarray(cell_box.detach().cpu() if isinstance(cell_box, torch.Tensor)
+                           else cell_box, np.float64)
+            if b.ndim == 2:
+                # a cell matrix binned without fractional coordinates: the
+                # reference's all(cutoff < box / 3) fails on its zero entries
+                return False, None, None
+        Lbox = np.array(_box_list(cell_box, dim), np.float32)
+        return bool(np.all(cutoff < Lbox / np.float32(3.0))), cutoff, cell_box
+
+    def make_nl(dim, use_cells, cell_cap, max_occ, cell_box=None) -> N.NList:
         nl = N.NList()
-        nl.space = _space_struct(displacement_or_metric, dim, box)
+        nl.space = _space_struct(displacement_or_metric, dim, box, cell_box)
         nl.cutoff_sq = float(cutoff_sq)
         nl.use_cell_list = 1 if use_cells else 0
         if use_cells:
-            cps, cs, _ = cell_dimensions(dim, box, cutoff)
+            _, mcs, bbox = cell_grid(dim, box if cell_box is None else cell_box)
+            cps, cs, _ = cell_dimensions(dim, bbox, mcs)
             for d in range(dim):
                 nl.cells_per_side[d] = int(cps[d])
                 nl.cell_size[d] = float(cs[d])
@@ -442,19 +499,19 @@ def neighbor_list(displacement_or_metric, box, r_cutoff, dr_threshold=0.0,
     run_build = _run_build
 
     def allocate_fn(position, extra_capacity: int = 0, **kwargs):
-        if 'box' in kwargs:
+        if 'box' in kwargs and not fractional_coordinates:
             raise ValueError('Neighbor list cannot accept a box keyword argument if '
                              'fractional_coordinates is not enabled.')
+        cell_box = kwargs.get('box')
         R, rs = _rows(position)
         n, dim = R.shape
         dev = R.device
-        Lbox = np.array(_box_list(box, dim), np.float32)
-        use_cells = (not disable_cell_list) and bool(np.all(cutoff < Lbox / np.float32(3.0)))
+        use_cells, mcs, _ = cell_grid(dim, box if cell_box is None else cell_box)
         cell_cap = None
         if use_cells:
-            probe = make_nl(dim, True, 1, 0)
+            probe = make_nl(dim, True, 1, 0, cell_box)
             cell_cap = int(_max_filling(R, rs, probe) * capacity_multiplier) + extra_capacity
-        nl = make_nl(dim, use_cells, cell_cap or 1, 2 ** 62)
+        nl = make_nl(dim, use_cells, cell_cap or 1, 2 ** 62, cell_box)
         L = N.lib()
         wsz = L.jmd_neighbor_list_workspace_bytes(C_ref(nl), n)
         plan = _Plan(nl=nl, dim=dim, n=n, threshold_sq=float(threshold_sq),
@@ -497,12 +554,13 @@ def neighbor_list(displacement_or_metric, box, r_cutoff, dr_threshold=0.0,
             plan.count = torch.zeros(n, dtype=torch.int32, device=dev)
         plan.ld = ld
         run_build(plan, R, rs, store, ld, error, ref, False)
+        plan.space0 = nl.space
         return NeighborList(idx, ref, PartitionError(error), cell_cap, max_occ, format,
-                            float(cutoff) if use_cells else None, plan if use_cells else None,
+                            float(mcs) if use_cells else None, plan if use_cells else None,
                             update_fn, plan)
 
     def update_fn(position, neighbors: NeighborList, **kwargs):
-        if 'box' in kwargs:
+        if 'box' in kwargs and not fractional_coordinates:
             raise ValueError('Neighbor list cannot accept a box keyword argument if '
                              'fractional_coordinates is not enabled.')
         plan = neighbors.plan
@@ -511,6 +569,23 @@ def neighbor_list(displacement_or_metric, box, r_cutoff, dr_threshold=0.0,
         R, rs = _rows(position)
         if R.shape[0] != plan.n or R.shape[1] != plan.dim:
             raise ValueError('position shape changed since allocate; call allocate again')
+        if 'box' in kwargs:
+            # partition.py:1123-1139: the new cell must not need larger cells
+            # than the list was binned with; distances use the new cell
+            new_box = kwargs['box']
+            if plan.nl.use_cell_list and neighbors.cell_size is not None:
+                cur = _cell_size(1.0, neighbors.cell_size)
+                new = _cell_size(1.0, fractional_cell_size(new_box, cutoff))
+                if new > cur:
+                    neighbors.error.code |= int(PEC.CELL_SIZE_TOO_SMALL)
+            M = _space.cell_matrix(new_box, plan.dim)
+            if not np.array_equal(np.triu(M), M):
+                neighbors.error.code |= int(PEC.MALFORMED_BOX)
+                raise ValueError('the kernels take upper-triangular cell matrices '
+                                 '(partition.is_box_valid)')
+            plan.nl.space = _space_struct(displacement_or_metric, plan.dim, box, new_box)
+        elif plan.space0 is not None:
+            plan.nl.space = plan.space0
         ref = neighbors.reference_position
         store = neighbors.idx
         L = N.lib()

@@ -146,8 +146,7 @@ def _shift_space(shift_fn, dim) -> N.Space:
     s.dim = dim
     periodic = isinstance(shift_fn, _space.Shift) and shift_fn.periodic and shift_fn.wrapped
     if isinstance(shift_fn, _space.GeneralShift):
-        raise NotImplementedError('the integrator kernels take space.periodic / space.free shifts; '
-                                  'periodic_general cells are not implemented by them yet')
+        return shift_fn.space(dim)
     if not isinstance(shift_fn, _space.Shift):
         raise NotImplementedError('the GB300 integrators need a shift_fn from jax_md_gb300.space')
     s.periodic = 1 if periodic else 0
@@ -783,6 +782,10 @@ def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bo
     if isinstance(e, smap.PairNeighborListEnergy) and e.has_particle_arrays():
         # per-particle parameter arrays: the generic pair kernels, step by
         # step -- the reference's own loop (partition.py:841-854)
+        return _run_loop(apply_fn, state, neighbor, n_steps, neighbor_fn, max_reallocations)
+    if isinstance(st.shift_fn, _space.GeneralShift) or isinstance(
+            getattr(e, 'geometry', None), _space.GeneralDisplacement):
+        # periodic_general cells: the same loop on the generic kernels
         return _run_loop(apply_fn, state, neighbor, n_steps, neighbor_fn, max_reallocations)
     nvt = isinstance(state, NVTNoseHooverState)
     if not (isinstance(state, NVEState) or nvt):

@@ -305,7 +305,7 @@ class PairNeighborListEnergy:
         R, rs = partition._rows(R)
         n, dim = R.shape
         species, pair = self._resolve(R, dynamic)
-        sp = self.geometry.space(dim)
+        sp = self.geometry.space(dim, dynamic.get('box'), dynamic.get('new_box'))
         fmt = {partition.Dense: N.DENSE, partition.Sparse: N.SPARSE,
                partition.OrderedSparse: N.ORDERED_SPARSE}[neighbor.format]
         idx = neighbor.idx
@@ -375,7 +375,7 @@ class PairNeighborListEnergy:
         R, rs = partition._rows(R)
         n, dim = R.shape
         species, pair = self._resolve(R, dynamic)
-        sp = self.geometry.space(dim)
+        sp = self.geometry.space(dim, dynamic.get('box'), dynamic.get('new_box'))
         idx = neighbor.idx
         if lam.stride(-1) != 1:
             lam = lam.contiguous()

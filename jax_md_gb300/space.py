@@ -11,6 +11,7 @@ from __future__ import annotations
 
 from typing import Optional
 
+import numpy as np
 import torch
 
 from . import _native as N
@@ -76,7 +77,10 @@ class Displacement:
             dR = dR * p if p.dim() <= 1 else torch.einsum('ij,...j->...i', p, dR)
         return dR
 
-    def space(self, dim: int) -> N.Space:
+    def space(self, dim: int, box=None, new_box=None) -> N.Space:
+        if (box is not None or new_box is not None) and self.periodic:
+            raise UnexpectedBoxException('`space.periodic` does not accept a box argument. '
+                                         'Perhaps you meant to use `space.periodic_general`?')
         s = N.Space()
         s.dim = dim
         s.periodic = 1 if self.periodic else 0
@@ -147,13 +151,79 @@ def transform(box, R: torch.Tensor) -> torch.Tensor:
     return _Transform.apply(b, R)
 
 
+def cell_matrix(box, dim: int) -> np.ndarray:
+    """The cell T as a [dim, dim] float64 matrix: a scalar or per-axis sides
+    become a diagonal (space.py:125-148 treats them as such)."""
+    b = box.detach().cpu().double().numpy() if isinstance(box, torch.Tensor) else np.asarray(
+        box, np.float64)
+    if b.ndim == 0 or b.size == 1:
+        return np.eye(dim) * float(b.reshape(-1)[0])
+    if b.ndim == 1:
+        if b.size != dim:
+            raise ValueError(f'box has {b.size} sides for a {dim}-dimensional system')
+        return np.diag(b)
+    if b.shape != (dim, dim):
+        raise ValueError(f'cell matrix of shape {b.shape} for a {dim}-dimensional system')
+    return b
+
+
+def general_space(box, dim: int) -> N.Space:
+    """The kernels' geometry of a general cell with fractional coordinates:
+    minimum image in the unit cube, displacement T d, shift by T^-1 dR.  The
+    kernels take upper-triangular cells (the reference's is_box_valid,
+    partition.py:676-681)."""
+    T = cell_matrix(box, dim)
+    if not np.array_equal(np.triu(T), T):
+        raise ValueError('the kernels take upper-triangular cell matrices (partition.is_box_valid)')
+    if np.any(np.diag(T) <= 0):
+        raise ValueError('the cell matrix needs a positive diagonal')
+    Ti = np.linalg.inv(T)
+    s = N.Space()
+    s.dim = dim
+    s.periodic = N.GENERAL_CELL
+    for d in range(3):
+        s.box[d] = 1.0
+    for a in range(dim):
+        for b in range(dim):
+            s.cell[3 * a + b] = float(np.float32(T[a, b]))
+            s.inv_cell[3 * a + b] = float(np.float32(Ti[a, b]))
+    if dim == 2:
+        s.cell[8] = s.inv_cell[8] = 1.0
+    return s
+
+
 class GeneralDisplacement:
     """Displacement of space.periodic_general (space.py:413-434)."""
+
+    periodic = True
 
     def __init__(self, box, fractional_coordinates: bool):
         self.box = box
         self.inv_box = inverse(box)
         self.fractional_coordinates = fractional_coordinates
+
+    def space(self, dim: int, box=None, new_box=None) -> N.Space:
+        """Kernel geometry; ``box`` / ``new_box`` replace the cell as the
+        keywords of the displacement do (space.py:417-429)."""
+        T = new_box if new_box is not None else (box if box is not None else self.box)
+        if self.fractional_coordinates:
+            return general_space(T, dim)
+        # real coordinates: the kernels bin and wrap in the cell's own frame
+        # only for an orthorhombic cell (then T^-1 x, d_U and T give the
+        # minimum image of space.periodic)
+        if new_box is not None:
+            raise NotImplementedError('new_box with real coordinates is not implemented by the '
+                                      'kernels')
+        M = cell_matrix(T, dim)
+        if not np.array_equal(np.diag(np.diag(M)), M):
+            raise NotImplementedError('general cells in the kernels take fractional coordinates '
+                                      '(periodic_general(box, fractional_coordinates=True))')
+        s = N.Space()
+        s.dim = dim
+        s.periodic = 1
+        for d in range(dim):
+            s.box[d] = float(M[d, d])
+        return s
 
     def __call__(self, Ra, Rb, perturbation=None, **kwargs):
         box, inv = self.box, self.inv_box
@@ -175,6 +245,22 @@ class GeneralDisplacement:
 class GeneralShift:
     """Shift of space.periodic_general (space.py:436-466): dR lives in the
     cell; R in the unit cube (fractional) or in the cell."""
+
+    def space(self, dim: int) -> N.Space:
+        """Kernel geometry of the shift (see GeneralDisplacement.space)."""
+        if self.fractional_coordinates and self.wrapped:
+            return general_space(self.box, dim)
+        M = cell_matrix(self.box, dim)
+        if self.fractional_coordinates or not np.array_equal(np.diag(np.diag(M)), M):
+            raise NotImplementedError('the integrator kernels take wrapped fractional coordinates '
+                                      'for general cells')
+        s = N.Space()
+        s.dim = dim
+        s.periodic = 1 if self.wrapped else 0
+        if self.wrapped:
+            for d in range(dim):
+                s.box[d] = float(M[d, d])
+        return s
 
     def __init__(self, box, fractional_coordinates: bool, wrapped: bool):
         self.box = box
@@ -204,8 +290,9 @@ def periodic_general(box, fractional_coordinates: bool = True, wrapped: bool = T
     """space.periodic_general (space.py:332-468): periodic boundary conditions
     on the cell T [0, 1]^d (T a scalar, per-axis sides or a cell matrix),
     positions in the unit cube (fractional_coordinates) or in the cell.  These
-    are tensor functions; the pair and neighbour-list kernels take
-    space.periodic / space.free geometries."""
+    are tensor functions and carry the geometry for the kernels (fractional
+    coordinates with an upper-triangular cell; real coordinates with an
+    orthorhombic one)."""
     return (GeneralDisplacement(box, fractional_coordinates),
             GeneralShift(box, fractional_coordinates, wrapped))
 
@@ -242,10 +329,10 @@ def geometry_of(displacement_or_metric):
     inner = getattr(d, 'displacement', None)
     if isinstance(inner, Displacement):
         return inner
-    if isinstance(d, GeneralDisplacement) or isinstance(inner, GeneralDisplacement):
-        raise NotImplementedError('the pair and neighbour-list kernels take space.periodic or '
-                                  'space.free geometries; periodic_general cells are not '
-                                  'implemented by the kernels yet')
+    if isinstance(d, GeneralDisplacement):
+        return d
+    if isinstance(inner, GeneralDisplacement):
+        return inner
     raise TypeError('jax_md_gb300 kernels need a displacement from jax_md_gb300.space.periodic '
                     'or space.free; got ' + repr(d))
 

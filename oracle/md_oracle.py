@@ -155,6 +155,31 @@ def cell_dimensions(box, minimum_cell_size, dim, dtype=np.float32):
     return cps, cell_size, int(np.prod(cps))
 
 
+def fractional_cell_size(box, cutoff, dtype=np.float32):
+    """jax_md/partition.py:595-634 (_fractional_cell_size): the unit-cube
+    cell edge whose perpendicular width in the cell T is >= cutoff, in
+    ``dtype``: 1 / floor(min perpendicular width / cutoff) for a matrix."""
+    b = np.asarray(box, dtype)
+    c = dtype(cutoff)
+    if b.ndim == 0:
+        return dtype(c / b)
+    if b.ndim == 1:
+        return dtype(c / b.min())
+    if b.shape[0] == 1:
+        return dtype(1 / np.floor(b[0, 0] / c))
+    if b.shape[0] == 2:
+        xy = dtype(b[0, 1] / b[1, 1])
+        widths = [dtype(b[0, 0] / np.sqrt(dtype(1) + xy * xy)), b[1, 1]]
+    else:
+        xy, xz, yz = (dtype(b[0, 1] / b[1, 1]), dtype(b[0, 2] / b[2, 2]),
+                      dtype(b[1, 2] / b[2, 2]))
+        widths = [dtype(b[0, 0] / np.sqrt(dtype(1) + xy * xy + (xy * yz - xz) ** 2)),
+                  dtype(b[1, 1] / np.sqrt(dtype(1) + yz * yz)), b[2, 2]]
+    nmin = np.floor(min(widths) / c)
+    nmin = dtype(1) if nmin == 0 else dtype(nmin)
+    return dtype(dtype(1) / nmin)
+
+
 def cell_index(R, cell_size, cps, dtype=np.float32):
     """jax_md/partition.py:421-423: int(x / cell_size) mod cells_per_side.
 
@@ -233,13 +258,17 @@ class NeighborListOracle:
     """Restates jax_md/partition.py:801-1164 (neighbor_list) for one box.
 
     ``box=None`` means free space (space.free): no minimum image; the cell list
-    still bins with ``cell_box`` (partition.py:1044-1054 uses ``box``)."""
+    still bins with ``cell_box`` (partition.py:1044-1054 uses ``box``).
+    ``space`` (a PeriodicGeneral) replaces the displacement; with
+    ``fractional`` the cell list bins the unit cube with the cell edge of
+    fractional_cell_size(box, cutoff) (partition.py:1046-1051)."""
 
     def __init__(self, box, r_cutoff, dr_threshold=0.0, capacity_multiplier=1.25,
                  disable_cell_list=False, mask_self=True, fmt=DENSE,
-                 periodic=True, binning_dtype=np.float32):
+                 periodic=True, binning_dtype=np.float32, space=None, fractional=False):
         self.box = np.asarray(box, np.float64)
         self.periodic = periodic
+        self.space = space
         self.r_cutoff = float(r_cutoff)
         self.dr_threshold = float(dr_threshold)
         self.cutoff = self.r_cutoff + self.dr_threshold
@@ -250,10 +279,16 @@ class NeighborListOracle:
         self.mask_self = mask_self
         self.fmt = fmt
         self.bdt = binning_dtype
+        if fractional:
+            self.bin_box = np.float64(1.0)
+            self.bin_min = float(fractional_cell_size(box, self.cutoff, binning_dtype))
+        else:
+            self.bin_box, self.bin_min = self.box, self.cutoff
 
     # d^2 between every candidate, partition.py:911-951 / 960-975.
     def _d2(self, Ri, Rj):
-        d = displacement(Ri, Rj, self.box if self.periodic else None)
+        d = displacement(Ri, Rj, self.space if self.space is not None else
+                         (self.box if self.periodic else None))
         return (d * d).sum(-1)
 
     def _candidates(self, R, cl):
@@ -276,13 +311,13 @@ class NeighborListOracle:
         cl = None
         if use_cell_list is None:
             use_cell_list = (not self.disable_cell_list) and bool(
-                np.all(self.cutoff < _box_vector(self.box, dim) / 3.0))
+                np.all(self.bin_min < _box_vector(self.bin_box, dim) / 3.0))
         if use_cell_list:
             if cl_capacity is None:
                 cl_capacity = estimate_cell_capacity(
-                    R, self.box, self.cutoff, self.capacity_multiplier, dim,
+                    R, self.bin_box, self.bin_min, self.capacity_multiplier, dim,
                     self.bdt) + extra_capacity
-            cl = cell_list(R, self.box, self.cutoff, cl_capacity, self.bdt)
+            cl = cell_list(R, self.bin_box, self.bin_min, cl_capacity, self.bdt)
             if cl.did_buffer_overflow:
                 err |= CELL_LIST_OVERFLOW
         cand, _ = self._candidates(R, cl)
@@ -340,7 +375,7 @@ class NeighborListOracle:
         R = np.asarray(R)
         N, dim = R.shape
         atoms = np.asarray(atoms, np.int64)
-        cl = cell_list(R, self.box, self.cutoff, cl_capacity, self.bdt)
+        cl = cell_list(R, self.bin_box, self.bin_min, cl_capacity, self.bdt)
         shifts = neighboring_cells(dim)
         cps = cl.cells_per_side
         shifted = np.mod(cl.particle_cell_id[atoms][:, None, :] + shifts[None], cps)
@@ -363,7 +398,8 @@ class NeighborListOracle:
     def update(self, R, nbrs: NeighborListO):
         """partition.py:1141-1154: rebuild iff any |R - R_ref|^2 > (skin/2)^2."""
         if self.dr_threshold != 0.0:
-            d = displacement(R, nbrs.reference_position, self.box if self.periodic else None)
+            d = displacement(R, nbrs.reference_position, self.space if self.space is not None
+                             else (self.box if self.periodic else None))
             if not np.any((d * d).sum(-1) > self.threshold_sq):
                 return nbrs
         return self.build(R, nbrs.max_occupancy, nbrs.error, nbrs.cell_list_capacity,
@@ -625,8 +661,13 @@ def pair_force_vjp(spec: PairSpec, R, nbrs_idx, fmt, lam, box=None):
 # ---------------------------------------------------------------------------
 # simulate.py
 def velocity_verlet(force_fn, R, P, F, mass, dt, box):
-    """jax_md/simulate.py:227-243 with periodic_shift (space.py:250-252)."""
+    """jax_md/simulate.py:227-243 with periodic_shift (space.py:250-252), or
+    the shift of a PeriodicGeneral ``box`` (space.py:436-466)."""
     P = P + 0.5 * dt * F
+    if hasattr(box, 'shift'):
+        R = box.shift(R, dt * P / mass)
+        F = force_fn(R)
+        return R, P + 0.5 * dt * F, F
     R = R + dt * P / mass
     if box is not None:
         R = np.mod(R, box)

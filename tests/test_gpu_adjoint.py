@@ -283,10 +283,12 @@ def _oracle_nvt_loss(R0, P0, L, sig, steps, dt=0.005, kT=0.722):
     return O.pair_energy_forces(spec, R, nl.build(R).idx, O.DENSE, box)[0] / n
 
 
-def test_nvt_trajectory_gradient_matches_fd(cuda):
+@pytest.mark.parametrize('k', [None, 5], ids=['stored', 'checkpointed'])
+def test_nvt_trajectory_gradient_matches_fd(cuda, k):
     """Gradient of PE/N after 12 Nose-Hoover steps (chain 5, tau = 100 dt)
     with respect to sigma and along random directions of R0 and P0, against
-    FP64 central differences of the oracle's NVT step (simulate.py:649-667)."""
+    FP64 central differences of the oracle's NVT step (simulate.py:649-667);
+    every step recorded, or checkpoints every 5 steps with replayed segments."""
     from jax_md_gb300 import adjoint, energy, partition, space
     from tests.helpers import fcc_system
     R, P, L = fcc_system(5)
@@ -295,7 +297,7 @@ def test_nvt_trajectory_gradient_matches_fd(cuda):
     Rt = torch.tensor(R, device=cuda)
     nb = nfn.allocate(Rt)
     steps = 12
-    traj = adjoint.nvt_trajectory(efn, nfn, shift, 0.005, 0.722, steps)
+    traj = adjoint.nvt_trajectory(efn, nfn, shift, 0.005, 0.722, steps, checkpoint_every=k)
     sig = torch.tensor(1.0, device=cuda, requires_grad=True)
     R0 = Rt.clone().requires_grad_(True)
     P0 = torch.tensor(P, device=cuda).requires_grad_(True)
@@ -307,7 +309,7 @@ def test_nvt_trajectory_gradient_matches_fd(cuda):
     assert abs(float(loss.detach()) - L0) <= 1e-4 * abs(L0)
     hh = 1e-4
     fd = (_oracle_nvt_loss(R, P, L, 1 + hh, steps) - _oracle_nvt_loss(R, P, L, 1 - hh, steps)) / (2 * hh)
-    assert abs(float(sig.grad) - fd) <= 1e-3 * max(abs(fd), 1e-2), (float(sig.grad), fd)
+    assert abs(float(sig.grad) - fd) <= 1e-4 * max(abs(fd), 1e-2), (float(sig.grad), fd)
     rng = np.random.default_rng(6)
     e = 1e-4
     for which, grad in (('R', R0.grad), ('P', P0.grad)):
@@ -321,4 +323,4 @@ def test_nvt_trajectory_gradient_matches_fd(cuda):
             lm = _oracle_nvt_loss(R, P - e * v, L, 1.0, steps)
         fdv = (lp - lm) / (2 * e)
         ad = float((grad.cpu().numpy() * v).sum())
-        assert abs(ad - fdv) <= 1e-3 * max(abs(fdv), 1e-2), (which, ad, fdv)
+        assert abs(ad - fdv) <= 1e-4 * max(abs(fdv), 1e-2), (which, ad, fdv)
