@@ -326,7 +326,8 @@ int seg_check_smem(const SegGrid& g) {
   }
   const int64_t per_slot = 16 + (g.half ? 12 : 0);  // + reaction accumulators
   const int64_t need = (int64_t)(g.cap + 1) * per_slot + g.lcap + (int64_t)sizeof(SegShared) +
-                       64 * (int64_t)sizeof(PairCoef) + 64;
+                       64 * (int64_t)sizeof(PairCoef) + 64 +
+                       (g.half ? 4 * (int64_t)(g.pmax + 1) + 4 * (kSegMaxThreads / 32 + 1) : 0);
   JMD_REQUIRE(need <= optin, "segment staging (positions + list block) exceeds a CTA's shared memory");
   return JMD_OK;
 }

@@ -1020,7 +1020,7 @@ k_seg_search(SegGrid sg, const float4* __restrict__ x, Bins b, Geo geo, float cu
         // far slot) and its bit is masked below
         const int nb = min(32, j1 - jb);
         uint32_t hits = 0u;
-        for (int k = 0; k < nb; k += 2) {
+        auto test2 = [&](int k) {  // candidates jb + k, jb + k + 1 -> bits k, k + 1
           const int j = jb + k;
           const float4 b0 = spos[j];
           const float4 b1 = spos[j + 1];
@@ -1041,8 +1041,15 @@ k_seg_search(SegGrid sg, const float4* __restrict__ x, Bins b, Geo geo, float cu
           r2 = fma2(dy, dy, r2);
           if (DIM == 3) r2 = fma2(dz, dz, r2);
           hits |= ((r2.x < cut2 ? 1u : 0u) | (r2.y < cut2 ? 2u : 0u)) << k;
+        };
+        if (nb == 32) {
+          // a full batch: unrolled, the bit positions are constants
+#pragma unroll
+          for (int k = 0; k < 32; k += 2) test2(k);
+        } else {
+          for (int k = 0; k < nb; k += 2) test2(k);
+          hits &= (1u << nb) - 1u;
         }
-        if (nb < 32) hits &= (1u << nb) - 1u;
         if (HALF && r == 0) {
           // keep j > is: bits of candidates at or before the lane's atom go
           const int cut_bits = is + 1 - jb;

@@ -239,6 +239,46 @@ __device__ __forceinline__ void red_global_v4(float4* dst, float x, float y, flo
 // fixed-point shared-memory accumulator per staged atom, which the CTA then
 // adds to `f` in global memory with one vector reduction per staged atom
 // (f is zero before the kernel; k_seg_integrate consumes and clears it).
+// cpre[0..n) = exclusive prefix of f(o) over o < n, cpre[n] = the total;
+// every thread of the block calls it (warp shuffles + one value per warp).
+template <typename F>
+__device__ void seg_chunk_prefix(int n, int* cpre, F f) {
+  __shared__ int wsum[kSegMaxThreads / 32];
+  __shared__ int carry;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < n; base += blockDim.x) {
+    const int o = base + threadIdx.x;
+    const int v = o < n ? f(o) : 0;
+    int x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      int t = lane < nw ? wsum[lane] : 0;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, t, d);
+        if (lane >= d) t += y;
+      }
+      if (lane < nw) wsum[lane] = t;
+    }
+    __syncthreads();
+    const int excl = carry + (w ? wsum[w - 1] : 0) + x - v;
+    if (o < n) cpre[o] = excl;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) cpre[n] = carry;
+  __syncthreads();
+}
+
 template <int DIM, int KIND, bool SPECIES, bool FRAME>
 __global__ void __maxnreg__(72)
 k_seg_half(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
@@ -250,6 +290,7 @@ k_seg_half(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
   int* fx = reinterpret_cast<int*>(spos + sg.cap + 1);
   int* fy = fx + (sg.cap + 1);
   int* fz = fy + (sg.cap + 1);
+  int* cpre = fz + (sg.cap + 1);  // [pmax + 1] chunk prefix
   const SegRecord* rec = a.recs + blockIdx.x;
   const uint8_t* gblk = a.blocks + (int64_t)blockIdx.x * sg.stride;
   const SegHead hd = seg_stage_record<DIM>(sg, a.x, rec, spos, sh, a.status, gblk, nullptr);
@@ -286,15 +327,66 @@ k_seg_half(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
   }
   const float rc2m = tab.rc2_max;
   const Coef2 c0 = coef2(tab.c[0]);
-  for (int o = threadIdx.x; o < hd.own_cnt; o += blockDim.x) {
+  // chunk-balanced work: the threads take the segment's 8-entry list chunks
+  // in atom order (cpre = exclusive prefix of the atoms' chunk counts), so
+  // a row's length decides how many threads share it rather than how long
+  // one thread runs
+  const uint16_t* cnts = reinterpret_cast<const uint16_t*>(gblk + 16);
+  const int nown = blk_ok ? hd.own_cnt : 0;  // cpre holds pmax + 1 entries
+  seg_chunk_prefix(nown, cpre, [&](int o) {
+    const int c = min((int)cnts[o], 8 * nck_seg);
+    return (c + 7) >> 3;
+  });
+  const int nchunks = cpre[nown];
+  // chunk u -> (own atom o, its chunk kc), and that chunk's list entries
+  auto locate = [&](int u, int& o, int& kc) {
+    int lo = 0, hi = nown - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (cpre[mid] <= u) lo = mid; else hi = mid - 1;
+    }
+    o = lo;
+    kc = u - cpre[lo];
+  };
+  int o_next = 0, kc_next = 0;
+  uint4 next = make_uint4(0u, 0u, 0u, 0u);
+  if (threadIdx.x < nchunks) {
+    locate(threadIdx.x, o_next, kc_next);
+    next = *reinterpret_cast<const uint4*>(gblk + seg_chunk_off(P, kc_next, o_next));
+  }
+  for (int u = threadIdx.x; u < nchunks; u += blockDim.x) {
+    const int o = o_next, kc = kc_next;
+    const uint4 cur = next;
+    // the next chunk's entries are in flight while this one is evaluated
+    if (u + (int)blockDim.x < nchunks) {
+      locate(u + blockDim.x, o_next, kc_next);
+      next = *reinterpret_cast<const uint4*>(gblk + seg_chunk_off(P, kc_next, o_next));
+    }
+    (void)kc;
     const int is = hd.own_sm + o;
     const float4 xi = spos[is];
-    const int c = blk_ok ? min((int)reinterpret_cast<const uint16_t*>(gblk + 16)[o], 8 * nck_seg) : 0;
-    const uint4* lp = reinterpret_cast<const uint4*>(gblk + seg_chunk_off(P, 0, o));
     const bool inner = FRAME || interior<DIM>(xi, a.geo, a.margin);
     const int si = SPECIES ? sclamp(__float_as_int(xi.w), tab.nsp) : 0;
     const float2 xx = f2s(xi.x), xy = f2s(xi.y), xz = f2s(xi.z);
     float2 ax = f2s(0.f), ay = f2s(0.f), az = f2s(0.f);
+    // a force into a staged slot: 32-bit fixed point in shared memory, or a
+    // close contact straight to the atom's sorted slot (the pieces partition
+    // the staged slots; a slot outside them is skipped rather than written)
+    auto deposit = [&](int j, float vx, float vy, float vz) {
+      if (fabsf(vx) < kFixMax && fabsf(vy) < kFixMax && fabsf(vz) < kFixMax) {
+        red_shared_s32(fx + j, __float2int_rn(vx * kFixScale));
+        red_shared_s32(fy + j, __float2int_rn(vy * kFixScale));
+        if (DIM == 3) red_shared_s32(fz + j, __float2int_rn(vz * kFixScale));
+      } else {
+        for (int q = 0; q < kSegMaxPieces; ++q) {
+          const int ps = __ldg(rec->ps + q), pn = __ldg(rec->pn + q);
+          if (pn > 0 && j >= ps && j < ps + pn) {
+            red_global_v4(a.f + __ldg(rec->pg + q) + (j - ps), vx, vy, vz);
+            break;
+          }
+        }
+      }
+    };
     auto pair2 = [&](int j0, int j1) {
       const float4 b0 = spos[j0], b1 = spos[j1];
       float2 dx = sub2(xx, f2(b0.x, b1.x));
@@ -332,43 +424,16 @@ k_seg_half(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
         az = add2(az, gz);
       }
       // reactions (masked pairs, the far slot included, add nothing)
-      auto react = [&](int j, float vx, float vy, float vz) {
-        if (fabsf(vx) < kFixMax && fabsf(vy) < kFixMax && fabsf(vz) < kFixMax) {
-          red_shared_s32(fx + j, __float2int_rn(vx * kFixScale));
-          red_shared_s32(fy + j, __float2int_rn(vy * kFixScale));
-          if (DIM == 3) red_shared_s32(fz + j, __float2int_rn(vz * kFixScale));
-        } else {
-          // a close contact: straight to the partner's sorted slot (the
-          // pieces partition the staged slots; a slot outside them is
-          // skipped rather than written anywhere)
-          for (int q = 0; q < kSegMaxPieces; ++q) {
-            const int ps = __ldg(rec->ps + q), pn = __ldg(rec->pn + q);
-            if (pn > 0 && j >= ps && j < ps + pn) {
-              red_global_v4(a.f + __ldg(rec->pg + q) + (j - ps), vx, vy, vz);
-              break;
-            }
-          }
-        }
-      };
-      if (m0) react(j0, gx.x, gy.x, DIM == 3 ? gz.x : 0.f);
-      if (m1) react(j1, gx.y, gy.y, DIM == 3 ? gz.y : 0.f);
+      if (m0) deposit(j0, gx.x, gy.x, DIM == 3 ? gz.x : 0.f);
+      if (m1) deposit(j1, gx.y, gy.y, DIM == 3 ? gz.y : 0.f);
     };
-    const int nck = (c + 7) >> 3;
-    const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
-    uint4 n1 = nck > 0 ? lp[0] : z4;
-    uint4 n2 = nck > 1 ? lp[P] : z4;
-    for (int kc = 0; kc < nck; ++kc) {
-      const uint4 cur = n1;
-      n1 = n2;
-      if (kc + 2 < nck) n2 = lp[(int64_t)(kc + 2) * P];
-      pair2((int)(cur.x & 0xFFFFu), (int)(cur.x >> 16));
-      pair2((int)(cur.y & 0xFFFFu), (int)(cur.y >> 16));
-      pair2((int)(cur.z & 0xFFFFu), (int)(cur.z >> 16));
-      pair2((int)(cur.w & 0xFFFFu), (int)(cur.w >> 16));
-    }
-    // the own atom's force, F_i = -sum g d (the reactions were +g d)
-    red_global_v4(a.f + hd.own_beg + o, -(ax.x + ax.y), -(ay.x + ay.y),
-                  DIM == 3 ? -(az.x + az.y) : 0.f);
+    pair2((int)(cur.x & 0xFFFFu), (int)(cur.x >> 16));
+    pair2((int)(cur.y & 0xFFFFu), (int)(cur.y >> 16));
+    pair2((int)(cur.z & 0xFFFFu), (int)(cur.z >> 16));
+    pair2((int)(cur.w & 0xFFFFu), (int)(cur.w >> 16));
+    // this chunk's share of the own atom's force, F_i = -sum g d (the
+    // reactions were +g d), into the own atom's staged slot
+    deposit(is, -(ax.x + ax.y), -(ay.x + ay.y), DIM == 3 ? -(az.x + az.y) : 0.f);
   }
   __syncthreads();
   // flush: every staged atom's accumulated force to its sorted slot
@@ -433,7 +498,8 @@ __global__ void k_seg_integrate(int n, float4* f, float4* p, const float4* x, fl
 
 template <int DIM, int KIND, bool SP, bool FRAME>
 int seg_half_go(const SegGrid& g, const SegStepArgs& a, const PairTable& t, cudaStream_t st) {
-  const size_t smem = (size_t)(g.cap + 1) * (sizeof(float4) + (DIM == 3 ? 3 : 2) * sizeof(float));
+  const size_t smem = (size_t)(g.cap + 1) * (sizeof(float4) + 3 * sizeof(int)) +
+                      (size_t)(g.pmax + 1) * sizeof(int);
   auto k = k_seg_half<DIM, KIND, SP, FRAME>;
   if (smem > 48 * 1024)
     JMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -122,6 +122,10 @@ def segment_candidates(nl):
                 out.append((K, t, 1, 0))
                 out.append((K, t, 0, 0))
                 out.append((K, t, 0, 1))   # half lists (Newton's third law)
+        # the half-list kernel spreads list chunks over the threads, so it
+        # can use more threads than a segment has atoms
+        if t0 + 32 < 256:
+            out.append((K, 256, 0, 1))
     return out
 
 
