@@ -198,13 +198,16 @@ def morse_section(dev, R, P, L, steps, warmup):
 
 
 def batched_section(dev, n_sys=512, fire_steps=200, nve_steps=200, seed=0, use_graph=True,
-                    with_plain=True):
+                    with_plain=True, f_tol=1e-6, fire_max=100000, nve_run=2000):
     """512 uneven 2D bidisperse soft-sphere systems (N ~ U[64, 4096], phi
-    0.84, sigma_ij = (d_i + d_j) / 2 with d in {1.0, 1.4}): a fixed number of
-    FIRE steps, then NVE at kT = 1e-4, as one graph launch per run over all
-    systems, against the same steps run system by system through the
-    single-system API (FIRE: per-step launches; NVE: one engine graph per
-    system)."""
+    0.84, sigma_ij = (d_i + d_j) / 2 with d in {1.0, 1.4}).  The run as
+    stated: FIRE from the random start until every system has max |F_i| <
+    f_tol (a system that gets there stops; the ones that stall at the
+    float32 floor run to fire_max, and the floor is reported), then nve_run
+    NVE steps at kT = 1e-4 -- all systems in one graph launch per chunk.
+    Throughput against the single-system API, system by system on the same
+    GPU, over the same number of steps (fire_steps FIRE steps, nve_steps NVE
+    steps; one CUDA graph per system on both)."""
     import torch
     from jax_md_gb300 import batch, energy, minimize, partition, simulate, space
     from oracle import md_oracle as O
@@ -230,10 +233,10 @@ def batched_section(dev, n_sys=512, fire_steps=200, nve_steps=200, seed=0, use_g
         e0, e1 = _events(dev)
         torch.cuda.synchronize()
         e0.record(cur)
-        fn()
+        out = fn()
         e1.record(cur)
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / 1e3
+        return e0.elapsed_time(e1) / 1e3, out
 
     def restore():
         bt.position.copy_(x0)
@@ -241,24 +244,67 @@ def batched_section(dev, n_sys=512, fire_steps=200, nve_steps=200, seed=0, use_g
         fns._build(nb, bt.position)
         run.fire_init(0.0)
 
+    def max_force_per_system():
+        f = run.force[:, :2].double().norm(dim=1)
+        out = torch.zeros(n_sys, dtype=torch.float64, device=dev)
+        return out.scatter_reduce(0, bt.atom_sys.long(), f, reduce='amax', include_self=True)
+
+    # throughput legs: fixed step counts, graph-replayed
     restore()
     run.fire(fire_steps, use_graph)          # records the graph
     restore()
-    t_bfire = timed(lambda: run.fire(fire_steps, use_graph))
+    t_bfire, _ = timed(lambda: run.fire(fire_steps, use_graph))
+    # the stated run: FIRE to f_tol, then NVE; the per-system max force is
+    # read back between chunks (a system under f_tol stops)
+    chunk = 10000
+    restore()
+    run.fire_init(f_tol)
+    run.fire(chunk, use_graph)                # records the chunk's graph
+    restore()
+    run.fire_init(f_tol)
+    progress, fire_taken, t_min = [], 0, 0.0
+    while fire_taken < fire_max:
+        dt_chunk, _ = timed(lambda: run.fire(chunk, use_graph))
+        t_min += dt_chunk
+        fire_taken += chunk
+        fm = max_force_per_system()
+        progress.append([fire_taken, int(run.n_done.item()), float(fm.max()), float(fm.median())])
+        if progress[-1][1] == n_sys:
+            break
+    fmax = max_force_per_system()
+    converged = int((fmax < f_tol).sum())
+    # float32 resolution of the positions: one ulp of the box side L
+    boxes = torch.as_tensor([float(L) for R, L, sp in systems], dtype=torch.float64, device=dev)
+    ulp = torch.pow(2.0, torch.floor(torch.log2(boxes)) - 23)
+    floor_ratio = fmax / ulp
     run.set_momenta(1e-4, seed=7)
     p0 = run.momentum.clone()
     run.nve(nve_steps, use_graph)            # records the graph
     run.momentum.copy_(p0)
-    t_bnve = timed(lambda: run.nve(nve_steps, use_graph))
-    overflow = nb.did_buffer_overflow
+    t_bnve, _ = timed(lambda: run.nve(nve_steps, use_graph))
+    t_run_nve, _ = timed(lambda: run.nve(nve_run, use_graph))
+    overflow = bool(nb.did_buffer_overflow)
+    stated = {'fire_f_tol': f_tol, 'fire_steps_run': int(fire_taken), 'fire_s': t_min,
+              'systems_converged': converged, 'systems': n_sys,
+              'max_force_after_fire': float(fmax.max()),
+              'median_max_force_after_fire': float(fmax.median()),
+              'progress_steps_done_maxF_medianF': progress,
+              'max_force_over_position_ulp': {'median': float(floor_ratio.median()),
+                                              'max': float(floor_ratio.max())},
+              'nve_steps': nve_run, 'nve_s': t_run_nve,
+              'note': 'the float32 floor: a position carries one ulp of the box side, so with '
+                      'unit contact stiffness the residual force of a packing cannot fall much '
+                      'below a few ulp(L); the systems that reach the tolerance are the small '
+                      'boxes, the others stall at max_force_over_position_ulp ulps'}
     if not with_plain:
         return {'workload': f'{n_sys} 2D bidisperse soft-sphere systems (total {n_tot})',
-                'autotune': tuned,
+                'autotune': tuned, 'stated_run': stated,
                 'batched_fire_atom_steps_per_s': n_tot * fire_steps / t_bfire,
                 'batched_nve_atom_steps_per_s': n_tot * nve_steps / t_bnve,
                 'launch': 'cuda graph' if use_graph else 'direct', 'overflow': overflow}
 
-    # plain: the same systems one at a time through the single-system API
+    # plain: the same systems one at a time through the single-system API,
+    # each system's FIRE steps captured in its own CUDA graph
     plain = []
     for k, (R, L, sp) in enumerate(systems):
         d_k, s_k = space.periodic(float(L))
@@ -266,15 +312,25 @@ def batched_section(dev, n_sys=512, fire_steps=200, nve_steps=200, seed=0, use_g
                                                         sigma=sigma, format=partition.Dense)
         Rk = torch.tensor(R, device=dev)
         plain.append((nfn_k, efn_k, s_k, Rk, nfn_k.allocate(Rk, extra_capacity=4)))
+    chunk = 50
+    graphs = []
+    for nfn_k, efn_k, s_k, Rk, nb_k in plain:
+        init, apply = minimize.fire_descent(efn_k, s_k)
+        st = init(Rk.clone(), neighbor=nb_k)
+        apply(st, neighbor=nb_k.update(st.position))    # allocates the kernels' scratch
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            for _ in range(chunk):
+                apply(st, neighbor=nb_k.update(st.position))
+        graphs.append(g)
 
     def plain_fire():
-        for nfn_k, efn_k, s_k, Rk, nb_k in plain:
-            init, apply = minimize.fire_descent(efn_k, s_k)
-            st = init(Rk, neighbor=nb_k)
-            for _ in range(fire_steps):
-                nb_k = nb_k.update(st.position)
-                st = apply(st, neighbor=nb_k)
-    t_pfire = timed(plain_fire)
+        for g in graphs:
+            for _ in range(fire_steps // chunk):
+                g.replay()
+    t_pfire, _ = timed(plain_fire)
+    del graphs
     states = []
     for k, (nfn_k, efn_k, s_k, Rk, nb_k) in enumerate(plain):
         init, apply = simulate.nve(efn_k, s_k, 0.01)
@@ -286,46 +342,63 @@ def batched_section(dev, n_sys=512, fire_steps=200, nve_steps=200, seed=0, use_g
     def plain_nve():
         for apply, st, nb_k in states:
             simulate.run(apply, st, nb_k, nve_steps)
-    t_pnve = timed(plain_nve)
+    t_pnve, _ = timed(plain_nve)
+    fire_plain_steps = (fire_steps // chunk) * chunk
     return {
         'workload': f'{n_sys} 2D bidisperse soft-sphere systems, N~U[64,4096] (total {n_tot}), '
-                    'phi=0.84, skin 0.2, FIRE then NVE kT=1e-4 dt=0.01',
+                    f'phi=0.84, skin 0.2, FIRE to max|F|<{f_tol:g} then {nve_run} NVE steps '
+                    'kT=1e-4 dt=0.01',
+        'stated_run': stated,
         'fire_steps': fire_steps, 'nve_steps': nve_steps, 'autotune': tuned,
         'batched_fire_atom_steps_per_s': n_tot * fire_steps / t_bfire,
-        'plain_fire_atom_steps_per_s': n_tot * fire_steps / t_pfire,
-        'fire_speedup': t_pfire / t_bfire,
+        'plain_fire_atom_steps_per_s': n_tot * fire_plain_steps / t_pfire,
+        'fire_speedup': (n_tot * fire_steps / t_bfire) / (n_tot * fire_plain_steps / t_pfire),
         'batched_nve_atom_steps_per_s': n_tot * nve_steps / t_bnve,
         'plain_nve_atom_steps_per_s': n_tot * nve_steps / t_pnve,
         'nve_speedup': t_pnve / t_bnve,
-        'plain': 'per-system calls of the single-system API on the same GPU (FIRE: per-step '
-                 'launches; NVE: simulate.run, one CUDA graph per system)',
+        'plain': 'per-system calls of the single-system API on the same GPU (FIRE: each '
+                 f'system\'s {chunk} steps captured in its own CUDA graph; NVE: simulate.run, '
+                 'one engine graph per system)',
         'overflow': overflow,
     }
 
 
+def _ka_replica(rng, n):
+    """A seeded Kob-Andersen replica of exactly n atoms at rho = 1.2: n
+    distinct sites drawn from the smallest cubic lattice that has n, jittered
+    by +-0.05 of the spacing; 20% B; momenta Gaussian at kT = 0.6."""
+    L = float(np.float32((n / 1.2) ** (1 / 3)))
+    m = int(np.ceil(n ** (1 / 3) - 1e-9))
+    while m ** 3 < n:
+        m += 1
+    g = np.stack(np.meshgrid(*[np.arange(m)] * 3, indexing='ij'), -1).reshape(-1, 3)
+    g = g[np.sort(rng.choice(len(g), n, replace=False))]
+    a = L / m
+    R = np.mod((g + 0.5) * a + rng.uniform(-0.05, 0.05, g.shape) * a, L).astype(np.float32)
+    sp = np.zeros(n, np.int32)
+    sp[rng.permutation(n)[: n // 5]] = 1
+    P = (rng.standard_normal(R.shape) * np.sqrt(0.6)).astype(np.float32)
+    P -= P.mean(0, keepdims=True)
+    return R, P, L, sp
+
+
 def batched_adjoint_section(dev, n_sys=128, steps=500, seed=0):
-    """128 Kob-Andersen replicas (80:20, rho = 1.2, N from U[500, 20000]
-    rounded to a cubic lattice n^3, jittered, momenta at kT = 0.6): gradient of
-    the ensemble-mean PE/N after 500 NVE steps with respect to the shared
-    sigma / epsilon matrices, by the batched adjoint, against the cost of
-    finite differences with plain per-replica forward runs (one ensemble pass
-    timed; central differences of the two AB parameters need five)."""
+    """128 Kob-Andersen replicas (80:20, rho = 1.2, N drawn uniformly from
+    [500, 20000], seeded random lattice-site states, momenta at kT = 0.6):
+    gradient of the ensemble-mean PE/N after 500 Nose-Hoover steps (chain 5,
+    tau = 100 dt, kT = 0.6) with respect to the shared sigma / epsilon
+    matrices, by the batched adjoint (record length chosen to fit HBM),
+    against the cost of finite differences with plain per-replica forward
+    runs (one CUDA graph per replica; central differences of the two AB
+    parameters need five ensemble passes, one is timed).  The NVE adjoint of
+    the same replicas is reported beside it."""
     import torch
     from jax_md_gb300 import batch, energy, partition, simulate, space
     rng = np.random.default_rng(seed)
     sig = np.array([[1.0, 0.8], [0.8, 0.88]])
     eps = np.array([[1.0, 1.5], [1.5, 0.5]])
-    systems = []
-    for k in range(n_sys):
-        m = int(round(rng.uniform(500, 20000) ** (1 / 3)))
-        L = float(np.float32((m ** 3 / 1.2) ** (1 / 3)))
-        g = np.stack(np.meshgrid(*[np.arange(m)] * 3, indexing='ij'), -1).reshape(-1, 3)
-        R = np.mod((g + 0.5) * (L / m) + rng.uniform(-0.05, 0.05, g.shape), L).astype(np.float32)
-        sp = np.zeros(len(R), np.int32)
-        sp[rng.permutation(len(R))[: len(R) // 5]] = 1
-        P = (rng.standard_normal(R.shape) * np.sqrt(0.6)).astype(np.float32)
-        P -= P.mean(0, keepdims=True)
-        systems.append((R, P, L, sp))
+    sizes_n = rng.integers(500, 20001, n_sys)
+    systems = [_ka_replica(rng, int(n)) for n in sizes_n]
     n_tot = sum(len(x[0]) for x in systems)
     bt = batch.pack([torch.tensor(R, device=dev) for R, P, L, sp in systems],
                     [L for R, P, L, sp in systems], species=[sp for R, P, L, sp in systems])
@@ -336,26 +409,11 @@ def batched_adjoint_section(dev, n_sys=128, steps=500, seed=0):
     fns = batch.neighbor_list(2.5, 0.3)
     nb = fns.allocate(bt, extra_capacity=12)
     ef = batch.BatchPairEnergy(efn)
-    traj = batch.BatchTrajectory(bt, fns, nb, ef, 0.005, steps)
     R0 = bt.R.clone()
     P0 = torch.tensor(np.concatenate([P for R, P, L, sp in systems]), device=dev)
     sizes = torch.tensor(bt.sizes, dtype=torch.float64, device=dev)
     sig_t = torch.tensor(sig, dtype=torch.float32, device=dev, requires_grad=True)
     eps_t = torch.tensor(eps, dtype=torch.float32, device=dev, requires_grad=True)
-
-    def forward():
-        with torch.no_grad():
-            return traj(R0, P0, sigma=sig_t.detach(), epsilon=eps_t.detach())
-
-    def forward_backward():
-        sig_t.grad = None
-        eps_t.grad = None
-        xn, pn = traj(R0, P0, sigma=sig_t, epsilon=eps_t)
-        fns.update(torch.nn.functional.pad(xn.detach(), (0, 1)).contiguous(), nb)
-        E = ef.energy_fn_autograd(bt, nb)(xn, sigma=sig_t, epsilon=eps_t)
-        loss = (E / sizes).mean()
-        loss.backward()
-        return loss
 
     def timed(fn):
         e0, e1 = _events(dev)
@@ -366,80 +424,87 @@ def batched_adjoint_section(dev, n_sys=128, steps=500, seed=0):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / 1e3, out
 
-    forward()
-    forward_backward()
-    t_f, _ = timed(forward)
-    t_fb, loss = timed(forward_backward)
-    g_sab = float((sig_t.grad[0, 1] + sig_t.grad[1, 0]).detach())
-    g_eab = float((eps_t.grad[0, 1] + eps_t.grad[1, 0]).detach())
-    overflow = nb.did_buffer_overflow
-    # plain: the same replicas one at a time, single-system API, direct launches
-    runs = []
-    for R, P, L, sp in systems:
-        d_k, s_k = space.periodic(L)
-        nfn_k, efn_k = energy.lennard_jones_neighbor_list(d_k, L, torch.tensor(sp, device=dev),
-                                                          sigma=sig, epsilon=eps, dr_threshold=0.3,
-                                                          format=partition.Dense)
-        Rk = torch.tensor(R, device=dev)
-        nb_k = nfn_k.allocate(Rk, extra_capacity=12)
-        init, apply = simulate.nve(efn_k, s_k, 0.005)
-        runs.append((apply, init(0, Rk, momenta=torch.tensor(P, device=dev), neighbor=nb_k), nb_k))
-
-    def plain():
-        for apply, st, nb_k in runs:
-            simulate.run(apply, st, nb_k, steps, use_graph=False)
-    t_plain, _ = timed(plain)
-    # the same replicas under Nose-Hoover (a chain per replica, kT = 0.6): the
-    # batched NVT adjoint, every step recorded, per-step orchestration
-    try:
-        trn = batch.BatchNvtTrajectory(bt, fns, nb, ef, 0.005, 0.6, steps)
-
-        def nvt_forward():
+    def adjoint_leg(traj):
+        def forward():
             with torch.no_grad():
-                return trn(R0, P0, sigma=sig_t.detach(), epsilon=eps_t.detach())
+                return traj(R0, P0, sigma=sig_t.detach(), epsilon=eps_t.detach())
 
-        def nvt_forward_backward():
+        def forward_backward():
             sig_t.grad = None
             eps_t.grad = None
-            xn, pn = trn(R0, P0, sigma=sig_t, epsilon=eps_t)
+            xn, pn = traj(R0, P0, sigma=sig_t, epsilon=eps_t)
             fns.update(torch.nn.functional.pad(xn.detach(), (0, 1)).contiguous(), nb)
             E = ef.energy_fn_autograd(bt, nb)(xn, sigma=sig_t, epsilon=eps_t)
-            loss_n = (E / sizes).mean()
-            loss_n.backward()
-            return loss_n
-        nvt_forward_backward()
-        t_nf, _ = timed(nvt_forward)
-        t_nfb, loss_n = timed(nvt_forward_backward)
-        nose_hoover = {
-            'workload': f'same replicas, {steps} Nose-Hoover steps (chain 5, tau=100 dt, kT=0.6)',
-            'forward_s': t_nf, 'forward_backward_s': t_nfb,
-            'gradient_cost_ratio': t_nfb / t_nf,
-            'dloss_dsigma_AB': float((sig_t.grad[0, 1] + sig_t.grad[1, 0]).detach()),
-            'dloss_depsilon_AB': float((eps_t.grad[0, 1] + eps_t.grad[1, 0]).detach()),
-            'loss': float(loss_n.detach()),
-            'overflow': nb.did_buffer_overflow,
-        }
-    except (RuntimeError, MemoryError) as ex:
-        nose_hoover = {'error': str(ex)[:300]}
-    return {
-        'workload': f'{n_sys} Kob-Andersen replicas, N=n^3 from U[500,20000] (total {n_tot}), '
-                    f'rho=1.2, kT=0.6, {steps} NVE steps dt=0.005, loss mean_b PE_b/N_b, '
-                    'grad wrt shared sigma[2x2], epsilon[2x2]',
-        'forward_s': t_f, 'forward_backward_s': t_fb,
-        'gradient_cost_ratio': t_fb / t_f,
-        'batched_forward_atom_steps_per_s': n_tot * steps / t_f,
-        'plain_forward_ensemble_s': t_plain,
-        'plain_finite_difference_s': 5 * t_plain,
-        'speedup_vs_finite_differences': 5 * t_plain / t_fb,
-        'dloss_dsigma_AB': g_sab, 'dloss_depsilon_AB': g_eab, 'loss': float(loss.detach()),
-        'note': 'over 500 steps the gradient of a chaotic trajectory is large; the FP64 '
-                'finite-difference checks run 20 steps (tests)',
-        'plain': 'per-replica simulate.run with direct launches; central differences of the two '
-                 'AB parameters = 5 ensemble passes (one timed)',
-        'dynamics': 'NVE; the Nose-Hoover run of the same replicas is under nose_hoover',
-        'overflow': overflow,
-        'nose_hoover': nose_hoover,
+            loss = (E / sizes).mean()
+            loss.backward()
+            return loss
+        forward()
+        forward_backward()
+        t_f, _ = timed(forward)
+        t_fb, loss = timed(forward_backward)
+        return {'forward_s': t_f, 'forward_backward_s': t_fb,
+                'gradient_cost_ratio': t_fb / t_f,
+                'batched_forward_atom_steps_per_s': n_tot * steps / t_f,
+                'dloss_dsigma_AB': float((sig_t.grad[0, 1] + sig_t.grad[1, 0]).detach()),
+                'dloss_depsilon_AB': float((eps_t.grad[0, 1] + eps_t.grad[1, 0]).detach()),
+                'loss': float(loss.detach()), 'overflow': bool(nb.did_buffer_overflow)}
+
+    def plain_leg(nvt):
+        runs = []
+        for R, P, L, sp in systems:
+            d_k, s_k = space.periodic(L)
+            nfn_k, efn_k = energy.lennard_jones_neighbor_list(
+                d_k, L, torch.tensor(sp, device=dev), sigma=sig, epsilon=eps, dr_threshold=0.3,
+                format=partition.Dense)
+            Rk = torch.tensor(R, device=dev)
+            nb_k = nfn_k.allocate(Rk, extra_capacity=12)
+            if nvt:
+                init, apply = simulate.nvt_nose_hoover(efn_k, s_k, 0.005, 0.6)
+            else:
+                init, apply = simulate.nve(efn_k, s_k, 0.005)
+            st = init(0, Rk, momenta=torch.tensor(P, device=dev), neighbor=nb_k)
+            simulate.run(apply, st, nb_k, steps)   # captures this replica's graph
+            runs.append((apply, st, nb_k))
+
+        def plain():
+            for apply, st, nb_k in runs:
+                simulate.run(apply, st, nb_k, steps)
+        t, _ = timed(plain)
+        return t
+
+    trn = batch.BatchNvtTrajectory(bt, fns, nb, ef, 0.005, 0.6, steps)
+    seg = trn.segment_length(bt.n, 3)
+    out = {
+        'workload': f'{n_sys} Kob-Andersen replicas, N from U[500,20000] (total {n_tot}), '
+                    f'rho=1.2, {steps} Nose-Hoover steps (chain 5, tau=100 dt, kT=0.6) dt=0.005, '
+                    'loss mean_b PE_b/N_b, grad wrt shared sigma[2x2], epsilon[2x2]',
+        'record': {'steps_per_segment': seg, 'checkpointed': seg < steps,
+                   'bytes_per_step': 3 * bt.n * 3 * 4 + 2 * n_sys * 66 * 8},
     }
+    try:
+        out.update(adjoint_leg(trn))
+        t_plain = plain_leg(True)
+        out.update({'plain_forward_ensemble_s': t_plain,
+                    'plain_finite_difference_s': 5 * t_plain,
+                    'speedup_vs_finite_differences': 5 * t_plain / out['forward_backward_s'],
+                    'plain': 'per-replica simulate.run of nvt_nose_hoover, one CUDA graph per '
+                             'replica; central differences of the two AB parameters = 5 ensemble '
+                             'passes (one timed)'})
+    except (RuntimeError, MemoryError) as ex:
+        out['error'] = str(ex)[:300]
+    # the NVE adjoint of the same replicas (graph-replayed segments)
+    try:
+        nve = adjoint_leg(batch.BatchTrajectory(bt, fns, nb, ef, 0.005, steps))
+        t_plain_nve = plain_leg(False)
+        nve.update({'workload': f'same replicas, {steps} NVE steps',
+                    'plain_forward_ensemble_s': t_plain_nve,
+                    'speedup_vs_finite_differences': 5 * t_plain_nve / nve['forward_backward_s']})
+    except (RuntimeError, MemoryError) as ex:
+        nve = {'error': str(ex)[:300]}
+    out['nve'] = nve
+    out['note'] = ('over 500 steps the gradient of a chaotic trajectory is large; the FP64 '
+                   'finite-difference checks run 12-20 steps (tests)')
+    return out
 
 
 def adjoint_section(dev, steps=2000, checkpoint_every=100, seed=0):
@@ -599,6 +664,9 @@ def main():
                     help='batched: only the batched soft-sphere workload (FIRE + NVE)')
     ap.add_argument('--no-tune', action='store_true',
                     help='skip the segment autotuner (default cells per segment and threads)')
+    ap.add_argument('--segment', default=None,
+                    help='cells,threads,stage_lists,half: use this segment launch shape '
+                         'instead of autotuning (for profiling a chosen shape)')
     ap.add_argument('--direct', action='store_true',
                     help='launch the engine kernels directly instead of replaying its CUDA '
                          'graph (profilers list every kernel of the timed region this way)')
@@ -645,7 +713,11 @@ def main():
     # launch shape: project autotuner (cells per segment, threads per CTA of
     # the engine's segment-local list), timed on copies of this state
     from jax_md_gb300 import tune
-    if args.no_tune:
+    if args.segment:
+        seg_choice = tuple(int(v) for v in args.segment.split(','))
+        simulate._segment_choice[simulate._grid_key(nb.plan.nl)] = seg_choice
+        seg_ms = {}
+    elif args.no_tune:
         seg_choice, seg_ms = None, {}
     else:
         seg_choice, seg_ms = tune.autotune_segment(apply, st, nb, steps=20, use_cache=False)
@@ -782,7 +854,7 @@ def main():
                    'segment': {'cells': sb.seg_cells, 'threads': sb.seg_threads,
                                'list_smem_bytes': sb.seg_list_smem,
                                'half_lists': bool(getattr(sb, 'seg_half', 0)),
-                               'autotuned': seg_choice is not None,
+                               'autotuned': seg_choice is not None and not args.segment,
                                'autotune_ms_per_step': {'x'.join(str(int(v)) for v in k): t
                                                         for k, t in seg_ms.items()}},
                    'energy_drift_per_atom': (E1 - E0) / n, 'overflow': overflow},

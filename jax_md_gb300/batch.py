@@ -745,18 +745,47 @@ class _BatchNvtTrajectoryFn(torch.autograd.Function):
                                               p.data_ptr(), None, tr.mass, update_mass, measure,
                                               scale.data_ptr(), N.ptr(ke_out), N.stream_ptr()),
                     'batch_nhc_half_step')
-        tape = []
-        for k in range(steps):
-            x_k, p_k, chain_a = x[:, :dim].clone(), p[:, :dim].clone(), chain.clone()
-            half(1, 0, s1[k], None)
-            N.check(L.jmd_batch_nve_run(ctypes.byref(sysd), 1, 0, N.stream_ptr()), 'batch_nve_run')
-            r, chain_b = p[:, :dim].clone(), chain.clone()
-            half(0, 1, s2[k], ke2[k])
-            tape.append((x_k, p_k, chain_a, r, chain_b))
+
+        def run_steps(k0, count, tape):
+            """Steps k0 .. k0 + count - 1 on (x, p, f, chain); with ``tape``
+            each step's (x_k, p_k, chain_a, r, chain_b) is appended."""
+            for k in range(k0, k0 + count):
+                if tape is not None:
+                    x_k, p_k, chain_a = x[:, :dim].clone(), p[:, :dim].clone(), chain.clone()
+                half(1, 0, s1[k], None)
+                N.check(L.jmd_batch_nve_run(ctypes.byref(sysd), 1, 0, N.stream_ptr()),
+                        'batch_nve_run')
+                if tape is not None:
+                    r, chain_b = p[:, :dim].clone(), chain.clone()
+                half(0, 1, s2[k], ke2[k])
+                if tape is not None:
+                    tape.append((x_k, p_k, chain_a, r, chain_b))
+
+        seg = tr.segment_length(n, dim)
+        tape, checkpoints = [], []
+        if seg >= steps:
+            run_steps(0, steps, tape)
+        else:
+            for k0 in range(0, steps, seg):
+                # a segment starts from a fresh list, so its replay in the
+                # reverse pass repeats it bit for bit
+                tr.neighbor_fns._build(nb, x)
+                checkpoints.append((x.clone(), p.clone(), f.clone(), chain.clone()))
+                run_steps(k0, min(seg, steps - k0), None)
         if nb.did_buffer_overflow:
             raise RuntimeError('a batched neighbour list overflowed during the trajectory; '
                                'allocate it with more capacity')
-        ctx.cfg = (tr, species, pair, tape, x[:, :dim].clone(), s1, s2, ke2)
+
+        def replay(si, k0, count):
+            ck = checkpoints[si]
+            for buf, v in zip((x, p, f, chain), ck):
+                buf.copy_(v)
+            tr.neighbor_fns._build(nb, x)
+            out = []
+            run_steps(k0, count, out)
+            return out
+        ctx.cfg = (tr, species, pair, tape, x[:, :dim].clone(), s1, s2, ke2,
+                   (seg, checkpoints, replay, (sysd, x, p, f, chain)))
         ctx.has = (sigma is not None, epsilon is not None)
         ctx.save_for_backward(sigma if sigma is not None else torch.empty(0),
                               epsilon if epsilon is not None else torch.empty(0))
@@ -764,7 +793,7 @@ class _BatchNvtTrajectoryFn(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, gx, gp):
-        tr, species, pair, tape, x_n, s1, s2, ke2 = ctx.cfg
+        tr, species, pair, full_tape, x_n, s1, s2, ke2, (seg, checkpoints, replay, _) = ctx.cfg
         sigma, epsilon = ctx.saved_tensors
         sigma = sigma if ctx.has[0] else None
         epsilon = epsilon if ctx.has[1] else None
@@ -818,9 +847,9 @@ class _BatchNvtTrajectoryFn(torch.autograd.Function):
         # chain VJPs and the force VJP
         pending = None
         upd = L.jmd_batch_nvt_adjoint_update
-        for k in range(len(tape) - 1, -1, -1):
-            x_k, p_k, chain_a, r, chain_b = tape[k]
-            x1 = tape[k + 1][0] if k + 1 < len(tape) else x_n
+
+        def reverse_step(k, entry, x1, pending):
+            x_k, p_k, chain_a, r, chain_b = entry
             N.check(L.jmd_batch_dot_per_system(g, pbar.data_ptr(), dim, r.data_ptr(), r.stride(0),
                                                sbar2.data_ptr(), N.stream_ptr()), 'dot')
             chain_vjp(chain_b, ke2[k], 0, pxi, sbar2, pxi1)
@@ -839,9 +868,24 @@ class _BatchNvtTrajectoryFn(torch.autograd.Function):
                         kebar.data_ptr(), inv_m, 0.0, None, pbar.data_ptr(), None, None,
                         N.stream_ptr()), 'nvt adjoint pbar')
             pend.copy_(qbar)
-            pending = pend
+            return pend
+
+        # segments in reverse; a checkpointed segment is replayed from its
+        # checkpoint to rebuild its tape
+        steps = tr.n_steps
+        segs = ([(k0, min(seg, steps - k0)) for k0 in range(0, steps, seg)] if checkpoints
+                else [(0, steps)])
+        x_end = x_n
+        for si in range(len(segs) - 1, -1, -1):
+            k0, count = segs[si]
+            tape = replay(si, k0, count) if checkpoints else full_tape
+            for kk in range(len(tape) - 1, -1, -1):
+                x1 = tape[kk + 1][0] if kk + 1 < len(tape) else x_end
+                pending = reverse_step(k0 + kk, tape[kk], x1, pending)
+            x_end = tape[0][0]
+            del tape
         lam4[:, :dim] = h * pending
-        vjp_at(tape[0][0])
+        vjp_at(x_end)
         gs, ge = _bins_to_grads(bins, None, sigma, epsilon) if want else (None, None)
         return xbar[:, :dim].clone(), pbar.contiguous(), gs, ge, None
 
@@ -851,12 +895,17 @@ class BatchNvtTrajectory:
     Nose-Hoover NVT of every system of a batch (a fresh chain per system at
     kT, simulate.nvt_nose_hoover), differentiable with respect to R0, P0 and
     sigma / epsilon shared by all systems.  Every step is recorded (positions,
-    momenta and the chains), so memory grows with n_steps; ``nbrs`` is
-    rebuilt in place.  Unit mass unless ``mass`` is given."""
+    momenta and the chains) while that fits a quarter of the free device
+    memory (``checkpoint_every=None``); otherwise, or with
+    ``checkpoint_every=k``, (x, p, F, chains) are kept every k steps and each
+    segment is replayed from its checkpoint (and a fresh list) before its
+    reverse pass.  ``nbrs`` is rebuilt in place.  Unit mass unless ``mass``
+    is given."""
 
     def __init__(self, batch: Batch, neighbor_fns: BatchNeighborListFns, nbrs: BatchNeighborList,
                  energy: BatchPairEnergy, dt: float, kT, n_steps: int, chain_length: int = 5,
-                 chain_steps: int = 2, sy_steps: int = 3, tau=None, mass: float = 1.0):
+                 chain_steps: int = 2, sy_steps: int = 3, tau=None, mass: float = 1.0,
+                 checkpoint_every=None):
         if int(n_steps) < 1:
             raise ValueError('n_steps must be >= 1')
         if not 2 <= int(chain_length) <= 7:
@@ -864,6 +913,19 @@ class BatchNvtTrajectory:
         self.batch, self.neighbor_fns, self.nbrs, self.energy = batch, neighbor_fns, nbrs, energy
         self.dt, self.kT, self.n_steps, self.mass = float(dt), kT, int(n_steps), float(mass)
         self.nhc = _nhc_constants(dt, chain_length, chain_steps, sy_steps, tau)
+        self.checkpoint_every = checkpoint_every
+
+    def segment_length(self, n: int, dim: int) -> int:
+        """Steps per recorded segment: ``checkpoint_every``, or all steps when
+        their record (x, p, r per atom and two chains per system per step)
+        fits a quarter of the free device memory."""
+        if self.checkpoint_every is not None:
+            return max(1, min(int(self.checkpoint_every), self.n_steps))
+        per_step = 3 * n * dim * 4 + 2 * self.batch.n_systems * 66 * 8
+        free = torch.cuda.mem_get_info(self.batch.device)[0] if self.batch.device.type == 'cuda' \
+            else 1 << 34
+        fit = max(1, int((free // 4) // max(per_step, 1)))
+        return self.n_steps if fit >= self.n_steps else fit
 
     def __call__(self, R0, P0, sigma=None, epsilon=None):
         dyn = {}

@@ -426,15 +426,17 @@ def test_batch_nvt_graph_equals_direct(cuda):
     assert all(torch.equal(a, b) for a, b in zip(*out))
 
 
-def test_batch_nvt_trajectory_gradient_matches_fd(cuda):
+@pytest.mark.parametrize('k', [None, 5], ids=['stored', 'checkpointed'])
+def test_batch_nvt_trajectory_gradient_matches_fd(cuda, k):
     """Gradient of mean_b PE_b(x_n)/N_b after 12 batched Nose-Hoover steps (a
     chain per system, kT = 0.6) with respect to the shared sigma_AB,
     epsilon_AB and along random directions of R0 and P0, against FP64 central
-    differences of the oracle's NVT step."""
+    differences of the oracle's NVT step; every step recorded, or checkpoints
+    every 5 steps with replayed segments."""
     from jax_md_gb300 import batch
     systems, bt, fns, nb, ef = _ka_batch(cuda)
     steps, kT = 12, 0.6
-    traj = batch.BatchNvtTrajectory(bt, fns, nb, ef, 0.005, kT, steps)
+    traj = batch.BatchNvtTrajectory(bt, fns, nb, ef, 0.005, kT, steps, checkpoint_every=k)
     sig = torch.tensor(KA_SIG, dtype=torch.float32, device=cuda, requires_grad=True)
     eps = torch.tensor(KA_EPS, dtype=torch.float32, device=cuda, requires_grad=True)
     R0 = bt.R.clone().requires_grad_(True)
