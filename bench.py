@@ -37,10 +37,11 @@ sys.path.insert(0, str(ROOT))
 METRIC = 'atom-steps/s LJ N=864k NVE fp32'
 N_CELLS = 60
 DENSITY, KT, DT, SKIN = 0.8442, 0.722, 0.005, 0.3
-# DRAM bytes per atom of one segment fused-step launch, from one ncu capture
-# at N=864,000 (dram__bytes_read.sum + dram__bytes_write.sum); None until
-# captured
-SEG_DRAM_BYTES_PER_ATOM = None
+# DRAM bytes per atom of the timed fused step of each engine list, from ncu
+# captures at N=864,000 (dram__bytes_read.sum + dram__bytes_write.sum of the
+# launches of one step, divided by N): the half-list step k_seg_half +
+# k_seg_integrate, the tiled step k_tiled; None where not captured
+DRAM_BYTES_PER_ATOM = {'half': 230.4, 'full': None, 'tiled': 378.4}
 
 
 def workload(cells: int, n: int) -> str:
@@ -714,7 +715,8 @@ def main():
     # the engine's segment-local list), timed on copies of this state
     from jax_md_gb300 import tune
     if args.segment:
-        seg_choice = tuple(int(v) for v in args.segment.split(','))
+        seg_choice = ('tiled' if args.segment == 'tiled' else
+                      tuple(int(v) for v in args.segment.split(',')))
         simulate._segment_choice[simulate._grid_key(nb.plan.nl)] = seg_choice
         seg_ms = {}
     elif args.no_tune:
@@ -801,6 +803,7 @@ def main():
     # the count, position read + write, momentum read + write, reference read
     list_bytes = chunk_bytes if seg_on else 4 * nbar + 4
     half = bool(getattr(sb, 'seg_half', 0)) and seg_on
+    layout_name = 'half' if half else ('full' if seg_on else 'tiled')
     # half lists: + the force accumulator, reduced into, read and cleared
     kern_bytes = n * (list_bytes + 80 + (48 if half else 0))
     hbm, src = peaks()
@@ -855,15 +858,17 @@ def main():
                                'list_smem_bytes': sb.seg_list_smem,
                                'half_lists': bool(getattr(sb, 'seg_half', 0)),
                                'autotuned': seg_choice is not None and not args.segment,
-                               'autotune_ms_per_step': {'x'.join(str(int(v)) for v in k): t
+                               'autotune_ms_per_step': {(k if isinstance(k, str) else
+                                                         'x'.join(str(int(v)) for v in k)): t
                                                         for k, t in seg_ms.items()}},
                    'energy_drift_per_atom': (E1 - E0) / n, 'overflow': overflow},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
                      'frac': achieved / hbm,
-                     'traffic': (SEG_DRAM_BYTES_PER_ATOM * n
-                                 if (seg_on and SEG_DRAM_BYTES_PER_ATOM) else None),
-                     'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one '
-                                       'k_seg_step launch at N=864000, scaled by N',
+                     'traffic': (DRAM_BYTES_PER_ATOM[layout_name] * n
+                                 if DRAM_BYTES_PER_ATOM.get(layout_name) else None),
+                     'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of the '
+                                       'timed step\'s launches at N=864000, per atom x N',
+                     'layout': layout_name,
                      'peak_source': src,
                      'kernel': (('k_seg_half + k_seg_integrate (LJ, segment-local half lists, '
                                  'Newton\'s third law, FP32x2)') if half else

@@ -688,7 +688,7 @@ class _SortedBuffers:
 def _segment_shape(nbrs, layout):
     """(cells per segment, threads per CTA, list bytes, list staging bytes,
     half lists) for a run, or None for the tiled list.  `layout`: None
-    (autotuned choice, else half segment lists with the default width),
+    (autotuned choice, else full segment lists with the default width),
     'segment' / 'half' (full / half lists, default width), an int (cells), a
     (cells, threads[, stage_lists[, half]]) tuple, or 'tiled'."""
     if layout == 'tiled':
@@ -696,7 +696,11 @@ def _segment_shape(nbrs, layout):
     nl = nbrs.plan.nl
     threads, stage, half = None, True, False
     if layout is None:
-        choice = _segment_choice.get(_grid_key(nl), (SEGMENT_CELLS_DEFAULT, None, False, True))
+        # untuned default: full lists, which are bitwise reproducible run to
+        # run (the half lists' cross-segment force sums are float atomics)
+        choice = _segment_choice.get(_grid_key(nl), (SEGMENT_CELLS_DEFAULT, None, True, False))
+        if choice == 'tiled':
+            return None
         cells, threads, stage, half = (tuple(choice) + (True, False))[:4]
     elif layout in ('segment', 'half'):
         cells, half = SEGMENT_CELLS_DEFAULT, layout == 'half'

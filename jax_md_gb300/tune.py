@@ -109,7 +109,8 @@ def segment_candidates(nl):
     """(cells, threads, stage_lists, half) to try: K in 2..8 (those the
     grid admits) with the default thread count and the neighbouring multiples
     of 32, each with full lists (block staged in shared memory or read from
-    global memory) or half lists (Newton's third law)."""
+    global memory) or half lists (Newton's third law); and 'tiled', the
+    engine's tiled int32 list."""
     from . import simulate
     out = []
     for K in (2, 3, 4, 5, 6, 8):
@@ -126,7 +127,12 @@ def segment_candidates(nl):
         # can use more threads than a segment has atoms
         if t0 + 32 < 256:
             out.append((K, 256, 0, 1))
+    out.append('tiled')   # the tiled int32 list, thread per atom
     return out
+
+
+def _unkey(k):
+    return k if isinstance(k, str) else tuple(k)
 
 
 def autotune_segment(apply_fn, state, neighbor, steps: int = 20, reps: int = 2,
@@ -143,9 +149,10 @@ def autotune_segment(apply_fn, state, neighbor, steps: int = 20, reps: int = 2,
     gk = simulate._grid_key(nl)
     cache = _load() if use_cache else {}
     if key in cache:
-        choice = tuple(cache[key]['choice'])
+        c = cache[key]['choice']
+        choice = c if isinstance(c, str) else tuple(c)
         simulate._segment_choice[gk] = choice
-        return choice, {tuple(json.loads(k)): v for k, v in cache[key]['ms'].items()}
+        return choice, {_unkey(json.loads(k)): v for k, v in cache[key]['ms'].items()}
     cands = list(candidates) if candidates is not None else segment_candidates(nl)
     if not cands:
         return None, {}
@@ -168,6 +175,8 @@ def autotune_segment(apply_fn, state, neighbor, steps: int = 20, reps: int = 2,
     choice = min(timings, key=timings.get)
     simulate._segment_choice[gk] = choice
     if use_cache:
-        cache[key] = {'choice': list(choice), 'ms': {json.dumps(list(k)): v for k, v in timings.items()}}
+        cache[key] = {'choice': choice if isinstance(choice, str) else list(choice),
+                      'ms': {json.dumps(k if isinstance(k, str) else list(k)): v
+                             for k, v in timings.items()}}
         _save(cache)
     return choice, timings
