@@ -327,6 +327,20 @@ int jmd_fire_update(float* momentum, const float* force, int64_t n, int32_t dim,
 int jmd_scale_momentum(float* momentum, int64_t p_stride, int64_t n,
                        int32_t dim, const double* scale, void* stream);
 
+/* The exp(iL) maps of simulate.npt_nose_hoover's inner step
+ * (simulate.py:925-940), on float4 rows:
+ *   mode 0 (exp_iL1): R <- shift(R, c0 R + c1 P / m), the shift of `space`
+ *          (a general cell: u <- mod(u + T^-1 dR, 1));
+ *          c0 = exp(x) - 1, c1 = dt exp(x / 2) sinh(x / 2) / (x / 2), x = v_box dt;
+ *   mode 1 (exp_iL2): P <- c0 P + c1 F,
+ *          c0 = exp(-x), c1 = (dt / 2) exp(-x / 2) sinh(x / 2) / (x / 2),
+ *          x = (1 + 1/N) v_box dt / 2.
+ * The coefficients are computed by the caller (the box variables are host
+ * scalars). */
+int jmd_npt_map(int32_t mode, float* position, float* momentum, const float* force,
+                const float* mass, float mass_scalar, int64_t n, const jmd_space* space,
+                float c0, float c1, void* stream);
+
 /* The O step of simulate.nvt_langevin's BAOAB step (stochastic_step,
  * simulate.py:1102-1110): p <- c1 p + c2 sqrt(m) xi with c1 = exp(-gamma dt),
  * c2 = sqrt(kT (1 - c1^2)).  xi is standard normal, drawn per atom from

@@ -192,6 +192,7 @@ SIGNATURES = {
     'jmd_batch_pair_forces': (C.c_int, [C.POINTER(Pair), C.POINTER(Batch), C.POINTER(BatchNList),
                                         P, P, P, P, P]),
     'jmd_batch_kinetic_energy': (C.c_int, [C.POINTER(Batch), P, P, P, F32, P, P, P]),
+    'jmd_npt_map': (C.c_int, [I32, P, P, P, P, F32, I64, C.POINTER(Space), F32, F32, P]),
     'jmd_batch_dot_per_system': (C.c_int, [C.POINTER(Batch), P, I64, P, I64, P, P]),
     'jmd_batch_nvt_adjoint_update': (C.c_int, [C.POINTER(Batch), I32, P, P, I64, P, P, F32, F32,
                                                P, P, P, P, P]),

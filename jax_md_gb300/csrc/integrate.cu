@@ -189,6 +189,39 @@ struct FireParams {
   float dt_max, n_min, f_inc, f_dec, alpha_start, f_alpha;
 };
 
+// simulate.npt_nose_hoover's exp(iL1) (mode 0: positions) and exp(iL2)
+// (mode 1: momenta) with caller-computed coefficients (jmd_npt_map).
+template <int DIM>
+__global__ void k_npt_map(int mode, float4* x, float4* p, const float4* f, const float* mass,
+                          float m0, int n, Geo g, float c0, float c1) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 q = p[i];
+  if (mode == 1) {
+    const float4 ff = f[i];
+    q.x = fmaf(c1, ff.x, c0 * q.x);
+    q.y = fmaf(c1, ff.y, c0 * q.y);
+    if (DIM == 3) q.z = fmaf(c1, ff.z, c0 * q.z);
+    p[i] = q;
+    return;
+  }
+  float4 r = x[i];
+  const float m = mass ? mass[i] : m0;
+  float dx = fmaf(c1, q.x / m, c0 * r.x), dy = fmaf(c1, q.y / m, c0 * r.y);
+  float dz = DIM == 3 ? fmaf(c1, q.z / m, c0 * r.z) : 0.f;
+  if (g.general) cell_apply<DIM>(g.Ti, dx, dy, dz);
+  if (g.periodic) {
+    r.x = wrap(r.x + dx, g.L[0]);
+    r.y = wrap(r.y + dy, g.L[1]);
+    if (DIM == 3) r.z = wrap(r.z + dz, g.L[2]);
+  } else {
+    r.x += dx;
+    r.y += dy;
+    if (DIM == 3) r.z += dz;
+  }
+  x[i] = r;
+}
+
 template <int DIM>
 __global__ void k_fire_kick_drift(float4* x, float4* p, const float4* f, const float* mass,
                                   float m0, int n, Geo g, const float* fs) {
@@ -417,6 +450,29 @@ int jmd_scale_momentum(float* momentum, int64_t p_stride, int64_t n, int32_t dim
   if (dim == 3) k_scale<3><<<gr, 256, 0, as_stream(stream)>>>(momentum, p_stride, (int)n, scale);
   else k_scale<2><<<gr, 256, 0, as_stream(stream)>>>(momentum, p_stride, (int)n, scale);
   return check_launch("jmd_scale_momentum");
+}
+
+int jmd_npt_map(int32_t mode, float* position, float* momentum, const float* force,
+                const float* mass, float mass_scalar, int64_t n, const jmd_space* space,
+                float c0, float c1, void* stream) {
+  JMD_REQUIRE(space && (space->dim == 2 || space->dim == 3), "bad space");
+  JMD_REQUIRE(mode == 0 || mode == 1, "mode must be 0 (positions) or 1 (momenta)");
+  JMD_REQUIRE(n >= 0 && n < INT32_MAX, "atom count out of range");
+  JMD_REQUIRE(momentum && is_vec4(momentum, 4), "momenta must be 16-byte aligned float4 rows");
+  JMD_REQUIRE(mode == 1 || (position && is_vec4(position, 4)),
+              "positions must be 16-byte aligned float4 rows");
+  JMD_REQUIRE(mode == 0 || (force && is_vec4(force, 4)), "forces must be 16-byte aligned float4 rows");
+  if (n == 0) return JMD_OK;
+  const unsigned gr = (unsigned)ceil_div(n, 256);
+  const Geo g = make_geo(*space);
+  auto* x = reinterpret_cast<float4*>(position);
+  auto* p = reinterpret_cast<float4*>(momentum);
+  auto* f = reinterpret_cast<const float4*>(force);
+  if (space->dim == 3)
+    k_npt_map<3><<<gr, 256, 0, as_stream(stream)>>>(mode, x, p, f, mass, mass_scalar, (int)n, g, c0, c1);
+  else
+    k_npt_map<2><<<gr, 256, 0, as_stream(stream)>>>(mode, x, p, f, mass, mass_scalar, (int)n, g, c0, c1);
+  return check_launch("jmd_npt_map");
 }
 
 int jmd_langevin_o_step(float* momentum, int64_t p_stride, int64_t n, int32_t dim,

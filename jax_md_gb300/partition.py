@@ -554,7 +554,7 @@ def neighbor_list(displacement_or_metric, box, r_cutoff, dr_threshold=0.0,
             plan.count = torch.zeros(n, dtype=torch.int32, device=dev)
         plan.ld = ld
         run_build(plan, R, rs, store, ld, error, ref, False)
-        plan.space0 = nl.space
+        plan.space0 = _space_struct(displacement_or_metric, dim, box)
         return NeighborList(idx, ref, PartitionError(error), cell_cap, max_occ, format,
                             float(mcs) if use_cells else None, plan if use_cells else None,
                             update_fn, plan)

@@ -17,6 +17,7 @@ import torch
 
 from . import _native as N
 from . import smap
+from . import space as _space
 
 
 def _kernel_energy(fn):
@@ -126,14 +127,25 @@ def temperature(*unused_args, momentum=None, velocity=None, mass=1.0):
     return (2.0 * ke / momentum.numel()).to(momentum.dtype)
 
 
-def _virial(energy_fn, position, **kwargs):
+def _virial(energy_fn, position, box=None, **kwargs):
+    """dU/d(strain) as a [d, d] f64 matrix; ``box`` reaches the energy as its
+    keyword (a general cell's current cell), and is dropped for a space that
+    refuses it, as quantity.py:225-229 does."""
     if not _kernel_energy(energy_fn):
         raise NotImplementedError('pressure/stress need a CUDA-backed energy function')
-    if isinstance(energy_fn, smap.PairAllEnergy):
-        _, _, _, W = energy_fn.compute(position, force=False, virial=True, **kwargs)
+    nb = kwargs.pop('neighbor', None)
+
+    def run(**kw):
+        if isinstance(energy_fn, smap.PairAllEnergy):
+            return energy_fn.compute(position, force=False, virial=True, **kw)[3]
+        return energy_fn.compute(position, nb, force=False, virial=True, **kw)[3]
+    if box is not None:
+        try:
+            W = run(box=box, **kwargs)
+        except _space.UnexpectedBoxException:
+            W = run(**kwargs)
     else:
-        nb = kwargs.pop('neighbor')
-        _, _, _, W = energy_fn.compute(position, nb, force=False, virial=True, **kwargs)
+        W = run(**kwargs)
     dim = position.shape[1]
     if dim == 3:
         xx, yy, zz, xy, xz, yz = W
@@ -146,7 +158,7 @@ def _virial(energy_fn, position, **kwargs):
 def pressure(energy_fn, position, box, kinetic_energy=0.0, **kwargs):
     """quantity.py:202-235: (2 KE - tr dU/d(strain)) / (d V)."""
     dim = position.shape[1]
-    W = _virial(energy_fn, position, **kwargs)
+    W = _virial(energy_fn, position, box=box, **kwargs)
     V = volume(dim, box)
     ke = kinetic_energy if isinstance(kinetic_energy, torch.Tensor) else torch.tensor(
         float(kinetic_energy), dtype=torch.float64, device=position.device)
@@ -156,7 +168,7 @@ def pressure(energy_fn, position, box, kinetic_energy=0.0, **kwargs):
 def stress(energy_fn, position, box, mass=1.0, velocity=None, **kwargs):
     """quantity.py:238-282: (sum m v v^T - dU/d(strain)) / V."""
     dim = position.shape[1]
-    W = _virial(energy_fn, position, **kwargs)
+    W = _virial(energy_fn, position, box=box, **kwargs)
     V = volume(dim, box)
     VxV = torch.zeros((dim, dim), dtype=torch.float64, device=position.device)
     if velocity is not None:

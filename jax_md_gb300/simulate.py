@@ -544,6 +544,207 @@ def nvt_nose_hoover_invariant(energy_fn, state: NVTNoseHooverState, kT, **kwargs
 
 
 # ---------------------------------------------------------------------------
+# NPT: simulate.py:704-1047
+@dataclasses.dataclass
+class NPTNoseHooverState(_StateMixin):
+    """simulate.py:704-760.  Particle arrays live on the device; the box
+    degrees of freedom (box_position = (1/d) log(V / V_0), its momentum and
+    mass, and dU/dV of the last force evaluation) are host f64 scalars, since
+    every kernel launch takes the current cell by value.  The two chains are
+    device chains (the thermostat's with N d degrees of freedom, the
+    barostat's with one)."""
+    position: torch.Tensor
+    momentum: torch.Tensor
+    force: torch.Tensor
+    mass: object
+    reference_box: np.ndarray
+    box_position: float
+    box_momentum: float
+    box_mass: float
+    dUdV: float
+    barostat: NoseHooverChain
+    thermostat: NoseHooverChain
+
+    @property
+    def velocity(self):
+        return self.momentum / _mass_col(self.mass)
+
+    @property
+    def box(self):
+        return npt_box(self)
+
+
+def sinhx_x(x: float) -> float:
+    """simulate.py:763-772: the Taylor series of sinh(x) / x."""
+    return 1 + x ** 2 / 6 + x ** 4 / 120 + x ** 6 / 5040 + x ** 8 / 362_880 + x ** 10 / 39_916_800
+
+
+def _npt_box_info(state: NPTNoseHooverState):
+    """simulate.py:775-783: (V, V -> box)."""
+    dim = state.position.shape[1]
+    ref = state.reference_box
+    V_0 = quantity.volume(dim, ref)
+    V = V_0 * math.exp(dim * state.box_position)
+    return V, (lambda v: (v / V_0) ** (1 / dim) * ref)
+
+
+def npt_box(state: NPTNoseHooverState) -> np.ndarray:
+    """simulate.py:786-792: the current cell."""
+    V, box_fn = _npt_box_info(state)
+    return box_fn(V)
+
+
+def _force_stress(energy_fn, R, box, F_out, **kwargs):
+    """(E, dU/dV) at R in the cell ``box``, with -dE/dR written into F_out:
+    the kernel's energy, forces and virial; dU/dV of the reference's
+    perturbation (1 + eps) (simulate.py:852-860) is the virial's trace."""
+    if isinstance(energy_fn, smap.PairAllEnergy):
+        e, F, _, W = energy_fn.compute(R, force=True, virial=True, box=box, **kwargs)
+    elif isinstance(energy_fn, smap.PairNeighborListEnergy):
+        nbrs = kwargs.pop('neighbor')
+        e, F, _, W = energy_fn.compute(R, nbrs, force=True, virial=True, box=box, **kwargs)
+    else:
+        raise NotImplementedError('npt_nose_hoover needs an energy from jax_md_gb300.energy')
+    F_out.copy_(F)
+    dim = R.shape[1]
+    return e, float(W[:dim].sum())
+
+
+def npt_nose_hoover(energy_fn, shift_fn, dt, pressure, kT, barostat_kwargs=None,
+                    thermostat_kwargs=None):
+    """simulate.npt_nose_hoover (simulate.py:795-1004): NPT with one
+    Nose-Hoover chain on the particles and one on the box (isotropic volume
+    moves of a periodic_general cell, fractional coordinates).  The forces,
+    virial and the exp(iL) maps of every step are kernels; the box scalars
+    are updated on the host between them."""
+    if not isinstance(shift_fn, _space.GeneralShift):
+        raise NotImplementedError('npt_nose_hoover needs the shift of space.periodic_general')
+    dt32 = float(np.float32(dt))
+    dt_2 = float(np.float32(dt / 2))
+
+    def nhc_kwargs(tau, overrides):
+        kw = {'chain_length': 3, 'chain_steps': 2, 'sy_steps': 3, 'tau': tau}  # simulate.py:520-537
+        kw.update(overrides or {})
+        return kw
+    bk = nhc_kwargs(1000 * dt, barostat_kwargs)
+    tk = nhc_kwargs(100 * dt, thermostat_kwargs)
+    bchain = _Chain(dt32, bk['chain_length'], bk['chain_steps'], bk['sy_steps'],
+                    float(np.float32(bk['tau'])))
+    tchain = _Chain(dt32, tk['chain_length'], tk['chain_steps'], tk['sy_steps'],
+                    float(np.float32(tk['tau'])))
+    L = N.lib()
+
+    def box_mass(n, dim, kT_):
+        return dim * (n + 1) * kT_ * bchain.tau ** 2
+
+    def init_fn(key, R, box, mass=1.0, momenta=None, **kwargs):
+        _kT = float(kwargs.pop('kT', kT))
+        n, dim = R.shape
+        R4 = _rows4(R.detach().to(torch.float32))
+        F4 = _rows4(torch.zeros_like(R4))
+        ref = _space.cell_matrix(box, dim)
+        _, dUdV = _force_stress(energy_fn, R4, ref, F4, **kwargs)
+        m = canonicalize_mass(mass, n, R.device)
+        P = initialize_momenta(R4, m, key, _kT) if momenta is None else momenta
+        P4 = _rows4(P)
+        KE = float(quantity._ke_f64(P4, m))
+        barostat = bchain.init(1, 0.0, _kT, R.device)
+        thermostat = tchain.init(quantity.count_dof(R), KE, _kT, R.device)
+        return NPTNoseHooverState(R4, P4, F4, m, ref, 0.0, 0.0, box_mass(n, dim, _kT), dUdV,
+                                  barostat, thermostat)
+
+    def apply_fn(state: NPTNoseHooverState, **kwargs):
+        _kT = float(kwargs.pop('kT', kT))
+        _pressure = float(kwargs.pop('pressure', pressure))
+        R, P, F, m = state.position, state.momentum, state.force, state.mass
+        n, dim = R.shape
+        dev = R.device
+        mptr, m0 = _mass_ptr(m)
+        scale = torch.empty((), dtype=torch.float64, device=dev)
+        # update_mass (both chains and the box), then the first half steps
+        # (simulate.py:975-985)
+        state.barostat.buffer[65] = _kT
+        state.thermostat.buffer[65] = _kT
+        M_b = box_mass(n, dim, _kT)
+        bchain.half_step(state.barostat, scale, update_mass=True)
+        P_b = state.box_momentum * float(scale)
+        tchain.half_step(state.thermostat, scale, update_mass=True)
+        N.check(L.jmd_scale_momentum(P.data_ptr(), P.stride(0), n, dim, scale.data_ptr(),
+                                     N.stream_ptr()), 'scale_momentum')
+        # inner step (simulate.py:938-973)
+        ref = state.reference_box
+        V_0 = quantity.volume(dim, ref)
+        alpha = 1 + 1 / n
+        R_b, dUdV = state.box_position, state.dUdV
+
+        def G_e(vol):  # box_force, simulate.py:915-923
+            KE2 = 2 * float(quantity._ke_f64(P, m))
+            return alpha * KE2 - dUdV - _pressure * vol * dim
+
+        def exp_iL2(v_b):
+            x = alpha * v_b * dt_2
+            c0 = math.exp(-x)
+            c1 = dt_2 * sinhx_x(x / 2) * math.exp(-x / 2)
+            N.check(L.jmd_npt_map(1, None, P.data_ptr(), F.data_ptr(), mptr, m0, n,
+                                  ctypes.byref(sp), c0, c1, N.stream_ptr()), 'npt_map')
+        vol = V_0 * math.exp(dim * R_b)
+        P_b = P_b + dt_2 * G_e(vol)
+        sp = shift_fn.space(dim, box=ref)   # exp_iL2 ignores the geometry
+        exp_iL2(P_b / M_b)
+        R_b = R_b + P_b / M_b * dt32
+        vol = V_0 * math.exp(dim * R_b)
+        box = (vol / V_0) ** (1 / dim) * ref
+        x = P_b / M_b * dt32
+        sp = shift_fn.space(dim, box=box)
+        N.check(L.jmd_npt_map(0, R.data_ptr(), P.data_ptr(), None, mptr, m0, n,
+                              ctypes.byref(sp), math.exp(x) - 1,
+                              dt32 * math.exp(x / 2) * sinhx_x(x / 2), N.stream_ptr()), 'npt_map')
+        _, dUdV = _force_stress(energy_fn, R, box, F, **kwargs)
+        exp_iL2(P_b / M_b)
+        P_b = P_b + dt_2 * G_e(vol)
+        # second half steps (simulate.py:987-1001)
+        quantity._ke_f64(P, m, out=state.thermostat.buffer[64])
+        state.barostat.buffer[64] = P_b ** 2 / (2 * M_b)
+        tchain.half_step(state.thermostat, scale)
+        N.check(L.jmd_scale_momentum(P.data_ptr(), P.stride(0), n, dim, scale.data_ptr(),
+                                     N.stream_ptr()), 'scale_momentum')
+        bchain.half_step(state.barostat, scale)
+        P_b = P_b * float(scale)
+        state.box_position, state.box_momentum, state.box_mass, state.dUdV = R_b, P_b, M_b, dUdV
+        return state
+
+    apply_fn.chains = (bchain, tchain)
+    return init_fn, apply_fn
+
+
+def npt_nose_hoover_invariant(energy_fn, state: NPTNoseHooverState, pressure, kT, **kwargs):
+    """simulate.py:1007-1047 (f64): potential and kinetic energy, both
+    chains, P V and the box's kinetic energy."""
+    V, box_fn = _npt_box_info(state)
+    box = box_fn(V)
+    if isinstance(energy_fn, smap.PairAllEnergy):
+        PE = float(energy_fn.compute(state.position, force=False, box=box, **kwargs)[0])
+    elif isinstance(energy_fn, smap.PairNeighborListEnergy):
+        nbrs = kwargs.pop('neighbor')
+        PE = float(energy_fn.compute(state.position, nbrs, force=False, box=box, **kwargs)[0])
+    else:
+        PE = float(energy_fn(state.position, box=box, **kwargs))
+    E = PE + float(quantity._ke_f64(state.momentum, state.mass))
+    dof = quantity.count_dof(state.position)
+    c = state.thermostat
+    xi, p, Q = (c.position.cpu().numpy(), c.momentum.cpu().numpy(), c.mass.cpu().numpy())
+    E += p[0] ** 2 / (2 * Q[0]) + dof * kT * xi[0]
+    for r, pp, mm in zip(xi[1:], p[1:], Q[1:]):
+        E += pp ** 2 / (2 * mm) + kT * r
+    c = state.barostat
+    xi, p, Q = (c.position.cpu().numpy(), c.momentum.cpu().numpy(), c.mass.cpu().numpy())
+    for r, pp, mm in zip(xi, p, Q):
+        E += pp ** 2 / (2 * mm) + kT * r
+    E += pressure * V + state.box_momentum ** 2 / (2 * state.box_mass)
+    return E
+
+
+# ---------------------------------------------------------------------------
 # Device-resident runner
 def _nve_system(st: '_Stepper', state: NVEState, nbrs, alt: torch.Tensor) -> N.NveSystem:
     e = st.energy_fn

@@ -436,34 +436,43 @@ class PairAllEnergy:
         self.geometry = self.inner.geometry
         self._cache = {}
 
-    def _neighbors(self, R):
+    def _neighbors(self, R, box=None):
+        """The all-pairs list at R (pruned at the cutoff, rebuilt every call);
+        ``box`` is a general cell's ``box`` keyword.  A list that overflows
+        (pairs came closer) is re-allocated, so every pair is always kept."""
         n, dim = R.shape
         key = (n, dim, R.device)
+        geo = self.geometry
+        frac = isinstance(geo, _space.GeneralDisplacement) and geo.fractional_coordinates
+        kw = {'box': box} if (box is not None and frac) else {}
         nb = self._cache.get(key)
         if nb is None:
-            geo = self.geometry
-            box = geo.box if geo.periodic else 1.0e30
+            lbox = geo.box if geo.periodic else 1.0e30
             rc = self.fn.r_cutoff
             if self.fn.kind == N.SOFT_SPHERE:
                 sig = self.inner.params.get('sigma', 1.0)
                 rc = float(np.max(np.asarray(sig.detach().cpu() if isinstance(sig, torch.Tensor) else sig)))
             if not np.isfinite(rc):
                 rc = 1.0e18
-            fns = partition.neighbor_list(geo, box, rc, 0.0, capacity_multiplier=1.0,
-                                          disable_cell_list=True)
-            nb = (fns, fns.allocate(R))
+            fns = partition.neighbor_list(geo, lbox, rc, 0.0, capacity_multiplier=1.0,
+                                          disable_cell_list=True, fractional_coordinates=frac)
+            nb = (fns, fns.allocate(R, **kw))
             self._cache = {key: nb}
             return nb[1]
-        return nb[0].update(R, nb[1])
+        lst = nb[0].update(R, nb[1], **kw)
+        if kw and bool(lst.did_buffer_overflow):
+            lst = nb[0].allocate(R, extra_capacity=max(8, lst.max_occupancy // 4), **kw)
+            self._cache = {key: (nb[0], lst)}
+        return lst
 
     def __call__(self, R, **dynamic):
-        return self.inner(R, self._neighbors(R.detach()), **dynamic)
+        return self.inner(R, self._neighbors(R.detach(), dynamic.get('box')), **dynamic)
 
     def compute(self, R, **kw):
-        return self.inner.compute(R, self._neighbors(R), **kw)
+        return self.inner.compute(R, self._neighbors(R, kw.get('box')), **kw)
 
     def forces(self, R, **kw):
-        return self.inner.forces(R, self._neighbors(R), **kw)
+        return self.inner.forces(R, self._neighbors(R, kw.get('box')), **kw)
 
 
 def pair(fn, displacement_or_metric, species=None, reduce_axis=None, **kwargs):

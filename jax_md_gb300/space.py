@@ -246,10 +246,15 @@ class GeneralShift:
     """Shift of space.periodic_general (space.py:436-466): dR lives in the
     cell; R in the unit cube (fractional) or in the cell."""
 
-    def space(self, dim: int) -> N.Space:
-        """Kernel geometry of the shift (see GeneralDisplacement.space)."""
+    def space(self, dim: int, box=None) -> N.Space:
+        """Kernel geometry of the shift (see GeneralDisplacement.space);
+        ``box`` replaces the cell, as the shift's keyword does."""
+        T = self.box if box is None else box
         if self.fractional_coordinates and self.wrapped:
-            return general_space(self.box, dim)
+            return general_space(T, dim)
+        if box is not None:
+            raise NotImplementedError('a box keyword with real coordinates is not implemented by '
+                                      'the integrator kernels')
         M = cell_matrix(self.box, dim)
         if self.fractional_coordinates or not np.array_equal(np.diag(np.diag(M)), M):
             raise NotImplementedError('the integrator kernels take wrapped fractional coordinates '

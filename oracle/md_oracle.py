@@ -843,6 +843,102 @@ def nvt_nose_hoover_step(force_fn, R, P, F, mass, c, dt, kT, box,
     return R, P, F, c
 
 
+def sinhx_x(x):
+    """simulate.py:763-772 (Taylor series of sinh(x) / x)."""
+    return 1 + x ** 2 / 6 + x ** 4 / 120 + x ** 6 / 5040 + x ** 8 / 362_880 + x ** 10 / 39_916_800
+
+
+def _chain_masses(c: ChainO, kT):
+    """simulate.py:509-517 (update_mass): Q = kT tau^2, Q_0 x dof."""
+    Q = kT * c.tau ** 2 * np.ones(len(c.Q))
+    Q[0] *= c.dof
+    return ChainO(c.xi, c.p_xi, Q, c.tau, c.KE, c.dof)
+
+
+def npt_init(force_stress, R, P, box, mass, kT, dt, chain_length=3):
+    """simulate.py:862-903 (init_fn of npt_nose_hoover) from given momenta:
+    box_position = box_momentum = 0, box mass d (N + 1) kT tau_b^2, a
+    one-degree barostat chain (tau_b = 1000 dt) and a thermostat chain on
+    N d degrees of freedom (tau = 100 dt)."""
+    R = np.asarray(R, np.float64)
+    P = np.asarray(P, np.float64)
+    n, dim = R.shape
+    ref = np.asarray(box, np.float64)
+    if ref.ndim == 0:
+        ref = np.eye(dim) * float(ref)
+    _, F, dUdV = force_stress(R, ref)
+    tau_b, tau_t = 1000 * dt, 100 * dt
+    return {'R': R, 'P': P, 'F': F, 'mass': mass, 'ref': ref, 'R_b': 0.0, 'P_b': 0.0,
+            'M_b': dim * (n + 1) * kT * tau_b ** 2, 'dUdV': dUdV,
+            'bc': nhc_init(1, 0.0, kT, tau_b, chain_length),
+            'tc': nhc_init(n * dim, kinetic_energy(P, mass), kT, tau_t, chain_length)}
+
+
+def npt_box(s):
+    """simulate.py:786-792."""
+    dim = s['R'].shape[1]
+    V0 = float(np.linalg.det(s['ref']))
+    V = V0 * np.exp(dim * s['R_b'])
+    return (V / V0) ** (1 / dim) * s['ref'], V
+
+
+def npt_nose_hoover_step(force_stress, s, pressure, kT, dt, chain_steps=2, sy_steps=3):
+    """simulate.py:938-1001 (inner_step and apply_fn of npt_nose_hoover) in
+    FP64; positions fractional in the cell, shifted by the
+    PeriodicGeneral shift with the new cell."""
+    s = dict(s)
+    R, P, F, m = s['R'], s['P'], s['F'], s['mass']
+    n, dim = R.shape
+    dt_2 = dt / 2
+    bc, tc = _chain_masses(s['bc'], kT), _chain_masses(s['tc'], kT)
+    M_b = dim * (n + 1) * kT * bc.tau ** 2
+    P_b, bc = nhc_half_step(s['P_b'], bc, kT, dt, chain_steps, sy_steps)
+    P, tc = nhc_half_step(P, tc, kT, dt, chain_steps, sy_steps)
+    V0 = float(np.linalg.det(s['ref']))
+    alpha = 1 + 1 / n
+    R_b, dUdV = s['R_b'], s['dUdV']
+
+    def G(vol, P, dUdV):
+        return alpha * float(np.sum(P ** 2 / m)) - dUdV - pressure * vol * dim
+
+    def exp_iL2(P, F, v_b):
+        x = alpha * v_b * dt_2
+        return P * np.exp(-x) + dt_2 * F * sinhx_x(x / 2) * np.exp(-x / 2)
+    vol = V0 * np.exp(dim * R_b)
+    P_b = P_b + dt_2 * G(vol, P, dUdV)
+    P = exp_iL2(P, F, P_b / M_b)
+    R_b = R_b + P_b / M_b * dt
+    vol = V0 * np.exp(dim * R_b)
+    box = (vol / V0) ** (1 / dim) * s['ref']
+    x = P_b / M_b * dt
+    dR = R * (np.exp(x) - 1) + dt * (P / m) * np.exp(x / 2) * sinhx_x(x / 2)
+    R = PeriodicGeneral(s['ref']).shift(R, dR, box=box)
+    _, F, dUdV = force_stress(R, box)
+    P = exp_iL2(P, F, P_b / M_b)
+    P_b = P_b + dt_2 * G(vol, P, dUdV)
+    tc = ChainO(tc.xi, tc.p_xi, tc.Q, tc.tau, kinetic_energy(P, m), tc.dof)
+    bc = ChainO(bc.xi, bc.p_xi, bc.Q, bc.tau, P_b ** 2 / (2 * M_b), bc.dof)
+    P, tc = nhc_half_step(P, tc, kT, dt, chain_steps, sy_steps)
+    P_b, bc = nhc_half_step(P_b, bc, kT, dt, chain_steps, sy_steps)
+    s.update(R=R, P=P, F=F, R_b=R_b, P_b=float(P_b), M_b=M_b, dUdV=dUdV, bc=bc, tc=tc)
+    return s
+
+
+def npt_invariant(PE, s, pressure, kT):
+    """simulate.py:1007-1047."""
+    _, V = npt_box(s)
+    n, dim = s['R'].shape
+    E = PE + kinetic_energy(s['P'], s['mass'])
+    c = s['tc']
+    E += c.p_xi[0] ** 2 / (2 * c.Q[0]) + n * dim * kT * c.xi[0]
+    for x, p, q in zip(c.xi[1:], c.p_xi[1:], c.Q[1:]):
+        E += p ** 2 / (2 * q) + kT * x
+    c = s['bc']
+    for x, p, q in zip(c.xi, c.p_xi, c.Q):
+        E += p ** 2 / (2 * q) + kT * x
+    return E + pressure * V + s['P_b'] ** 2 / (2 * s['M_b'])
+
+
 def nvt_invariant(PE, P, mass, c: ChainO, kT):
     """simulate.py:672-701."""
     E = PE + kinetic_energy(P, mass)

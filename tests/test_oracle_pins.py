@@ -438,3 +438,36 @@ def test_oracle_dense_rows_of_a_subset_match_build(dim):
     assert np.array_equal(rows[:, :w], full.idx[atoms])
     assert np.all(rows[:, w:] == 700)
     assert np.array_equal(counts, (full.idx[atoms] < 700).sum(1))
+
+
+def _jammed_npt_system():
+    g = np.load(GOLDEN / 'jammed_soft_sphere_2d.npz')
+    spec = O.PairSpec(kind='soft_sphere', sigma=g['sigma'], epsilon=1.0, alpha=2.0,
+                      species=g['species'])
+
+    def force_stress(R, box):
+        E, F, W = O.all_pairs_energy_forces(spec, R, O.PeriodicGeneral(box))
+        return E, F, float(np.trace(W))
+    return g, spec, force_stress
+
+
+def test_npt_nose_hoover_jammed_conserves_invariant():
+    """tests/simulate_test.py:360-400 on the oracle: NPT Nose-Hoover of the
+    golden jammed soft-sphere packing in its periodic_general cell (kT 1e-3,
+    dt 1e-3, target pressure the packing's own) keeps the extended
+    Hamiltonian to the reference's f64 tolerance (1.2e-4) over 800 steps and
+    the pressure near its target (5%)."""
+    g, spec, fs = _jammed_npt_system()
+    R = g['fractional_position']
+    kT, dt, Pt = 1e-3, 1e-3, float(g['pressure'])
+    P = O.maxwell_boltzmann(len(R), 2, kT, seed=3, dtype=np.float64)
+    s = O.npt_init(fs, R, P, g['box'], 1.0, kT, dt)
+    H0 = O.npt_invariant(fs(s['R'], O.npt_box(s)[0])[0], s, Pt, kT)
+    for _ in range(800):
+        s = O.npt_nose_hoover_step(fs, s, Pt, kT, dt)
+        box, V = O.npt_box(s)
+        E, _, dUdV = fs(s['R'], box)
+        H = O.npt_invariant(E, s, Pt, kT)
+        assert abs(H - H0) <= 1.2e-4 * max(1.0, abs(H0)), (H, H0)
+        p = (2 * O.kinetic_energy(s['P']) - dUdV) / (2 * V)
+        assert abs(p - Pt) <= 0.05 + 0.05 * abs(Pt), (p, Pt)
