@@ -798,18 +798,24 @@ def main():
     torch.cuda.synchronize()
     kern_ms = e0.elapsed_time(e1) / reps
     assert int(sb.seg_status) == 0, 'segment staging reported a problem'
-    # algorithmic bytes of one fused-step launch: the list as read (16-byte
-    # chunks of 8 two-byte staged slots; int32 entries on the tiled list),
-    # the count, position read + write, momentum read + write, reference read
+    # algorithmic bytes of one atom-step of the path (plain Dense LJ NVE,
+    # fp32): 4 n-bar (the Dense list entries) + 96 (position, momentum and
+    # force rows read and written, 16 B each), n-bar the mean stored
+    # neighbour count -- the path's figure, independent of the layout that
+    # runs it.  The timed layout itself needs fewer: `layout_bytes_per_atom`
+    # (the list as read -- 16-byte chunks of 8 two-byte staged slots, or int32
+    # entries on the tiled list -- with the count, position read + write,
+    # momentum read + write, reference read, and for half lists the force
+    # accumulator reduced into, read and cleared), and the ncu DRAM bytes in
+    # `traffic`.
+    path_bytes = 4.0 * nbar + 96.0
     list_bytes = chunk_bytes if seg_on else 4 * nbar + 4
     half = bool(getattr(sb, 'seg_half', 0)) and seg_on
     layout_name = 'half' if half else ('full' if seg_on else 'tiled')
-    # half lists: + the force accumulator, reduced into, read and cleared
-    kern_bytes = n * (list_bytes + 80 + (48 if half else 0))
+    layout_bytes = list_bytes + 80 + (48 if half else 0)
+    kern_bytes = n * path_bytes
     hbm, src = peaks()
     achieved = kern_bytes / (kern_ms / 1e3) / 1e9
-    # per step: + force row written by the closing kick and read by the next
-    # opening kick is fused away; the skin flag and rebuilds are extra
     step_bytes = kern_bytes
 
     # e2e: host pinned buffers through the public API (simulate.run, default
@@ -875,7 +881,10 @@ def main():
                                 ('k_seg_step fused NVE step (LJ, segment-local list, FP32x2)'
                                  if seg_on else 'k_tiled fused NVE step (LJ, Dense tiled, FP32x2)')),
                      'kernel_ms': kern_ms,
-                     'bytes_per_atom': kern_bytes / n,
+                     'bytes_per_atom': path_bytes,
+                     'bytes_per_atom_rule': '4 n_bar + 96 (Dense list entries + position, '
+                                            'momentum and force rows read and written)',
+                     'layout_bytes_per_atom': layout_bytes,
                      'step_algorithmic_GBps': step_bytes * args.steps / (ms / 1e3) / 1e9},
         'e2e': {'value': e2e_value, 'unit': 'atom-steps/s', 'h2d_bytes_per_step': 2 * n * 12,
                 'd2h_bytes_per_step': 2 * n * 12, 'call': e2e_call,

@@ -423,9 +423,27 @@ k_seg_half(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
         gz = mul2(g, dz);
         az = add2(az, gz);
       }
-      // reactions (masked pairs, the far slot included, add nothing)
-      if (m0) deposit(j0, gx.x, gy.x, DIM == 3 ? gz.x : 0.f);
-      if (m1) deposit(j1, gx.y, gy.y, DIM == 3 ? gz.y : 0.f);
+      // reactions (masked pairs, the far slot included, add nothing).  One
+      // packed test of both pair forces' squared magnitudes, g^2 r^2 <
+      // kFixMax^2, clears both for the fixed-point path (each component is
+      // at most the magnitude); otherwise each pair goes through deposit's
+      // per-component test
+      const float2 f2m = mul2(mul2(g, g), r2);
+      if (f2m.x < kFixMax * kFixMax && f2m.y < kFixMax * kFixMax) {
+        if (m0) {
+          red_shared_s32(fx + j0, __float2int_rn(gx.x * kFixScale));
+          red_shared_s32(fy + j0, __float2int_rn(gy.x * kFixScale));
+          if (DIM == 3) red_shared_s32(fz + j0, __float2int_rn(gz.x * kFixScale));
+        }
+        if (m1) {
+          red_shared_s32(fx + j1, __float2int_rn(gx.y * kFixScale));
+          red_shared_s32(fy + j1, __float2int_rn(gy.y * kFixScale));
+          if (DIM == 3) red_shared_s32(fz + j1, __float2int_rn(gz.y * kFixScale));
+        }
+      } else {
+        if (m0) deposit(j0, gx.x, gy.x, DIM == 3 ? gz.x : 0.f);
+        if (m1) deposit(j1, gx.y, gy.y, DIM == 3 ? gz.y : 0.f);
+      }
     };
     pair2((int)(cur.x & 0xFFFFu), (int)(cur.x >> 16));
     pair2((int)(cur.y & 0xFFFFu), (int)(cur.y >> 16));
