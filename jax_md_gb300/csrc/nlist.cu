@@ -1135,13 +1135,21 @@ __global__ void k_seg_zero_counts(int32_t* count, int n, const int32_t* flag) {
 __global__ void k_seg_occupancy(const int32_t* count, int n, int width, Bins b,
                                 const int32_t* flag) {
   if (skip(flag)) return;
+  __shared__ unsigned wmax[32];
   int m = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     m = max(m, count[i]);
   m = __reduce_max_sync(0xffffffffu, (unsigned)m);
-  if ((threadIdx.x & 31) == 0 && m > 0) {
-    atomicMax(&b.sc->occupancy, (unsigned long long)m);
-    if (m > width) atomicOr(&b.sc->flags, (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
+  // one atomic per block (thousands of warps on one address serialise)
+  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = (unsigned)m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const unsigned v = threadIdx.x < (blockDim.x >> 5) ? wmax[threadIdx.x] : 0u;
+    const unsigned bm = __reduce_max_sync(0xffffffffu, v);
+    if (threadIdx.x == 0 && bm > 0) {
+      atomicMax(&b.sc->occupancy, (unsigned long long)bm);
+      if ((int)bm > width) atomicOr(&b.sc->flags, (unsigned)JMD_NEIGHBOR_LIST_OVERFLOW);
+    }
   }
 }
 
@@ -1210,7 +1218,9 @@ int build_segment_after_sort(const jmd_nlist* nl, const SegGrid& sg, const float
       else e = sg.frame ? go(k_seg_search<2, true, false>) : go(k_seg_search<2, false, false>);
     }
     if (e) return e;
-    if (sg.half) k_seg_occupancy<<<zgrid, 256, 0, st>>>(nbr_count, (int)n, width, b, rebuild_flag);
+    if (sg.half)
+      k_seg_occupancy<<<(unsigned)std::min<int64_t>(zgrid, 4 * 152), 256, 0, st>>>(
+          nbr_count, (int)n, width, b, rebuild_flag);
   }
   FinalizeArgs f{JMD_DENSE, nl->max_occupancy, 1, nl->cell_capacity, (int)n};
   k_finalize<<<1, 1, 0, st>>>(b, f, occupancy, error_code, rebuild_flag);
