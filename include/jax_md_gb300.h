@@ -516,6 +516,13 @@ typedef struct {
 /* jmd_sorted_state.flags: leave the caller's Dense list unbuilt on exit (the
  * caller builds it at reference_position when it is read). */
 #define JMD_RUN_SKIP_EXIT_LIST 1
+/* jmd_sorted_state.flags: the private copy holds the cell order, list and
+ * reference positions a previous run of the same system left.  The caller's
+ * state is loaded in that order and the run's first rebuild is taken only
+ * when it is needed: a rebuild pending from the previous run, an error or
+ * staging status left by it, or an atom of the loaded state farther than
+ * the skin threshold from its reference position (partition.py:1146-1154). */
+#define JMD_RUN_WARM_START 2
 
 /* Segment-local engine list of a cell grid (no reference counterpart: the
  * engine's private layout).  A segment is `cells` consecutive cells along x

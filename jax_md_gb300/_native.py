@@ -81,6 +81,7 @@ class SortedState(C.Structure):
 
 
 RUN_SKIP_EXIT_LIST = 1
+RUN_WARM_START = 2
 
 
 class Nvt(C.Structure):

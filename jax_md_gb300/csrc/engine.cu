@@ -283,6 +283,29 @@ __global__ void k_load_user(int n, const float4* x, const float4* p, const float
   perm[i] = i;
 }
 
+// Warm start: the caller's state into the private cell order of the previous
+// run (slot s takes atom perm[s]); a rebuild is forced when the previous run
+// left an error bit or a staging status.
+__global__ void k_load_user_warm(int n, const float4* x, const float4* p, const float4* f,
+                                 const int32_t* species, float4* xs, float4* ps, float4* fs,
+                                 int32_t* ss, const int32_t* perm, uint8_t* err,
+                                 int32_t* seg_status, bool species_in_w, int32_t* rebuild_flag) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) {
+    if (*err || (seg_status && *seg_status)) *rebuild_flag = 1;
+    *err = 0;
+    if (seg_status) *seg_status = 0;
+  }
+  if (s >= n) return;
+  const int i = perm[s];
+  float4 r = x[i];
+  r.w = (species_in_w && species) ? __int_as_float(species[i]) : 0.f;
+  xs[s] = r;
+  ps[s] = p[i];
+  fs[s] = f[i];
+  if (species) ss[s] = species[i];
+}
+
 __global__ void k_store_user(int n, const int32_t* perm, const float4* xs, const float4* ps,
                              const float4* fs, const float4* rs, float4* x, float4* p, float4* f,
                              float4* ref) {
@@ -412,15 +435,40 @@ int enqueue_run_sorted(const jmd_nve_system& s, const jmd_sorted_state& z, int64
     return rebuild_at(x, true, false, st);
   };
   int rc;
-  k_load_user<<<gr, 256, 0, st>>>(n, reinterpret_cast<const float4*>(s.position),
-                                  reinterpret_cast<const float4*>(s.momentum),
-                                  reinterpret_cast<const float4*>(s.force), s.species,
-                                  reinterpret_cast<float4*>(z.position_a),
-                                  reinterpret_cast<float4*>(z.momentum),
-                                  reinterpret_cast<float4*>(z.force), z.species, z.perm,
-                                  z.error_code, seg ? z.seg_status : nullptr, seg);
-  JMD_CUDA(cudaGetLastError());
-  if ((rc = rebuild_at(z.position_a, false, true, st))) return rc;
+  const bool warm = (z.flags & JMD_RUN_WARM_START) != 0 && !always;
+  if (warm) {
+    k_load_user_warm<<<gr, 256, 0, st>>>(n, reinterpret_cast<const float4*>(s.position),
+                                         reinterpret_cast<const float4*>(s.momentum),
+                                         reinterpret_cast<const float4*>(s.force), s.species,
+                                         reinterpret_cast<float4*>(z.position_a),
+                                         reinterpret_cast<float4*>(z.momentum),
+                                         reinterpret_cast<float4*>(z.force), z.species, z.perm,
+                                         z.error_code, seg ? z.seg_status : nullptr, seg,
+                                         z.rebuild_flag);
+    JMD_CUDA(cudaGetLastError());
+    if ((rc = jmd_skin_check(z.position_a, 4, z.reference_position, 4, s.n, &s.space,
+                             s.threshold_sq, z.rebuild_flag, st)))
+      return rc;
+    // the first rebuild (with the forces, which the sort permutes) only when
+    // the flag asks for it
+    if (graphed)
+      rc = conditional(z.rebuild_flag,
+                       [&](cudaStream_t b) { return rebuild_at(z.position_a, true, true, b); },
+                       st, body_st);
+    else
+      rc = rebuild_at(z.position_a, true, true, st);
+    if (rc) return rc;
+  } else {
+    k_load_user<<<gr, 256, 0, st>>>(n, reinterpret_cast<const float4*>(s.position),
+                                    reinterpret_cast<const float4*>(s.momentum),
+                                    reinterpret_cast<const float4*>(s.force), s.species,
+                                    reinterpret_cast<float4*>(z.position_a),
+                                    reinterpret_cast<float4*>(z.momentum),
+                                    reinterpret_cast<float4*>(z.force), z.species, z.perm,
+                                    z.error_code, seg ? z.seg_status : nullptr, seg);
+    JMD_CUDA(cudaGetLastError());
+    if ((rc = rebuild_at(z.position_a, false, true, st))) return rc;
+  }
   float* cur = z.position_a;
   float* nxt = z.position_b;
   const int64_t width = s.nlist.max_occupancy;

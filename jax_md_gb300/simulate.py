@@ -1013,7 +1013,14 @@ def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bo
         if use_sort:
             seg = _segment_shape(neighbor, layout)
             sb = _sorted_buffers(state, neighbor, species, seg)
-            sb.flags = N.RUN_SKIP_EXIT_LIST if lazy_list else 0
+            # the private copy continues the previous run of this state on
+            # this list: its first rebuild is taken only if the skin test
+            # (or a pending flag, an error) asks for it
+            warm_key = (id(neighbor.plan), neighbor.plan.nl.max_occupancy,
+                        neighbor.plan.nl.cell_capacity, seg, nvt)
+            warm = getattr(sb, 'warm_key', None) == warm_key
+            sb.flags = ((N.RUN_SKIP_EXIT_LIST if lazy_list else 0) |
+                        (N.RUN_WARM_START if warm else 0))
             z = sb.struct()
             neighbor.set_pending_build(None)
             if nvt:
@@ -1025,6 +1032,7 @@ def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bo
                 N.check(N.lib().jmd_nve_run_sorted(ctypes.byref(sysd), ctypes.byref(z),
                                                    int(n_steps), 1 if use_graph else 0,
                                                    N.stream_ptr()), 'nve_run_sorted')
+            sb.warm_key = warm_key
             if lazy_list:
                 nb = neighbor
                 neighbor.set_pending_build(lambda: partition.build_at_reference(nb))
