@@ -377,3 +377,42 @@ def test_half_list_occupancy_and_overflow_follow_full_rows(cuda):
     assert out['half'][0] == out['segment'][0]
     assert torch.equal(out['half'][1], out['segment'][1])
     assert out['half'][2] and out['segment'][2]
+
+
+@pytest.mark.parametrize('layout', ['segment', 'half', 'tiled'])
+def test_warm_start_rebuilds_when_the_caller_moves_atoms(cuda, layout):
+    """A run that continues the previous run of the same state takes its
+    first rebuild only when needed: after the caller moves a few atoms by
+    half a lattice constant between runs (onto octahedral sites, far beyond
+    the skin threshold), the next run's forces still match the FP64 oracle
+    at its final positions, and an unchanged state continues as one run
+    would."""
+    from jax_md_gb300 import simulate
+    spatial = pytest.importorskip('scipy.spatial')
+    _, _, L, _, _, _, apply_a, st_a, nb_a = _setup(cuda, n_cells=10)
+    simulate.run(apply_a, st_a, nb_a, 5, layout=layout)
+    # move every 97th atom by a / 2 along x (wrapped), then continue
+    with torch.no_grad():
+        moved = torch.arange(0, st_a.position.shape[0], 97, device=cuda)
+        st_a.position[moved, 0] = torch.remainder(st_a.position[moved, 0] + L / 20, L)
+    simulate.run(apply_a, st_a, nb_a, 2, layout=layout)
+    torch.cuda.synchronize()
+    assert simulate.last_run_status(st_a) == 0
+    X = st_a.position.double().cpu().numpy()
+    pairs = spatial.cKDTree(np.mod(X, L), boxsize=L).query_pairs(2.5, output_type='ndarray')
+    idx = np.stack([pairs.min(1), pairs.max(1)])
+    _, Fo, _ = O.pair_energy_forces(lj_spec(), X, idx, O.ORDERED_SPARSE, np.full(3, L))
+    F = st_a.force.cpu().numpy()
+    # moved atoms may overlap their new neighbours: compare to the fp32
+    # conditioning of the pair sums
+    tol = 1e-4 + 4e-6 * np.abs(Fo).max()
+    assert np.abs(F - Fo).max() < tol, np.abs(F - Fo).max()
+    # an unchanged state: two warm runs of 4 steps against one run of 8
+    _, _, _, _, _, _, apply_b, st_b, nb_b = _setup(cuda, n_cells=10)
+    _, _, _, _, _, _, apply_c, st_c, nb_c = _setup(cuda, n_cells=10)
+    simulate.run(apply_b, st_b, nb_b, 4, layout=layout)
+    simulate.run(apply_b, st_b, nb_b, 4, layout=layout)
+    simulate.run(apply_c, st_c, nb_c, 8, layout=layout)
+    torch.cuda.synchronize()
+    assert (st_b.position - st_c.position).abs().max().item() < 1e-5
+    assert (st_b.momentum - st_c.momentum).abs().max().item() < 1e-3
