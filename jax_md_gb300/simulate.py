@@ -963,7 +963,8 @@ def _run_loop(apply_fn, state, neighbor, n_steps, neighbor_fn, max_reallocations
 
 
 def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bool = True,
-        max_reallocations: int = 4, sort=None, layout=None, lazy_list: bool = True):
+        max_reallocations: int = 4, sort=None, layout=None, lazy_list: bool = True,
+        warm_start: bool = True):
     """Runs the reference loop body ``n_steps`` times on the device:
 
         nbrs = nbrs.update(state.position); state = apply_fn(state, neighbor=nbrs)
@@ -981,7 +982,11 @@ def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bo
     before returning.  ``layout`` picks the private list of a sorted run:
     None / 'segment' (the segment-local list wherever it applies, with the
     autotuned or default cells per segment), an int (that many cells per
-    segment), or 'tiled' (the tiled int32 list).  Returns (state, neighbor)."""
+    segment), or 'tiled' (the tiled int32 list).  A sorted run that continues
+    the previous run of the same state and list keeps its private cell order
+    and list (``warm_start``) and rebuilds only when the skin test asks;
+    ``warm_start=False`` re-sorts and rebuilds at the start of every run (one
+    CUDA graph per run length instead of two).  Returns (state, neighbor)."""
     st = apply_fn.stepper
     e = st.energy_fn
     if isinstance(e, smap.PairNeighborListEnergy) and e.has_particle_arrays():
@@ -1018,7 +1023,7 @@ def run(apply_fn, state, neighbor, n_steps: int, neighbor_fn=None, use_graph: bo
             # (or a pending flag, an error) asks for it
             warm_key = (id(neighbor.plan), neighbor.plan.nl.max_occupancy,
                         neighbor.plan.nl.cell_capacity, seg, nvt)
-            warm = getattr(sb, 'warm_key', None) == warm_key
+            warm = warm_start and getattr(sb, 'warm_key', None) == warm_key
             sb.flags = ((N.RUN_SKIP_EXIT_LIST if lazy_list else 0) |
                         (N.RUN_WARM_START if warm else 0))
             z = sb.struct()
