@@ -107,3 +107,22 @@ def test_segment_threads_default():
     assert simulate.segment_threads_default(5, 40) == 160
     assert simulate.segment_threads_default(1, 46) == 64
     assert simulate.segment_threads_default(14, 60) == 256
+
+
+def test_segment_autotuner_candidates_and_cache_keys():
+    """The autotuner's candidates on the benchmark's grid: every admitted K
+    with full lists (staged or global), half lists (also at 256 threads),
+    and the tiled list; a tiled choice survives the cache's JSON round trip
+    as a name, a segment choice as a tuple."""
+    import json
+    from jax_md_gb300 import tune
+    cands = tune.segment_candidates(_nl(35, 40, 3))
+    assert 'tiled' in cands
+    shapes = [c for c in cands if c != 'tiled']
+    assert {c[0] for c in shapes} == {2, 3, 4, 5, 6, 8}
+    assert (5, 160, 1, 0) in shapes and (5, 160, 0, 0) in shapes and (5, 160, 0, 1) in shapes
+    assert (5, 256, 0, 1) in shapes
+    assert all(64 <= c[1] <= 256 and c[1] % 32 == 0 for c in shapes)
+    for c in ('tiled', (5, 160, 0, 1)):
+        k = json.dumps(c if isinstance(c, str) else list(c))
+        assert tune._unkey(json.loads(k)) == c
