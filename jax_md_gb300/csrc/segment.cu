@@ -36,6 +36,7 @@ struct SegStepArgs {
   float thr2;
   int32_t* flag;
   int32_t* status;
+  float fix_max;             // half lists: largest reaction component kept in fixed point
 };
 
 __device__ __forceinline__ int sclamp(int s, int nsp) { return s < 0 ? 0 : (s >= nsp ? nsp - 1 : s); }
@@ -212,15 +213,17 @@ k_seg_step(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
 }
 
 // Reaction accumulators of the half-list kernel are fixed point: 32-bit
-// integer additions in shared memory are single native reductions on this
-// part, while float (and 64-bit) ones are compare-and-swap loops.  A reaction
-// component v with |v| < kFixMax is added as round(v 2^19) (resolution
-// 1.9e-6); an atom takes at most ~60 contributions within one CTA, so the
-// sum stays below 60 x 64 x 2^19 < 2^31.  Larger reactions (close contacts)
-// and the own atoms' forces go to global memory as float reductions.
+// integer reductions in shared memory measured several times faster than
+// float (and 64-bit) ones on this part.  A force component v with |v| <
+// fix_max is added as round(v 2^19) (resolution 1.9e-6).  A staged atom takes
+// at most (list width + 16) contributions within one CTA (as a partner of
+// the segment's own atoms, plus its own chunk sums), so fix_max =
+// min(64, 2^31 / (2^19 (width + 16))) keeps every slot's sum inside 32 bits;
+// larger components (close contacts) go to global memory as float
+// reductions.
 constexpr float kFixScale = 524288.0f;  // 2^19
 constexpr float kFixInv = 1.0f / 524288.0f;
-constexpr float kFixMax = 64.0f;
+constexpr float kFixMaxCap = 64.0f;
 
 // (two's complement: an unsigned 32-bit add is the signed one)
 __device__ __forceinline__ void red_shared_s32(int* p, int v) {
@@ -373,7 +376,7 @@ k_seg_half(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
     // close contact straight to the atom's sorted slot (the pieces partition
     // the staged slots; a slot outside them is skipped rather than written)
     auto deposit = [&](int j, float vx, float vy, float vz) {
-      if (fabsf(vx) < kFixMax && fabsf(vy) < kFixMax && fabsf(vz) < kFixMax) {
+      if (fabsf(vx) < a.fix_max && fabsf(vy) < a.fix_max && fabsf(vz) < a.fix_max) {
         red_shared_s32(fx + j, __float2int_rn(vx * kFixScale));
         red_shared_s32(fy + j, __float2int_rn(vy * kFixScale));
         if (DIM == 3) red_shared_s32(fz + j, __float2int_rn(vz * kFixScale));
@@ -425,11 +428,12 @@ k_seg_half(SegGrid sg, SegStepArgs a, const __grid_constant__ PairTable tab) {
       }
       // reactions (masked pairs, the far slot included, add nothing).  One
       // packed test of both pair forces' squared magnitudes, g^2 r^2 <
-      // kFixMax^2, clears both for the fixed-point path (each component is
+      // fix_max^2, clears both for the fixed-point path (each component is
       // at most the magnitude); otherwise each pair goes through deposit's
       // per-component test
       const float2 f2m = mul2(mul2(g, g), r2);
-      if (f2m.x < kFixMax * kFixMax && f2m.y < kFixMax * kFixMax) {
+      const float fix2 = a.fix_max * a.fix_max;
+      if (f2m.x < fix2 && f2m.y < fix2) {
         if (m0) {
           red_shared_s32(fx + j0, __float2int_rn(gx.x * kFixScale));
           red_shared_s32(fy + j0, __float2int_rn(gy.x * kFixScale));
@@ -609,6 +613,8 @@ int seg_step(int mode, const jmd_pair& pp, const jmd_space& space, const SegGrid
   a.thr2 = thr2;
   a.flag = flag;
   a.status = status;
+  // rows hold at most 8 nch entries
+  a.fix_max = fminf(kFixMaxCap, 2147483648.0f / (kFixScale * (float)(8 * g.nch + 16)));
   if (g.half) {
     // forces into f (zero on entry), then the integration
     a.f = reinterpret_cast<float4*>(f);
