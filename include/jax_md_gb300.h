@@ -702,8 +702,6 @@ int jmd_batch_pair_forces(const jmd_pair* pair, const jmd_batch* batch,
                           const int32_t* species, float* force, double* energy,
                           void* stream);
 
-/* Per-system f64 kinetic energy ke[B] (quantity.kinetic_energy) and
- * largest atom force norm fmax[B] (either may be NULL). */
 /* Per-system dot products out[b] = sum over system b's atoms of a_i . c_i
  * (dim components of rows of the given strides), f64 sums of fp32 products.
  * The reductions of the batched Nose-Hoover adjoint (sum_i pbar_i . r_i):
@@ -728,6 +726,8 @@ int jmd_batch_nvt_adjoint_update(const jmd_batch* batch, int32_t stage, const fl
                                  const float* pending, float* out_a, float* out_b,
                                  double* sums, void* stream);
 
+/* Per-system f64 kinetic energy ke[B] (quantity.kinetic_energy) and
+ * largest atom force norm fmax[B] (either may be NULL). */
 int jmd_batch_kinetic_energy(const jmd_batch* batch, const float* momentum,
                              const float* force, const float* mass, float mass_scalar,
                              double* ke, float* fmax, void* stream);
