@@ -1219,6 +1219,7 @@ int build_segment_after_sort(const jmd_nlist* nl, const SegGrid& sg, const float
     }
     if (e) return e;
     if (sg.half)
+      // grid-stride: four blocks per SM of the 152-SM part cover any n
       k_seg_occupancy<<<(unsigned)std::min<int64_t>(zgrid, 4 * 152), 256, 0, st>>>(
           nbr_count, (int)n, width, b, rebuild_flag);
   }
